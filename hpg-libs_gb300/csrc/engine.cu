@@ -1,0 +1,534 @@
+// engine.cu -- GPU context: index upload, workspace and pipeline orchestration.
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "engine.hpp"
+#include "fm_device.cuh"
+#include "kernels.cuh"
+
+namespace hpgbwt {
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+#define HPG_CUDA(call, msg)                                                        \
+  do {                                                                             \
+    cudaError_t _e = (call);                                                       \
+    if (_e != cudaSuccess) {                                                       \
+      if (err) *err = std::string(msg) + ": " + cudaGetErrorString(_e);            \
+      return -1;                                                                   \
+    }                                                                              \
+  } while (0)
+
+}  // namespace
+
+struct Engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevIndex X{};
+  OccBlock* d_occ[2] = {nullptr, nullptr};
+  uint32_t* d_S[2] = {nullptr, nullptr};
+  uint64_t* d_kar_off = nullptr;
+  uint64_t* d_kar_start = nullptr;
+  uint8_t* d_table = nullptr;
+  uint32_t* d_err = nullptr;
+  uint8_t h_table[256];
+
+  // workspace
+  DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
+      loc_off, locs, census;
+  uint32_t ovf_cap = 0;
+  size_t chunk = 0;  // reads per chunk, 0 = automatic
+  bool census_on = false;
+  unsigned long long census_val = 0;
+  cudaEvent_t ev[kStageCount + 1];
+  cudaEvent_t cev[4];
+  float stage_ms[kStageCount] = {0, 0, 0, 0};
+  DeviceResult last;
+};
+
+namespace {
+
+// Grow-only device buffer; `keep` preserves the old contents.
+bool ensure(Engine* e, DevBuf& b, size_t bytes, bool keep = false) {
+  if (bytes <= b.cap) return true;
+  size_t want = std::max(bytes, b.cap + b.cap / 2);
+  void* p = nullptr;
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    want = bytes;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  if (keep && b.p && b.cap) cudaMemcpyAsync(p, b.p, b.cap, cudaMemcpyDeviceToDevice, e->stream);
+  if (b.p) {
+    cudaStreamSynchronize(e->stream);
+    cudaFree(b.p);
+  }
+  b.p = p;
+  b.cap = want;
+  return true;
+}
+
+template <typename T>
+T* ptr(DevBuf& b) {
+  return static_cast<T*>(b.p);
+}
+
+// Repack the reference's O/count tables (column c = row c-1) into 32-byte
+// blocks of 64 rows with 2-bit codes and block-start counts.
+std::string pack_occ(const OccTable& o, std::vector<OccBlock>* out, uint32_t* dollar) {
+  const uint64_t rows = (uint64_t)o.siz - 1;  // n + 1
+  const uint64_t nblk = (rows >> 6) + 1;
+  out->assign(nblk, OccBlock{});
+  int64_t dollar_row = -1;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t q = 0; q < (int64_t)nblk; ++q) {
+    OccBlock& B = (*out)[(size_t)q];
+    for (int b = 0; b < 4; ++b) {
+      const size_t idx = (size_t)b * o.m + (size_t)q;
+      B.cnt[b] = q < (int64_t)o.m ? o.desp[idx] + (uint32_t)(o.count[idx] & 1u) : 0u;
+    }
+    uint32_t w[4] = {0, 0, 0, 0};
+    for (int t = 0; t < 64; ++t) {
+      const uint64_t row = (uint64_t)q * 64 + t;
+      if (row >= rows) break;
+      const uint64_t col = row + 1, cq = col >> 6, cb = col & 63;
+      int sym = -1, nset = 0;
+      for (int b = 0; b < 4; ++b)
+        if (cq < o.m && ((o.count[(size_t)b * o.m + cq] >> cb) & 1u)) {
+          sym = b;
+          ++nset;
+        }
+      if (nset > 1) bad = 1;
+      if (sym < 0) {
+#pragma omp critical
+        {
+          if (dollar_row >= 0) bad = 1;
+          dollar_row = (int64_t)row;
+        }
+        sym = 0;
+      }
+      w[t >> 4] |= (uint32_t)sym << (2 * (t & 15));
+    }
+    for (int i = 0; i < 4; ++i) B.bits[i] = w[i];
+  }
+  if (bad || dollar_row < 0) return "occurrence table is not a valid BWT";
+  // Block counts must equal the running counts of the codes (so every rank,
+  // and with a consistent C every LF step, stays inside [0, n]).
+  uint64_t run[4] = {0, 0, 0, 0};
+  for (uint64_t q = 0; q < nblk; ++q) {
+    const OccBlock& B = (*out)[q];
+    for (int b = 0; b < 4; ++b)
+      if (B.cnt[b] != run[b]) return "occurrence counts disagree with the BWT";
+    for (int t = 0; t < 64; ++t) {
+      const uint64_t row = q * 64 + t;
+      if (row >= rows) break;
+      if ((int64_t)row == dollar_row) continue;
+      run[(B.bits[t >> 4] >> (2 * (t & 15))) & 3u]++;
+    }
+  }
+  *dollar = (uint32_t)dollar_row;
+  return "";
+}
+
+// C must be the cumulative symbol counts (C1 = C + 1) for LF to stay in range.
+std::string check_C(const HostIndex& h, const std::vector<OccBlock>& blk, uint32_t dollar) {
+  uint64_t tot[4] = {0, 0, 0, 0};
+  const uint64_t rows = (uint64_t)h.O.siz - 1;
+  const OccBlock& last = blk.back();
+  const uint64_t q = blk.size() - 1;
+  for (int b = 0; b < 4; ++b) {
+    tot[b] = last.cnt[b];
+    for (int t = 0; t < 64; ++t) {
+      const uint64_t row = q * 64 + t;
+      if (row >= rows) break;
+      if (row == dollar) continue;
+      if (((last.bits[t >> 4] >> (2 * (t & 15))) & 3u) == (uint32_t)b) tot[b]++;
+    }
+  }
+  uint64_t acc = 0;
+  for (int b = 0; b < 4; ++b) {
+    if (h.C[b] != acc || h.C1[b] != acc + 1) return "C/C1 vectors disagree with the occurrence table";
+    acc += tot[b];
+  }
+  if (acc + 1 != rows) return "occurrence table size disagrees with its counts";
+  return "";
+}
+
+}  // namespace
+
+Engine* engine_create(const HostIndex& h, int device, std::string* err) {
+  Alphabet a;
+  std::string e = make_alphabet(h.alphabet, &a);
+  if (!e.empty()) {
+    *err = e;
+    return nullptr;
+  }
+  if (h.S.ratio != h.Si.ratio || h.S.ratio == 0) {
+    *err = "S and Si sampling ratios differ";
+    return nullptr;
+  }
+  std::vector<OccBlock> blk[2];
+  uint32_t dollar[2] = {0, 0};
+  if (!(e = pack_occ(h.O, &blk[0], &dollar[0])).empty() || !(e = pack_occ(h.Oi, &blk[1], &dollar[1])).empty() ||
+      !(e = check_C(h, blk[0], dollar[0])).empty() || !(e = check_C(h, blk[1], dollar[1])).empty()) {
+    *err = e;
+    return nullptr;
+  }
+  for (int d = 0; d < 2; ++d) {
+    const SampledVec& S = d ? h.Si : h.S;
+    if ((uint64_t)S.n * S.ratio < (uint64_t)h.O.siz - 1 || S.siz + 1 != h.O.siz) {
+      *err = "sampled suffix array does not cover every row";
+      return nullptr;
+    }
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    *err = "no CUDA device available: the GB300 mapping path has no CPU fallback";
+    return nullptr;
+  }
+  Engine* en = new Engine();
+  en->device = device;
+  auto fail = [&](const char* what, cudaError_t ce) {
+    *err = std::string(what) + ": " + cudaGetErrorString(ce);
+    engine_destroy(en);
+    return (Engine*)nullptr;
+  };
+  cudaError_t ce;
+  if ((ce = cudaSetDevice(device)) != cudaSuccess) return fail("cudaSetDevice", ce);
+  if ((ce = cudaStreamCreateWithFlags(&en->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return fail("cudaStreamCreate", ce);
+  for (int i = 0; i <= kStageCount; ++i) cudaEventCreate(&en->ev[i]);
+  for (int i = 0; i < 4; ++i) cudaEventCreate(&en->cev[i]);
+  const SampledVec* S[2] = {&h.S, &h.Si};
+  for (int d = 0; d < 2; ++d) {
+    if ((ce = cudaMalloc(&en->d_occ[d], blk[d].size() * sizeof(OccBlock))) != cudaSuccess)
+      return fail("cudaMalloc(occ)", ce);
+    if ((ce = cudaMemcpy(en->d_occ[d], blk[d].data(), blk[d].size() * sizeof(OccBlock), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      return fail("upload occ", ce);
+    if ((ce = cudaMalloc(&en->d_S[d], (size_t)S[d]->n * 4 + 4)) != cudaSuccess) return fail("cudaMalloc(S)", ce);
+    if ((ce = cudaMemcpy(en->d_S[d], S[d]->v.data(), (size_t)S[d]->n * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail("upload S", ce);
+    en->X.dir[d].occ = en->d_occ[d];
+    en->X.dir[d].S = en->d_S[d];
+    en->X.dir[d].dollar = dollar[d];
+    en->X.dir[d].nblk = (uint32_t)blk[d].size();
+  }
+  const size_t nk = h.kar.start.size();
+  if ((ce = cudaMalloc(&en->d_kar_off, (nk + 1) * 8)) != cudaSuccess) return fail("cudaMalloc(karyotype)", ce);
+  if ((ce = cudaMalloc(&en->d_kar_start, (nk + 1) * 8)) != cudaSuccess) return fail("cudaMalloc(karyotype)", ce);
+  cudaMemcpy(en->d_kar_off, h.kar.offset.data(), (nk + 1) * 8, cudaMemcpyHostToDevice);
+  if (nk) cudaMemcpy(en->d_kar_start, h.kar.start.data(), nk * 8, cudaMemcpyHostToDevice);
+  std::memcpy(en->h_table, a.code_of, 256);
+  if ((ce = cudaMalloc(&en->d_table, 256)) != cudaSuccess) return fail("cudaMalloc(table)", ce);
+  cudaMemcpy(en->d_table, en->h_table, 256, cudaMemcpyHostToDevice);
+  if ((ce = cudaMalloc(&en->d_err, 4)) != cudaSuccess) return fail("cudaMalloc(err)", ce);
+  cudaMemset(en->d_err, 0, 4);
+  en->X.err = en->d_err;
+
+  for (int b = 0; b < 4; ++b) {
+    en->X.C[b] = h.C[b];
+    en->X.C1[b] = h.C1[b];
+    en->X.comp[b] = a.comp[b];
+  }
+  en->X.ratio = h.S.ratio;
+  en->X.ratio_shift = 0xFFFFFFFFu;
+  for (uint32_t s = 0; s < 32; ++s)
+    if ((1u << s) == h.S.ratio) en->X.ratio_shift = s;
+  en->X.walk_mod = h.O.siz - 1;
+  en->X.top = h.S.siz - 1;
+  en->X.kar_offset = en->d_kar_off;
+  en->X.kar_start = en->d_kar_start;
+  en->X.kar_size = (uint32_t)nk;
+  if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return fail("index upload", ce);
+  return en;
+}
+
+void engine_destroy(Engine* e) {
+  if (!e) return;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  for (int d = 0; d < 2; ++d) {
+    cudaFree(e->d_occ[d]);
+    cudaFree(e->d_S[d]);
+  }
+  cudaFree(e->d_kar_off);
+  cudaFree(e->d_kar_start);
+  cudaFree(e->d_table);
+  cudaFree(e->d_err);
+  DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
+                    &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
+                    &e->census};
+  for (DevBuf* b : bufs) cudaFree(b->p);
+  for (int i = 0; i <= kStageCount; ++i)
+    if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+  for (int i = 0; i < 4; ++i)
+    if (e->cev[i]) cudaEventDestroy(e->cev[i]);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+void* engine_stream(Engine* e) { return (void*)e->stream; }
+int engine_device(Engine* e) { return e->device; }
+void engine_set_census(Engine* e, int on) { e->census_on = on != 0; }
+unsigned long long engine_census(Engine* e) { return e->census_val; }
+void engine_set_chunk(Engine* e, size_t reads) { e->chunk = reads; }
+
+void engine_stage_ms(Engine* e, float* out, int n) {
+  for (int i = 0; i < n && i < kStageCount; ++i) out[i] = e->stage_ms[i];
+}
+
+int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
+                         uint64_t total_bases, uint32_t max_len, uint32_t max_results, DeviceResult* out,
+                         std::string* err) {
+  if (mode != HPG_BWT_MODE_EXACT && mode != HPG_BWT_MODE_SEARCH1) {
+    *err = "unknown search mode";
+    return -1;
+  }
+  if (form != kFormPlain) {
+    *err = "unknown pipeline form";
+    return -1;
+  }
+  if (n_reads >= (1ull << 31)) {
+    *err = "too many reads in one batch";
+    return -1;
+  }
+  if (max_len > 32767) {
+    *err = "reads longer than 32767 bases are not supported";
+    return -1;
+  }
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  cudaStream_t s = e->stream;
+  const uint32_t n = (uint32_t)n_reads;
+  const uint32_t len_cap = std::max<uint32_t>(max_len, 3);
+
+  if (!ensure(e, e->codes, total_bases + 16) || !ensure(e, e->ok, n + 16) || !ensure(e, e->rs_count, 8ull * n + 16) ||
+      !ensure(e, e->rs_trunc, 2ull * n + 16) || !ensure(e, e->census, 16) || !ensure(e, e->ovf_count, 16)) {
+    *err = "out of device memory (read buffers)";
+    return -1;
+  }
+  // Sector census (bench only): counted per launch, summed on the host.
+  unsigned long long* census = e->census_on ? ptr<unsigned long long>(e->census) : nullptr;
+  e->census_val = 0;
+  auto census_take = [&]() -> int {
+    if (!census) return 0;
+    unsigned long long v = 0;
+    HPG_CUDA(cudaMemcpyAsync(&v, census, 8, cudaMemcpyDeviceToHost, s), "census");
+    HPG_CUDA(cudaStreamSynchronize(s), "census");
+    e->census_val += v;
+    return 0;
+  };
+
+  // Chunk so that the plain form's vector scratch stays within ~8 GB.
+  size_t chunk = e->chunk;
+  if (chunk == 0) {
+    const size_t per_read = (mode == HPG_BWT_MODE_SEARCH1) ? 2ull * 2 * len_cap * 8 : 0;
+    chunk = per_read ? std::max<size_t>(1024, (8ull << 30) / per_read) : n_reads;
+  }
+  chunk = std::max<size_t>(1, std::min(chunk, std::max<size_t>(n_reads, 1)));
+
+  cudaEventRecord(e->ev[0], s);
+  launch_encode(d_seqs, d_offs, n, e->d_table, ptr<uint8_t>(e->codes), ptr<uint8_t>(e->ok), s);
+  cudaEventRecord(e->ev[1], s);
+
+  size_t n_hits = 0, n_locs = 0;
+  float t_search = 0, t_final = 0, t_loc = 0;
+  cudaEvent_t a = e->cev[0], b = e->cev[1], c = e->cev[2], d = e->cev[3];
+  for (size_t r0 = 0; r0 < n_reads; r0 += chunk) {
+    const uint32_t nr = (uint32_t)std::min(chunk, n_reads - r0);
+    const size_t T = 2ull * nr;
+    if (!ensure(e, e->slots, T * kSlotCap * sizeof(uint4)) || !ensure(e, e->hit_off, (T + 1) * 8) ||
+        !ensure(e, e->scan_part, scan_parts(T) * 8)) {
+      *err = "out of device memory (hit slots)";
+      return -1;
+    }
+    if (mode == HPG_BWT_MODE_SEARCH1) {
+      if (!ensure(e, e->vecs, 2ull * len_cap * T * sizeof(uint2))) {
+        *err = "out of device memory (vector scratch)";
+        return -1;
+      }
+      if (e->ovf_cap < T) {
+        if (!ensure(e, e->ovf, T * sizeof(OvfEntry))) {
+          *err = "out of device memory (overflow pool)";
+          return -1;
+        }
+        e->ovf_cap = (uint32_t)std::min<size_t>(e->ovf.cap / sizeof(OvfEntry), 0xFFFFFFFFu);
+      }
+    }
+    cudaEventRecord(a, s);
+    for (int attempt = 0;; ++attempt) {
+      if (census) cudaMemsetAsync(census, 0, 8, s);
+      if (mode == HPG_BWT_MODE_EXACT) {
+        launch_exact(e->X, ptr<uint8_t>(e->codes), d_offs, ptr<uint8_t>(e->ok), (uint32_t)r0, nr,
+                     ptr<uint4>(e->slots), ptr<uint32_t>(e->rs_count), ptr<uint8_t>(e->rs_trunc), census, s);
+        break;
+      }
+      cudaMemsetAsync(e->ovf_count.p, 0, 4, s);
+      launch_plain_search1(e->X, ptr<uint8_t>(e->codes), d_offs, ptr<uint8_t>(e->ok), (uint32_t)r0, nr, max_results,
+                           len_cap, ptr<uint2>(e->vecs), ptr<uint4>(e->slots), ptr<OvfEntry>(e->ovf), e->ovf_cap,
+                           ptr<uint32_t>(e->ovf_count), ptr<uint32_t>(e->rs_count), ptr<uint8_t>(e->rs_trunc),
+                           census, s);
+      uint32_t used = 0;
+      HPG_CUDA(cudaMemcpyAsync(&used, e->ovf_count.p, 4, cudaMemcpyDeviceToHost, s), "overflow count");
+      HPG_CUDA(cudaStreamSynchronize(s), "search kernel");
+      if (used <= e->ovf_cap) break;
+      if (!ensure(e, e->ovf, (size_t)used * 2 * sizeof(OvfEntry))) {
+        *err = "out of device memory (overflow pool)";
+        return -1;
+      }
+      e->ovf_cap = (uint32_t)std::min<size_t>(e->ovf.cap / sizeof(OvfEntry), 0xFFFFFFFFu);
+    }
+    cudaEventRecord(b, s);
+    if (census_take() != 0) return -1;
+    // ordered hits of this chunk
+    launch_scan(ptr<uint32_t>(e->rs_count) + 2 * r0, T, ptr<uint64_t>(e->hit_off), ptr<uint64_t>(e->scan_part), s);
+    uint64_t h_tot = 0;
+    HPG_CUDA(cudaMemcpyAsync(&h_tot, ptr<uint64_t>(e->hit_off) + T, 8, cudaMemcpyDeviceToHost, s), "hit count");
+    HPG_CUDA(cudaStreamSynchronize(s), "hit scan");
+    if (!ensure(e, e->hits, (n_hits + h_tot + 1) * sizeof(hpg_hit_t), true)) {
+      *err = "out of device memory (hits)";
+      return -1;
+    }
+    hpg_hit_t* hits = ptr<hpg_hit_t>(e->hits) + n_hits;
+    launch_gather_hits(ptr<uint4>(e->slots), mode == HPG_BWT_MODE_SEARCH1 ? ptr<OvfEntry>(e->ovf) : nullptr,
+                       ptr<uint32_t>(e->ovf_count), mode == HPG_BWT_MODE_SEARCH1 ? e->ovf_cap : 0,
+                       ptr<uint32_t>(e->rs_count), ptr<uint64_t>(e->hit_off), (uint32_t)r0, nr, hits, s);
+    // rows to locate
+    if (!ensure(e, e->rows, (h_tot + 1) * 4) || !ensure(e, e->loc_off, (h_tot + 2) * 8) ||
+        !ensure(e, e->scan_part, scan_parts(h_tot) * 8)) {
+      *err = "out of device memory (locate offsets)";
+      return -1;
+    }
+    launch_hit_rows(hits, (uint32_t)h_tot, ptr<uint32_t>(e->rows), s);
+    launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
+    uint64_t l_tot = 0;
+    HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
+    HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
+    if (census) cudaMemsetAsync(census, 0, 8, s);
+    cudaEventRecord(c, s);
+    if (!ensure(e, e->locs, (n_locs + l_tot + 1) * sizeof(hpg_loc_t), true)) {
+      *err = "out of device memory (locate output)";
+      return -1;
+    }
+    launch_locate(e->X, hits, ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs, (uint32_t)n_hits,
+                  ptr<hpg_loc_t>(e->locs) + n_locs, census, s);
+    cudaEventRecord(d, s);
+    HPG_CUDA(cudaStreamSynchronize(s), "locate kernel");
+    if (census_take() != 0) return -1;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    t_search += ms;
+    cudaEventElapsedTime(&ms, b, c);
+    t_final += ms;
+    cudaEventElapsedTime(&ms, c, d);
+    t_loc += ms;
+    n_hits += h_tot;
+    n_locs += l_tot;
+  }
+  cudaEventRecord(e->ev[kStageCount], s);
+  HPG_CUDA(cudaStreamSynchronize(s), "pipeline");
+  HPG_CUDA(cudaGetLastError(), "kernel launch");
+  {
+    uint32_t derr = 0;
+    HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+    if (derr) {
+      cudaMemset(e->d_err, 0, 4);
+      *err = "corrupt index: suffix-array walk did not reach a sampled row";
+      return -1;
+    }
+  }
+  cudaEventElapsedTime(&e->stage_ms[kStageEncode], e->ev[0], e->ev[1]);
+  e->stage_ms[kStageSearch] = t_search;
+  e->stage_ms[kStageFinalize] = t_final;
+  e->stage_ms[kStageLocate] = t_loc;
+  DeviceResult r;
+  r.n_reads = n_reads;
+  r.n_hits = n_hits;
+  r.hits = ptr<hpg_hit_t>(e->hits);
+  r.n_locs = n_locs;
+  r.locs = ptr<hpg_loc_t>(e->locs);
+  r.rs_count = ptr<uint32_t>(e->rs_count);
+  r.rs_truncated = ptr<uint8_t>(e->rs_trunc);
+  e->last = r;
+  *out = r;
+  return 0;
+}
+
+int engine_copy_result(Engine* e, const DeviceResult& r, hpg_hit_t* hits, hpg_loc_t* locs, uint32_t* rs_count,
+                       uint8_t* rs_truncated, std::string* err) {
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  cudaStream_t s = e->stream;
+  if (hits && r.n_hits)
+    HPG_CUDA(cudaMemcpyAsync(hits, r.hits, r.n_hits * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s), "copy hits");
+  if (locs && r.n_locs)
+    HPG_CUDA(cudaMemcpyAsync(locs, r.locs, r.n_locs * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, s), "copy locs");
+  if (rs_count && r.n_reads)
+    HPG_CUDA(cudaMemcpyAsync(rs_count, r.rs_count, 2 * r.n_reads * 4, cudaMemcpyDeviceToHost, s), "copy counts");
+  if (rs_truncated && r.n_reads)
+    HPG_CUDA(cudaMemcpyAsync(rs_truncated, r.rs_truncated, 2 * r.n_reads, cudaMemcpyDeviceToHost, s), "copy flags");
+  HPG_CUDA(cudaStreamSynchronize(s), "copy result");
+  return 0;
+}
+
+int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
+                       uint32_t max_results, hpg_result_set_t* out, std::string* err) {
+  std::memset(out, 0, sizeof(*out));
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  const uint64_t total = n_reads ? offs[n_reads] - offs[0] : 0;
+  uint32_t max_len = 0;
+  for (size_t i = 0; i < n_reads; ++i) {
+    if (offs[i + 1] < offs[i]) {
+      *err = "read offsets must be non-decreasing";
+      return -1;
+    }
+    const uint64_t L = offs[i + 1] - offs[i];
+    if (L > 32767) {
+      *err = "reads longer than 32767 bases are not supported";
+      return -1;
+    }
+    max_len = std::max<uint32_t>(max_len, (uint32_t)L);
+  }
+  if (!ensure(e, e->seqs, total + 16) || !ensure(e, e->offs, (n_reads + 1) * 8)) {
+    *err = "out of device memory (reads)";
+    return -1;
+  }
+  std::vector<uint64_t> rel(n_reads + 1);
+  for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
+  cudaStream_t s = e->stream;
+  if (total) HPG_CUDA(cudaMemcpyAsync(e->seqs.p, seqs + offs[0], total, cudaMemcpyHostToDevice, s), "upload reads");
+  HPG_CUDA(cudaMemcpyAsync(e->offs.p, rel.data(), (n_reads + 1) * 8, cudaMemcpyHostToDevice, s), "upload offsets");
+  DeviceResult r;
+  if (engine_search_device(e, mode, form, ptr<uint8_t>(e->seqs), ptr<uint64_t>(e->offs), n_reads, total, max_len,
+                           max_results, &r, err) != 0)
+    return -1;
+  out->n_reads = n_reads;
+  out->n_hits = r.n_hits;
+  out->n_locs = r.n_locs;
+  out->hits = (hpg_hit_t*)std::malloc((r.n_hits + 1) * sizeof(hpg_hit_t));
+  out->locs = (hpg_loc_t*)std::malloc((r.n_locs + 1) * sizeof(hpg_loc_t));
+  out->rs_count = (uint32_t*)std::malloc((2 * n_reads + 1) * 4);
+  out->rs_truncated = (uint8_t*)std::malloc(2 * n_reads + 1);
+  if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
+    *err = "out of host memory";
+    return -1;
+  }
+  return engine_copy_result(e, r, out->hits, out->locs, out->rs_count, out->rs_truncated, err);
+}
+
+}  // namespace hpgbwt

@@ -1,0 +1,60 @@
+// engine.hpp -- one GPU context per loaded index: the HBM-resident index, a
+// CUDA stream, a grow-only device workspace and the mapping pipeline.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "hpg_bwt_records.h"
+#include "index_format.hpp"
+
+namespace hpgbwt {
+
+// Pipeline forms.
+enum Form : int {
+  kFormPlain = 0,    // one thread per (read, strand), one launch per stage
+  kFormBatched = 1,  // persistent work-queue kernel replayed from a CUDA graph
+};
+
+// Device-resident output of one search call; valid until the next call.
+struct DeviceResult {
+  size_t n_reads = 0;
+  size_t n_hits = 0;
+  const hpg_hit_t* hits = nullptr;
+  size_t n_locs = 0;
+  const hpg_loc_t* locs = nullptr;
+  const uint32_t* rs_count = nullptr;
+  const uint8_t* rs_truncated = nullptr;
+};
+
+// Per-stage device times of the last call (ms), measured with CUDA events on
+// the engine's stream.
+enum Stage : int { kStageEncode = 0, kStageSearch, kStageFinalize, kStageLocate, kStageCount };
+
+struct Engine;
+
+Engine* engine_create(const HostIndex& h, int device, std::string* err);
+void engine_destroy(Engine* e);
+void* engine_stream(Engine* e);
+int engine_device(Engine* e);
+
+// Reads already in device memory: ASCII bytes and n_reads+1 offsets.
+int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
+                         uint64_t total_bases, uint32_t max_len, uint32_t max_results, DeviceResult* out,
+                         std::string* err);
+
+// Host reads in, host records out (malloc'ed; free with hpg_result_free).
+int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
+                       uint32_t max_results, hpg_result_set_t* out, std::string* err);
+
+// Copy the last device result into caller buffers (any host memory).
+int engine_copy_result(Engine* e, const DeviceResult& r, hpg_hit_t* hits, hpg_loc_t* locs, uint32_t* rs_count,
+                       uint8_t* rs_truncated, std::string* err);
+
+void engine_stage_ms(Engine* e, float* out, int n);
+void engine_set_census(Engine* e, int on);
+unsigned long long engine_census(Engine* e);
+void engine_set_chunk(Engine* e, size_t reads_per_chunk);
+
+}  // namespace hpgbwt

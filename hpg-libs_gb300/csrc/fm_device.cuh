@@ -1,0 +1,184 @@
+// fm_device.cuh -- HBM-resident FM-index layout and the device-side rank,
+// backward-extension, LF and locate primitives shared by every kernel.
+//
+// Layout (one per physical direction: 0 = backward index of the text,
+// 1 = forward index = backward index of the reversed text):
+//
+//   OccBlock occ[nblk]   32-byte blocks, one per 64 BWT rows:
+//       cnt[b]   number of symbol b in BWT rows [0, 64q), '$' excluded
+//       bits[4]  2-bit codes of rows 64q..64q+63 (row r: word (r%64)/16,
+//                bits 2*(r%16)); the '$' row is stored as code 0 and
+//                corrected in rank_block().
+//   uint32 S[]           sampled SA, S[i/ratio] = SA[i] (the reference's S.vec)
+//
+// One rank query therefore touches exactly one 32-byte sector, against two
+// separate arrays (a 4-byte desp and an 8-byte count word) per query in the
+// reference's comp_matrix (search/csafm.h:51-64,166-181).
+//
+// Reverse-complement views (backward_rev / forward_rev, search/csafm.c:3-100)
+// swap C and O rows by complement; here the query symbol is complemented
+// instead, so no table is copied.
+#pragma once
+
+#include <cstdint>
+
+namespace hpgbwt {
+
+struct __align__(32) OccBlock {
+  uint32_t cnt[4];
+  uint32_t bits[4];
+};
+
+struct DevDir {
+  const OccBlock* occ;
+  const uint32_t* S;
+  uint32_t dollar;  // BWT row holding '$'
+  uint32_t nblk;
+};
+
+struct DevIndex {
+  DevDir dir[2];
+  uint32_t C[4], C1[4];   // C counts symbols < b without '$'; C1 = C + 1
+  uint32_t comp[4];       // complement of each code
+  uint32_t ratio;         // SA sampling ratio
+  uint32_t ratio_shift;   // log2(ratio) when ratio is a power of two, else 0xFFFFFFFF
+  uint32_t walk_mod;      // O.siz - 1 = n + 1: modulus of the SA walk (csafm.h:233)
+  uint32_t top;           // n = size_SA - 1: initial l of every search
+  const uint64_t* kar_offset;  // kar_size + 1 entries
+  const uint64_t* kar_start;
+  uint32_t kar_size;
+  uint32_t* err;          // device error word (bit 0: LF walk exceeded n+1 steps)
+};
+
+constexpr uint32_t kErrWalk = 1u;
+
+// A search view: physical direction plus whether query symbols are complemented.
+struct View {
+  uint32_t d;
+  uint32_t comp;
+};
+
+#ifdef __CUDACC__
+
+__device__ __forceinline__ void load_block(const OccBlock* p, uint32_t (&cnt)[4], uint4& bits) {
+  const uint4* q = reinterpret_cast<const uint4*>(p);
+  uint4 c = __ldg(q);
+  bits = __ldg(q + 1);
+  cnt[0] = c.x;
+  cnt[1] = c.y;
+  cnt[2] = c.z;
+  cnt[3] = c.w;
+}
+
+// Number of symbol p among the first r rows (0..64) of a block's 2-bit codes.
+__device__ __forceinline__ uint32_t count_prefix(const uint4& bits, uint32_t p, uint32_t r) {
+  const uint64_t lo = ((uint64_t)bits.y << 32) | bits.x;
+  const uint64_t hi = ((uint64_t)bits.w << 32) | bits.z;
+  const uint64_t pat = 0x5555555555555555ull * p;
+  const uint64_t xl = lo ^ pat, xh = hi ^ pat;
+  const uint64_t ml = ~(xl | (xl >> 1)) & 0x5555555555555555ull;
+  const uint64_t mh = ~(xh | (xh >> 1)) & 0x5555555555555555ull;
+  const uint32_t sh = 2 * r;  // 0..128
+  const uint64_t keep_lo = sh >= 64 ? ~0ull : ((1ull << sh) - 1ull);
+  const uint64_t keep_hi = sh <= 64 ? 0ull : (sh >= 128 ? ~0ull : ((1ull << (sh - 64)) - 1ull));
+  return (uint32_t)(__popcll(ml & keep_lo) + __popcll(mh & keep_hi));
+}
+
+// Occurrences of physical symbol p in BWT rows [64q, 64q + r) plus cnt, with
+// the '$' row (stored as code 0) taken out.
+__device__ __forceinline__ uint32_t rank_block(const DevDir& D, uint32_t q, uint32_t p, uint32_t r,
+                                               const uint32_t (&cnt)[4], const uint4& bits) {
+  uint32_t v = cnt[p] + count_prefix(bits, p, r);
+  if (p == 0 && q == (D.dollar >> 6) && r > (D.dollar & 63)) v -= 1;
+  return v;
+}
+
+// get_O(p, k): symbol p in rows [0, k).  k in [0, n+1].
+__device__ __forceinline__ uint32_t rank_lo(const DevDir& D, uint32_t p, uint32_t k) {
+  uint32_t cnt[4];
+  uint4 bits;
+  const uint32_t q = k >> 6;
+  load_block(D.occ + q, cnt, bits);
+  return rank_block(D, q, p, k & 63, cnt, bits);
+}
+
+// get_O(p, l + 1): symbol p in rows [0, l].  l in [0, n].
+__device__ __forceinline__ uint32_t rank_hi(const DevDir& D, uint32_t p, uint32_t l) {
+  uint32_t cnt[4];
+  uint4 bits;
+  const uint32_t q = l >> 6;
+  load_block(D.occ + q, cnt, bits);
+  return rank_block(D, q, p, (l & 63) + 1, cnt, bits);
+}
+
+// BWiteration (search/runtime.h:38-42) over a view, on 32-bit interval ends.
+// k in [0, n+1], l in [0, n] always hold for the intervals the search forms.
+__device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, uint32_t& k, uint32_t& l) {
+  const uint32_t p = v.comp ? X.comp[b] : b;
+  const DevDir& D = X.dir[v.d];
+  const uint32_t q0 = k >> 6, q1 = l >> 6;
+  uint32_t cnt[4];
+  uint4 bits;
+  load_block(D.occ + q0, cnt, bits);
+  const uint32_t rk = rank_block(D, q0, p, k & 63, cnt, bits);
+  uint32_t rl;
+  if (q1 == q0) {
+    rl = rank_block(D, q0, p, (l & 63) + 1, cnt, bits);
+  } else {
+    load_block(D.occ + q1, cnt, bits);
+    rl = rank_block(D, q1, p, (l & 63) + 1, cnt, bits);
+  }
+  k = X.C1[p] + rk;
+  l = X.C[p] + rl;
+}
+
+// LF of row i on a physical direction: row 0 for the '$' row, else
+// C[b] + get_O(b, i+1) with b the row's symbol (csafm.h:215-231).
+__device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, uint32_t i) {
+  if (i == D.dollar) return 0;
+  const uint32_t q = i >> 6, r = i & 63;
+  uint32_t cnt[4];
+  uint4 bits;
+  load_block(D.occ + q, cnt, bits);
+  const uint32_t w = r < 32 ? (r < 16 ? bits.x : bits.y) : (r < 48 ? bits.z : bits.w);
+  const uint32_t b = (w >> (2 * (r & 15))) & 3u;
+  return X.C[b] + rank_block(D, q, b, r + 1, cnt, bits);
+}
+
+__device__ __forceinline__ bool sampled_row(const DevIndex& X, uint32_t i) {
+  return X.ratio_shift != 0xFFFFFFFFu ? (i & ((1u << X.ratio_shift) - 1u)) == 0 : (i % X.ratio) == 0;
+}
+
+// getScompValue (csafm.h:208-235): walk LF to a sampled row, add the steps.
+__device__ __forceinline__ uint32_t sa_value(const DevIndex& X, uint32_t d, uint32_t m) {
+  const DevDir& D = X.dir[d];
+  uint32_t i = m, j = 0;
+  while (!sampled_row(X, i)) {
+    i = lf_step(X, D, i);
+    if (++j > X.walk_mod) {  // LF is one cycle over n+1 rows: only a corrupt index gets here
+      atomicOr(X.err, kErrWalk);
+      break;
+    }
+  }
+  const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
+  return (s + j) % X.walk_mod;
+}
+
+// binsearch (search/io.h:43-64): first offset greater than key.
+__device__ __forceinline__ uint32_t kar_search(const DevIndex& X, uint64_t key) {
+  uint32_t lo = 0, size = X.kar_size;
+  while (size > 0) {
+    const uint32_t w = size >> 1;
+    if (X.kar_offset[lo + w] <= key) {
+      lo += w + 1;
+      size -= w + 1;
+    } else {
+      size = w;
+    }
+  }
+  return lo;
+}
+
+#endif  // __CUDACC__
+
+}  // namespace hpgbwt

@@ -1,0 +1,55 @@
+// kernels.cuh -- launch wrappers of the search pipeline kernels (kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "fm_device.cuh"
+#include "hpg_bwt_records.h"
+
+namespace hpgbwt {
+
+// Hit slot written by the search kernels: {k, l, packed meta, 0}.
+// Overflow entries carry the owning (read, strand) slot id and list index.
+struct OvfEntry {
+  uint32_t k, l, meta, t, idx, pad0, pad1, pad2;
+};
+
+constexpr uint32_t kSlotCap = 8;  // hits kept in place per (read, strand); the rest overflow
+
+// ASCII -> 2-bit codes (0xFF outside the alphabet) and a per-read validity flag.
+void launch_encode(const uint8_t* ascii, const uint64_t* offs, uint32_t n_reads, const uint8_t* d_table,
+                   uint8_t* codes, uint8_t* ok, cudaStream_t s);
+
+// Exact backward search on both strands (mode EXACT), one thread per (read, strand).
+void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,
+                  uint32_t nr, uint4* slots, uint32_t* rs_count, uint8_t* rs_trunc,
+                  unsigned long long* census, cudaStream_t s);
+
+// Plain BWSearch1: one thread per (read, strand) runs the two vector searches
+// into `vecs` and then the helper with its continuation searches.
+void launch_plain_search1(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok,
+                          uint32_t r0, uint32_t nr, uint32_t max_results, uint32_t max_len, uint2* vecs,
+                          uint4* slots, OvfEntry* ovf, uint32_t ovf_cap, uint32_t* ovf_count,
+                          uint32_t* rs_count, uint8_t* rs_trunc, unsigned long long* census, cudaStream_t s);
+
+// Exclusive scan: out[0..n] with out[n] = total.  `part` needs scan_parts(n) entries.
+size_t scan_parts(size_t n);
+void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cudaStream_t s);
+
+// Slots + overflow pool -> ordered hpg_hit_t records, hit i of (read, strand) t at off[t] + i.
+void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t* ovf_count, uint32_t ovf_cap,
+                        const uint32_t* rs_count, const uint64_t* off, uint32_t r0, uint32_t nr,
+                        hpg_hit_t* out, cudaStream_t s);
+
+// Rows per hit (l - k + 1 or 0).
+void launch_hit_rows(const hpg_hit_t* hits, uint32_t n_hits, uint32_t* rows, cudaStream_t s);
+
+// Locate every row of every hit (bwt.c:2158-2166); hit ids are offset by hit_base.
+void launch_locate(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
+                   uint64_t n_locs, const uint64_t* read_offs, uint32_t hit_base, hpg_loc_t* out,
+                   unsigned long long* census, cudaStream_t s);
+
+}  // namespace hpgbwt

@@ -1,0 +1,167 @@
+"""ctypes binding of libhpgbwt.so (the C ABI declared in include/hpg_bwt.h).
+
+This is how the tests and the benchmark drive the library; C callers link the
+shared library directly.  There is no Python compute path: every search runs
+in the CUDA kernels behind the C ABI, and opening an index without a CUDA
+device fails.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent.parent / "libhpgbwt.so"
+
+MODE_EXACT = 0
+MODE_SEARCH1 = 1
+FORM_PLAIN = 0
+FORM_BATCHED = 1
+
+HIT_DTYPE = np.dtype([("read", "<u4"), ("strand", "u1"), ("dir", "u1"), ("nm", "u1"), ("err_kind", "u1"),
+                      ("err_base", "u1"), ("pad0", "u1"), ("err_pos", "<i2"), ("pad1", "<u4"), ("k", "<i8"),
+                      ("l", "<i8")])
+LOC_DTYPE = np.dtype([("key", "<u8"), ("position", "<u8"), ("hit", "<u4"), ("chrom", "<u4"), ("valid", "<u4"),
+                      ("pad", "<u4")])
+assert HIT_DTYPE.itemsize == 32 and LOC_DTYPE.itemsize == 32
+
+
+class ResultSetC(ctypes.Structure):
+    _fields_ = [("n_reads", ctypes.c_size_t), ("n_hits", ctypes.c_size_t), ("hits", ctypes.c_void_p),
+                ("n_locs", ctypes.c_size_t), ("locs", ctypes.c_void_p), ("rs_count", ctypes.c_void_p),
+                ("rs_truncated", ctypes.c_void_p)]
+
+
+@dataclass
+class Result:
+    """Flat search output (see include/hpg_bwt_records.h for the ordering)."""
+    hits: np.ndarray
+    locs: np.ndarray
+    rs_count: np.ndarray
+    rs_truncated: np.ndarray
+
+    def equal(self, other: "Result") -> bool:
+        return (np.array_equal(self.hits, other.hits) and np.array_equal(self.locs, other.locs)
+                and np.array_equal(self.rs_count, other.rs_count)
+                and np.array_equal(self.rs_truncated, other.rs_truncated))
+
+
+def _arr(ptr: int | None, n: int, dt: np.dtype) -> np.ndarray:
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype=dt)
+    return np.frombuffer(ctypes.string_at(ptr, n * dt.itemsize), dtype=dt).copy()
+
+
+def result_from_c(rs: ResultSetC, n_reads: int) -> Result:
+    return Result(_arr(rs.hits, rs.n_hits, HIT_DTYPE), _arr(rs.locs, rs.n_locs, LOC_DTYPE),
+                  _arr(rs.rs_count, 2 * n_reads, np.dtype("<u4")), _arr(rs.rs_truncated, 2 * n_reads, np.dtype("u1")))
+
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load the shared library (it must have been built; see build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with hpg-libs_gb300/hpgbwt/build.py")
+    lib = ctypes.CDLL(str(LIB_PATH), mode=ctypes.RTLD_GLOBAL)
+    vp, sz, u32, u64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64
+    lib.bwt_index_open.restype = vp
+    lib.bwt_index_open.argtypes = [ctypes.c_char_p, ctypes.c_bool, ctypes.c_int, ctypes.c_char_p, sz]
+    lib.bwt_index_free.argtypes = [vp]
+    lib.bwt_gpu_search_batch.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, sz, u32, ctypes.POINTER(ResultSetC)]
+    lib.bwt_gpu_search_device.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, vp, sz, u64, u32, u32,
+                                          ctypes.POINTER(ResultSetC)]
+    lib.bwt_gpu_copy_result.argtypes = [vp, ctypes.POINTER(ResultSetC), vp, vp, vp, vp]
+    lib.bwt_gpu_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
+    lib.bwt_gpu_stream.restype = vp
+    lib.bwt_gpu_stream.argtypes = [vp]
+    lib.bwt_gpu_stage_ms.argtypes = [vp, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+    lib.bwt_gpu_set_census.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_census.restype = ctypes.c_ulonglong
+    lib.bwt_gpu_census.argtypes = [vp]
+    lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
+    lib.bwt_gpu_last_error.restype = ctypes.c_char_p
+    lib.hpg_bwt_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
+                                        ctypes.c_char_p, ctypes.c_char_p, sz]
+    _lib = lib
+    return lib
+
+
+def build_index(fasta: str, outdir: str, ratio: int = 16, bases: str = "ACGT") -> None:
+    lib = load()
+    err = ctypes.create_string_buffer(1024)
+    if lib.hpg_bwt_build_index(fasta.encode(), outdir.encode(), ratio, 0, bases.encode(), err, 1024) != 0:
+        raise RuntimeError(err.value.decode())
+
+
+class GpuIndex:
+    """An index loaded into GPU memory through bwt_index_open."""
+
+    def __init__(self, index_dir: str, device: int = -1, inverse_sa: bool = False):
+        self.lib = load()
+        err = ctypes.create_string_buffer(2048)
+        h = self.lib.bwt_index_open(index_dir.encode(), inverse_sa, device, err, 2048)
+        if not h:
+            raise RuntimeError(err.value.decode())
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.bwt_index_free(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise RuntimeError(self.lib.bwt_gpu_last_error().decode())
+
+    def search(self, reads, mode: int = MODE_SEARCH1, form: int = FORM_PLAIN, max_results: int = 1 << 16) -> Result:
+        """Search a synth.ReadSet-like object (seq: uint8 ASCII, offsets: uint64)."""
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        rs = ResultSetC()
+        self._check(self.lib.bwt_gpu_search_batch(self.handle, mode, form, seq.ctypes.data, offs.ctypes.data, n,
+                                                  max_results, ctypes.byref(rs)))
+        try:
+            return result_from_c(rs, n)
+        finally:
+            self.lib.bwt_gpu_result_free(ctypes.byref(rs))
+
+    def search_device(self, d_seqs: int, d_offs: int, n_reads: int, total_bases: int, max_len: int,
+                      mode: int = MODE_SEARCH1, form: int = FORM_PLAIN, max_results: int = 1 << 16) -> ResultSetC:
+        rs = ResultSetC()
+        self._check(self.lib.bwt_gpu_search_device(self.handle, mode, form, d_seqs, d_offs, n_reads, total_bases,
+                                                   max_len, max_results, ctypes.byref(rs)))
+        return rs
+
+    def copy_result(self, rs: ResultSetC, hits: int, locs: int, rs_count: int, rs_trunc: int) -> None:
+        self._check(self.lib.bwt_gpu_copy_result(self.handle, ctypes.byref(rs), hits, locs, rs_count, rs_trunc))
+
+    def stream(self) -> int:
+        return self.lib.bwt_gpu_stream(self.handle)
+
+    def stage_ms(self) -> list[float]:
+        a = (ctypes.c_float * 4)()
+        self.lib.bwt_gpu_stage_ms(self.handle, a, 4)
+        return list(a)
+
+    def set_census(self, on: bool) -> None:
+        self.lib.bwt_gpu_set_census(self.handle, 1 if on else 0)
+
+    def census(self) -> int:
+        return int(self.lib.bwt_gpu_census(self.handle))
+
+    def set_chunk(self, reads: int) -> None:
+        self.lib.bwt_gpu_set_chunk(self.handle, reads)

@@ -1,0 +1,255 @@
+"""Seeded synthetic genomes and reads with the shapes of the benchmark workloads.
+
+No public dataset is involved: every genome and read set is generated here
+from a seed, with the sizes, base composition, repeat structure and error
+model of the named workload.  Bases are 2-bit codes in the alphabet order
+A=0, C=1, G=2, T=3 (the default ``config.txt`` of the reference builder,
+c/src/aligners/bwt/bwt.c:744-757).
+
+Workloads
+---------
+- ``iid``:      i.i.d. uniform A/C/G/T (4 Mbp exact-search workload).
+- ``repeats``:  GC 41 % background plus 5 % of the length as copies of
+                300 bp elements at 85-95 % identity (100 Mbp workloads).
+- ``human_like``: GC 41 %, 45 % repeats: 300 bp elements (10 %), 6 kbp
+                elements (17 %) at 80-98 % identity, the rest (18 %) 1-6 bp
+                tandem repeats (3.1 Gbp workloads).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+ALPHABET = b"ACGT"
+_COMP = np.array([3, 2, 1, 0], dtype=np.uint8)
+_ASCII = np.frombuffer(ALPHABET, dtype=np.uint8)
+
+
+def background(n: int, rng: np.random.Generator, gc: float = 0.5) -> np.ndarray:
+    p_at = (1.0 - gc) / 2.0
+    p_cg = gc / 2.0
+    return rng.choice(4, size=n, p=[p_at, p_cg, p_cg, p_at]).astype(np.uint8)
+
+
+def _mutate(seq: np.ndarray, identity: float, rng: np.random.Generator) -> np.ndarray:
+    out = seq.copy()
+    m = rng.random(len(out)) > identity
+    out[m] = (out[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
+    return out
+
+
+def _plant_elements(g: np.ndarray, frac: float, elem_len: int, families: int, ident: tuple[float, float],
+                    gc: float, rng: np.random.Generator) -> None:
+    """Overwrite ~frac*len(g) bases with mutated copies of `families` elements."""
+    n = len(g)
+    copies = int(frac * n) // elem_len
+    if copies == 0:
+        return
+    elems = [background(elem_len, rng, gc) for _ in range(families)]
+    fam = rng.integers(0, families, size=copies)
+    starts = rng.integers(0, n - elem_len, size=copies)
+    idents = rng.uniform(ident[0], ident[1], size=copies)
+    for f, s, idt in zip(fam, starts, idents):
+        g[s:s + elem_len] = _mutate(elems[f], idt, rng)
+
+
+def _plant_tandem(g: np.ndarray, frac: float, rng: np.random.Generator) -> None:
+    n = len(g)
+    target = int(frac * n)
+    done = 0
+    while done < target:
+        unit = rng.integers(0, 4, size=int(rng.integers(1, 7)), dtype=np.uint8)
+        length = int(rng.integers(20, 400))
+        s = int(rng.integers(0, n - length))
+        g[s:s + length] = np.resize(unit, length)
+        done += length
+
+
+def genome(kind: str, n: int, seed: int) -> np.ndarray:
+    """Genome codes (uint8, values 0..3) of length n."""
+    rng = np.random.default_rng(seed)
+    if kind == "iid":
+        return rng.integers(0, 4, size=n, dtype=np.uint8)
+    if kind == "repeats":
+        g = background(n, rng, 0.41)
+        _plant_elements(g, 0.05, 300, 16, (0.85, 0.95), 0.41, rng)
+        return g
+    if kind == "human_like":
+        g = background(n, rng, 0.41)
+        _plant_elements(g, 0.10, 300, 64, (0.80, 0.98), 0.41, rng)
+        _plant_elements(g, 0.17, 6000, 32, (0.80, 0.98), 0.41, rng)
+        _plant_tandem(g, 0.18, rng)
+        return g
+    raise ValueError(f"unknown genome kind {kind!r}")
+
+
+def write_fasta(path: str, g: np.ndarray, chrom_lengths: list[int] | None = None, width: int = 80) -> None:
+    """Write codes as FASTA; chrom_lengths splits the genome into chromosomes."""
+    if chrom_lengths is None:
+        chrom_lengths = [len(g)]
+    assert sum(chrom_lengths) == len(g)
+    with open(path, "wb") as f:
+        pos = 0
+        for ci, cl in enumerate(chrom_lengths):
+            f.write(b">chr%d synthetic\n" % (ci + 1))
+            seq = _ASCII[g[pos:pos + cl]]
+            pos += cl
+            full = (cl // width) * width
+            if full:
+                block = np.empty((full // width, width + 1), dtype=np.uint8)
+                block[:, :width] = seq[:full].reshape(-1, width)
+                block[:, width] = ord("\n")
+                f.write(block.tobytes())
+            if cl > full:
+                f.write(seq[full:].tobytes() + b"\n")
+
+
+def revcomp_codes(codes: np.ndarray) -> np.ndarray:
+    return _COMP[codes[::-1]]
+
+
+class ReadSet:
+    """Reads as concatenated ASCII bytes plus offsets (n+1 entries)."""
+
+    def __init__(self, seq: np.ndarray, offsets: np.ndarray, truth_pos: np.ndarray, truth_strand: np.ndarray,
+                 edit: np.ndarray):
+        self.seq = seq            # uint8 ASCII, concatenated
+        self.offsets = offsets    # uint64, n+1
+        self.truth_pos = truth_pos
+        self.truth_strand = truth_strand
+        self.edit = edit          # 0 none, 1 substitution, 2 insertion in read, 3 deletion from read
+
+    def __len__(self) -> int:
+        return len(self.offsets) - 1
+
+    def read(self, i: int) -> bytes:
+        return self.seq[self.offsets[i]:self.offsets[i + 1]].tobytes()
+
+    def lengths(self) -> np.ndarray:
+        return np.diff(self.offsets).astype(np.int64)
+
+    def subset(self, idx) -> "ReadSet":
+        idx = np.asarray(idx)
+        lens = self.lengths()[idx]
+        offs = np.zeros(len(idx) + 1, dtype=np.uint64)
+        np.cumsum(lens, out=offs[1:])
+        parts = [self.seq[self.offsets[i]:self.offsets[i + 1]] for i in idx]
+        seq = np.concatenate(parts) if parts else np.zeros(0, dtype=np.uint8)
+        return ReadSet(seq, offs, self.truth_pos[idx], self.truth_strand[idx], self.edit[idx])
+
+
+def _edit_plan(kind: str, n: int, lens: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+    """Per-read edit: 0 none, 1 substitution, 2 insertion, 3 deletion."""
+    if kind == "none":
+        return np.zeros(n, dtype=np.int8)
+    if kind == "per_base_capped":  # 0.5 % subst, 0.02 % ins, 0.02 % del per base, at most one edit
+        p_s, p_i, p_d = 0.005, 0.0002, 0.0002
+        p_any = 1.0 - (1.0 - p_s - p_i - p_d) ** lens
+        has = rng.random(n) < p_any
+        which = rng.choice(3, size=n, p=np.array([p_s, p_i, p_d]) / (p_s + p_i + p_d)) + 1
+        return np.where(has, which, 0).astype(np.int8)
+    if kind == "mix_30_50_20":  # 30 % exact, 50 % one substitution, 20 % one indel
+        u = rng.random(n)
+        e = np.zeros(n, dtype=np.int8)
+        e[(u >= 0.30) & (u < 0.80)] = 1
+        indel = u >= 0.80
+        e[indel] = np.where(rng.random(int(indel.sum())) < 0.5, 2, 3)
+        return e
+    raise ValueError(kind)
+
+
+def reads(g: np.ndarray, n: int, seed: int, length: int | tuple[int, int] = 100, edits: str = "none",
+          subst_rate: float = 0.0) -> ReadSet:
+    """Sample n reads from uniform positions on either strand (50/50).
+
+    `length` is fixed or (lo, hi) uniform inclusive.  `edits` selects the
+    capped single-edit models; `subst_rate` adds independent per-base
+    substitutions (uncapped) on top.
+    """
+    rng = np.random.default_rng(seed)
+    if isinstance(length, tuple):
+        lens = rng.integers(length[0], length[1] + 1, size=n)
+    else:
+        lens = np.full(n, int(length))
+    plan = _edit_plan(edits, n, lens, rng)
+    glen = len(g)
+    span = lens + 1  # room for one deleted base
+    pos = (rng.random(n) * (glen - span)).astype(np.int64)
+    strand = (rng.random(n) < 0.5).astype(np.int8)
+    out = np.empty(int(lens.sum()), dtype=np.uint8)
+    offs = np.zeros(n + 1, dtype=np.uint64)
+    np.cumsum(lens, out=offs[1:])
+    for i in range(n):
+        L = int(lens[i])
+        p = int(pos[i])
+        e = int(plan[i])
+        if e == 3:  # one base of the fragment is left out of the read
+            frag = g[p:p + L + 1].copy()
+            cut = int(rng.integers(1, L))
+            frag = np.delete(frag, cut)
+        elif e == 2:  # one extra base inside the read
+            frag = g[p:p + L - 1].copy()
+            at = int(rng.integers(1, L - 1))
+            frag = np.insert(frag, at, np.uint8(rng.integers(0, 4)))
+        else:
+            frag = g[p:p + L].copy()
+            if e == 1:
+                at = int(rng.integers(0, L))
+                frag[at] = (frag[at] + rng.integers(1, 4)) % 4
+        if subst_rate > 0:
+            m = rng.random(L) < subst_rate
+            frag[m] = (frag[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
+        if strand[i]:
+            frag = revcomp_codes(frag)
+        out[offs[i]:offs[i + 1]] = _ASCII[frag]
+    return ReadSet(out, offs, pos, strand, plan)
+
+
+def reads_fast(g: np.ndarray, n: int, seed: int, length: int = 100, edits: str = "none",
+               subst_rate: float = 0.0) -> ReadSet:
+    """Vectorised sampler for fixed-length reads (large read sets)."""
+    rng = np.random.default_rng(seed)
+    L = int(length)
+    lens = np.full(n, L)
+    plan = _edit_plan(edits, n, lens, rng)
+    glen = len(g)
+    pos = (rng.random(n) * (glen - L - 1)).astype(np.int64)
+    strand = (rng.random(n) < 0.5).astype(np.int8)
+    idx = pos[:, None] + np.arange(L + 1)[None, :]
+    frag = g[idx]                                   # n x (L+1)
+    # deletions: drop column `cut`, keeping L of the L+1 bases
+    cut = rng.integers(1, L, size=n)
+    col = np.arange(L)[None, :]
+    del_src = np.where(col >= cut[:, None], col + 1, col)
+    # insertions: an extra random base at `at`, the rest shifted right
+    at = rng.integers(1, L - 1, size=n)
+    ins_src = np.where(col > at[:, None], col - 1, col)
+    base = frag[:, :L].copy()
+    d = plan == 3
+    base[d] = np.take_along_axis(frag[d], del_src[d], axis=1)
+    ii = plan == 2
+    if ii.any():
+        shifted = np.take_along_axis(frag[ii], ins_src[ii], axis=1)
+        rows = np.nonzero(ii)[0]
+        shifted[np.arange(len(rows)), at[ii]] = rng.integers(0, 4, size=len(rows), dtype=np.uint8)
+        base[ii] = shifted
+    s = plan == 1
+    sat = rng.integers(0, L, size=n)
+    rows = np.nonzero(s)[0]
+    base[rows, sat[s]] = (base[rows, sat[s]] + rng.integers(1, 4, size=len(rows), dtype=np.uint8)) % 4
+    if subst_rate > 0:
+        m = rng.random((n, L)) < subst_rate
+        base[m] = (base[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
+    rc = strand == 1
+    base[rc] = _COMP[base[rc][:, ::-1]]
+    seq = _ASCII[base].reshape(-1)
+    offs = np.arange(n + 1, dtype=np.uint64) * np.uint64(L)
+    return ReadSet(seq, offs, pos, strand, plan)
+
+
+def from_strings(seqs: list[bytes]) -> ReadSet:
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    offs = np.zeros(len(seqs) + 1, dtype=np.uint64)
+    np.cumsum(lens, out=offs[1:])
+    seq = np.frombuffer(b"".join(seqs), dtype=np.uint8).copy()
+    z = np.zeros(len(seqs), dtype=np.int64)
+    return ReadSet(seq, offs, z, z.astype(np.int8), z.astype(np.int8))

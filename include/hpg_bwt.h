@@ -1,0 +1,157 @@
+/*
+ * hpg_bwt.h -- drop-in C ABI of the GB300 FM-index read-mapping path.
+ *
+ * Replaces the FM-index mapping entry points of opencb/hpg-libs
+ * (c/src/aligners/bwt/bwt.h).  Host code stays C: link libhpgbwt.so in place
+ * of the bwt objects of libhpg.a.  The index lives in GPU memory; every
+ * search runs as sm_103a CUDA kernels and there is no CPU fallback (without a
+ * CUDA device, opening an index fails).
+ *
+ * The record types (bwt_optarg_t, bwt_index_t's leading fields, exome,
+ * bwt_config_t) keep the reference's field layout so existing callers that
+ * read them keep working.  bwt_index_t appends private fields after the
+ * reference's ones.
+ */
+#ifndef HPG_BWT_H
+#define HPG_BWT_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "hpg_bwt_records.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ types ---- */
+
+/* c/src/aligners/bwt/search/io.h:22-29 (chromosome table of the index). */
+#ifndef _SEARCH_IO_
+#define IDMAX 500
+typedef struct {
+  int max_chromosomes;
+  char *chromosome; /* names, IDMAX bytes each */
+  uintmax_t *start;
+  uintmax_t *end;
+  uintmax_t *offset; /* size + 1 entries */
+  uintmax_t size;
+} exome;
+#endif
+
+/* c/src/aligners/bwt/bwt_commons.h:20-32 */
+#ifndef BWT_COMMONS_H
+typedef struct {
+  uint8_t *table;
+  char *nucleotides;
+  char *reverse;
+  uint8_t nA;
+  uint8_t AA, CC, GG, TT;
+  bool inverse_sa;
+  bool duplicate_strand;
+} bwt_config_t;
+#endif
+
+/* c/src/aligners/bwt/bwt.h:256-261 */
+typedef struct bwt_optarg {
+  size_t num_errors;
+  size_t num_threads;
+  int filter_read_mappings;
+  int filter_seed_mappings;
+} bwt_optarg_t;
+
+/* c/src/aligners/bwt/bwt.h:273-281.  The four bwt_index pointers are opaque
+ * here (the reference's host tables are replaced by the GPU index). */
+typedef struct hpg_bwt_view hpg_bwt_view_t;
+typedef struct {
+  exome *karyotype;
+  bwt_config_t bwt_config;
+  hpg_bwt_view_t *backward;
+  hpg_bwt_view_t *forward;
+  hpg_bwt_view_t *backward_rev;
+  hpg_bwt_view_t *forward_rev;
+  char *dirname;
+  void *gpu_; /* private: GPU context */
+} bwt_index_t;
+
+/* ---------------------------------------------------- index + options -- */
+
+/* bwt.h:283 (bwt.c:682-713).  Loads <dirname> (reference on-disk format) and
+ * uploads it to the current CUDA device.  Like the reference, an unreadable
+ * index ends the process with EXIT_FAILURE; bwt_index_open reports instead. */
+bwt_index_t *bwt_index_new(const char *dirname, bool inverse_sa);
+
+/* bwt.h:285 (bwt.c:717-740) */
+void bwt_index_free(bwt_index_t *index);
+
+/* Non-exiting form of bwt_index_new: NULL and a message in errbuf on error.
+ * device < 0 selects the current CUDA device.  No reference counterpart. */
+bwt_index_t *bwt_index_open(const char *dirname, bool inverse_sa, int device, char *errbuf, size_t errlen);
+
+/* bwt.h:263-268 (bwt.c:435-447) */
+bwt_optarg_t *bwt_optarg_new(const size_t num_errors, const size_t num_threads, const int filter_read_mappings,
+                             const int filter_seed_mappings);
+/* bwt.h:268 (bwt.c:449-453) */
+void bwt_optarg_free(bwt_optarg_t *optarg);
+
+/* bwt.h:287-289 (bwt.c:744-819): writes the reference on-disk index format.
+ * Ends the process on error, like the reference. */
+void bwt_generate_index_files(char *ref_file, char *output_dir, unsigned int s_ratio, bool duplicate_strand,
+                              char *bases);
+
+/* Status-returning builder (0 ok, -1 with errbuf).  No reference counterpart. */
+int hpg_bwt_build_index(const char *ref_file, const char *output_dir, unsigned int s_ratio, int duplicate_strand,
+                        const char *bases, char *errbuf, size_t errlen);
+
+/* ------------------------------------------------ GPU batch search ---- */
+
+/* Pipeline forms of the batch search. */
+#define HPG_BWT_FORM_PLAIN   0 /* one thread per read and strand, one launch per stage */
+#define HPG_BWT_FORM_BATCHED 1 /* persistent work-queue kernel launched from a CUDA graph */
+
+/* Batched GPU form of the reference's search layer: for every read, mode
+ * HPG_BWT_MODE_SEARCH1 runs the four vector searches and
+ * BWSearch1VectorHelper per strand exactly as bwt.c:1940-2002 (declared at
+ * search/search.h:202-205), keeping at most max_results hits per strand
+ * (results_list capacity), then locates every row of every hit with the
+ * sampled suffix array (get_SA, search/runtime.h:87) and the karyotype
+ * (bwt.c:2158-2166).  Mode HPG_BWT_MODE_EXACT runs BWExactSearchBackward on
+ * both strands (search/search.h:9-36).
+ *
+ * Reads: seqs[offsets[i] .. offsets[i+1]) in ASCII, n_reads + 1 offsets.
+ * Reads shorter than 3 bases, or with characters outside the index alphabet
+ * (undefined in the reference), get no hits.
+ * Output: host arrays malloc'ed by the library; release with
+ * bwt_gpu_result_free.  Returns 0, or -1 (see bwt_gpu_last_error). */
+int bwt_gpu_search_batch(bwt_index_t *index, int mode, int form, const char *seqs, const uint64_t *offsets,
+                         size_t n_reads, uint32_t max_results, hpg_result_set_t *out);
+void bwt_gpu_result_free(hpg_result_set_t *out);
+
+/* Device-resident form for callers that keep reads in GPU memory: d_seqs and
+ * d_offsets are device pointers (offsets relative to d_seqs).  Results stay
+ * on the device until the next call; sizes are returned in out (its pointer
+ * fields are device pointers).  Copy them with bwt_gpu_copy_result. */
+int bwt_gpu_search_device(bwt_index_t *index, int mode, int form, const uint8_t *d_seqs, const uint64_t *d_offsets,
+                          size_t n_reads, uint64_t total_bases, uint32_t max_len, uint32_t max_results,
+                          hpg_result_set_t *out);
+int bwt_gpu_copy_result(bwt_index_t *index, const hpg_result_set_t *dev, hpg_hit_t *hits, hpg_loc_t *locs,
+                        uint32_t *rs_count, uint8_t *rs_truncated);
+
+/* The CUDA stream (cudaStream_t) every kernel of this index runs on. */
+void *bwt_gpu_stream(bwt_index_t *index);
+/* Device times (ms) of the last call: encode, search, finalize, locate. */
+void bwt_gpu_stage_ms(bwt_index_t *index, float *out, int n);
+/* Count touched 32-byte index sectors during searches (for roofline figures). */
+void bwt_gpu_set_census(bwt_index_t *index, int on);
+unsigned long long bwt_gpu_census(bwt_index_t *index);
+/* Reads per internal chunk of the plain form (0 = automatic). */
+void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
+/* Message of the last failed call on this thread. */
+const char *bwt_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HPG_BWT_H */

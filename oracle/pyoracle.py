@@ -1,0 +1,98 @@
+"""TEST INFRASTRUCTURE ONLY: Python loaders for the CPU oracles.
+
+- ``PortOracle``: oracle/liboracle.so, the C restatement in oracle/fm_oracle.c.
+- ``RefOracle``: oracle/_ref/libhpgref.so, the reference's own sources driven by
+  oracle/ref/ref_harness.c (exists only where the reference tree was present
+  at build time).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT / "hpg-libs_gb300"))
+from hpgbwt.lib import ResultSetC, Result, result_from_c  # noqa: E402
+
+PORT_LIB = ROOT / "oracle" / "liboracle.so"
+REF_LIB = ROOT / "oracle" / "_ref" / "libhpgref.so"
+
+
+class PortOracle:
+    def __init__(self, index_dir: str):
+        if not PORT_LIB.exists():
+            raise RuntimeError(f"{PORT_LIB} missing; run hpg-libs_gb300/hpgbwt/build.py")
+        self.lib = ctypes.CDLL(str(PORT_LIB))
+        self.lib.fmo_index_load.restype = ctypes.c_void_p
+        self.lib.fmo_index_load.argtypes = [ctypes.c_char_p]
+        self.lib.fmo_index_free.argtypes = [ctypes.c_void_p]
+        self.lib.fmo_search.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ResultSetC)]
+        self.lib.fmo_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
+        self.lib.fmo_max_threads.restype = ctypes.c_int
+        self.h = self.lib.fmo_index_load(index_dir.encode())
+        if not self.h:
+            raise RuntimeError(f"oracle cannot load index {index_dir}")
+
+    def max_threads(self) -> int:
+        return int(self.lib.fmo_max_threads())
+
+    def search(self, reads, mode: int = 1, max_results: int = 1 << 16, threads: int = 1) -> Result:
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        rs = ResultSetC()
+        self.lib.fmo_search(self.h, mode, seq.ctypes.data, offs.ctypes.data, n, max_results, threads,
+                            ctypes.byref(rs))
+        try:
+            return result_from_c(rs, n)
+        finally:
+            self.lib.fmo_result_free(ctypes.byref(rs))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.fmo_index_free(self.h)
+            self.h = None
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+class RefOracle:
+    def __init__(self, index_dir: str | None = None):
+        self.lib = ctypes.CDLL(str(REF_LIB))
+        self.lib.ref_index_load.restype = ctypes.c_void_p
+        self.lib.ref_index_load.argtypes = [ctypes.c_char_p]
+        self.lib.ref_index_free.argtypes = [ctypes.c_void_p]
+        self.lib.ref_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint]
+        self.lib.ref_search.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_uint32, ctypes.POINTER(ResultSetC)]
+        self.lib.ref_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
+        self.h = self.lib.ref_index_load(index_dir.encode()) if index_dir else None
+
+    def build_index(self, fasta: str, outdir: str, ratio: int = 16) -> None:
+        Path(outdir).mkdir(parents=True, exist_ok=True)
+        self.lib.ref_build_index(fasta.encode(), outdir.encode(), ratio)
+
+    def search(self, reads, mode: int = 1, max_results: int = 1 << 16) -> Result:
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        rs = ResultSetC()
+        self.lib.ref_search(self.h, mode, seq.ctypes.data, offs.ctypes.data, n, max_results, ctypes.byref(rs))
+        try:
+            return result_from_c(rs, n)
+        finally:
+            self.lib.ref_result_free(ctypes.byref(rs))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.ref_index_free(self.h)
+            self.h = None

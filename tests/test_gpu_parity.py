@@ -1,0 +1,74 @@
+"""GPU parity: the CUDA pipeline (through the C ABI) against the CPU oracle, bit-exact."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from hpgbwt import lib, synth
+from oracle.pyoracle import PortOracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _assert_same(gpu: lib.Result, ref: lib.Result):
+    assert np.array_equal(gpu.rs_count, ref.rs_count), "per-strand hit counts differ"
+    assert np.array_equal(gpu.rs_truncated, ref.rs_truncated), "truncation flags differ"
+    assert len(gpu.hits) == len(ref.hits)
+    assert np.array_equal(gpu.hits, ref.hits), "hits differ"
+    assert len(gpu.locs) == len(ref.locs)
+    assert np.array_equal(gpu.locs, ref.locs), "located rows differ"
+
+
+@pytest.mark.parametrize("mode", [lib.MODE_EXACT, lib.MODE_SEARCH1])
+@pytest.mark.parametrize("kind,n,chroms,edits,length", [
+    ("iid", 200_000, 1, "none", 100),
+    ("repeats", 300_000, 3, "per_base_capped", 100),
+    ("repeats", 300_000, 3, "mix_30_50_20", (36, 250)),
+    ("human_like", 200_000, 5, "mix_30_50_20", (20, 150)),
+])
+def test_plain_matches_oracle(case_factory, mode, kind, n, chroms, edits, length):
+    c = case_factory(kind, n, 3, chroms)
+    reads = synth.reads(c.genome, 4000, 17, length=length, edits=edits)
+    ora = PortOracle(c.index)
+    with lib.GpuIndex(c.index) as g:
+        got = g.search(reads, mode=mode, form=lib.FORM_PLAIN, max_results=1 << 16)
+    want = ora.search(reads, mode=mode, max_results=1 << 16, threads=8)
+    _assert_same(got, want)
+
+
+@pytest.mark.parametrize("max_results", [0, 1, 2, 3, 9, 17])
+def test_truncation_matches_oracle(case_factory, max_results):
+    c = case_factory("human_like", 100_000, 5, 2)
+    reads = synth.reads(c.genome, 3000, 23, length=(20, 120), edits="mix_30_50_20")
+    ora = PortOracle(c.index)
+    with lib.GpuIndex(c.index) as g:
+        got = g.search(reads, mode=lib.MODE_SEARCH1, max_results=max_results)
+    want = ora.search(reads, mode=lib.MODE_SEARCH1, max_results=max_results, threads=8)
+    assert want.rs_truncated.any() or max_results > 3
+    _assert_same(got, want)
+
+
+def test_edge_reads(case_factory):
+    c = case_factory("iid", 50_000, 9, 1)
+    g0 = c.genome
+    A = np.frombuffer(b"ACGT", dtype=np.uint8)
+    seqs = [b"", b"A", b"AC", b"ACG", A[g0[100:105]].tobytes(), b"ACGTN" * 10, b"acgt" * 20,
+            A[g0[1000:1100]].tobytes(), A[g0[-80:]].tobytes(), A[g0[:64]].tobytes(),
+            A[g0[5000:6000]].tobytes(), b"T" * 300]
+    reads = synth.from_strings(seqs)
+    ora = PortOracle(c.index)
+    with lib.GpuIndex(c.index) as g:
+        for mode in (lib.MODE_EXACT, lib.MODE_SEARCH1):
+            got = g.search(reads, mode=mode)
+            want = ora.search(reads, mode=mode, threads=1)
+            _assert_same(got, want)
+
+
+def test_chunked_equals_single_pass(case_factory):
+    c = case_factory("repeats", 300_000, 3, 3)
+    reads = synth.reads(c.genome, 5000, 29, length=(36, 250), edits="mix_30_50_20")
+    with lib.GpuIndex(c.index) as g:
+        whole = g.search(reads)
+        g.set_chunk(777)
+        parts = g.search(reads)
+    assert whole.equal(parts)
