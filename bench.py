@@ -1,0 +1,419 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 FM-index read-mapping path.
+
+Metric: reads/s of 100 bp reads mapped with at most one error (BWSearch1:
+four vector searches + the 1-error helper on both strands, every hit located
+with the sampled suffix array and the karyotype), bit-exact to the reference.
+
+Workload (default ``c2``): a seeded 100 Mbp synthetic genome (GC 41 %, plus
+5 % of its length as copies of 300 bp elements at 85-95 % identity) and 2 M
+reads of 100 bp per GPU with per-base 0.5 % substitutions, 0.02 % insertions
+and 0.02 % deletions, capped at one edit per read, from either strand.  The
+index is built by this repository's builder at the reference's default
+ratios (O table every 64 rows, SA sample every 16 rows).  No public dataset
+is used.
+
+One step = one mapping call over the whole read batch.  ``value`` is measured
+with the reads already resident in HBM (CUDA events on the library's stream,
+L2 flushed with a 256 MiB write before every step); ``e2e`` goes through the
+C ABI call ``bwt_gpu_search_batch`` with pinned host reads and host result
+arrays, host<->device copies inside the timed region.
+
+``--impl reference`` times the reference algorithm on the host cores (the C
+restatement in oracle/, OpenMP over all cores) on a bounded sample of the
+same workload.
+
+Multi-GPU: reads are independent, so each rank maps its own read batch
+against its own copy of the index (weak scaling, no collective on the data
+path); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "hpg-libs_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "reads/s, 100bp ≤1 err bit-exact; batched+served vs plain, 1 GB300; p50/p99 ms"
+
+WORKLOADS = {
+    "c2": dict(desc="100 Mbp genome (GC 41%, 5% 300 bp repeat copies at 85-95% identity); 2M x 100 bp reads "
+                    "per GPU, 0.5%/0.02%/0.02% subst/ins/del per base capped at one edit; BWSearch1 + locate",
+               genome="repeats", genome_bp=100_000_000, reads=2_000_000, read_len=100, edits="per_base_capped"),
+    "c1": dict(desc="4 Mbp i.i.d. genome; 200k x 100 bp error-free reads; BWSearch1 + locate",
+               genome="iid", genome_bp=4_000_000, reads=200_000, read_len=100, edits="none"),
+    "small": dict(desc="2 Mbp genome (repeats); 100k x 100 bp reads; BWSearch1 + locate (smoke-size)",
+                  genome="repeats", genome_bp=2_000_000, reads=100_000, read_len=100, edits="per_base_capped"),
+}
+
+MAX_RESULTS = 1024
+SA_RATIO = 16
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class Dist:
+    def __init__(self, gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{self.local}")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{self.local}")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def prepare(wl: dict, rank: int, dist):
+    """Genome + index (shared by ranks, cached per call) and this rank's reads."""
+    from hpgbwt import lib, synth
+    key = f"{wl['genome']}_{wl['genome_bp']}_r{SA_RATIO}"
+    base = Path(os.environ.get("HPG_BENCH_CACHE", tempfile.gettempdir())) / "hpgbwt_bench" / key
+    t0 = time.time()
+    genome = synth.genome(wl["genome"], wl["genome_bp"], 1)
+    if rank == 0 and not (base / "index" / "Si.vec").exists():
+        base.mkdir(parents=True, exist_ok=True)
+        synth.write_fasta(str(base / "genome.fa"), genome)
+        lib.build_index(str(base / "genome.fa"), str(base / "index"), SA_RATIO)
+    dist.barrier()
+    reads = synth.reads_fast(genome, wl["reads"], 2 + rank, wl["read_len"], wl["edits"])
+    log(f"[bench] rank {rank}: genome+index+reads ready in {time.time() - t0:.1f}s")
+    return str(base / "index"), reads
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.rows: list[list[str]] = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm = []
+        mx = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for nm, v in zip(names, r[4:8]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_read() -> float | None:
+    """DRAM bytes per read of the search kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "plain_search1_kernel_c2.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_read:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(index_dir: str, reads, seconds: float = 12.0) -> dict:
+    from oracle.pyoracle import PortOracle
+    ora = PortOracle(index_dir)
+    threads = os.cpu_count() or 1
+    n_total = len(reads)
+    probe = reads.subset(np.arange(min(2000, n_total)))
+    t = time.perf_counter()
+    ora.search(probe, mode=1, max_results=MAX_RESULTS, threads=threads)
+    rate = len(probe) / max(time.perf_counter() - t, 1e-6)
+    n = int(min(n_total, max(len(probe), rate * seconds)))
+    sample = reads.subset(np.arange(n))
+    t = time.perf_counter()
+    ora.search(sample, mode=1, max_results=MAX_RESULTS, threads=threads)
+    dt = time.perf_counter() - t
+    ora.close()
+    return {"value": n / dt, "unit": "reads/s", "cores": threads, "kind": "port",
+            "sample": f"first {n} reads of the rank-0 read batch, same index, OpenMP over {threads} host threads "
+                      f"({dt:.1f}s)"}
+
+
+def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
+    import torch
+    from hpgbwt import lib
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    index_dir, reads = prepare(wl, dist.rank, dist)
+    gi = lib.GpuIndex(index_dir, device=dev)
+    n = len(reads)
+    total = int(reads.offsets[-1])
+    max_len = int(np.diff(reads.offsets).max())
+    d_seq = torch.from_numpy(reads.seq).to(f"cuda:{dev}")
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).to(f"cuda:{dev}")
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(gi.stream(), device=f"cuda:{dev}")
+    form = lib.FORM_PLAIN
+
+    def step():
+        return gi.search_device(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, lib.MODE_SEARCH1, form,
+                                MAX_RESULTS)
+
+    # census run (untimed): touched index sectors per stage
+    gi.set_census(True)
+    rs = step()
+    sectors = gi.census()
+    census_stage = gi.stage_ms()
+    gi.set_census(False)
+    n_hits, n_locs = int(rs.n_hits), int(rs.n_locs)
+
+    for _ in range(args.warmup):
+        step()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage_sum = [0.0, 0.0, 0.0, 0.0]
+    dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.launch_count()
+    with ClockSampler(dev) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+            ev[i][1].synchronize()
+            st = gi.stage_ms()
+            stage_sum = [a + b for a, b in zip(stage_sum, st)]
+    launches = lib.launch_count() - launches0
+    torch.cuda.synchronize()
+    dist.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms_max = dist.max(ms)
+    total_reads = dist.sum(float(n))
+    value = total_reads * args.steps / (ms_max / 1e3)
+
+    # e2e: host buffers through the C ABI (pinned reads in, host records out)
+    pin_seq = torch.from_numpy(reads.seq).pin_memory()
+    pin_off = torch.from_numpy(reads.offsets.view(np.int64)).pin_memory()
+    rsc = lib.ResultSetC()
+    e2e_t = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        rc = gi.lib.bwt_gpu_search_batch(gi.handle, lib.MODE_SEARCH1, form, pin_seq.data_ptr(), pin_off.data_ptr(),
+                                         n, MAX_RESULTS, lib.ctypes.byref(rsc))
+        dt = time.perf_counter() - t
+        if rc != 0:
+            raise RuntimeError(gi.lib.bwt_gpu_last_error().decode())
+        if i >= args.warmup:
+            e2e_t.append(dt)
+        e_hits, e_locs = int(rsc.n_hits), int(rsc.n_locs)
+        gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rsc))
+    e2e_s = dist.max(sum(e2e_t))
+    e2e_value = total_reads * args.steps / e2e_s
+    h2d = total + 8 * (n + 1)
+    d2h = 32 * e_hits + 32 * e_locs + 2 * n * 4 + 2 * n
+
+    # roofline of the dominant kernel (the search kernel)
+    per_step = [x / args.steps for x in stage_sum]
+    search_ms = per_step[1]
+    search_sectors = sectors
+    peak, peak_kind = measured_peaks()
+    algo_bytes = 32.0 * search_sectors + total + 16.0 * n_hits
+    achieved = algo_bytes / (search_ms * 1e-3) / 1e9
+    tpr = profiled_traffic_per_read()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": (tpr * n if tpr else None),
+                "kernel": "plain_search1_kernel", "peak_kind": peak_kind,
+                "algorithmic_bytes_per_read": round(algo_bytes / n, 1)}
+    gather = None
+    if dist.rank == 0:
+        ib = gi.index_bytes()
+        best = 0.0
+        for blocks in (152 * 8, 152 * 16):
+            best = max(best, lib.gather_ceiling(dev, ib, blocks, 1024))
+        rate = search_sectors / (search_ms * 1e-3)
+        gather = {"sectors_per_s": round(rate, 1), "ceiling_sectors_per_s": round(best, 1),
+                  "frac": round(rate / best, 4), "buffer_bytes": ib,
+                  "sectors_per_read": round(search_sectors / n, 2)}
+    out = None
+    if dist.rank == 0:
+        base = cpu_baseline(index_dir, reads) if not args.no_cpu_baseline else None
+        out = {
+            "metric": METRIC, "value": round(value, 1), "unit": "reads/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded genome and reads; no public dataset)",
+            "config": {"workload": wl["desc"], "genome_bp": wl["genome_bp"], "reads_per_gpu": n,
+                       "read_len": wl["read_len"], "max_results": MAX_RESULTS, "sa_ratio": SA_RATIO,
+                       "o_ratio": 64, "form": "plain", "l2": "flushed (256 MiB write) before every step; "
+                       "reads 200 MB > L2", "parallelism": f"replica x{dist.world} (reads sharded)"},
+            "e2e": {"value": round(e2e_value, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "bwt_gpu_search_batch"},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "gather_roofline": gather,
+            "cpu_baseline": base,
+            "clocks": clk.summary(),
+            "stages_ms": {"encode": round(per_step[0], 3), "search": round(per_step[1], 3),
+                          "finalize": round(per_step[2], 3), "locate": round(per_step[3], 3)},
+            "hits_per_step": n_hits, "located_rows_per_step": n_locs,
+            "forms": {"plain": {"reads_per_s": round(value, 1)}},
+        }
+    gi.close()
+    return out
+
+
+def run_reference(args, wl: dict, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    index_dir, reads = prepare(wl, 0, dist)
+    from oracle.pyoracle import PortOracle
+    ora = PortOracle(index_dir)
+    threads = os.cpu_count() or 1
+    probe = reads.subset(np.arange(min(2000, len(reads))))
+    t = time.perf_counter()
+    ora.search(probe, mode=1, max_results=MAX_RESULTS, threads=threads)
+    rate = len(probe) / max(time.perf_counter() - t, 1e-6)
+    per_step = int(min(len(reads), max(len(probe), rate * 20.0 / max(1, args.steps))))
+    sample = reads.subset(np.arange(per_step))
+    for _ in range(min(args.warmup, 1)):
+        ora.search(probe, mode=1, max_results=MAX_RESULTS, threads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        ora.search(sample, mode=1, max_results=MAX_RESULTS, threads=threads)
+    dt = time.perf_counter() - t
+    value = per_step * args.steps / dt
+    desc = (f"{per_step} reads per step (bounded sample of the {len(reads)}-read batch), OpenMP over {threads} "
+            f"host threads")
+    return {"metric": METRIC, "value": round(value, 1), "unit": "reads/s", "impl": "reference",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt * 1e3 / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded genome and reads; no public dataset)",
+            "config": {"workload": wl["desc"], "genome_bp": wl["genome_bp"], "reads_per_gpu": len(reads),
+                       "read_len": wl["read_len"], "max_results": MAX_RESULTS, "sa_ratio": SA_RATIO},
+            "cpu_baseline": {"value": round(value, 1), "unit": "reads/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": round(value, 1), "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        if rank != 0:
+            return 0
+        from hpgbwt import build as hbuild
+        hbuild.build_lib()
+        hbuild.build_oracle()
+        out = run_reference(args, wl, _Rank0())
+    else:
+        from hpgbwt import build as hbuild
+        hbuild.build_lib()
+        hbuild.build_oracle()
+        dist = Dist(args.gpus)
+        try:
+            out = run_gb300(args, wl, dist)
+        finally:
+            dist.close()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+class _Rank0:
+    """Rank 0 of a reference-arm run: no process group, nothing to wait for."""
+    rank = 0
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+
+    def barrier(self):
+        pass
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -8,10 +8,16 @@
 #include <string>
 
 #include "engine.hpp"
+#include "kernels.cuh"
 #include "hpg_bwt.h"
 #include "index_format.hpp"
 
 using namespace hpgbwt;
+
+namespace hpgbwt {
+int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s,
+                   std::string* err);
+}
 
 namespace {
 
@@ -223,6 +229,20 @@ void bwt_gpu_set_census(bwt_index_t* index, int on) {
 unsigned long long bwt_gpu_census(bwt_index_t* index) {
   Engine* e = engine_of(index);
   return e ? engine_census(e) : 0ull;
+}
+
+unsigned long long bwt_gpu_launch_count(void) { return launch_count(); }
+
+int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s) {
+  std::string err;
+  if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err) != 0)
+    return fail(err.empty() ? "bwt_gpu_gather_ceiling: null argument" : err);
+  return 0;
+}
+
+size_t bwt_gpu_index_bytes(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_index_bytes(e) : 0;
 }
 
 void bwt_gpu_set_chunk(bwt_index_t* index, size_t reads) {

@@ -289,6 +289,9 @@ int engine_device(Engine* e) { return e->device; }
 void engine_set_census(Engine* e, int on) { e->census_on = on != 0; }
 unsigned long long engine_census(Engine* e) { return e->census_val; }
 void engine_set_chunk(Engine* e, size_t reads) { e->chunk = reads; }
+size_t engine_index_bytes(Engine* e) {
+  return ((size_t)e->X.dir[0].nblk + e->X.dir[1].nblk) * sizeof(OccBlock);
+}
 
 void engine_stage_ms(Engine* e, float* out, int n) {
   for (int i = 0; i < n && i < kStageCount; ++i) out[i] = e->stage_ms[i];

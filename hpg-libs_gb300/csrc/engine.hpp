@@ -56,5 +56,6 @@ void engine_stage_ms(Engine* e, float* out, int n);
 void engine_set_census(Engine* e, int on);
 unsigned long long engine_census(Engine* e);
 void engine_set_chunk(Engine* e, size_t reads_per_chunk);
+size_t engine_index_bytes(Engine* e);
 
 }  // namespace hpgbwt

@@ -3,10 +3,17 @@
 // device-wide scan, ordered hit gather and the locate pass.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "kernels.cuh"
 #include "search_core.cuh"
 
 namespace hpgbwt {
+
+std::atomic<unsigned long long> g_launches{0};
+
+unsigned long long launch_count() { return g_launches.load(); }
+void count_launches(unsigned n) { g_launches += n; }
 
 namespace {
 
@@ -319,6 +326,7 @@ __global__ void __launch_bounds__(kTpb)
 void launch_encode(const uint8_t* ascii, const uint64_t* offs, uint32_t n_reads, const uint8_t* d_table,
                    uint8_t* codes, uint8_t* ok, cudaStream_t s) {
   if (!n_reads) return;
+  count_launches(1);
   encode_kernel<<<grid_for(n_reads, 256), 256, 0, s>>>(ascii, offs, n_reads, d_table, codes, ok);
 }
 
@@ -326,6 +334,7 @@ void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs,
                   uint32_t nr, uint4* slots, uint32_t* rs_count, uint8_t* rs_trunc,
                   unsigned long long* census, cudaStream_t s) {
   if (!nr) return;
+  count_launches(1);
   exact_kernel<<<grid_for(2ull * nr, kTpb), kTpb, 0, s>>>(X, codes, offs, ok, r0, nr, slots, rs_count, rs_trunc,
                                                            census);
 }
@@ -335,6 +344,7 @@ void launch_plain_search1(const DevIndex& X, const uint8_t* codes, const uint64_
                           uint4* slots, OvfEntry* ovf, uint32_t ovf_cap, uint32_t* ovf_count,
                           uint32_t* rs_count, uint8_t* rs_trunc, unsigned long long* census, cudaStream_t s) {
   if (!nr) return;
+  count_launches(1);
   plain_search1_kernel<<<grid_for(2ull * nr, kTpb), kTpb, 0, s>>>(X, codes, offs, ok, r0, nr, max_results, max_len,
                                                                    vecs, slots, ovf, ovf_cap, ovf_count, rs_count,
                                                                    rs_trunc, census);
@@ -348,8 +358,11 @@ void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cu
     return;
   }
   const unsigned nb = (unsigned)((n + kScanTile - 1) / kScanTile);
+  count_launches(1);
   scan_reduce_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part);
+  count_launches(1);
   scan_parts_kernel<<<1, 1024, 0, s>>>(part, nb);
+  count_launches(1);
   scan_apply_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part, out);
 }
 
@@ -357,13 +370,16 @@ void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t*
                         const uint32_t* rs_count, const uint64_t* off, uint32_t r0, uint32_t nr,
                         hpg_hit_t* out, cudaStream_t s) {
   if (!nr) return;
+  count_launches(1);
   gather_slots_kernel<<<grid_for(2ull * nr, 256), 256, 0, s>>>(slots, rs_count, off, r0, nr, out);
   if (ovf && ovf_cap)
+    count_launches(1);
     gather_ovf_kernel<<<grid_for(ovf_cap, 256), 256, 0, s>>>(ovf, ovf_count, ovf_cap, rs_count, off, r0, out);
 }
 
 void launch_hit_rows(const hpg_hit_t* hits, uint32_t n_hits, uint32_t* rows, cudaStream_t s) {
   if (!n_hits) return;
+  count_launches(1);
   hit_rows_kernel<<<grid_for(n_hits, 256), 256, 0, s>>>(hits, n_hits, rows);
 }
 
@@ -371,6 +387,7 @@ void launch_locate(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc
                    uint64_t n_locs, const uint64_t* read_offs, uint32_t hit_base, hpg_loc_t* out,
                    unsigned long long* census, cudaStream_t s) {
   if (!n_locs) return;
+  count_launches(1);
   locate_kernel<<<grid_for(n_locs, kTpb), kTpb, 0, s>>>(X, hits, loc_off, n_hits, n_locs, read_offs, hit_base, out,
                                                         census);
 }

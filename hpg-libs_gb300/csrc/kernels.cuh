@@ -19,6 +19,10 @@ struct OvfEntry {
 
 constexpr uint32_t kSlotCap = 8;  // hits kept in place per (read, strand); the rest overflow
 
+// Kernels launched by this library since load (the benchmark's launch count).
+unsigned long long launch_count();
+void count_launches(unsigned n);
+
 // ASCII -> 2-bit codes (0xFF outside the alphabet) and a per-read validity flag.
 void launch_encode(const uint8_t* ascii, const uint64_t* offs, uint32_t n_reads, const uint8_t* d_table,
                    uint8_t* codes, uint8_t* ok, cudaStream_t s);

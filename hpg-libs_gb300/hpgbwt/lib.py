@@ -87,10 +87,26 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_census.argtypes = [vp]
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
+    lib.bwt_gpu_launch_count.restype = ctypes.c_ulonglong
+    lib.bwt_gpu_index_bytes.restype = sz
+    lib.bwt_gpu_index_bytes.argtypes = [vp]
+    lib.bwt_gpu_gather_ceiling.argtypes = [ctypes.c_int, sz, u32, u32, ctypes.POINTER(ctypes.c_double)]
     lib.hpg_bwt_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
                                         ctypes.c_char_p, ctypes.c_char_p, sz]
     _lib = lib
     return lib
+
+
+def launch_count() -> int:
+    return int(load().bwt_gpu_launch_count())
+
+
+def gather_ceiling(device: int, nbytes: int, blocks: int, steps: int) -> float:
+    lib = load()
+    v = ctypes.c_double()
+    if lib.bwt_gpu_gather_ceiling(device, nbytes, blocks, steps, ctypes.byref(v)) != 0:
+        raise RuntimeError(lib.bwt_gpu_last_error().decode())
+    return v.value
 
 
 def build_index(fasta: str, outdir: str, ratio: int = 16, bases: str = "ACGT") -> None:
@@ -162,6 +178,9 @@ class GpuIndex:
 
     def census(self) -> int:
         return int(self.lib.bwt_gpu_census(self.handle))
+
+    def index_bytes(self) -> int:
+        return int(self.lib.bwt_gpu_index_bytes(self.handle))
 
     def set_chunk(self, reads: int) -> None:
         self.lib.bwt_gpu_set_chunk(self.handle, reads)

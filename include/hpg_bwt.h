@@ -147,6 +147,13 @@ void bwt_gpu_set_census(bwt_index_t *index, int on);
 unsigned long long bwt_gpu_census(bwt_index_t *index);
 /* Reads per internal chunk of the plain form (0 = automatic). */
 void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
+/* Number of kernels this library has launched since it was loaded. */
+unsigned long long bwt_gpu_launch_count(void);
+/* Device bytes of the index's occurrence blocks (both directions). */
+size_t bwt_gpu_index_bytes(bwt_index_t *index);
+/* Measured ceiling of dependent random 32-byte sector reads over a buffer of
+ * `bytes` on `device` (blocks x 128 threads, `steps` hops each), in sectors/s. */
+int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double *sectors_per_s);
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
