@@ -52,6 +52,9 @@ WORKLOADS = {
     "c2": dict(desc="100 Mbp genome (GC 41%, 5% 300 bp repeat copies at 85-95% identity); 2M x 100 bp reads "
                     "per GPU, 0.5%/0.02%/0.02% subst/ins/del per base capped at one edit; BWSearch1 + locate",
                genome="repeats", genome_bp=100_000_000, reads=2_000_000, read_len=100, edits="per_base_capped"),
+    "c2_profile": dict(desc="profiling size of c2: the same 100 Mbp genome and index, 200k x 100 bp reads",
+                       genome="repeats", genome_bp=100_000_000, reads=200_000, read_len=100,
+                       edits="per_base_capped"),
     "c1": dict(desc="4 Mbp i.i.d. genome; 200k x 100 bp error-free reads; BWSearch1 + locate",
                genome="iid", genome_bp=4_000_000, reads=200_000, read_len=100, edits="none"),
     "small": dict(desc="2 Mbp genome (repeats); 100k x 100 bp reads; BWSearch1 + locate (smoke-size)",

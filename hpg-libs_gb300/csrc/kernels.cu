@@ -372,9 +372,10 @@ void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t*
   if (!nr) return;
   count_launches(1);
   gather_slots_kernel<<<grid_for(2ull * nr, 256), 256, 0, s>>>(slots, rs_count, off, r0, nr, out);
-  if (ovf && ovf_cap)
+  if (ovf && ovf_cap) {
     count_launches(1);
     gather_ovf_kernel<<<grid_for(ovf_cap, 256), 256, 0, s>>>(ovf, ovf_count, ovf_cap, rs_count, off, r0, out);
+  }
 }
 
 void launch_hit_rows(const hpg_hit_t* hits, uint32_t n_hits, uint32_t* rows, cudaStream_t s) {
