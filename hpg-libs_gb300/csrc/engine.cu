@@ -285,6 +285,12 @@ void engine_destroy(Engine* e) {
 }
 
 void* engine_stream(Engine* e) { return (void*)e->stream; }
+
+// Accessors for the allocation-free entry point (noalloc.cu).
+DevIndex engine_dev_index(void* e) { return static_cast<Engine*>(e)->X; }
+const uint8_t* engine_code_table(void* e) { return static_cast<Engine*>(e)->d_table; }
+int engine_device_of(void* e) { return static_cast<Engine*>(e)->device; }
+void* engine_stream_of(void* e) { return (void*)static_cast<Engine*>(e)->stream; }
 int engine_device(Engine* e) { return e->device; }
 void engine_set_census(Engine* e, int on) { e->census_on = on != 0; }
 unsigned long long engine_census(Engine* e) { return e->census_val; }

@@ -157,6 +157,45 @@ int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t s
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
+/* ------------------------------------------- allocation-free search ---- */
+
+/* No counterpart in the reference: an extra entry point of this library.
+ *
+ * BWSearch1 (both strands, as bwt_gpu_search_batch in mode
+ * HPG_BWT_MODE_SEARCH1, without the locate step) for callers that must not
+ * allocate device memory: processes whose HBM is owned by another allocator
+ * (a serving runtime that has reserved the whole device for its own pool and
+ * forbids side allocations), and latency-critical threads, where a
+ * cudaMalloc/cudaFree can stall on device-wide synchronisation.  This call
+ * allocates nothing: its scratch is one fixed 16 MiB array that every GPU
+ * loading the library holds until the process exits
+ * (bwt_gpu_noalloc_scratch_bytes()).
+ *
+ * All buffers are the caller's device memory: d_seqs/d_offsets as in
+ * bwt_gpu_search_device (max_len must cover the longest read; longer reads
+ * get no hits); d_hits holds 2 * n_reads * max_results records,
+ * hit i of (read r, strand s) at [(2*r + s) * max_results + i]; d_counts and
+ * d_truncated hold 2 * n_reads entries.  The kernel is launched on `stream`
+ * (the index's stream when NULL) and the call returns without waiting.
+ *
+ * Limit: n_reads * max(max_len, 3) may not exceed about 490 000 bases
+ * (2 * n_reads * max_len * 17 bytes of scratch plus alignment); larger
+ * batches are rejected with -1 and a message in
+ * bwt_gpu_noalloc_last_error().  The scratch is fully rewritten before it is
+ * read, so no call depends on what an earlier call left there, but every call
+ * on a device shares it: calls whose kernels overlap on the GPU race and must
+ * be serialised by the caller (one stream, or events).  The first call on a
+ * device looks up the scratch's device address (cudaGetSymbolAddress with
+ * that device current); make that first call before any stream capture.
+ * Returns 0 once the kernel is queued. */
+int bwt_gpu_search1_noalloc(bwt_index_t *index, const char *d_seqs, const uint64_t *d_offsets, size_t n_reads,
+                            uint32_t max_len, uint32_t max_results, hpg_hit_t *d_hits, uint32_t *d_counts,
+                            uint8_t *d_truncated, void *stream);
+/* Size of the fixed scratch array, in bytes. */
+size_t bwt_gpu_noalloc_scratch_bytes(void);
+/* Message of the last failed bwt_gpu_search1_noalloc call on this thread. */
+const char *bwt_gpu_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
