@@ -69,7 +69,7 @@ def load() -> ctypes.CDLL:
         return _lib
     if not LIB_PATH.exists():
         raise RuntimeError(f"{LIB_PATH} is missing: build it with hpg-libs_gb300/hpgbwt/build.py")
-    lib = ctypes.CDLL(str(LIB_PATH), mode=ctypes.RTLD_GLOBAL)
+    lib = ctypes.CDLL(str(LIB_PATH), mode=ctypes.RTLD_LOCAL)
     vp, sz, u32, u64 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64
     lib.bwt_index_open.restype = vp
     lib.bwt_index_open.argtypes = [ctypes.c_char_p, ctypes.c_bool, ctypes.c_int, ctypes.c_char_p, sz]

@@ -1,0 +1,106 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own code.
+
+Run in a container that has the read-only reference tree (the fixtures are
+committed; the GPU machine and CI only read them):
+
+    python hpg-libs_gb300/hpgbwt/build.py          # builds oracle/_ref/libhpgref.so
+    python tests/golden/make_golden.py
+
+For every case it stores the genome (2-bit codes + chromosome lengths), the
+SHA-256 of every index file written by the reference builder
+(bwt_generate_index_files, bwt.c:744-819, at SA ratio 16), the reads, and the
+reference's search outputs (oracle/ref/ref_harness.c: BWExactSearchBackward
+on both strands, and the four vector searches + BWSearch1VectorHelper per
+strand with the bwt.c:2158-2166 locate) for several result-list capacities.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "hpg-libs_gb300"))
+sys.path.insert(0, str(ROOT))
+
+from hpgbwt import synth  # noqa: E402
+from oracle.pyoracle import RefOracle, ref_available  # noqa: E402
+
+CASES = [
+    # name, genome kind, length, seed, chromosome lengths, reads: (n, seed, length, edits), max_results list
+    ("iid_1chr", "iid", 30_000, 101, None, (1200, 5, 100, "mix_30_50_20"), [1 << 16, 4]),
+    ("repeats_3chr", "repeats", 60_000, 102, [25_000, 20_000, 15_000], (1500, 6, (20, 150), "mix_30_50_20"),
+     [1 << 16, 3]),
+    ("lowcomplexity_2chr", "human_like", 16_000, 103, [10_000, 6_000], (250, 7, (3, 120), "mix_30_50_20"),
+     [1 << 16, 0, 2, 17]),
+]
+
+A = np.frombuffer(b"ACGT", dtype=np.uint8)
+
+
+def edge_reads(g: np.ndarray, chrom_lengths: list[int]) -> list[bytes]:
+    """Reads the reference's edge behaviour hinges on."""
+    out = [b"", b"A", b"AC", b"ACG", b"ACGT", A[g[10:15]].tobytes(), b"ACGTN" * 8, A[g[100:160]].tobytes().lower(),
+           A[g[:50]].tobytes(), A[g[-50:]].tobytes(), b"T" * 200, b"GA" * 60]
+    pos = 0
+    for cl in chrom_lengths[:-1]:  # reads spanning chromosome junctions (located but invalid)
+        pos += cl
+        out.append(A[g[pos - 40:pos + 40]].tobytes())
+    return out
+
+
+def sha(path: Path) -> str:
+    return hashlib.sha256(path.read_bytes()).hexdigest()
+
+
+def main() -> int:
+    if not ref_available():
+        print("oracle/_ref/libhpgref.so is missing: build it where the reference tree exists", file=sys.stderr)
+        return 1
+    manifest = {}
+    for name, kind, n, seed, chroms, rd, maxes in CASES:
+        g = synth.genome(kind, n, seed)
+        cl = chroms or [n]
+        reads = synth.reads(g, rd[0], rd[1], length=rd[2], edits=rd[3])
+        extra = synth.from_strings(edge_reads(g, cl))
+        seq = np.concatenate([reads.seq, extra.seq])
+        offs = np.concatenate([reads.offsets, extra.offsets[1:] + reads.offsets[-1]]).astype(np.uint64)
+        with tempfile.TemporaryDirectory() as td:
+            fa = Path(td) / "genome.fa"
+            synth.write_fasta(str(fa), g, cl)
+            ref = RefOracle()
+            ref.build_index(str(fa), str(Path(td) / "index"), 16)
+            hashes = {p.name: sha(p) for p in sorted((Path(td) / "index").iterdir())}
+            ro = RefOracle(str(Path(td) / "index"))
+
+            class RS:
+                pass
+            rs = RS()
+            rs.seq, rs.offsets = seq, offs
+            arrays = {"genome_2bit": np.packbits(np.unpackbits(g[:, None], axis=1)[:, 6:].reshape(-1)),
+                      "genome_len": np.array([len(g)]), "chrom_lengths": np.array(cl, dtype=np.int64),
+                      "seq": seq, "offsets": offs}
+            for mode in (0, 1):
+                for mr in (maxes if mode == 1 else [1 << 16]):
+                    r = ro.search(rs, mode=mode, max_results=mr)
+                    tag = f"m{mode}_r{mr}"
+                    arrays[f"{tag}_hits"] = r.hits
+                    arrays[f"{tag}_locs"] = r.locs
+                    arrays[f"{tag}_count"] = r.rs_count
+                    arrays[f"{tag}_trunc"] = r.rs_truncated
+            ro.close()
+        np.savez_compressed(HERE / f"{name}.npz", **arrays)
+        manifest[name] = {"kind": kind, "length": n, "seed": seed, "chrom_lengths": cl, "sa_ratio": 16,
+                          "index_sha256": hashes, "max_results": maxes, "reads": len(offs) - 1}
+        print(name, {k: v.shape for k, v in arrays.items() if k.endswith("_hits")})
+    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

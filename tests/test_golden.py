@@ -1,0 +1,55 @@
+"""Golden pins (CPU): the product's index builder and the CPU oracle against
+outputs of the reference's own code, committed in tests/golden/."""
+from __future__ import annotations
+
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from golden_cases import GoldenCase, names
+from oracle.pyoracle import PortOracle
+
+
+@pytest.fixture(scope="module", params=names())
+def built_case(request, tmp_path_factory):
+    c = GoldenCase(request.param)
+    return c, c.build(tmp_path_factory.mktemp(request.param))
+
+
+def test_builder_writes_reference_index_files(built_case):
+    c, index = built_case
+    want = c.meta["index_sha256"]
+    got = {p.name: hashlib.sha256(p.read_bytes()).hexdigest() for p in Path(index).iterdir()}
+    assert sorted(got) == sorted(want)
+    for f in want:
+        assert got[f] == want[f], f"{f} differs from the reference builder's file"
+
+
+def test_oracle_matches_reference_outputs(built_case):
+    c, index = built_case
+    ora = PortOracle(index)
+    for tag in c.tags():
+        mode = int(tag[1])
+        mr = int(tag.split("_r")[1])
+        got = ora.search(c.reads, mode=mode, max_results=mr, threads=2)
+        want = c.expected(tag)
+        assert np.array_equal(got.rs_count, want.rs_count), tag
+        assert np.array_equal(got.rs_truncated, want.rs_truncated), tag
+        assert np.array_equal(got.hits, want.hits), tag
+        assert np.array_equal(got.locs, want.locs), tag
+    ora.close()
+
+
+def test_golden_cases_exercise_edges():
+    seen_trunc = seen_invalid = seen_quirk = seen_multi = False
+    for name in names():
+        c = GoldenCase(name)
+        for tag in c.tags():
+            e = c.expected(tag)
+            seen_trunc |= bool(e.rs_truncated.any())
+            seen_invalid |= bool(len(e.locs) and (e.locs["valid"] == 0).any())
+            seen_quirk |= bool(((e.hits["err_kind"] == 3) & (e.hits["err_base"] == 3) & (e.hits["dir"] == 0)).any())
+            seen_multi |= bool(((e.hits["l"] - e.hits["k"]) > 0).any())
+    assert seen_trunc and seen_invalid and seen_quirk and seen_multi

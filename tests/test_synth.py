@@ -1,0 +1,39 @@
+"""Seeded generators (CPU): deterministic, with the configured shapes and error models."""
+from __future__ import annotations
+
+import numpy as np
+
+from hpgbwt import synth
+
+
+def test_genomes_are_seeded():
+    for kind in ("iid", "repeats", "human_like"):
+        a = synth.genome(kind, 50_000, 7)
+        b = synth.genome(kind, 50_000, 7)
+        assert np.array_equal(a, b) and a.max() <= 3
+    g = synth.genome("repeats", 200_000, 1)
+    gc = np.isin(g, [1, 2]).mean()
+    assert 0.38 < gc < 0.44
+
+
+def test_reads_shapes_and_edits():
+    g = synth.genome("iid", 100_000, 1)
+    r = synth.reads(g, 2000, 3, length=(36, 250), edits="mix_30_50_20")
+    L = r.lengths()
+    assert L.min() >= 36 and L.max() <= 250
+    frac = np.bincount(r.edit, minlength=4) / len(r)
+    assert abs(frac[0] - 0.3) < 0.05 and abs(frac[1] - 0.5) < 0.05 and abs(frac[2] + frac[3] - 0.2) < 0.05
+    f = synth.reads_fast(g, 20000, 4, 100, "per_base_capped")
+    assert np.all(f.lengths() == 100)
+    assert 0.35 < (f.edit > 0).mean() < 0.48  # 1 - (1 - 0.0054)^100 ~ 0.42
+
+
+def test_error_free_reads_come_from_the_genome():
+    g = synth.genome("iid", 20_000, 5)
+    r = synth.reads_fast(g, 200, 6, 50, "none")
+    A = np.frombuffer(b"ACGT", dtype=np.uint8)
+    text = A[g].tobytes()
+    rc = A[synth.revcomp_codes(g)].tobytes()
+    for i in range(len(r)):
+        s = r.read(i)
+        assert s in text or s in rc
