@@ -245,6 +245,16 @@ size_t bwt_gpu_index_bytes(bwt_index_t* index) {
   return e ? engine_index_bytes(e) : 0;
 }
 
+void bwt_gpu_set_tuning(bwt_index_t* index, int blocks_per_sm, int stack_depth, int chains_per_claim) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_tuning(e, 128, blocks_per_sm, stack_depth, chains_per_claim);
+}
+
+void bwt_gpu_get_tuning(bwt_index_t* index, int* out4) {
+  Engine* e = engine_of(index);
+  if (e && out4) engine_get_tuning(e, out4);
+}
+
 void bwt_gpu_set_chunk(bwt_index_t* index, size_t reads) {
   Engine* e = engine_of(index);
   if (e) engine_set_chunk(e, reads);

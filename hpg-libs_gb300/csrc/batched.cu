@@ -1,0 +1,558 @@
+// batched.cu -- persistent work-queue search, ordered finalize and persistent
+// locate of the batched pipeline form.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "batched.cuh"
+#include "kernels.cuh"
+#include "search_core.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace hpgbwt {
+
+namespace {
+
+constexpr int kBlock = 128;
+
+// Change-point entry types.
+enum : uint32_t { kCpBwd = 0, kCpFwd = 1, kBlk1 = 2, kBlkN = 3 };
+// Lane phases.
+enum : uint32_t { kIdle = 0, kChainB = 1, kChainF = 2, kEntry = 3 };
+// Sub-operations of an entry: 0 deletion, then per base b: 1+3b aux step,
+// 2+3b insertion, 3+3b mismatch; 13 = finished.
+constexpr uint32_t kSubEnd = 13;
+
+// Order keys: section << 28 | t << 8 | slot, following the helper's emission
+// order: exact hit, j=1 block, backward j ascending, j=n-1 block, forward j descending.
+__device__ __forceinline__ uint32_t order_key(uint32_t section, uint32_t t, uint32_t slot) {
+  return (section << 28) | (t << 8) | slot;
+}
+
+__device__ __forceinline__ void emit_hit(const BatchedParams& p, uint32_t rs, uint32_t key, uint32_t k, uint32_t l,
+                                         uint32_t meta) {
+  const uint32_t idx = atomicAdd(&p.rs_count[rs], 1u);
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(p.res_total, (unsigned)g.size());
+  base = g.shfl(base, 0) + g.thread_rank();
+  if (base < p.res_cap) {
+    PendingHit h;
+    h.rs = rs;
+    h.key = key;
+    h.k = k;
+    h.l = l;
+    h.meta = meta;
+    h.idx = idx;
+    p.res[base] = h;
+  } else {
+    atomicOr(p.status, kStatusResFull);
+  }
+}
+
+__device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(ctr, (unsigned)g.size() * n);
+  return g.shfl(base, 0) + g.thread_rank() * n;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) batched_search_kernel(DevIndex X, BatchedParams p, int drain, int chunk) {
+  __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
+  const int tid = threadIdx.x;
+  const uint32_t n_chains = 4u * p.n_reads;
+  const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
+
+  int sp = 0;                         // stack depth of this lane
+  uint32_t phase = kIdle;
+  uint32_t rs = 0;                    // 2 * read + strand
+  const uint8_t* W = nullptr;
+  int len = 0;
+  uint32_t k = 0, l = 0;              // interval of the pending / last step
+  int pos = 0;                        // read position of the pending step
+  uint32_t nb = 0;                    // base of the pending step
+  uint32_t vsel = 0;                  // 0: the strand's backward view, 1: its forward view
+  uint32_t ak = 0, al = 0;            // chains: previous interval; entries: aux interval
+  uint32_t ek = 0, el = 0, ej = 0, etype = 0, sub = 0, bpos = 0;
+  bool cont = false;                  // pending step belongs to a continuation search
+  uint32_t chain_next = 0, chain_left = 0;
+  uint32_t sectors = 0;
+  bool has_step = false;
+
+  for (;;) {
+    // ---- the one gather of this iteration ---------------------------------
+    if (has_step) {
+      const uint32_t strand = rs & 1u;
+      const View v{vsel ^ strand, strand};
+      sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
+      bw_step(X, v, nb, k, l);
+      has_step = false;
+      const int end = len - 1;
+      const int n = end;
+      if (phase == kChainB) {
+        // k,l = vec[pos]; ak,al = vec[pos+1]
+        const int J = pos + 1;
+        const int half = n / 2;
+        const bool differ = ((int64_t)l - (int64_t)k) != ((int64_t)al - (int64_t)ak);
+        if (J >= 2 && J <= half && differ) {
+          if (sp < D) {
+            stk_k[sp][tid] = ak;
+            stk_l[sp][tid] = al;
+            stk_j[sp][tid] = (uint32_t)J | (kCpBwd << 16);
+            ++sp;
+          } else {
+            const unsigned s = claim(p.spill_tail, 1);
+            if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, (uint32_t)J | (kCpBwd << 16)};
+            else atomicOr(p.status, kStatusSpillFull);
+          }
+        }
+        if (k > l || pos == 0) {
+          if (pos == 0) {
+            if (k <= l) emit_hit(p, rs, order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
+            if (differ) {  // the j = 1 block runs on vec[1]
+              if (sp < D) {
+                stk_k[sp][tid] = ak;
+                stk_l[sp][tid] = al;
+                stk_j[sp][tid] = 1u | (kBlk1 << 16);
+                ++sp;
+              } else {
+                const unsigned s = claim(p.spill_tail, 1);
+                if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, 1u | (kBlk1 << 16)};
+                else atomicOr(p.status, kStatusSpillFull);
+              }
+            }
+          }
+          phase = kIdle;
+        } else {
+          ak = k;
+          al = l;
+          --pos;
+          nb = W[pos];
+          has_step = true;
+        }
+      } else if (phase == kChainF) {
+        // k,l = vec_i[pos]; ak,al = vec_i[pos-1]
+        const int J = pos - 1;
+        const int half_f = n / 2 - 1;
+        const bool differ = ((int64_t)l - (int64_t)k) != ((int64_t)al - (int64_t)ak);
+        if (pos >= 1 && differ && ((J >= half_f && J <= n - 2) || J == n - 1)) {
+          const uint32_t t = J == n - 1 ? kBlkN : kCpFwd;
+          if (sp < D) {
+            stk_k[sp][tid] = ak;
+            stk_l[sp][tid] = al;
+            stk_j[sp][tid] = (uint32_t)J | (t << 16);
+            ++sp;
+          } else {
+            const unsigned s = claim(p.spill_tail, 1);
+            if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, (uint32_t)J | (t << 16)};
+            else atomicOr(p.status, kStatusSpillFull);
+          }
+        }
+        if (k > l || pos == n) {
+          phase = kIdle;
+        } else {
+          ak = k;
+          al = l;
+          ++pos;
+          nb = W[pos];
+          has_step = true;
+        }
+      } else {  // kEntry
+        const bool bwd = (etype == kCpBwd || etype == kBlk1);
+        const uint32_t b = (sub - 1) / 3;
+        if (cont) {
+          if (k <= l) {
+            pos += bwd ? -1 : 1;
+            if (pos < 0 || pos > end) {
+              // continuation reached the read end: emit (search.c:1580-1600, 1676-1698)
+              const uint32_t kind = sub == 0 ? 1u : (((sub - 1) % 3) == 1 ? 3u : 2u);
+              const uint32_t slot = sub == 0 ? 0u : (kind == 3 ? 1u + 2 * b : 2u + 2 * b);
+              const uint32_t basev = sub == 0 ? 0xFFu : b;
+              if (bwd)
+                emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
+              else
+                emit_hit(p, rs, order_key(4, (uint32_t)(n - (int)ej), slot), k, l,
+                         pack_meta(1, 1, kind, basev, (int32_t)ej + 1));
+              cont = false;
+              ++sub;
+            } else {
+              nb = W[pos];
+              has_step = true;
+            }
+          } else {
+            cont = false;
+            ++sub;
+          }
+        } else if ((sub - 1) % 3 == 0) {  // aux step done
+          if (k > l) {
+            sub += 3;
+          } else {
+            ak = k;
+            al = l;
+            if (etype == kBlk1 || etype == kBlkN) {
+              const uint32_t w = etype == kBlk1 ? W[0] : W[end];
+              if (b != w) {
+                if (etype == kBlk1)
+                  emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)bpos));
+                else
+                  emit_hit(p, rs, order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
+              }
+            }
+            ++sub;
+          }
+        } else {  // block insertion step done
+          if (k <= l) {
+            if (etype == kBlk1) {
+              emit_hit(p, rs, order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
+              bpos = b;
+            } else {
+              emit_hit(p, rs, order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, end));
+            }
+          }
+          sub += 2;
+        }
+      }
+    }
+
+    // ---- find the next step: advance entries, pop the stack, refill -------
+    while (!has_step) {
+      if (phase == kEntry) {
+        const int end = len - 1;
+        const bool bwd = (etype == kCpBwd || etype == kBlk1);
+        const bool blk = etype >= kBlk1;
+        if (sub >= kSubEnd) {
+          phase = kIdle;
+          continue;
+        }
+        if (sub == 0) {
+          if (blk) {  // direct deletion result of the block
+            if (etype == kBlk1)
+              emit_hit(p, rs, order_key(1, 0, 0), ek, el, pack_meta(0, 1, 1, 0xFF, 0));
+            else
+              emit_hit(p, rs, order_key(3, 0, 0), ek, el, pack_meta(1, 1, 1, 0xFF, end));
+            sub = 1;
+            continue;
+          }
+          k = ek;
+          l = el;
+          pos = bwd ? (int)ej - 2 : (int)ej + 2;
+        } else {
+          const uint32_t b = (sub - 1) / 3, r = (sub - 1) % 3;
+          if (r == 0) {  // aux step with base b
+            k = ek;
+            l = el;
+            nb = b;
+            vsel = bwd ? 0u : 1u;
+            has_step = true;
+            cont = false;
+            break;
+          }
+          if (blk) {
+            if (r == 1) {  // block insertion: one step with the read's end base
+              k = ak;
+              l = al;
+              nb = etype == kBlk1 ? W[0] : W[end];
+              vsel = bwd ? 0u : 1u;
+              has_step = true;
+              cont = false;
+              break;
+            }
+            ++sub;  // blocks emit their mismatch right after the aux step
+            continue;
+          }
+          if (r == 2) {  // mismatch only where b differs from the read base
+            const uint32_t w = bwd ? W[ej - 1] : W[ej + 1];
+            if (b == w) {
+              ++sub;
+              continue;
+            }
+          }
+          k = ak;
+          l = al;
+          pos = bwd ? (int)ej - (r == 1 ? 1 : 2) : (int)ej + (r == 1 ? 1 : 2);
+        }
+        // continuation search from (k, l) at pos
+        vsel = bwd ? 0u : 1u;
+        if (pos < 0 || pos > end) {  // nothing left to match: the interval itself is the hit
+          const uint32_t b = sub == 0 ? 0u : (sub - 1) / 3;
+          const uint32_t kind = sub == 0 ? 1u : (((sub - 1) % 3) == 1 ? 3u : 2u);
+          const uint32_t slot = sub == 0 ? 0u : (kind == 3 ? 1u + 2 * b : 2u + 2 * b);
+          if (k <= l) {
+            if (bwd)
+              emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, sub == 0 ? 0xFF : b,
+                                                                      (int32_t)ej - 1));
+            else
+              emit_hit(p, rs, order_key(4, (uint32_t)(end - (int)ej), slot), k, l,
+                       pack_meta(1, 1, kind, sub == 0 ? 0xFF : b, (int32_t)ej + 1));
+          }
+          ++sub;
+          continue;
+        }
+        nb = W[pos];
+        cont = true;
+        has_step = true;
+        break;
+      }
+      if (sp > 0) {  // next change point of this lane's read
+        --sp;
+        ek = stk_k[sp][tid];
+        el = stk_l[sp][tid];
+        const uint32_t jt = stk_j[sp][tid];
+        ej = jt & 0xFFFFu;
+        etype = jt >> 16;
+        sub = 0;
+        bpos = 0;
+        cont = false;
+        phase = kEntry;
+        continue;
+      }
+      if (drain) {
+        const unsigned s = claim(p.spill_head, 1);
+        if (s >= spill_end) break;
+        const SpillEntry e = p.spill[s];
+        rs = e.rs;
+        const uint32_t read = rs >> 1;
+        const uint64_t b0 = p.offs[read];
+        W = p.codes + b0;
+        len = (int)(p.offs[read + 1] - b0);
+        ek = e.k;
+        el = e.l;
+        ej = e.jtype & 0xFFFFu;
+        etype = e.jtype >> 16;
+        sub = 0;
+        bpos = 0;
+        cont = false;
+        phase = kEntry;
+        continue;
+      }
+      if (chain_left == 0) {
+        chain_next = claim(p.chain_ctr, (unsigned)chunk);
+        chain_left = (unsigned)chunk;
+      }
+      if (chain_next >= n_chains) break;
+      const uint32_t c = chain_next++;
+      --chain_left;
+      const uint32_t read = c >> 2;
+      const uint64_t b0 = p.offs[read];
+      const int L = (int)(p.offs[read + 1] - b0);
+      if (!p.ok[read] || L < 3 || L > 32767) continue;
+      rs = (read << 1) | ((c >> 1) & 1u);
+      W = p.codes + b0;
+      len = L;
+      k = 0;
+      l = X.top;
+      ak = 0;
+      al = X.top;
+      if (c & 1u) {
+        phase = kChainF;
+        vsel = 1;
+        pos = 0;
+      } else {
+        phase = kChainB;
+        vsel = 0;
+        pos = L - 1;
+      }
+      nb = W[pos];
+      has_step = true;
+    }
+    if (!has_step) break;
+  }
+  if (p.census) atomicAdd(p.census, (unsigned long long)sectors);
+}
+
+// ------------------------------------------------------------- finalize --
+
+__global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const unsigned int* res_total,
+                                    const uint64_t* __restrict__ seg_off, PendingHit* __restrict__ sorted,
+                                    uint32_t res_cap) {
+  const uint32_t n = min(*res_total, res_cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const PendingHit h = res[i];
+    sorted[seg_off[h.rs] + h.idx] = h;
+  }
+}
+
+__global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
+                                     uint32_t n_rs, uint32_t max_results, uint32_t* __restrict__ kept,
+                                     uint8_t* __restrict__ trunc) {
+  const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rs >= n_rs) return;
+  const uint64_t b = seg_off[rs], e = seg_off[rs + 1];
+  // insertion sort by key (lists are short; keys are unique within a list)
+  for (uint64_t i = b + 1; i < e; ++i) {
+    const PendingHit x = sorted[i];
+    uint64_t j = i;
+    while (j > b && sorted[j - 1].key > x.key) {
+      sorted[j] = sorted[j - 1];
+      --j;
+    }
+    sorted[j] = x;
+  }
+  const uint64_t cnt = e - b;
+  kept[rs] = (uint32_t)(cnt < max_results ? cnt : max_results);
+  trunc[rs] = cnt > max_results ? 1 : 0;
+}
+
+__global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
+                                   const uint64_t* __restrict__ hit_off, const uint32_t* __restrict__ kept,
+                                   uint32_t n_rs, hpg_hit_t* __restrict__ hits, uint32_t* __restrict__ rows) {
+  const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
+  if (rs >= n_rs) return;
+  const uint32_t m = kept[rs];
+  const uint64_t b = seg_off[rs], o = hit_off[rs];
+  for (uint32_t i = 0; i < m; ++i) {
+    const PendingHit x = sorted[b + i];
+    hpg_hit_t h;
+    h.read = rs >> 1;
+    h.strand = (uint8_t)(rs & 1u);
+    h.dir = (uint8_t)(x.meta & 1u);
+    h.nm = (uint8_t)((x.meta >> 1) & 1u);
+    h.err_kind = (uint8_t)((x.meta >> 2) & 3u);
+    h.err_base = (uint8_t)((x.meta >> 4) & 0xFFu);
+    h.pad0 = 0;
+    h.err_pos = (int16_t)(uint16_t)(x.meta >> 16);
+    h.pad1 = 0;
+    h.k = (int64_t)x.k;
+    h.l = (int64_t)x.l;
+    hits[o + i] = h;
+    rows[o + i] = x.k <= x.l ? x.l - x.k + 1 : 0u;
+  }
+}
+
+// --------------------------------------------------------------- locate --
+
+__global__ void __launch_bounds__(kBlock)
+    locate_persistent_kernel(DevIndex X, const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
+                             uint32_t n_hits, uint64_t n_locs, const uint64_t* __restrict__ read_offs,
+                             hpg_loc_t* __restrict__ out, unsigned int* row_ctr, unsigned long long* census) {
+  uint64_t r = 0;
+  uint32_t i = 0, j = 0, phys = 0, hid = 0;
+  uint64_t len_calc = 0;
+  bool active = false;
+  uint32_t sectors = 0;
+  for (;;) {
+    if (!active) {
+      const unsigned c = claim(row_ctr, 1);
+      if (c >= n_locs) break;
+      r = c;
+      uint32_t lo = 0, hi = n_hits;
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (loc_off[mid] <= r) lo = mid;
+        else hi = mid;
+      }
+      hid = lo;
+      const hpg_hit_t h = hits[lo];
+      i = (uint32_t)((uint64_t)h.k + (r - loc_off[lo]));
+      j = 0;
+      const uint64_t len = read_offs[h.read + 1] - read_offs[h.read];
+      const uint32_t err = h.nm ? h.err_kind : 0u;
+      len_calc = len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0);
+      phys = (uint32_t)h.dir ^ (uint32_t)h.strand;
+      active = true;
+    }
+    if (!sampled_row(X, i)) {
+      i = lf_step(X, X.dir[phys], i);
+      ++sectors;
+      if (++j > X.walk_mod) {
+        atomicOr(X.err, kErrWalk);
+        i = 0;
+      }
+      continue;
+    }
+    const DevDir& D = X.dir[phys];
+    const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
+    ++sectors;
+    const uint32_t sa = (s + j) % X.walk_mod;
+    const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
+    const uint32_t id = kar_search(X, key);
+    hpg_loc_t o;
+    o.key = key;
+    o.hit = hid;
+    o.pad = 0;
+    if (key + len_calc <= X.kar_offset[id]) {
+      o.valid = 1;
+      o.chrom = id - 1;
+      o.position = X.kar_start[id - 1] + (key - X.kar_offset[id - 1]);
+    } else {
+      o.valid = 0;
+      o.chrom = 0;
+      o.position = 0;
+    }
+    out[r] = o;
+    active = false;
+  }
+  if (census) atomicAdd(census, (unsigned long long)sectors);
+}
+
+template <int D>
+void launch_search_d(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
+                     cudaStream_t s) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D>, kBlock, 0);
+  if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+  if (per_sm < 1) per_sm = 1;
+  count_launches(1);
+  batched_search_kernel<D><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, t.chunk < 1 ? 1 : t.chunk);
+}
+
+}  // namespace
+
+int batched_max_blocks_per_sm(const BatchedTuning& t) {
+  int per_sm = 0;
+  if (t.stack <= 2)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<2>, kBlock, 0);
+  else if (t.stack <= 4)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<4>, kBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<8>, kBlock, 0);
+  return per_sm;
+}
+
+void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
+                           cudaStream_t s) {
+  if (t.stack <= 2)
+    launch_search_d<2>(X, p, t, num_sms, drain, s);
+  else if (t.stack <= 4)
+    launch_search_d<4>(X, p, t, num_sms, drain, s);
+  else
+    launch_search_d<8>(X, p, t, num_sms, drain, s);
+}
+
+void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
+                         PendingHit* sorted, uint32_t res_cap, cudaStream_t s) {
+  count_launches(1);
+  scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap);
+}
+
+void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
+                          uint32_t* kept, uint8_t* trunc, cudaStream_t s) {
+  if (!n_rs) return;
+  count_launches(1);
+  sort_truncate_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, n_rs, max_results, kept, trunc);
+}
+
+void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
+                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s) {
+  if (!n_rs) return;
+  count_launches(1);
+  expand_hits_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, hit_off, kept, n_rs, hits, rows);
+}
+
+void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, unsigned int* row_ctr,
+                              unsigned long long* census, int num_sms, cudaStream_t s) {
+  if (!n_locs) return;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = (uint64_t)num_sms * per_sm;
+  const uint64_t need = (n_locs + kBlock - 1) / kBlock;
+  if (need < blocks) blocks = need;
+  count_launches(1);
+  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, hits, loc_off, n_hits, n_locs, read_offs, out,
+                                                               row_ctr, census);
+}
+
+}  // namespace hpgbwt

@@ -1,0 +1,91 @@
+// batched.cuh -- the batched (persistent, work-queue) form of the mapping pipeline.
+//
+// Search: one persistent kernel whose lanes each run a small state machine
+// that issues exactly one backward-extension step per loop iteration, so the
+// lanes of a warp stay converged on the gather regardless of what each lane
+// is doing (a vector search, a branch continuation, a j=1 block).  Work comes
+// from a global chain counter (4 chains per read: 2 strands x 2 halves) and
+// from each lane's own stack of change points; a change point that does not
+// fit on the stack spills to a device queue that a drain launch empties.
+// Every hit carries an order key that reproduces BWSearch1VectorHelper's
+// emission order (search/search.c:1491-1709); the finalize kernels sort each
+// (read, strand) list by key and truncate it at max_results like add_result
+// (search/results.h:93-103).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "fm_device.cuh"
+#include "hpg_bwt_records.h"
+
+namespace hpgbwt {
+
+// One emitted hit before ordering.
+struct PendingHit {
+  uint32_t rs;    // 2 * read + strand
+  uint32_t key;   // emission order within the (read, strand) list
+  uint32_t k, l;
+  uint32_t meta;  // packed as pack_meta()
+  uint32_t idx;   // arrival index within the (read, strand) list
+};
+
+// A spilled change point.
+struct SpillEntry {
+  uint32_t k, l;
+  uint32_t rs;
+  uint32_t jtype;  // J | type << 16
+};
+
+struct BatchedParams {
+  // inputs
+  const uint8_t* codes;
+  const uint64_t* offs;
+  const uint8_t* ok;
+  uint32_t n_reads;
+  uint32_t max_results;
+  // work queues
+  unsigned int* chain_ctr;   // next chain id
+  unsigned int* spill_head;  // next spill entry to drain
+  unsigned int* spill_tail;  // spill entries written
+  SpillEntry* spill;
+  uint32_t spill_cap;
+  // results
+  unsigned int* res_total;
+  PendingHit* res;
+  uint32_t res_cap;
+  uint32_t* rs_count;        // [2 * n_reads] arrivals per (read, strand)
+  unsigned int* status;      // bit 0: result pool full, bit 1: spill queue full
+  unsigned long long* census;
+};
+
+struct BatchedTuning {
+  int block = 128;        // threads per block
+  int blocks_per_sm = 0;  // 0: as many as fit
+  int stack = 4;          // change points per lane kept in shared memory (2, 4 or 8)
+  int chunk = 1;          // chains claimed per lane per refill (1, 2 or 4)
+};
+
+constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u;
+
+// Search kernels: `drain` empties the spill queue instead of pulling chains.
+void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
+                           cudaStream_t s);
+int batched_max_blocks_per_sm(const BatchedTuning& t);
+
+// Finalize: scatter pending hits into (read, strand) segments, sort each by
+// key, truncate; kept counts to `kept`, truncation flags to `trunc`.
+void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
+                         PendingHit* sorted, uint32_t res_cap, cudaStream_t s);
+void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
+                          uint32_t* kept, uint8_t* trunc, cudaStream_t s);
+void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
+                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s);
+
+// Persistent locate: lanes pull rows from a counter and refill when their walk ends.
+void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, unsigned int* row_ctr,
+                              unsigned long long* census, int num_sms, cudaStream_t s);
+
+}  // namespace hpgbwt

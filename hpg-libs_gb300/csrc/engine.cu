@@ -8,6 +8,7 @@
 #include <cstring>
 #include <vector>
 
+#include "batched.cuh"
 #include "engine.hpp"
 #include "fm_device.cuh"
 #include "kernels.cuh"
@@ -47,6 +48,11 @@ struct Engine {
   // workspace
   DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
       loc_off, locs, census;
+  // batched form
+  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg;
+  uint32_t b_res_cap = 0, b_spill_cap = 0;
+  BatchedTuning tuning;
+  int num_sms = 0;
   uint32_t ovf_cap = 0;
   size_t chunk = 0;  // reads per chunk, 0 = automatic
   bool census_on = false;
@@ -256,6 +262,7 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   en->X.kar_offset = en->d_kar_off;
   en->X.kar_start = en->d_kar_start;
   en->X.kar_size = (uint32_t)nk;
+  cudaDeviceGetAttribute(&en->num_sms, cudaDevAttrMultiProcessorCount, device);
   if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return fail("index upload", ce);
   return en;
 }
@@ -274,7 +281,7 @@ void engine_destroy(Engine* e) {
   cudaFree(e->d_err);
   DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
                     &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
-                    &e->census};
+                    &e->census, &e->b_ctr, &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg};
   for (DevBuf* b : bufs) cudaFree(b->p);
   for (int i = 0; i <= kStageCount; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -303,6 +310,139 @@ void engine_stage_ms(Engine* e, float* out, int n) {
   for (int i = 0; i < n && i < kStageCount; ++i) out[i] = e->stage_ms[i];
 }
 
+namespace {
+
+// Batched form: persistent search (+ drain of spilled change points), ordered
+// finalize, persistent locate.  Grows its pools and reruns on overflow.
+int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uint32_t n, uint32_t max_results,
+                unsigned long long* census, size_t* n_hits_out, size_t* n_locs_out, float* t_search, float* t_final,
+                float* t_loc, std::string* err) {
+  (void)d_offs_u8;
+  cudaStream_t s = e->stream;
+  const size_t T = 2ull * n;
+  if (!ensure(e, e->b_ctr, 64) || !ensure(e, e->b_arr, T * 4 + 16) || !ensure(e, e->b_seg, (T + 1) * 8) ||
+      !ensure(e, e->hit_off, (T + 1) * 8) || !ensure(e, e->scan_part, scan_parts(T) * 8)) {
+    *err = "out of device memory (batched counters)";
+    return -1;
+  }
+  if (e->b_res_cap < 4 * (size_t)n + 4096) e->b_res_cap = (uint32_t)std::min<size_t>(4 * (size_t)n + 4096, 0xFFFFFFF0u);
+  if (e->b_spill_cap < (size_t)n / 4 + 4096) e->b_spill_cap = (uint32_t)std::min<size_t>(n / 4 + 4096, 0xFFFFFFF0u);
+  unsigned int* ctr = ptr<unsigned int>(e->b_ctr);  // [0] chains [1] spill head [2] spill tail [3] results [4] status [5] rows
+  uint32_t status = 0, res_total = 0;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    if (!ensure(e, e->b_res, (size_t)e->b_res_cap * sizeof(PendingHit)) ||
+        !ensure(e, e->b_sorted, (size_t)e->b_res_cap * sizeof(PendingHit)) ||
+        !ensure(e, e->b_spill, (size_t)e->b_spill_cap * sizeof(SpillEntry))) {
+      *err = "out of device memory (batched pools)";
+      return -1;
+    }
+    cudaMemsetAsync(ctr, 0, 64, s);
+    cudaMemsetAsync(e->b_arr.p, 0, T * 4, s);
+    if (census) cudaMemsetAsync(census, 0, 8, s);
+    BatchedParams p;
+    p.codes = ptr<uint8_t>(e->codes);
+    p.offs = d_offs;
+    p.ok = ptr<uint8_t>(e->ok);
+    p.n_reads = n;
+    p.max_results = max_results;
+    p.chain_ctr = ctr + 0;
+    p.spill_head = ctr + 1;
+    p.spill_tail = ctr + 2;
+    p.spill = ptr<SpillEntry>(e->b_spill);
+    p.spill_cap = e->b_spill_cap;
+    p.res_total = ctr + 3;
+    p.res = ptr<PendingHit>(e->b_res);
+    p.res_cap = e->b_res_cap;
+    p.rs_count = ptr<uint32_t>(e->b_arr);
+    p.status = ctr + 4;
+    p.census = census;
+    cudaEventRecord(e->cev[0], s);
+    launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
+    launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
+    cudaEventRecord(e->cev[1], s);
+    uint32_t h[5];
+    HPG_CUDA(cudaMemcpyAsync(h, ctr, 20, cudaMemcpyDeviceToHost, s), "batched counters");
+    HPG_CUDA(cudaStreamSynchronize(s), "batched search");
+    status = h[4];
+    res_total = h[3];
+    if (!status) break;
+    if (status & kStatusResFull) e->b_res_cap = (uint32_t)std::min<size_t>((size_t)res_total * 2 + 4096, 0xFFFFFFF0u);
+    if (status & kStatusSpillFull) e->b_spill_cap = (uint32_t)std::min<size_t>((size_t)h[2] * 2 + 4096, 0xFFFFFFF0u);
+  }
+  if (status) {
+    *err = "batched search pools kept overflowing";
+    return -1;
+  }
+  if (census) {
+    unsigned long long v = 0;
+    HPG_CUDA(cudaMemcpy(&v, census, 8, cudaMemcpyDeviceToHost), "census");
+    e->census_val += v;
+  }
+  // ordered finalize
+  launch_scan(ptr<uint32_t>(e->b_arr), T, ptr<uint64_t>(e->b_seg), ptr<uint64_t>(e->scan_part), s);
+  launch_scatter_hits(ptr<PendingHit>(e->b_res), ctr + 3, ptr<uint64_t>(e->b_seg), ptr<PendingHit>(e->b_sorted),
+                      e->b_res_cap, s);
+  launch_sort_truncate(ptr<PendingHit>(e->b_sorted), ptr<uint64_t>(e->b_seg), (uint32_t)T, max_results,
+                       ptr<uint32_t>(e->rs_count), ptr<uint8_t>(e->rs_trunc), s);
+  launch_scan(ptr<uint32_t>(e->rs_count), T, ptr<uint64_t>(e->hit_off), ptr<uint64_t>(e->scan_part), s);
+  uint64_t h_tot = 0;
+  HPG_CUDA(cudaMemcpyAsync(&h_tot, ptr<uint64_t>(e->hit_off) + T, 8, cudaMemcpyDeviceToHost, s), "hit count");
+  HPG_CUDA(cudaStreamSynchronize(s), "hit scan");
+  if (!ensure(e, e->hits, (h_tot + 1) * sizeof(hpg_hit_t)) || !ensure(e, e->rows, (h_tot + 1) * 4) ||
+      !ensure(e, e->loc_off, (h_tot + 2) * 8) || !ensure(e, e->scan_part, scan_parts(h_tot) * 8)) {
+    *err = "out of device memory (hits)";
+    return -1;
+  }
+  launch_expand_hits(ptr<PendingHit>(e->b_sorted), ptr<uint64_t>(e->b_seg), ptr<uint64_t>(e->hit_off),
+                     ptr<uint32_t>(e->rs_count), (uint32_t)T, ptr<hpg_hit_t>(e->hits), ptr<uint32_t>(e->rows), s);
+  launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
+  uint64_t l_tot = 0;
+  HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
+  HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
+  cudaEventRecord(e->cev[2], s);
+  if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t))) {
+    *err = "out of device memory (locate output)";
+    return -1;
+  }
+  if (census) cudaMemsetAsync(census, 0, 8, s);
+  cudaMemsetAsync(ctr + 5, 0, 4, s);
+  launch_locate_persistent(e->X, ptr<hpg_hit_t>(e->hits), ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs,
+                           ptr<hpg_loc_t>(e->locs), ctr + 5, census, e->num_sms, s);
+  cudaEventRecord(e->cev[3], s);
+  HPG_CUDA(cudaStreamSynchronize(s), "locate kernel");
+  if (census) {
+    unsigned long long v = 0;
+    HPG_CUDA(cudaMemcpy(&v, census, 8, cudaMemcpyDeviceToHost), "census");
+    e->census_val += v;
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
+  *t_search += ms;
+  cudaEventElapsedTime(&ms, e->cev[1], e->cev[2]);
+  *t_final += ms;
+  cudaEventElapsedTime(&ms, e->cev[2], e->cev[3]);
+  *t_loc += ms;
+  *n_hits_out = h_tot;
+  *n_locs_out = l_tot;
+  return 0;
+}
+
+}  // namespace
+
+void engine_set_tuning(Engine* e, int block, int blocks_per_sm, int stack, int chunk) {
+  (void)block;
+  e->tuning.blocks_per_sm = blocks_per_sm;
+  e->tuning.stack = stack <= 2 ? 2 : (stack <= 4 ? 4 : 8);
+  e->tuning.chunk = chunk < 1 ? 1 : (chunk > 8 ? 8 : chunk);
+}
+
+void engine_get_tuning(Engine* e, int* out4) {
+  out4[0] = e->tuning.block;
+  out4[1] = e->tuning.blocks_per_sm > 0 ? e->tuning.blocks_per_sm : batched_max_blocks_per_sm(e->tuning);
+  out4[2] = e->tuning.stack;
+  out4[3] = e->tuning.chunk;
+}
+
 int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
                          uint64_t total_bases, uint32_t max_len, uint32_t max_results, DeviceResult* out,
                          std::string* err) {
@@ -310,10 +450,11 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
     *err = "unknown search mode";
     return -1;
   }
-  if (form != kFormPlain) {
+  if (form != kFormPlain && form != kFormBatched) {
     *err = "unknown pipeline form";
     return -1;
   }
+  if (form == kFormBatched && mode != HPG_BWT_MODE_SEARCH1) form = kFormPlain;  // exact search has no branches
   if (n_reads >= (1ull << 31)) {
     *err = "too many reads in one batch";
     return -1;
@@ -359,7 +500,13 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
   size_t n_hits = 0, n_locs = 0;
   float t_search = 0, t_final = 0, t_loc = 0;
   cudaEvent_t a = e->cev[0], b = e->cev[1], c = e->cev[2], d = e->cev[3];
-  for (size_t r0 = 0; r0 < n_reads; r0 += chunk) {
+  if (form == kFormBatched) {
+    if (run_batched(e, d_seqs, d_offs, n, max_results, census, &n_hits, &n_locs, &t_search, &t_final, &t_loc, err) !=
+        0)
+      return -1;
+    chunk = n_reads;  // skip the plain chunk loop
+  }
+  for (size_t r0 = (form == kFormBatched ? n_reads : 0); r0 < n_reads; r0 += chunk) {
     const uint32_t nr = (uint32_t)std::min(chunk, n_reads - r0);
     const size_t T = 2ull * nr;
     if (!ensure(e, e->slots, T * kSlotCap * sizeof(uint4)) || !ensure(e, e->hit_off, (T + 1) * 8) ||

@@ -57,5 +57,10 @@ void engine_set_census(Engine* e, int on);
 unsigned long long engine_census(Engine* e);
 void engine_set_chunk(Engine* e, size_t reads_per_chunk);
 size_t engine_index_bytes(Engine* e);
+// Batched-form tuning (threads per block is fixed at 128): blocks per SM
+// (0 = occupancy limit), change points per lane kept in shared memory, chains
+// claimed per refill.
+void engine_set_tuning(Engine* e, int block, int blocks_per_sm, int stack, int chunk);
+void engine_get_tuning(Engine* e, int* out4);
 
 }  // namespace hpgbwt

@@ -86,6 +86,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_census.restype = ctypes.c_ulonglong
     lib.bwt_gpu_census.argtypes = [vp]
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
+    lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.bwt_gpu_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
     lib.bwt_gpu_launch_count.restype = ctypes.c_ulonglong
     lib.bwt_gpu_index_bytes.restype = sz
@@ -178,6 +180,14 @@ class GpuIndex:
 
     def census(self) -> int:
         return int(self.lib.bwt_gpu_census(self.handle))
+
+    def set_tuning(self, blocks_per_sm: int, stack: int, chunk: int) -> None:
+        self.lib.bwt_gpu_set_tuning(self.handle, blocks_per_sm, stack, chunk)
+
+    def get_tuning(self) -> dict:
+        a = (ctypes.c_int * 4)()
+        self.lib.bwt_gpu_get_tuning(self.handle, a)
+        return {"threads_per_block": a[0], "blocks_per_sm": a[1], "stack": a[2], "chains_per_claim": a[3]}
 
     def index_bytes(self) -> int:
         return int(self.lib.bwt_gpu_index_bytes(self.handle))

@@ -147,6 +147,12 @@ void bwt_gpu_set_census(bwt_index_t *index, int on);
 unsigned long long bwt_gpu_census(bwt_index_t *index);
 /* Reads per internal chunk of the plain form (0 = automatic). */
 void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
+/* Batched-form tuning: resident blocks per SM (0 = occupancy limit), change
+ * points per lane held in shared memory (2, 4 or 8; more spill to the device
+ * queue), chains claimed per refill (1..8).  get: {threads per block, blocks
+ * per SM, stack depth, chains per claim}. */
+void bwt_gpu_set_tuning(bwt_index_t *index, int blocks_per_sm, int stack_depth, int chains_per_claim);
+void bwt_gpu_get_tuning(bwt_index_t *index, int *out4);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long bwt_gpu_launch_count(void);
 /* Device bytes of the index's occurrence blocks (both directions). */

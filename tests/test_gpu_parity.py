@@ -19,6 +19,7 @@ def _assert_same(gpu: lib.Result, ref: lib.Result):
     assert np.array_equal(gpu.locs, ref.locs), "located rows differ"
 
 
+@pytest.mark.parametrize("form", [lib.FORM_PLAIN, lib.FORM_BATCHED])
 @pytest.mark.parametrize("mode", [lib.MODE_EXACT, lib.MODE_SEARCH1])
 @pytest.mark.parametrize("kind,n,chroms,edits,length", [
     ("iid", 200_000, 1, "none", 100),
@@ -26,23 +27,24 @@ def _assert_same(gpu: lib.Result, ref: lib.Result):
     ("repeats", 300_000, 3, "mix_30_50_20", (36, 250)),
     ("human_like", 200_000, 5, "mix_30_50_20", (20, 150)),
 ])
-def test_plain_matches_oracle(case_factory, mode, kind, n, chroms, edits, length):
+def test_gpu_matches_oracle(case_factory, mode, form, kind, n, chroms, edits, length):
     c = case_factory(kind, n, 3, chroms)
     reads = synth.reads(c.genome, 4000, 17, length=length, edits=edits)
     ora = PortOracle(c.index)
     with lib.GpuIndex(c.index) as g:
-        got = g.search(reads, mode=mode, form=lib.FORM_PLAIN, max_results=1 << 16)
+        got = g.search(reads, mode=mode, form=form, max_results=1 << 16)
     want = ora.search(reads, mode=mode, max_results=1 << 16, threads=8)
     _assert_same(got, want)
 
 
+@pytest.mark.parametrize("form", [lib.FORM_PLAIN, lib.FORM_BATCHED])
 @pytest.mark.parametrize("max_results", [0, 1, 2, 3, 9, 17])
-def test_truncation_matches_oracle(case_factory, max_results):
+def test_truncation_matches_oracle(case_factory, max_results, form):
     c = case_factory("human_like", 100_000, 5, 2)
     reads = synth.reads(c.genome, 3000, 23, length=(20, 120), edits="mix_30_50_20")
     ora = PortOracle(c.index)
     with lib.GpuIndex(c.index) as g:
-        got = g.search(reads, mode=lib.MODE_SEARCH1, max_results=max_results)
+        got = g.search(reads, mode=lib.MODE_SEARCH1, form=form, max_results=max_results)
     want = ora.search(reads, mode=lib.MODE_SEARCH1, max_results=max_results, threads=8)
     assert want.rs_truncated.any() or max_results > 3
     _assert_same(got, want)
@@ -59,9 +61,10 @@ def test_edge_reads(case_factory):
     ora = PortOracle(c.index)
     with lib.GpuIndex(c.index) as g:
         for mode in (lib.MODE_EXACT, lib.MODE_SEARCH1):
-            got = g.search(reads, mode=mode)
-            want = ora.search(reads, mode=mode, threads=1)
-            _assert_same(got, want)
+            for form in (lib.FORM_PLAIN, lib.FORM_BATCHED):
+                got = g.search(reads, mode=mode, form=form)
+                want = ora.search(reads, mode=mode, threads=1)
+                _assert_same(got, want)
 
 
 def test_chunked_equals_single_pass(case_factory):
@@ -72,3 +75,28 @@ def test_chunked_equals_single_pass(case_factory):
         g.set_chunk(777)
         parts = g.search(reads)
     assert whole.equal(parts)
+
+
+@pytest.mark.parametrize("stack,chunk,per_sm", [(2, 1, 0), (4, 2, 0), (8, 4, 0), (2, 8, 1)])
+def test_batched_tunings_agree(case_factory, stack, chunk, per_sm):
+    """Every autotuner setting gives the oracle's answer; depth 2 forces spills to the drain path."""
+    c = case_factory("human_like", 200_000, 5, 5)
+    reads = synth.reads(c.genome, 4000, 37, length=(20, 150), edits="mix_30_50_20")
+    want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
+    with lib.GpuIndex(c.index) as g:
+        g.set_tuning(per_sm, stack, chunk)
+        got = g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED)
+    _assert_same(got, want)
+
+
+def test_batched_golden(tmp_path_factory):
+    """The batched form reproduces the reference's own outputs in the golden fixtures."""
+    from golden_cases import GoldenCase, names
+    for name in names():
+        gc = GoldenCase(name)
+        index = gc.build(tmp_path_factory.mktemp(name))
+        with lib.GpuIndex(index) as g:
+            for tag in gc.tags():
+                mode, mr = int(tag[1]), int(tag.split("_r")[1])
+                for form in (lib.FORM_PLAIN, lib.FORM_BATCHED):
+                    _assert_same(g.search(gc.reads, mode=mode, form=form, max_results=mr), gc.expected(tag))
