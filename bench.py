@@ -186,7 +186,7 @@ def measured_peaks() -> tuple[float, str]:
 
 def profiled_traffic_per_read() -> float | None:
     """DRAM bytes per read of the search kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "plain_search1_kernel_c2.txt"
+    p = ROOT / "profiles" / "batched_search_kernel_c2.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -232,45 +232,60 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     d_off = torch.from_numpy(reads.offsets.view(np.int64)).to(f"cuda:{dev}")
     torch.cuda.synchronize()
     stream = torch.cuda.ExternalStream(gi.stream(), device=f"cuda:{dev}")
-    form = lib.FORM_PLAIN
-
-    def step():
-        return gi.search_device(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, lib.MODE_SEARCH1, form,
-                                MAX_RESULTS)
-
-    # census run (untimed): touched index sectors per stage
-    gi.set_census(True)
-    rs = step()
-    sectors = gi.census()
-    census_stage = gi.stage_ms()
-    gi.set_census(False)
-    n_hits, n_locs = int(rs.n_hits), int(rs.n_locs)
-
-    for _ in range(args.warmup):
-        step()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stage_sum = [0.0, 0.0, 0.0, 0.0]
-    dist.barrier()
-    torch.cuda.synchronize()
-    launches0 = lib.launch_count()
-    with ClockSampler(dev) as clk:
-        for i in range(args.steps):
-            flush.fill_(i & 0xFF)
-            torch.cuda.synchronize()
-            ev[i][0].record(stream)
+
+    def make_step(form):
+        def step():
+            return gi.search_device(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, lib.MODE_SEARCH1, form,
+                                    MAX_RESULTS)
+        return step
+
+    def timed(form):
+        """census run, W warm-up steps, K timed steps (L2 flushed before each)."""
+        step = make_step(form)
+        gi.set_census(True)
+        rs = step()
+        sectors = gi.census()
+        gi.set_census(False)
+        for _ in range(args.warmup):
             step()
-            ev[i][1].record(stream)
-            ev[i][1].synchronize()
-            st = gi.stage_ms()
-            stage_sum = [a + b for a, b in zip(stage_sum, st)]
-    launches = lib.launch_count() - launches0
-    torch.cuda.synchronize()
-    dist.barrier()
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    ms_max = dist.max(ms)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        stage_sum = [0.0, 0.0, 0.0, 0.0]
+        dist.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.launch_count()
+        with ClockSampler(dev) as clk:
+            for i in range(args.steps):
+                flush.fill_(i & 0xFF)
+                torch.cuda.synchronize()
+                ev[i][0].record(stream)
+                step()
+                ev[i][1].record(stream)
+                ev[i][1].synchronize()
+                stage_sum = [a + b for a, b in zip(stage_sum, gi.stage_ms())]
+        launches = lib.launch_count() - l0
+        torch.cuda.synchronize()
+        dist.barrier()
+        ms = dist.max(sum(a.elapsed_time(b) for a, b in ev))
+        return {"ms": ms, "sectors": sectors, "stages": [x / args.steps for x in stage_sum], "launches": launches,
+                "clocks": clk_summary, "n_hits": int(rs.n_hits), "n_locs": int(rs.n_locs)}
+
     total_reads = dist.sum(float(n))
-    value = total_reads * args.steps / (ms_max / 1e3)
+    res = {}
+    for name, form in (("plain", lib.FORM_PLAIN), ("batched", lib.FORM_BATCHED)):
+        res[name] = timed(form)
+        res[name]["value"] = total_reads * args.steps / (res[name]["ms"] / 1e3)
+        log(f"[bench] {name}: {res[name]['value'] / 1e6:.1f} M reads/s, stages {res[name]['stages']}")
+    head = res["batched"]
+    form = lib.FORM_BATCHED
+    value = head["value"]
+    ms_max = head["ms"]
+    launches = head["launches"]
+    clk_summary = head["clocks"]
+    sectors = head["sectors"]
+    stage_sum = [x * args.steps for x in head["stages"]]
+    n_hits, n_locs = head["n_hits"], head["n_locs"]
 
     # e2e: host buffers through the C ABI (pinned reads in, host records out)
     pin_seq = torch.from_numpy(reads.seq).pin_memory()
@@ -293,7 +308,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     h2d = total + 8 * (n + 1)
     d2h = 32 * e_hits + 32 * e_locs + 2 * n * 4 + 2 * n
 
-    # roofline of the dominant kernel (the search kernel)
+    # roofline of the dominant kernel (the search kernel of the headline form)
     per_step = [x / args.steps for x in stage_sum]
     search_ms = per_step[1]
     search_sectors = sectors
@@ -303,7 +318,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     tpr = profiled_traffic_per_read()
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": (tpr * n if tpr else None),
-                "kernel": "plain_search1_kernel", "peak_kind": peak_kind,
+                "kernel": "batched_search_kernel", "peak_kind": peak_kind,
                 "algorithmic_bytes_per_read": round(algo_bytes / n, 1)}
     gather = None
     if dist.rank == 0:
@@ -325,7 +340,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "data": "synthetic (seeded genome and reads; no public dataset)",
             "config": {"workload": wl["desc"], "genome_bp": wl["genome_bp"], "reads_per_gpu": n,
                        "read_len": wl["read_len"], "max_results": MAX_RESULTS, "sa_ratio": SA_RATIO,
-                       "o_ratio": 64, "form": "plain", "l2": "flushed (256 MiB write) before every step; "
+                       "o_ratio": 64, "form": "batched", "l2": "flushed (256 MiB write) before every step; "
                        "reads 200 MB > L2", "parallelism": f"replica x{dist.world} (reads sharded)"},
             "e2e": {"value": round(e2e_value, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "bwt_gpu_search_batch"},
@@ -333,11 +348,15 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "roofline": roofline,
             "gather_roofline": gather,
             "cpu_baseline": base,
-            "clocks": clk.summary(),
+            "clocks": clk_summary,
             "stages_ms": {"encode": round(per_step[0], 3), "search": round(per_step[1], 3),
                           "finalize": round(per_step[2], 3), "locate": round(per_step[3], 3)},
             "hits_per_step": n_hits, "located_rows_per_step": n_locs,
-            "forms": {"plain": {"reads_per_s": round(value, 1)}},
+            "forms": {k: {"reads_per_s": round(v["value"], 1), "ms_per_step": round(v["ms"] / args.steps, 3),
+                          "stages_ms": [round(x, 3) for x in v["stages"]], "sectors_per_read": round(v["sectors"] / n, 2)}
+                      for k, v in res.items()},
+            "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
+            "tuning": gi.get_tuning(),
         }
     gi.close()
     return out
