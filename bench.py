@@ -269,7 +269,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
         dist.barrier()
         ms = dist.max(sum(a.elapsed_time(b) for a, b in ev))
         return {"ms": ms, "sectors": sectors, "stages": [x / args.steps for x in stage_sum], "launches": launches,
-                "clocks": clk_summary, "n_hits": int(rs.n_hits), "n_locs": int(rs.n_locs)}
+                "clocks": clk.summary(), "n_hits": int(rs.n_hits), "n_locs": int(rs.n_locs)}
 
     total_reads = dist.sum(float(n))
     res = {}
