@@ -272,6 +272,11 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                 "clocks": clk.summary(), "n_hits": int(rs.n_hits), "n_locs": int(rs.n_locs)}
 
     total_reads = dist.sum(float(n))
+    # autotune the batched form on this batch (untimed)
+    t0 = time.time()
+    table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
+    best = min(table, key=lambda r: r["search_us"])
+    log(f"[bench] autotune: {len(table)} settings in {time.time() - t0:.1f}s, best {best}")
     res = {}
     for name, form in (("plain", lib.FORM_PLAIN), ("batched", lib.FORM_BATCHED)):
         res[name] = timed(form)
@@ -357,6 +362,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "tuning": gi.get_tuning(),
+            "autotune": {"settings": len(table), "best_search_ms": best["search_us"] / 1e3,
+                         "worst_search_ms": max(r["search_us"] for r in table) / 1e3},
         }
     gi.close()
     return out

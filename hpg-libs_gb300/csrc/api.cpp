@@ -245,14 +245,27 @@ size_t bwt_gpu_index_bytes(bwt_index_t* index) {
   return e ? engine_index_bytes(e) : 0;
 }
 
-void bwt_gpu_set_tuning(bwt_index_t* index, int blocks_per_sm, int stack_depth, int chains_per_claim) {
+void bwt_gpu_set_tuning(bwt_index_t* index, int min_blocks, int blocks_per_sm, int stack_depth,
+                        int chains_per_claim) {
   Engine* e = engine_of(index);
-  if (e) engine_set_tuning(e, 128, blocks_per_sm, stack_depth, chains_per_claim);
+  if (e) engine_set_tuning(e, min_blocks, blocks_per_sm, stack_depth, chains_per_claim);
 }
 
-void bwt_gpu_get_tuning(bwt_index_t* index, int* out4) {
+void bwt_gpu_get_tuning(bwt_index_t* index, int* out5) {
   Engine* e = engine_of(index);
-  if (e && out4) engine_get_tuning(e, out4);
+  if (e && out5) engine_get_tuning(e, out5);
+}
+
+int bwt_gpu_autotune(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* d_offsets, size_t n_reads,
+                     uint64_t total_bases, uint32_t max_len, uint32_t max_results, int* table, int max_rows,
+                     int* rows) {
+  Engine* e = engine_of(index);
+  if (!e) return fail("bwt_gpu_autotune: null index");
+  std::string err;
+  if (engine_autotune(e, d_seqs, d_offsets, n_reads, total_bases, max_len, max_results, table, max_rows, rows,
+                      &err) != 0)
+    return fail(err);
+  return 0;
 }
 
 void bwt_gpu_set_chunk(bwt_index_t* index, size_t reads) {

@@ -57,8 +57,9 @@ __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
   return g.shfl(base, 0) + g.thread_rank() * n;
 }
 
-template <int D>
-__global__ void __launch_bounds__(kBlock) batched_search_kernel(DevIndex X, BatchedParams p, int drain, int chunk) {
+template <int D, int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
+                                                                      int chunk) {
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
   const int tid = threadIdx.x;
   const uint32_t n_chains = 4u * p.n_reads;
@@ -422,10 +423,17 @@ __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const 
 
 // --------------------------------------------------------------- locate --
 
+__global__ void expand_rows_kernel(const uint64_t* __restrict__ loc_off, uint32_t n_hits,
+                                   uint32_t* __restrict__ row_hit) {
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x)
+    for (uint64_t r = loc_off[h]; r < loc_off[h + 1]; ++r) row_hit[r] = h;
+}
+
 __global__ void __launch_bounds__(kBlock)
     locate_persistent_kernel(DevIndex X, const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
-                             uint32_t n_hits, uint64_t n_locs, const uint64_t* __restrict__ read_offs,
-                             hpg_loc_t* __restrict__ out, unsigned int* row_ctr, unsigned long long* census) {
+                             const uint32_t* __restrict__ row_hit, uint64_t n_locs,
+                             const uint64_t* __restrict__ read_offs, hpg_loc_t* __restrict__ out,
+                             unsigned int* row_ctr, unsigned long long* census) {
   uint64_t r = 0;
   uint32_t i = 0, j = 0, phys = 0, hid = 0;
   uint64_t len_calc = 0;
@@ -436,15 +444,9 @@ __global__ void __launch_bounds__(kBlock)
       const unsigned c = claim(row_ctr, 1);
       if (c >= n_locs) break;
       r = c;
-      uint32_t lo = 0, hi = n_hits;
-      while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (loc_off[mid] <= r) lo = mid;
-        else hi = mid;
-      }
-      hid = lo;
-      const hpg_hit_t h = hits[lo];
-      i = (uint32_t)((uint64_t)h.k + (r - loc_off[lo]));
+      hid = row_hit[r];
+      const hpg_hit_t h = hits[hid];
+      i = (uint32_t)((uint64_t)h.k + (r - loc_off[hid]));
       j = 0;
       const uint64_t len = read_offs[h.read + 1] - read_offs[h.read];
       const uint32_t err = h.nm ? h.err_kind : 0u;
@@ -453,7 +455,7 @@ __global__ void __launch_bounds__(kBlock)
       active = true;
     }
     if (!sampled_row(X, i)) {
-      i = lf_step(X, X.dir[phys], i);
+      i = lf_step(X, dir_of(X, phys), i);
       ++sectors;
       if (++j > X.walk_mod) {
         atomicOr(X.err, kErrWalk);
@@ -461,7 +463,7 @@ __global__ void __launch_bounds__(kBlock)
       }
       continue;
     }
-    const DevDir& D = X.dir[phys];
+    const DevDir D = dir_of(X, phys);
     const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
     ++sectors;
     const uint32_t sa = (s + j) % X.walk_mod;
@@ -486,28 +488,47 @@ __global__ void __launch_bounds__(kBlock)
   if (census) atomicAdd(census, (unsigned long long)sectors);
 }
 
-template <int D>
-void launch_search_d(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
-                     cudaStream_t s) {
+template <int D, int MINB>
+void launch_search_dm(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
+                      cudaStream_t s) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D>, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, MINB>, kBlock, 0);
   if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
   if (per_sm < 1) per_sm = 1;
   count_launches(1);
-  batched_search_kernel<D><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, t.chunk < 1 ? 1 : t.chunk);
+  batched_search_kernel<D, MINB><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, t.chunk < 1 ? 1 : t.chunk);
+}
+
+template <int D>
+void launch_search_d(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
+                     cudaStream_t s) {
+  if (t.min_blocks >= 16)
+    launch_search_dm<D, 16>(X, p, t, num_sms, drain, s);
+  else if (t.min_blocks >= 12)
+    launch_search_dm<D, 12>(X, p, t, num_sms, drain, s);
+  else
+    launch_search_dm<D, 1>(X, p, t, num_sms, drain, s);
+}
+
+template <int D>
+int occupancy_d(const BatchedTuning& t) {
+  int per_sm = 0;
+  if (t.min_blocks >= 16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 16>, kBlock, 0);
+  else if (t.min_blocks >= 12)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 12>, kBlock, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 1>, kBlock, 0);
+  if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+  return per_sm;
 }
 
 }  // namespace
 
 int batched_max_blocks_per_sm(const BatchedTuning& t) {
-  int per_sm = 0;
-  if (t.stack <= 2)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<2>, kBlock, 0);
-  else if (t.stack <= 4)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<4>, kBlock, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<8>, kBlock, 0);
-  return per_sm;
+  if (t.stack <= 2) return occupancy_d<2>(t);
+  if (t.stack <= 4) return occupancy_d<4>(t);
+  return occupancy_d<8>(t);
 }
 
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
@@ -541,9 +562,11 @@ void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const
 }
 
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
-                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, unsigned int* row_ctr,
-                              unsigned long long* census, int num_sms, cudaStream_t s) {
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, uint32_t* row_hit,
+                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s) {
   if (!n_locs) return;
+  count_launches(1);
+  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(loc_off, n_hits, row_hit);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
@@ -551,7 +574,7 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
   const uint64_t need = (n_locs + kBlock - 1) / kBlock;
   if (need < blocks) blocks = need;
   count_launches(1);
-  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, hits, loc_off, n_hits, n_locs, read_offs, out,
+  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, hits, loc_off, row_hit, n_locs, read_offs, out,
                                                                row_ctr, census);
 }
 

@@ -65,6 +65,7 @@ struct BatchedTuning {
   int blocks_per_sm = 0;  // 0: as many as fit
   int stack = 4;          // change points per lane kept in shared memory (2, 4 or 8)
   int chunk = 1;          // chains claimed per lane per refill (1, 2 or 4)
+  int min_blocks = 1;     // register bound: 1 (compiler's choice), 12 or 16 resident blocks per SM
 };
 
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u;
@@ -85,7 +86,7 @@ void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const
 
 // Persistent locate: lanes pull rows from a counter and refill when their walk ends.
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
-                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, unsigned int* row_ctr,
-                              unsigned long long* census, int num_sms, cudaStream_t s);
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, uint32_t* row_hit,
+                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s);
 
 }  // namespace hpgbwt

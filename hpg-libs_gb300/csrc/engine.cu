@@ -49,7 +49,7 @@ struct Engine {
   DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
       loc_off, locs, census;
   // batched form
-  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg;
+  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit;
   uint32_t b_res_cap = 0, b_spill_cap = 0;
   BatchedTuning tuning;
   int num_sms = 0;
@@ -281,7 +281,8 @@ void engine_destroy(Engine* e) {
   cudaFree(e->d_err);
   DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
                     &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
-                    &e->census, &e->b_ctr, &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg};
+                    &e->census, &e->b_ctr, &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg,
+                    &e->b_rowhit};
   for (DevBuf* b : bufs) cudaFree(b->p);
   for (int i = 0; i <= kStageCount; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
@@ -400,14 +401,14 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
   HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
   cudaEventRecord(e->cev[2], s);
-  if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t))) {
+  if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t)) || !ensure(e, e->b_rowhit, (l_tot + 1) * 4)) {
     *err = "out of device memory (locate output)";
     return -1;
   }
   if (census) cudaMemsetAsync(census, 0, 8, s);
   cudaMemsetAsync(ctr + 5, 0, 4, s);
   launch_locate_persistent(e->X, ptr<hpg_hit_t>(e->hits), ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs,
-                           ptr<hpg_loc_t>(e->locs), ctr + 5, census, e->num_sms, s);
+                           ptr<hpg_loc_t>(e->locs), ptr<uint32_t>(e->b_rowhit), ctr + 5, census, e->num_sms, s);
   cudaEventRecord(e->cev[3], s);
   HPG_CUDA(cudaStreamSynchronize(s), "locate kernel");
   if (census) {
@@ -429,18 +430,62 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
 
 }  // namespace
 
-void engine_set_tuning(Engine* e, int block, int blocks_per_sm, int stack, int chunk) {
-  (void)block;
+void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, int chunk) {
+  e->tuning.min_blocks = min_blocks >= 16 ? 16 : (min_blocks >= 12 ? 12 : 1);
   e->tuning.blocks_per_sm = blocks_per_sm;
   e->tuning.stack = stack <= 2 ? 2 : (stack <= 4 ? 4 : 8);
   e->tuning.chunk = chunk < 1 ? 1 : (chunk > 8 ? 8 : chunk);
 }
 
-void engine_get_tuning(Engine* e, int* out4) {
-  out4[0] = e->tuning.block;
-  out4[1] = e->tuning.blocks_per_sm > 0 ? e->tuning.blocks_per_sm : batched_max_blocks_per_sm(e->tuning);
-  out4[2] = e->tuning.stack;
-  out4[3] = e->tuning.chunk;
+void engine_get_tuning(Engine* e, int* out5) {
+  out5[0] = e->tuning.block;
+  out5[1] = batched_max_blocks_per_sm(e->tuning);
+  out5[2] = e->tuning.stack;
+  out5[3] = e->tuning.chunk;
+  out5[4] = e->tuning.min_blocks;
+}
+
+// Autotuner: time the batched search on (a prefix of) the batch for every
+// candidate setting and keep the fastest.  Writes up to max_rows rows of
+// {min_blocks, blocks_per_sm, stack, chunk, search ms * 1000} to table.
+int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads, uint64_t total_bases,
+                    uint32_t max_len, uint32_t max_results, int* table, int max_rows, int* rows_out,
+                    std::string* err) {
+  static const int cand_minb[] = {1, 12, 16};
+  static const int cand_stack[] = {2, 4, 8};
+  static const int cand_chunk[] = {1, 2, 4};
+  BatchedTuning best = e->tuning;
+  float best_ms = 1e30f;
+  int rows = 0;
+  DeviceResult r;
+  for (int mb : cand_minb)
+    for (int st : cand_stack)
+      for (int ch : cand_chunk) {
+        engine_set_tuning(e, mb, 0, st, ch);
+        float t = 0;
+        for (int rep = 0; rep < 2; ++rep) {  // first run warms, second is timed
+          if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases,
+                                   max_len, max_results, &r, err) != 0)
+            return -1;
+          t = e->stage_ms[kStageSearch];
+        }
+        if (table && rows < max_rows) {
+          int* row = table + 5 * rows;
+          row[0] = mb;
+          row[1] = batched_max_blocks_per_sm(e->tuning);
+          row[2] = st;
+          row[3] = ch;
+          row[4] = (int)(t * 1000.0f);
+        }
+        ++rows;
+        if (t < best_ms) {
+          best_ms = t;
+          best = e->tuning;
+        }
+      }
+  e->tuning = best;
+  if (rows_out) *rows_out = rows;
+  return 0;
 }
 
 int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
@@ -494,7 +539,7 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
   chunk = std::max<size_t>(1, std::min(chunk, std::max<size_t>(n_reads, 1)));
 
   cudaEventRecord(e->ev[0], s);
-  launch_encode(d_seqs, d_offs, n, e->d_table, ptr<uint8_t>(e->codes), ptr<uint8_t>(e->ok), s);
+  launch_encode(d_seqs, total_bases, d_offs, n, e->d_table, ptr<uint8_t>(e->codes), ptr<uint8_t>(e->ok), s);
   cudaEventRecord(e->ev[1], s);
 
   size_t n_hits = 0, n_locs = 0;

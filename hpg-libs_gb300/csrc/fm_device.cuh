@@ -60,6 +60,14 @@ struct View {
 
 #ifdef __CUDACC__
 
+// Entry p (0..3) of a 4-vector by selects, so that kernel-parameter arrays
+// are never indexed with a register (which would copy them to local memory).
+__device__ __forceinline__ uint32_t sel4(const uint32_t (&a)[4], uint32_t p) {
+  const uint32_t lo = (p & 1u) ? a[1] : a[0];
+  const uint32_t hi = (p & 1u) ? a[3] : a[2];
+  return (p & 2u) ? hi : lo;
+}
+
 __device__ __forceinline__ void load_block(const OccBlock* p, uint32_t (&cnt)[4], uint4& bits) {
   const uint4* q = reinterpret_cast<const uint4*>(p);
   uint4 c = __ldg(q);
@@ -88,7 +96,7 @@ __device__ __forceinline__ uint32_t count_prefix(const uint4& bits, uint32_t p, 
 // the '$' row (stored as code 0) taken out.
 __device__ __forceinline__ uint32_t rank_block(const DevDir& D, uint32_t q, uint32_t p, uint32_t r,
                                                const uint32_t (&cnt)[4], const uint4& bits) {
-  uint32_t v = cnt[p] + count_prefix(bits, p, r);
+  uint32_t v = sel4(cnt, p) + count_prefix(bits, p, r);
   if (p == 0 && q == (D.dollar >> 6) && r > (D.dollar & 63)) v -= 1;
   return v;
 }
@@ -111,11 +119,20 @@ __device__ __forceinline__ uint32_t rank_hi(const DevDir& D, uint32_t p, uint32_
   return rank_block(D, q, p, (l & 63) + 1, cnt, bits);
 }
 
+__device__ __forceinline__ DevDir dir_of(const DevIndex& X, uint32_t d) {
+  DevDir D;
+  D.occ = d ? X.dir[1].occ : X.dir[0].occ;
+  D.S = d ? X.dir[1].S : X.dir[0].S;
+  D.dollar = d ? X.dir[1].dollar : X.dir[0].dollar;
+  D.nblk = d ? X.dir[1].nblk : X.dir[0].nblk;
+  return D;
+}
+
 // BWiteration (search/runtime.h:38-42) over a view, on 32-bit interval ends.
 // k in [0, n+1], l in [0, n] always hold for the intervals the search forms.
 __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, uint32_t& k, uint32_t& l) {
-  const uint32_t p = v.comp ? X.comp[b] : b;
-  const DevDir& D = X.dir[v.d];
+  const uint32_t p = v.comp ? sel4(X.comp, b) : b;
+  const DevDir D = dir_of(X, v.d);
   const uint32_t q0 = k >> 6, q1 = l >> 6;
   uint32_t cnt[4];
   uint4 bits;
@@ -128,8 +145,8 @@ __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, u
     load_block(D.occ + q1, cnt, bits);
     rl = rank_block(D, q1, p, (l & 63) + 1, cnt, bits);
   }
-  k = X.C1[p] + rk;
-  l = X.C[p] + rl;
+  k = sel4(X.C1, p) + rk;
+  l = sel4(X.C, p) + rl;
 }
 
 // LF of row i on a physical direction: row 0 for the '$' row, else
@@ -142,7 +159,7 @@ __device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, 
   load_block(D.occ + q, cnt, bits);
   const uint32_t w = r < 32 ? (r < 16 ? bits.x : bits.y) : (r < 48 ? bits.z : bits.w);
   const uint32_t b = (w >> (2 * (r & 15))) & 3u;
-  return X.C[b] + rank_block(D, q, b, r + 1, cnt, bits);
+  return sel4(X.C, b) + rank_block(D, q, b, r + 1, cnt, bits);
 }
 
 __device__ __forceinline__ bool sampled_row(const DevIndex& X, uint32_t i) {
@@ -151,7 +168,7 @@ __device__ __forceinline__ bool sampled_row(const DevIndex& X, uint32_t i) {
 
 // getScompValue (csafm.h:208-235): walk LF to a sampled row, add the steps.
 __device__ __forceinline__ uint32_t sa_value(const DevIndex& X, uint32_t d, uint32_t m) {
-  const DevDir& D = X.dir[d];
+  const DevDir D = dir_of(X, d);
   uint32_t i = m, j = 0;
   while (!sampled_row(X, i)) {
     i = lf_step(X, D, i);

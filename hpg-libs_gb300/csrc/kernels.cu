@@ -21,22 +21,51 @@ constexpr int kTpb = 128;
 
 inline unsigned grid_for(size_t n, int tpb) { return (unsigned)((n + tpb - 1) / tpb); }
 
-__global__ void encode_kernel(const uint8_t* __restrict__ ascii, const uint64_t* __restrict__ offs,
+// Coalesced encoding: each thread translates 16 consecutive bytes; a byte
+// outside the alphabet clears its read's flag (found by binary search over
+// the offsets; such reads are rare).
+__global__ void encode_kernel(const uint8_t* __restrict__ ascii, uint64_t total, const uint64_t* __restrict__ offs,
                               uint32_t n_reads, const uint8_t* __restrict__ table, uint8_t* __restrict__ codes,
                               uint8_t* __restrict__ ok) {
   __shared__ uint8_t tab[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tab[i] = table[i];
   __syncthreads();
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_reads) return;
-  const uint64_t b = offs[r], e = offs[r + 1];
-  uint32_t bad = 0;
-  for (uint64_t i = b; i < e; ++i) {
-    const uint8_t c = tab[ascii[i]];
-    bad |= (c == 0xFF);
-    codes[i] = c;
+  const uint64_t base = 0;  // codes mirror d_seqs byte for byte over [0, total)
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c * 16 < total;
+       c += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = base + c * 16;
+    uint8_t in[16], out[16];
+    const uint64_t m = total - c * 16 < 16 ? total - c * 16 : 16;
+    if (m == 16 && (b & 15) == 0) {
+      *reinterpret_cast<uint4*>(in) = *reinterpret_cast<const uint4*>(ascii + b);
+    } else {
+      for (uint64_t i = 0; i < m; ++i) in[i] = ascii[b + i];
+    }
+    uint32_t bad = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      out[i] = tab[in[i]];
+      if (i < (int)m && out[i] == 0xFF) bad |= 1u << i;
+    }
+    if (m == 16 && (b & 15) == 0) {
+      *reinterpret_cast<uint4*>(codes + b) = *reinterpret_cast<const uint4*>(out);
+    } else {
+      for (uint64_t i = 0; i < m; ++i) codes[b + i] = out[i];
+    }
+    while (bad) {
+      const int i = __ffs(bad) - 1;
+      bad &= bad - 1;
+      const uint64_t at = b + i;
+      if (at < offs[0]) continue;
+      uint32_t lo = 0, hi = n_reads;  // read r with offs[r] <= at < offs[r+1]
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= at) lo = mid;
+        else hi = mid;
+      }
+      ok[lo] = 0;
+    }
   }
-  ok[r] = bad ? 0 : 1;
 }
 
 __device__ __forceinline__ View view_B(uint32_t strand) { return strand ? View{1, 1} : View{0, 0}; }
@@ -288,7 +317,7 @@ __global__ void __launch_bounds__(kTpb)
   uint32_t steps = 0;
   uint64_t key;
   {
-    const DevDir& D = X.dir[phys_fw];
+    const DevDir D = dir_of(X, phys_fw);
     uint32_t i = row, j = 0;
     while (!sampled_row(X, i)) {
       i = lf_step(X, D, i);
@@ -323,11 +352,15 @@ __global__ void __launch_bounds__(kTpb)
 
 }  // namespace
 
-void launch_encode(const uint8_t* ascii, const uint64_t* offs, uint32_t n_reads, const uint8_t* d_table,
-                   uint8_t* codes, uint8_t* ok, cudaStream_t s) {
+void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, uint32_t n_reads,
+                   const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s) {
   if (!n_reads) return;
+  cudaMemsetAsync(ok, 1, n_reads, s);
+  if (!total) return;
+  const uint64_t chunks = (total + 15) / 16;
+  const unsigned grid = (unsigned)(chunks < 152ull * 32 * 8 ? (chunks + 255) / 256 : 152ull * 32);
   count_launches(1);
-  encode_kernel<<<grid_for(n_reads, 256), 256, 0, s>>>(ascii, offs, n_reads, d_table, codes, ok);
+  encode_kernel<<<grid, 256, 0, s>>>(ascii, total, offs, n_reads, d_table, codes, ok);
 }
 
 void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,

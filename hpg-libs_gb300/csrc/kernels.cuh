@@ -24,8 +24,8 @@ unsigned long long launch_count();
 void count_launches(unsigned n);
 
 // ASCII -> 2-bit codes (0xFF outside the alphabet) and a per-read validity flag.
-void launch_encode(const uint8_t* ascii, const uint64_t* offs, uint32_t n_reads, const uint8_t* d_table,
-                   uint8_t* codes, uint8_t* ok, cudaStream_t s);
+void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, uint32_t n_reads,
+                   const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
 
 // Exact backward search on both strands (mode EXACT), one thread per (read, strand).
 void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,

@@ -86,8 +86,10 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_census.restype = ctypes.c_ulonglong
     lib.bwt_gpu_census.argtypes = [vp]
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
-    lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.bwt_gpu_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
     lib.bwt_gpu_launch_count.restype = ctypes.c_ulonglong
     lib.bwt_gpu_index_bytes.restype = sz
@@ -181,13 +183,23 @@ class GpuIndex:
     def census(self) -> int:
         return int(self.lib.bwt_gpu_census(self.handle))
 
-    def set_tuning(self, blocks_per_sm: int, stack: int, chunk: int) -> None:
-        self.lib.bwt_gpu_set_tuning(self.handle, blocks_per_sm, stack, chunk)
+    def set_tuning(self, blocks_per_sm: int, stack: int, chunk: int, min_blocks: int = 1) -> None:
+        self.lib.bwt_gpu_set_tuning(self.handle, min_blocks, blocks_per_sm, stack, chunk)
 
     def get_tuning(self) -> dict:
-        a = (ctypes.c_int * 4)()
+        a = (ctypes.c_int * 5)()
         self.lib.bwt_gpu_get_tuning(self.handle, a)
-        return {"threads_per_block": a[0], "blocks_per_sm": a[1], "stack": a[2], "chains_per_claim": a[3]}
+        return {"threads_per_block": a[0], "blocks_per_sm": a[1], "stack": a[2], "chains_per_claim": a[3],
+                "register_bound_blocks": a[4]}
+
+    def autotune(self, d_seqs: int, d_offs: int, n_reads: int, total_bases: int, max_len: int,
+                 max_results: int = 1 << 16) -> list[dict]:
+        table = (ctypes.c_int * (5 * 64))()
+        rows = ctypes.c_int()
+        self._check(self.lib.bwt_gpu_autotune(self.handle, d_seqs, d_offs, n_reads, total_bases, max_len,
+                                              max_results, table, 64, ctypes.byref(rows)))
+        return [{"register_bound_blocks": table[5 * i], "blocks_per_sm": table[5 * i + 1], "stack": table[5 * i + 2],
+                 "chains_per_claim": table[5 * i + 3], "search_us": table[5 * i + 4]} for i in range(rows.value)]
 
     def index_bytes(self) -> int:
         return int(self.lib.bwt_gpu_index_bytes(self.handle))

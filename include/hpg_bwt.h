@@ -129,7 +129,8 @@ int bwt_gpu_search_batch(bwt_index_t *index, int mode, int form, const char *seq
 void bwt_gpu_result_free(hpg_result_set_t *out);
 
 /* Device-resident form for callers that keep reads in GPU memory: d_seqs and
- * d_offsets are device pointers (offsets relative to d_seqs).  Results stay
+ * d_offsets are device pointers (offsets relative to d_seqs; total_bases =
+ * d_offsets[n_reads], the bytes of d_seqs in use; max_len = longest read).  Results stay
  * on the device until the next call; sizes are returned in out (its pointer
  * fields are device pointers).  Copy them with bwt_gpu_copy_result. */
 int bwt_gpu_search_device(bwt_index_t *index, int mode, int form, const uint8_t *d_seqs, const uint64_t *d_offsets,
@@ -147,12 +148,21 @@ void bwt_gpu_set_census(bwt_index_t *index, int on);
 unsigned long long bwt_gpu_census(bwt_index_t *index);
 /* Reads per internal chunk of the plain form (0 = automatic). */
 void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
-/* Batched-form tuning: resident blocks per SM (0 = occupancy limit), change
- * points per lane held in shared memory (2, 4 or 8; more spill to the device
- * queue), chains claimed per refill (1..8).  get: {threads per block, blocks
- * per SM, stack depth, chains per claim}. */
-void bwt_gpu_set_tuning(bwt_index_t *index, int blocks_per_sm, int stack_depth, int chains_per_claim);
-void bwt_gpu_get_tuning(bwt_index_t *index, int *out4);
+/* Batched-form tuning: register bound (1 = compiler's choice, 12 or 16
+ * resident 128-thread blocks per SM), resident blocks per SM actually
+ * launched (0 = occupancy limit), change points per lane held in shared
+ * memory (2, 4 or 8; more spill to the device queue), chains claimed per
+ * refill (1..8).  get: {threads per block, blocks per SM, stack depth,
+ * chains per claim, register bound}. */
+void bwt_gpu_set_tuning(bwt_index_t *index, int min_blocks, int blocks_per_sm, int stack_depth,
+                        int chains_per_claim);
+void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
+/* Autotuner: times the batched search on a device-resident read batch for
+ * every candidate setting (27) and keeps the fastest.  Optional table gets
+ * rows of {min_blocks, blocks_per_sm, stack, chains_per_claim, search us}. */
+int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
+                     uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
+                     int *rows);
 /* Number of kernels this library has launched since it was loaded. */
 unsigned long long bwt_gpu_launch_count(void);
 /* Device bytes of the index's occurrence blocks (both directions). */

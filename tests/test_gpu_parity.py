@@ -77,15 +77,34 @@ def test_chunked_equals_single_pass(case_factory):
     assert whole.equal(parts)
 
 
-@pytest.mark.parametrize("stack,chunk,per_sm", [(2, 1, 0), (4, 2, 0), (8, 4, 0), (2, 8, 1)])
-def test_batched_tunings_agree(case_factory, stack, chunk, per_sm):
+@pytest.mark.parametrize("stack,chunk,per_sm,minb", [(2, 1, 0, 1), (4, 2, 0, 12), (8, 4, 0, 16), (2, 8, 1, 1),
+                                                     (4, 1, 3, 16)])
+def test_batched_tunings_agree(case_factory, stack, chunk, per_sm, minb):
     """Every autotuner setting gives the oracle's answer; depth 2 forces spills to the drain path."""
     c = case_factory("human_like", 200_000, 5, 5)
     reads = synth.reads(c.genome, 4000, 37, length=(20, 150), edits="mix_30_50_20")
     want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
     with lib.GpuIndex(c.index) as g:
-        g.set_tuning(per_sm, stack, chunk)
+        g.set_tuning(per_sm, stack, chunk, minb)
         got = g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED)
+    _assert_same(got, want)
+
+
+def test_autotuner_keeps_results(case_factory):
+    torch = pytest.importorskip("torch")
+    c = case_factory("repeats", 300_000, 3, 3)
+    reads = synth.reads(c.genome, 6000, 39, length=(36, 250), edits="mix_30_50_20")
+    want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=64, threads=8)
+    d_seq = torch.from_numpy(reads.seq).cuda()
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).cuda()
+    with lib.GpuIndex(c.index) as g:
+        table = g.autotune(d_seq.data_ptr(), d_off.data_ptr(), len(reads), int(reads.offsets[-1]),
+                           int(np.diff(reads.offsets).max()), 64)
+        assert len(table) == 27 and all(r["search_us"] > 0 for r in table)
+        chosen = g.get_tuning()
+        best = min(table, key=lambda r: r["search_us"])
+        assert (chosen["stack"], chosen["chains_per_claim"]) == (best["stack"], best["chains_per_claim"])
+        got = g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED, max_results=64)
     _assert_same(got, want)
 
 
