@@ -273,10 +273,12 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
 
     total_reads = dist.sum(float(n))
     # autotune the batched form on this batch (untimed)
-    t0 = time.time()
-    table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
-    best = min(table, key=lambda r: r["search_us"])
-    log(f"[bench] autotune: {len(table)} settings in {time.time() - t0:.1f}s, best {best}")
+    table = []
+    if not args.no_autotune:
+        t0 = time.time()
+        table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
+        log(f"[bench] autotune: {len(table)} settings in {time.time() - t0:.1f}s, "
+            f"best {min(table, key=lambda r: r['search_us'])}")
     res = {}
     for name, form in (("plain", lib.FORM_PLAIN), ("batched", lib.FORM_BATCHED)):
         res[name] = timed(form)
@@ -362,8 +364,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "tuning": gi.get_tuning(),
-            "autotune": {"settings": len(table), "best_search_ms": best["search_us"] / 1e3,
-                         "worst_search_ms": max(r["search_us"] for r in table) / 1e3},
+            "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
+                          "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }
     gi.close()
     return out
@@ -410,6 +412,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]
