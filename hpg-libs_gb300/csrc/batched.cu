@@ -17,8 +17,6 @@ constexpr int kBlock = 128;
 
 // Change-point entry types.
 enum : uint32_t { kCpBwd = 0, kCpFwd = 1, kBlk1 = 2, kBlkN = 3 };
-// Lane phases.
-enum : uint32_t { kIdle = 0, kChainB = 1, kChainF = 2, kEntry = 3 };
 // Sub-operations of an entry: 0 deletion, then per base b: 1+3b aux step,
 // 2+3b insertion, 3+3b mismatch; 13 = finished.
 constexpr uint32_t kSubEnd = 13;
@@ -57,6 +55,9 @@ __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
   return g.shfl(base, 0) + g.thread_rank() * n;
 }
 
+// Lane modes.
+enum : uint32_t { kNone = 0, kChain = 1, kCont = 2, kSingle = 3 };
+
 template <int D, int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
@@ -65,169 +66,62 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   const uint32_t n_chains = 4u * p.n_reads;
   const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
 
-  int sp = 0;                         // stack depth of this lane
-  uint32_t phase = kIdle;
-  uint32_t rs = 0;                    // 2 * read + strand
+  int sp = 0;                       // change points on this lane's stack
+  uint32_t rs = 0;                  // 2 * read + strand
   const uint8_t* W = nullptr;
   int len = 0;
-  uint32_t k = 0, l = 0;              // interval of the pending / last step
-  int pos = 0;                        // read position of the pending step
-  uint32_t nb = 0;                    // base of the pending step
-  uint32_t vsel = 0;                  // 0: the strand's backward view, 1: its forward view
-  uint32_t ak = 0, al = 0;            // chains: previous interval; entries: aux interval
+  uint32_t k = 0, l = 0;            // interval of the pending / last step
+  uint32_t pk = 0, pl = 0;          // chain: previous interval; entry: aux interval
+  int pos = 0, stop = 0, dir = 0;   // read position of the pending step, last position, direction
+  uint32_t nb = 0;                  // base of the pending step
+  uint32_t mode = kNone, vsel = 0;  // vsel 0: the strand's backward view, 1: its forward view
+  int jlo = 0, jhi = 0;             // chain: window of change points the helper looks at
   uint32_t ek = 0, el = 0, ej = 0, etype = 0, sub = 0, bpos = 0;
-  bool cont = false;                  // pending step belongs to a continuation search
-  uint32_t chain_next = 0, chain_left = 0;
-  uint32_t sectors = 0;
-  bool has_step = false;
+  bool in_entry = false;
+  uint32_t chain_next = 0, chain_left = 0, sectors = 0;
+
+  auto push = [&](uint32_t a, uint32_t b, uint32_t jt) {
+    if (sp < D) {
+      stk_k[sp][tid] = a;
+      stk_l[sp][tid] = b;
+      stk_j[sp][tid] = jt;
+      ++sp;
+    } else {
+      const unsigned s = claim(p.spill_tail, 1);
+      if (s < p.spill_cap) p.spill[s] = SpillEntry{a, b, rs, jt};
+      else atomicOr(p.status, kStatusSpillFull);
+    }
+  };
+  // Result of a continuation search that matched to the read end.
+  auto emit_cont = [&]() {
+    const int end = len - 1;
+    const bool bwd = etype == kCpBwd;
+    const uint32_t b = sub == 0 ? 0u : (sub - 1) / 3;
+    const bool ins = sub != 0 && (sub - 1) % 3 == 1;
+    const uint32_t kind = sub == 0 ? 1u : (ins ? 3u : 2u);
+    const uint32_t slot = sub == 0 ? 0u : (ins ? 1u + 2 * b : 2u + 2 * b);
+    const uint32_t basev = sub == 0 ? 0xFFu : b;
+    if (bwd)
+      emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
+    else
+      emit_hit(p, rs, order_key(4, (uint32_t)(end - (int)ej), slot), k, l,
+               pack_meta(1, 1, kind, basev, (int32_t)ej + 1));
+  };
 
   for (;;) {
-    // ---- the one gather of this iteration ---------------------------------
-    if (has_step) {
-      const uint32_t strand = rs & 1u;
-      const View v{vsel ^ strand, strand};
-      sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
-      bw_step(X, v, nb, k, l);
-      has_step = false;
-      const int end = len - 1;
-      const int n = end;
-      if (phase == kChainB) {
-        // k,l = vec[pos]; ak,al = vec[pos+1]
-        const int J = pos + 1;
-        const int half = n / 2;
-        const bool differ = ((int64_t)l - (int64_t)k) != ((int64_t)al - (int64_t)ak);
-        if (J >= 2 && J <= half && differ) {
-          if (sp < D) {
-            stk_k[sp][tid] = ak;
-            stk_l[sp][tid] = al;
-            stk_j[sp][tid] = (uint32_t)J | (kCpBwd << 16);
-            ++sp;
-          } else {
-            const unsigned s = claim(p.spill_tail, 1);
-            if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, (uint32_t)J | (kCpBwd << 16)};
-            else atomicOr(p.status, kStatusSpillFull);
-          }
-        }
-        if (k > l || pos == 0) {
-          if (pos == 0) {
-            if (k <= l) emit_hit(p, rs, order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
-            if (differ) {  // the j = 1 block runs on vec[1]
-              if (sp < D) {
-                stk_k[sp][tid] = ak;
-                stk_l[sp][tid] = al;
-                stk_j[sp][tid] = 1u | (kBlk1 << 16);
-                ++sp;
-              } else {
-                const unsigned s = claim(p.spill_tail, 1);
-                if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, 1u | (kBlk1 << 16)};
-                else atomicOr(p.status, kStatusSpillFull);
-              }
-            }
-          }
-          phase = kIdle;
-        } else {
-          ak = k;
-          al = l;
-          --pos;
-          nb = W[pos];
-          has_step = true;
-        }
-      } else if (phase == kChainF) {
-        // k,l = vec_i[pos]; ak,al = vec_i[pos-1]
-        const int J = pos - 1;
-        const int half_f = n / 2 - 1;
-        const bool differ = ((int64_t)l - (int64_t)k) != ((int64_t)al - (int64_t)ak);
-        if (pos >= 1 && differ && ((J >= half_f && J <= n - 2) || J == n - 1)) {
-          const uint32_t t = J == n - 1 ? kBlkN : kCpFwd;
-          if (sp < D) {
-            stk_k[sp][tid] = ak;
-            stk_l[sp][tid] = al;
-            stk_j[sp][tid] = (uint32_t)J | (t << 16);
-            ++sp;
-          } else {
-            const unsigned s = claim(p.spill_tail, 1);
-            if (s < p.spill_cap) p.spill[s] = SpillEntry{ak, al, rs, (uint32_t)J | (t << 16)};
-            else atomicOr(p.status, kStatusSpillFull);
-          }
-        }
-        if (k > l || pos == n) {
-          phase = kIdle;
-        } else {
-          ak = k;
-          al = l;
-          ++pos;
-          nb = W[pos];
-          has_step = true;
-        }
-      } else {  // kEntry
-        const bool bwd = (etype == kCpBwd || etype == kBlk1);
-        const uint32_t b = (sub - 1) / 3;
-        if (cont) {
-          if (k <= l) {
-            pos += bwd ? -1 : 1;
-            if (pos < 0 || pos > end) {
-              // continuation reached the read end: emit (search.c:1580-1600, 1676-1698)
-              const uint32_t kind = sub == 0 ? 1u : (((sub - 1) % 3) == 1 ? 3u : 2u);
-              const uint32_t slot = sub == 0 ? 0u : (kind == 3 ? 1u + 2 * b : 2u + 2 * b);
-              const uint32_t basev = sub == 0 ? 0xFFu : b;
-              if (bwd)
-                emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
-              else
-                emit_hit(p, rs, order_key(4, (uint32_t)(n - (int)ej), slot), k, l,
-                         pack_meta(1, 1, kind, basev, (int32_t)ej + 1));
-              cont = false;
-              ++sub;
-            } else {
-              nb = W[pos];
-              has_step = true;
-            }
-          } else {
-            cont = false;
-            ++sub;
-          }
-        } else if ((sub - 1) % 3 == 0) {  // aux step done
-          if (k > l) {
-            sub += 3;
-          } else {
-            ak = k;
-            al = l;
-            if (etype == kBlk1 || etype == kBlkN) {
-              const uint32_t w = etype == kBlk1 ? W[0] : W[end];
-              if (b != w) {
-                if (etype == kBlk1)
-                  emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)bpos));
-                else
-                  emit_hit(p, rs, order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
-              }
-            }
-            ++sub;
-          }
-        } else {  // block insertion step done
-          if (k <= l) {
-            if (etype == kBlk1) {
-              emit_hit(p, rs, order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
-              bpos = b;
-            } else {
-              emit_hit(p, rs, order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, end));
-            }
-          }
-          sub += 2;
-        }
-      }
-    }
-
-    // ---- find the next step: advance entries, pop the stack, refill -------
-    while (!has_step) {
-      if (phase == kEntry) {
-        const int end = len - 1;
-        const bool bwd = (etype == kCpBwd || etype == kBlk1);
-        const bool blk = etype >= kBlk1;
+    // ---- transitions: next sub-operation, next change point, next chain ----
+    while (mode == kNone) {
+      if (in_entry) {
         if (sub >= kSubEnd) {
-          phase = kIdle;
+          in_entry = false;
           continue;
         }
+        const bool bwd = (etype == kCpBwd || etype == kBlk1);
+        const bool blk = etype >= kBlk1;
+        const int end = len - 1;
+        vsel = bwd ? 0u : 1u;
         if (sub == 0) {
-          if (blk) {  // direct deletion result of the block
+          if (blk) {  // the block's direct deletion result
             if (etype == kBlk1)
               emit_hit(p, rs, order_key(1, 0, 0), ek, el, pack_meta(0, 1, 1, 0xFF, 0));
             else
@@ -244,55 +138,37 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
             k = ek;
             l = el;
             nb = b;
-            vsel = bwd ? 0u : 1u;
-            has_step = true;
-            cont = false;
+            mode = kSingle;
             break;
           }
           if (blk) {
             if (r == 1) {  // block insertion: one step with the read's end base
-              k = ak;
-              l = al;
+              k = pk;
+              l = pl;
               nb = etype == kBlk1 ? W[0] : W[end];
-              vsel = bwd ? 0u : 1u;
-              has_step = true;
-              cont = false;
+              mode = kSingle;
               break;
             }
             ++sub;  // blocks emit their mismatch right after the aux step
             continue;
           }
-          if (r == 2) {  // mismatch only where b differs from the read base
-            const uint32_t w = bwd ? W[ej - 1] : W[ej + 1];
-            if (b == w) {
-              ++sub;
-              continue;
-            }
+          if (r == 2 && b == W[bwd ? ej - 1 : ej + 1]) {  // no mismatch with the read's own base
+            ++sub;
+            continue;
           }
-          k = ak;
-          l = al;
-          pos = bwd ? (int)ej - (r == 1 ? 1 : 2) : (int)ej + (r == 1 ? 1 : 2);
+          k = pk;
+          l = pl;
+          pos = bwd ? (int)ej - (int)r : (int)ej + (int)r;
         }
-        // continuation search from (k, l) at pos
-        vsel = bwd ? 0u : 1u;
-        if (pos < 0 || pos > end) {  // nothing left to match: the interval itself is the hit
-          const uint32_t b = sub == 0 ? 0u : (sub - 1) / 3;
-          const uint32_t kind = sub == 0 ? 1u : (((sub - 1) % 3) == 1 ? 3u : 2u);
-          const uint32_t slot = sub == 0 ? 0u : (kind == 3 ? 1u + 2 * b : 2u + 2 * b);
-          if (k <= l) {
-            if (bwd)
-              emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, sub == 0 ? 0xFF : b,
-                                                                      (int32_t)ej - 1));
-            else
-              emit_hit(p, rs, order_key(4, (uint32_t)(end - (int)ej), slot), k, l,
-                       pack_meta(1, 1, kind, sub == 0 ? 0xFF : b, (int32_t)ej + 1));
-          }
+        dir = bwd ? -1 : 1;
+        stop = bwd ? 0 : end;
+        if (bwd ? pos < 0 : pos > end) {  // nothing left to match: the interval is the hit
+          if (k <= l) emit_cont();
           ++sub;
           continue;
         }
         nb = W[pos];
-        cont = true;
-        has_step = true;
+        mode = kCont;
         break;
       }
       if (sp > 0) {  // next change point of this lane's read
@@ -304,8 +180,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         etype = jt >> 16;
         sub = 0;
         bpos = 0;
-        cont = false;
-        phase = kEntry;
+        in_entry = true;
         continue;
       }
       if (drain) {
@@ -323,8 +198,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         etype = e.jtype >> 16;
         sub = 0;
         bpos = 0;
-        cont = false;
-        phase = kEntry;
+        in_entry = true;
         continue;
       }
       if (chain_left == 0) {
@@ -343,21 +217,95 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       len = L;
       k = 0;
       l = X.top;
-      ak = 0;
-      al = X.top;
-      if (c & 1u) {
-        phase = kChainF;
+      pk = 0;
+      pl = X.top;
+      const int n = L - 1;
+      if (c & 1u) {  // forward vector search: change points J in [n/2 - 1, n - 2], block at n - 1
         vsel = 1;
         pos = 0;
-      } else {
-        phase = kChainB;
+        stop = n;
+        dir = 1;
+        jlo = n / 2 - 1;
+        jhi = n - 1;
+      } else {  // backward vector search: change points J in [2, n/2], block at 1
         vsel = 0;
-        pos = L - 1;
+        pos = n;
+        stop = 0;
+        dir = -1;
+        jlo = 2;
+        jhi = n / 2;
       }
       nb = W[pos];
-      has_step = true;
+      mode = kChain;
     }
-    if (!has_step) break;
+    if (mode == kNone) break;
+
+    // ---- the one gather of this iteration --------------------------------
+    {
+      const uint32_t strand = rs & 1u;
+      sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
+      bw_step(X, View{vsel ^ strand, strand}, nb, k, l);
+    }
+    if (mode == kChain) {
+      // (k,l) = vector entry at pos, (pk,pl) = entry at J = pos - dir
+      const int J = pos - dir;
+      const bool differ = (l - k) != (pl - pk);  // sizes are >= -1 here, so 32-bit differences suffice
+      if (differ && J >= jlo && J <= jhi)
+        push(pk, pl, (uint32_t)J | ((dir > 0 ? (J == stop - 1 ? kBlkN : kCpFwd) : kCpBwd) << 16));
+      if (k <= l && pos != stop) {
+        pk = k;
+        pl = l;
+        pos += dir;
+        nb = W[pos];
+        continue;
+      }
+      if (dir < 0 && pos == 0) {  // backward vector complete: exact hit, then the j = 1 block on vec[1]
+        if (k <= l) emit_hit(p, rs, order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
+        if (differ) push(pk, pl, 1u | (kBlk1 << 16));
+      }
+      mode = kNone;
+    } else if (mode == kCont) {
+      if (k <= l && pos != stop) {
+        pos += dir;
+        nb = W[pos];
+        continue;
+      }
+      if (k <= l) emit_cont();
+      ++sub;
+      mode = kNone;
+    } else {  // kSingle: an aux step or a block insertion step
+      const uint32_t b = (sub - 1) / 3;
+      if ((sub - 1) % 3 == 0) {
+        if (k > l) {
+          sub += 3;
+        } else {
+          pk = k;
+          pl = l;
+          if (etype >= kBlk1) {
+            const int end = len - 1;
+            const uint32_t w = etype == kBlk1 ? W[0] : W[end];
+            if (b != w) {
+              if (etype == kBlk1)
+                emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)bpos));
+              else
+                emit_hit(p, rs, order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
+            }
+          }
+          ++sub;
+        }
+      } else {
+        if (k <= l) {
+          if (etype == kBlk1) {
+            emit_hit(p, rs, order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
+            bpos = b;
+          } else {
+            emit_hit(p, rs, order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, len - 1));
+          }
+        }
+        sub += 2;
+      }
+      mode = kNone;
+    }
   }
   if (p.census) atomicAdd(p.census, (unsigned long long)sectors);
 }

@@ -93,6 +93,12 @@ T* ptr(DevBuf& b) {
   return static_cast<T*>(b.p);
 }
 
+// Code of row t (0..63) of a block (bit-plane layout).
+uint32_t block_code(const OccBlock& B, int t) {
+  const uint32_t lo = t < 32 ? B.bits[0] : B.bits[1], hi = t < 32 ? B.bits[2] : B.bits[3];
+  return ((lo >> (t & 31)) & 1u) | (((hi >> (t & 31)) & 1u) << 1);
+}
+
 // Repack the reference's O/count tables (column c = row c-1) into 32-byte
 // blocks of 64 rows with 2-bit codes and block-start counts.
 std::string pack_occ(const OccTable& o, std::vector<OccBlock>* out, uint32_t* dollar) {
@@ -108,7 +114,7 @@ std::string pack_occ(const OccTable& o, std::vector<OccBlock>* out, uint32_t* do
       const size_t idx = (size_t)b * o.m + (size_t)q;
       B.cnt[b] = q < (int64_t)o.m ? o.desp[idx] + (uint32_t)(o.count[idx] & 1u) : 0u;
     }
-    uint32_t w[4] = {0, 0, 0, 0};
+    uint64_t plane0 = 0, plane1 = 0;  // low and high code bit of each row
     for (int t = 0; t < 64; ++t) {
       const uint64_t row = (uint64_t)q * 64 + t;
       if (row >= rows) break;
@@ -128,9 +134,13 @@ std::string pack_occ(const OccTable& o, std::vector<OccBlock>* out, uint32_t* do
         }
         sym = 0;
       }
-      w[t >> 4] |= (uint32_t)sym << (2 * (t & 15));
+      plane0 |= (uint64_t)(sym & 1) << t;
+      plane1 |= (uint64_t)((sym >> 1) & 1) << t;
     }
-    for (int i = 0; i < 4; ++i) B.bits[i] = w[i];
+    B.bits[0] = (uint32_t)plane0;
+    B.bits[1] = (uint32_t)(plane0 >> 32);
+    B.bits[2] = (uint32_t)plane1;
+    B.bits[3] = (uint32_t)(plane1 >> 32);
   }
   if (bad || dollar_row < 0) return "occurrence table is not a valid BWT";
   // Block counts must equal the running counts of the codes (so every rank,
@@ -144,7 +154,7 @@ std::string pack_occ(const OccTable& o, std::vector<OccBlock>* out, uint32_t* do
       const uint64_t row = q * 64 + t;
       if (row >= rows) break;
       if ((int64_t)row == dollar_row) continue;
-      run[(B.bits[t >> 4] >> (2 * (t & 15))) & 3u]++;
+      run[block_code(B, t)]++;
     }
   }
   *dollar = (uint32_t)dollar_row;
@@ -163,7 +173,7 @@ std::string check_C(const HostIndex& h, const std::vector<OccBlock>& blk, uint32
       const uint64_t row = q * 64 + t;
       if (row >= rows) break;
       if (row == dollar) continue;
-      if (((last.bits[t >> 4] >> (2 * (t & 15))) & 3u) == (uint32_t)b) tot[b]++;
+      if (block_code(last, t) == (uint32_t)b) tot[b]++;
     }
   }
   uint64_t acc = 0;

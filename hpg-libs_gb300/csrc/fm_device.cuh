@@ -6,9 +6,11 @@
 //
 //   OccBlock occ[nblk]   32-byte blocks, one per 64 BWT rows:
 //       cnt[b]   number of symbol b in BWT rows [0, 64q), '$' excluded
-//       bits[4]  2-bit codes of rows 64q..64q+63 (row r: word (r%64)/16,
-//                bits 2*(r%16)); the '$' row is stored as code 0 and
-//                corrected in rank_block().
+//       bits[4]  the 2-bit codes of rows 64q..64q+63 as two bit planes:
+//                bits[0..1] = low code bit of rows 0..63 (one u64),
+//                bits[2..3] = high code bit; the '$' row is stored as
+//                code 0 and corrected in rank_block().  A rank inside the
+//                block is then two bitwise ops and one popcount.
 //   uint32 S[]           sampled SA, S[i/ratio] = SA[i] (the reference's S.vec)
 //
 // One rank query therefore touches exactly one 32-byte sector, against two
@@ -78,18 +80,19 @@ __device__ __forceinline__ void load_block(const OccBlock* p, uint32_t (&cnt)[4]
   cnt[3] = c.w;
 }
 
-// Number of symbol p among the first r rows (0..64) of a block's 2-bit codes.
-__device__ __forceinline__ uint32_t count_prefix(const uint4& bits, uint32_t p, uint32_t r) {
+// One bit per row of the block: set where the row's code is p.
+__device__ __forceinline__ uint64_t match_mask(const uint4& bits, uint32_t p) {
   const uint64_t lo = ((uint64_t)bits.y << 32) | bits.x;
   const uint64_t hi = ((uint64_t)bits.w << 32) | bits.z;
-  const uint64_t pat = 0x5555555555555555ull * p;
-  const uint64_t xl = lo ^ pat, xh = hi ^ pat;
-  const uint64_t ml = ~(xl | (xl >> 1)) & 0x5555555555555555ull;
-  const uint64_t mh = ~(xh | (xh >> 1)) & 0x5555555555555555ull;
-  const uint32_t sh = 2 * r;  // 0..128
-  const uint64_t keep_lo = sh >= 64 ? ~0ull : ((1ull << sh) - 1ull);
-  const uint64_t keep_hi = sh <= 64 ? 0ull : (sh >= 128 ? ~0ull : ((1ull << (sh - 64)) - 1ull));
-  return (uint32_t)(__popcll(ml & keep_lo) + __popcll(mh & keep_hi));
+  return (lo ^ ((uint64_t)(p & 1u) - 1ull)) & (hi ^ ((uint64_t)((p >> 1) & 1u) - 1ull));
+}
+
+// The first r rows (r in 0..64).
+__device__ __forceinline__ uint64_t prefix_mask(uint32_t r) { return r >= 64 ? ~0ull : ((1ull << r) - 1ull); }
+
+// Number of symbol p among the first r rows (0..64) of a block.
+__device__ __forceinline__ uint32_t count_prefix(const uint4& bits, uint32_t p, uint32_t r) {
+  return (uint32_t)__popcll(match_mask(bits, p) & prefix_mask(r));
 }
 
 // Occurrences of physical symbol p in BWT rows [64q, 64q + r) plus cnt, with
@@ -130,20 +133,27 @@ __device__ __forceinline__ DevDir dir_of(const DevIndex& X, uint32_t d) {
 
 // BWiteration (search/runtime.h:38-42) over a view, on 32-bit interval ends.
 // k in [0, n+1], l in [0, n] always hold for the intervals the search forms.
+// When k and l share a block (the common case once an interval is small)
+// one 32-byte sector serves both ranks.
 __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, uint32_t& k, uint32_t& l) {
   const uint32_t p = v.comp ? sel4(X.comp, b) : b;
   const DevDir D = dir_of(X, v.d);
   const uint32_t q0 = k >> 6, q1 = l >> 6;
+  const bool a0 = (p == 0) && (q0 == (D.dollar >> 6));  // '$' block correction applies
   uint32_t cnt[4];
   uint4 bits;
   load_block(D.occ + q0, cnt, bits);
-  const uint32_t rk = rank_block(D, q0, p, k & 63, cnt, bits);
+  uint64_t m = match_mask(bits, p);
+  const uint32_t c0 = sel4(cnt, p);
+  const uint32_t rk = c0 + (uint32_t)__popcll(m & prefix_mask(k & 63)) - ((a0 && k > D.dollar) ? 1u : 0u);
   uint32_t rl;
   if (q1 == q0) {
-    rl = rank_block(D, q0, p, (l & 63) + 1, cnt, bits);
+    rl = c0 + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a0 && l >= D.dollar) ? 1u : 0u);
   } else {
     load_block(D.occ + q1, cnt, bits);
-    rl = rank_block(D, q1, p, (l & 63) + 1, cnt, bits);
+    m = match_mask(bits, p);
+    const bool a1 = (p == 0) && (q1 == (D.dollar >> 6));
+    rl = sel4(cnt, p) + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a1 && l >= D.dollar) ? 1u : 0u);
   }
   k = sel4(X.C1, p) + rk;
   l = sel4(X.C, p) + rl;
@@ -157,8 +167,8 @@ __device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, 
   uint32_t cnt[4];
   uint4 bits;
   load_block(D.occ + q, cnt, bits);
-  const uint32_t w = r < 32 ? (r < 16 ? bits.x : bits.y) : (r < 48 ? bits.z : bits.w);
-  const uint32_t b = (w >> (2 * (r & 15))) & 3u;
+  const uint32_t lo = r < 32 ? bits.x : bits.y, hi = r < 32 ? bits.z : bits.w;
+  const uint32_t b = ((lo >> (r & 31)) & 1u) | (((hi >> (r & 31)) & 1u) << 1);
   return sel4(X.C, b) + rank_block(D, q, b, r + 1, cnt, bits);
 }
 
