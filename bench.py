@@ -279,6 +279,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
         table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
         log(f"[bench] autotune: {len(table)} settings in {time.time() - t0:.1f}s, "
             f"best {min(table, key=lambda r: r['search_us'])}")
+        for r in sorted(table, key=lambda r: r["search_us"])[:8]:
+            log(f"[bench]   {r}")
     res = {}
     for name, form in (("plain", lib.FORM_PLAIN), ("batched", lib.FORM_BATCHED)):
         res[name] = timed(form)

@@ -58,34 +58,50 @@ __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
 // Lane modes.
 enum : uint32_t { kNone = 0, kChain = 1, kCont = 2, kSingle = 3 };
 
-template <int D, int MINB>
+// Cold lane state lives in shared memory (one word per lane and field), so
+// that the registers hold only what every step touches.
+//   meta: J (16 bits) | entry type << 16 | sub-operation << 18 | block err_pos << 22 | in entry << 24
+//   misc: stack depth (4 bits) | chains left in the claimed chunk << 4
+__device__ __forceinline__ uint32_t meta_j(uint32_t m) { return m & 0xFFFFu; }
+__device__ __forceinline__ uint32_t meta_type(uint32_t m) { return (m >> 16) & 3u; }
+__device__ __forceinline__ uint32_t meta_sub(uint32_t m) { return (m >> 18) & 15u; }
+__device__ __forceinline__ uint32_t meta_bpos(uint32_t m) { return (m >> 22) & 3u; }
+__device__ __forceinline__ bool meta_in(uint32_t m) { return (m >> 24) & 1u; }
+__device__ __forceinline__ uint32_t make_meta(uint32_t j, uint32_t type, uint32_t sub, uint32_t bpos, bool in) {
+  return j | (type << 16) | (sub << 18) | (bpos << 22) | ((in ? 1u : 0u) << 24);
+}
+
+template <int D, int MINB, bool CENSUS>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
+  __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_next[kBlock], c_misc[kBlock];
   const int tid = threadIdx.x;
   const uint32_t n_chains = 4u * p.n_reads;
   const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
+  c_meta[tid] = 0;
+  c_misc[tid] = 0;
+  c_next[tid] = 0;
 
-  int sp = 0;                       // change points on this lane's stack
+  // hot state
   uint32_t rs = 0;                  // 2 * read + strand
   const uint8_t* W = nullptr;
   int len = 0;
   uint32_t k = 0, l = 0;            // interval of the pending / last step
   uint32_t pk = 0, pl = 0;          // chain: previous interval; entry: aux interval
-  int pos = 0, stop = 0, dir = 0;   // read position of the pending step, last position, direction
+  int pos = 0, dir = 0;             // read position of the pending step; -1 backward, +1 forward
   uint32_t nb = 0;                  // base of the pending step
-  uint32_t mode = kNone, vsel = 0;  // vsel 0: the strand's backward view, 1: its forward view
-  int jlo = 0, jhi = 0;             // chain: window of change points the helper looks at
-  uint32_t ek = 0, el = 0, ej = 0, etype = 0, sub = 0, bpos = 0;
-  bool in_entry = false;
-  uint32_t chain_next = 0, chain_left = 0, sectors = 0;
+  uint32_t mode = kNone;
+  uint32_t sectors = 0;
 
   auto push = [&](uint32_t a, uint32_t b, uint32_t jt) {
-    if (sp < D) {
+    const uint32_t misc = c_misc[tid];
+    const uint32_t sp = misc & 15u;
+    if (sp < (uint32_t)D) {
       stk_k[sp][tid] = a;
       stk_l[sp][tid] = b;
       stk_j[sp][tid] = jt;
-      ++sp;
+      c_misc[tid] = misc + 1;
     } else {
       const unsigned s = claim(p.spill_tail, 1);
       if (s < p.spill_cap) p.spill[s] = SpillEntry{a, b, rs, jt};
@@ -93,9 +109,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     }
   };
   // Result of a continuation search that matched to the read end.
-  auto emit_cont = [&]() {
-    const int end = len - 1;
-    const bool bwd = etype == kCpBwd;
+  auto emit_cont = [&](uint32_t m) {
+    const uint32_t ej = meta_j(m), sub = meta_sub(m);
+    const bool bwd = meta_type(m) == kCpBwd;
     const uint32_t b = sub == 0 ? 0u : (sub - 1) / 3;
     const bool ins = sub != 0 && (sub - 1) % 3 == 1;
     const uint32_t kind = sub == 0 ? 1u : (ins ? 3u : 2u);
@@ -104,39 +120,41 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     if (bwd)
       emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
     else
-      emit_hit(p, rs, order_key(4, (uint32_t)(end - (int)ej), slot), k, l,
+      emit_hit(p, rs, order_key(4, (uint32_t)(len - 1 - (int)ej), slot), k, l,
                pack_meta(1, 1, kind, basev, (int32_t)ej + 1));
   };
 
   for (;;) {
     // ---- transitions: next sub-operation, next change point, next chain ----
     while (mode == kNone) {
-      if (in_entry) {
+      uint32_t m = c_meta[tid];
+      if (meta_in(m)) {
+        const uint32_t sub = meta_sub(m), etype = meta_type(m), ej = meta_j(m);
         if (sub >= kSubEnd) {
-          in_entry = false;
+          c_meta[tid] = 0;
           continue;
         }
         const bool bwd = (etype == kCpBwd || etype == kBlk1);
         const bool blk = etype >= kBlk1;
         const int end = len - 1;
-        vsel = bwd ? 0u : 1u;
+        dir = bwd ? -1 : 1;
         if (sub == 0) {
           if (blk) {  // the block's direct deletion result
             if (etype == kBlk1)
-              emit_hit(p, rs, order_key(1, 0, 0), ek, el, pack_meta(0, 1, 1, 0xFF, 0));
+              emit_hit(p, rs, order_key(1, 0, 0), c_ek[tid], c_el[tid], pack_meta(0, 1, 1, 0xFF, 0));
             else
-              emit_hit(p, rs, order_key(3, 0, 0), ek, el, pack_meta(1, 1, 1, 0xFF, end));
-            sub = 1;
+              emit_hit(p, rs, order_key(3, 0, 0), c_ek[tid], c_el[tid], pack_meta(1, 1, 1, 0xFF, end));
+            c_meta[tid] = m + (1u << 18);
             continue;
           }
-          k = ek;
-          l = el;
+          k = c_ek[tid];
+          l = c_el[tid];
           pos = bwd ? (int)ej - 2 : (int)ej + 2;
         } else {
           const uint32_t b = (sub - 1) / 3, r = (sub - 1) % 3;
           if (r == 0) {  // aux step with base b
-            k = ek;
-            l = el;
+            k = c_ek[tid];
+            l = c_el[tid];
             nb = b;
             mode = kSingle;
             break;
@@ -149,38 +167,34 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
               mode = kSingle;
               break;
             }
-            ++sub;  // blocks emit their mismatch right after the aux step
+            c_meta[tid] = m + (1u << 18);  // blocks emit their mismatch right after the aux step
             continue;
           }
           if (r == 2 && b == W[bwd ? ej - 1 : ej + 1]) {  // no mismatch with the read's own base
-            ++sub;
+            c_meta[tid] = m + (1u << 18);
             continue;
           }
           k = pk;
           l = pl;
           pos = bwd ? (int)ej - (int)r : (int)ej + (int)r;
         }
-        dir = bwd ? -1 : 1;
-        stop = bwd ? 0 : end;
         if (bwd ? pos < 0 : pos > end) {  // nothing left to match: the interval is the hit
-          if (k <= l) emit_cont();
-          ++sub;
+          if (k <= l) emit_cont(m);
+          c_meta[tid] = m + (1u << 18);
           continue;
         }
         nb = W[pos];
         mode = kCont;
         break;
       }
-      if (sp > 0) {  // next change point of this lane's read
-        --sp;
-        ek = stk_k[sp][tid];
-        el = stk_l[sp][tid];
+      const uint32_t misc = c_misc[tid];
+      if (misc & 15u) {  // next change point of this lane's read
+        const uint32_t sp = (misc & 15u) - 1;
+        c_misc[tid] = misc - 1;
+        c_ek[tid] = stk_k[sp][tid];
+        c_el[tid] = stk_l[sp][tid];
         const uint32_t jt = stk_j[sp][tid];
-        ej = jt & 0xFFFFu;
-        etype = jt >> 16;
-        sub = 0;
-        bpos = 0;
-        in_entry = true;
+        c_meta[tid] = make_meta(jt & 0xFFFFu, jt >> 16, 0, 0, true);
         continue;
       }
       if (drain) {
@@ -192,22 +206,20 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         const uint64_t b0 = p.offs[read];
         W = p.codes + b0;
         len = (int)(p.offs[read + 1] - b0);
-        ek = e.k;
-        el = e.l;
-        ej = e.jtype & 0xFFFFu;
-        etype = e.jtype >> 16;
-        sub = 0;
-        bpos = 0;
-        in_entry = true;
+        c_ek[tid] = e.k;
+        c_el[tid] = e.l;
+        c_meta[tid] = make_meta(e.jtype & 0xFFFFu, e.jtype >> 16, 0, 0, true);
         continue;
       }
-      if (chain_left == 0) {
-        chain_next = claim(p.chain_ctr, (unsigned)chunk);
-        chain_left = (unsigned)chunk;
+      uint32_t left = misc >> 4, next = c_next[tid];
+      if (left == 0) {
+        next = claim(p.chain_ctr, (unsigned)chunk);
+        left = (unsigned)chunk;
       }
-      if (chain_next >= n_chains) break;
-      const uint32_t c = chain_next++;
-      --chain_left;
+      if (next >= n_chains) break;
+      const uint32_t c = next;
+      c_next[tid] = next + 1;
+      c_misc[tid] = (left - 1) << 4;
       const uint32_t read = c >> 2;
       const uint64_t b0 = p.offs[read];
       const int L = (int)(p.offs[read + 1] - b0);
@@ -219,22 +231,8 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       l = X.top;
       pk = 0;
       pl = X.top;
-      const int n = L - 1;
-      if (c & 1u) {  // forward vector search: change points J in [n/2 - 1, n - 2], block at n - 1
-        vsel = 1;
-        pos = 0;
-        stop = n;
-        dir = 1;
-        jlo = n / 2 - 1;
-        jhi = n - 1;
-      } else {  // backward vector search: change points J in [2, n/2], block at 1
-        vsel = 0;
-        pos = n;
-        stop = 0;
-        dir = -1;
-        jlo = 2;
-        jhi = n / 2;
-      }
+      dir = (c & 1u) ? 1 : -1;  // forward / backward vector search
+      pos = (c & 1u) ? 0 : L - 1;
       nb = W[pos];
       mode = kChain;
     }
@@ -243,15 +241,20 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     // ---- the one gather of this iteration --------------------------------
     {
       const uint32_t strand = rs & 1u;
-      sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
+      const uint32_t vsel = dir > 0 ? 1u : 0u;  // forward searches use the strand's forward view
+      if (CENSUS) sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
       bw_step(X, View{vsel ^ strand, strand}, nb, k, l);
     }
+    const int stop = dir > 0 ? len - 1 : 0;
     if (mode == kChain) {
-      // (k,l) = vector entry at pos, (pk,pl) = entry at J = pos - dir
-      const int J = pos - dir;
+      // (k,l) = vector entry at pos, (pk,pl) = entry at J = pos - dir.  The helper
+      // branches at J in [2, n/2] (backward, block at 1) and [n/2 - 1, n - 2]
+      // (forward, block at n - 1).
+      const int J = pos - dir, n = len - 1;
+      const int jlo = dir > 0 ? n / 2 - 1 : 2, jhi = dir > 0 ? n - 1 : n / 2;
       const bool differ = (l - k) != (pl - pk);  // sizes are >= -1 here, so 32-bit differences suffice
       if (differ && J >= jlo && J <= jhi)
-        push(pk, pl, (uint32_t)J | ((dir > 0 ? (J == stop - 1 ? kBlkN : kCpFwd) : kCpBwd) << 16));
+        push(pk, pl, (uint32_t)J | ((dir > 0 ? (J == n - 1 ? kBlkN : kCpFwd) : kCpBwd) << 16));
       if (k <= l && pos != stop) {
         pk = k;
         pl = l;
@@ -270,14 +273,17 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         nb = W[pos];
         continue;
       }
-      if (k <= l) emit_cont();
-      ++sub;
+      const uint32_t m = c_meta[tid];
+      if (k <= l) emit_cont(m);
+      c_meta[tid] = m + (1u << 18);
       mode = kNone;
     } else {  // kSingle: an aux step or a block insertion step
+      const uint32_t m = c_meta[tid];
+      const uint32_t sub = meta_sub(m), etype = meta_type(m);
       const uint32_t b = (sub - 1) / 3;
       if ((sub - 1) % 3 == 0) {
         if (k > l) {
-          sub += 3;
+          c_meta[tid] = m + (3u << 18);
         } else {
           pk = k;
           pl = l;
@@ -286,28 +292,29 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
             const uint32_t w = etype == kBlk1 ? W[0] : W[end];
             if (b != w) {
               if (etype == kBlk1)
-                emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)bpos));
+                emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)meta_bpos(m)));
               else
                 emit_hit(p, rs, order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
             }
           }
-          ++sub;
+          c_meta[tid] = m + (1u << 18);
         }
       } else {
+        uint32_t nm = m + (2u << 18);
         if (k <= l) {
           if (etype == kBlk1) {
             emit_hit(p, rs, order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
-            bpos = b;
+            nm = (nm & ~(3u << 22)) | (b << 22);
           } else {
             emit_hit(p, rs, order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, len - 1));
           }
         }
-        sub += 2;
+        c_meta[tid] = nm;
       }
       mode = kNone;
     }
   }
-  if (p.census) atomicAdd(p.census, (unsigned long long)sectors);
+  if (CENSUS && p.census) atomicAdd(p.census, (unsigned long long)sectors);
 }
 
 // ------------------------------------------------------------- finalize --
@@ -371,39 +378,59 @@ __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const 
 
 // --------------------------------------------------------------- locate --
 
-__global__ void expand_rows_kernel(const uint64_t* __restrict__ loc_off, uint32_t n_hits,
-                                   uint32_t* __restrict__ row_hit) {
-  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x)
-    for (uint64_t r = loc_off[h]; r < loc_off[h + 1]; ++r) row_hit[r] = h;
+// One locate work item per SA row: the row, the owning hit, the physical
+// direction and len_calc (bwt.c:2025-2036), so that a lane starting a walk
+// needs a single 16-byte load.
+struct RowItem {
+  uint32_t row, hit, phys, len_calc;
+};
+
+__global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
+                                   uint32_t n_hits, const uint64_t* __restrict__ read_offs,
+                                   RowItem* __restrict__ items) {
+  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x) {
+    const hpg_hit_t x = hits[h];
+    const uint64_t len = read_offs[x.read + 1] - read_offs[x.read];
+    const uint32_t err = x.nm ? x.err_kind : 0u;
+    RowItem it;
+    it.hit = h;
+    it.phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir, type = !strand
+    it.len_calc = (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
+    const uint64_t b = loc_off[h], e = loc_off[h + 1];
+    for (uint64_t r = b; r < e; ++r) {
+      it.row = (uint32_t)((uint64_t)x.k + (r - b));
+      items[r] = it;
+    }
+  }
 }
 
+constexpr unsigned kRowsPerClaim = 4;
+
 __global__ void __launch_bounds__(kBlock)
-    locate_persistent_kernel(DevIndex X, const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
-                             const uint32_t* __restrict__ row_hit, uint64_t n_locs,
-                             const uint64_t* __restrict__ read_offs, hpg_loc_t* __restrict__ out,
-                             unsigned int* row_ctr, unsigned long long* census) {
-  uint64_t r = 0;
-  uint32_t i = 0, j = 0, phys = 0, hid = 0;
-  uint64_t len_calc = 0;
+    locate_persistent_kernel(DevIndex X, const RowItem* __restrict__ items, uint64_t n_locs,
+                             hpg_loc_t* __restrict__ out, unsigned int* row_ctr, unsigned long long* census) {
+  uint32_t r = 0, left = 0;
+  uint32_t i = 0, j = 0;
+  RowItem it{0, 0, 0, 0};
   bool active = false;
   uint32_t sectors = 0;
   for (;;) {
     if (!active) {
-      const unsigned c = claim(row_ctr, 1);
-      if (c >= n_locs) break;
-      r = c;
-      hid = row_hit[r];
-      const hpg_hit_t h = hits[hid];
-      i = (uint32_t)((uint64_t)h.k + (r - loc_off[hid]));
+      if (left == 0) {
+        r = claim(row_ctr, kRowsPerClaim);
+        left = kRowsPerClaim;
+      } else {
+        ++r;
+      }
+      --left;
+      if (r >= n_locs) break;
+      it = items[r];
+      i = it.row;
       j = 0;
-      const uint64_t len = read_offs[h.read + 1] - read_offs[h.read];
-      const uint32_t err = h.nm ? h.err_kind : 0u;
-      len_calc = len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0);
-      phys = (uint32_t)h.dir ^ (uint32_t)h.strand;
       active = true;
     }
     if (!sampled_row(X, i)) {
-      i = lf_step(X, dir_of(X, phys), i);
+      i = lf_step(X, dir_of(X, it.phys), i);
       ++sectors;
       if (++j > X.walk_mod) {
         atomicOr(X.err, kErrWalk);
@@ -411,15 +438,16 @@ __global__ void __launch_bounds__(kBlock)
       }
       continue;
     }
-    const DevDir D = dir_of(X, phys);
+    const DevDir D = dir_of(X, it.phys);
     const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
     ++sectors;
     const uint32_t sa = (s + j) % X.walk_mod;
-    const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
+    const uint64_t len_calc = it.len_calc;
+    const uint64_t key = it.phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
     const uint32_t id = kar_search(X, key);
     hpg_loc_t o;
     o.key = key;
-    o.hit = hid;
+    o.hit = it.hit;
     o.pad = 0;
     if (key + len_calc <= X.kar_offset[id]) {
       o.valid = 1;
@@ -440,11 +468,15 @@ template <int D, int MINB>
 void launch_search_dm(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                       cudaStream_t s) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, MINB>, kBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, MINB, false>, kBlock, 0);
   if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
   if (per_sm < 1) per_sm = 1;
   count_launches(1);
-  batched_search_kernel<D, MINB><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, t.chunk < 1 ? 1 : t.chunk);
+  const int ch = t.chunk < 1 ? 1 : t.chunk;
+  if (p.census)
+    batched_search_kernel<D, MINB, true><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, ch);
+  else
+    batched_search_kernel<D, MINB, false><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, drain ? 1 : 0, ch);
 }
 
 template <int D>
@@ -462,11 +494,11 @@ template <int D>
 int occupancy_d(const BatchedTuning& t) {
   int per_sm = 0;
   if (t.min_blocks >= 16)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 16>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 16, false>, kBlock, 0);
   else if (t.min_blocks >= 12)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 12>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 12, false>, kBlock, 0);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 1>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 1, false>, kBlock, 0);
   if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
   return per_sm;
 }
@@ -510,20 +542,22 @@ void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const
 }
 
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
-                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, uint32_t* row_hit,
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, void* row_items,
                               unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s) {
   if (!n_locs) return;
+  RowItem* items = static_cast<RowItem*>(row_items);
   count_launches(1);
-  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(loc_off, n_hits, row_hit);
+  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(hits, loc_off, n_hits, read_offs, items);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
   uint64_t blocks = (uint64_t)num_sms * per_sm;
-  const uint64_t need = (n_locs + kBlock - 1) / kBlock;
+  const uint64_t need = (n_locs + kBlock * kRowsPerClaim - 1) / (kBlock * kRowsPerClaim);
   if (need < blocks) blocks = need;
   count_launches(1);
-  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, hits, loc_off, row_hit, n_locs, read_offs, out,
-                                                               row_ctr, census);
+  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, items, n_locs, out, row_ctr, census);
 }
+
+size_t locate_row_item_bytes() { return sizeof(RowItem); }
 
 }  // namespace hpgbwt

@@ -86,7 +86,8 @@ void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const
 
 // Persistent locate: lanes pull rows from a counter and refill when their walk ends.
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
-                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, uint32_t* row_hit,
+                              uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, void* row_items,
                               unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s);
+size_t locate_row_item_bytes();
 
 }  // namespace hpgbwt

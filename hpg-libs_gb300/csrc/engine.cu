@@ -411,14 +411,15 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
   HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
   cudaEventRecord(e->cev[2], s);
-  if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t)) || !ensure(e, e->b_rowhit, (l_tot + 1) * 4)) {
+  if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t)) ||
+      !ensure(e, e->b_rowhit, (l_tot + 1) * locate_row_item_bytes())) {
     *err = "out of device memory (locate output)";
     return -1;
   }
   if (census) cudaMemsetAsync(census, 0, 8, s);
   cudaMemsetAsync(ctr + 5, 0, 4, s);
   launch_locate_persistent(e->X, ptr<hpg_hit_t>(e->hits), ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs,
-                           ptr<hpg_loc_t>(e->locs), ptr<uint32_t>(e->b_rowhit), ctr + 5, census, e->num_sms, s);
+                           ptr<hpg_loc_t>(e->locs), e->b_rowhit.p, ctr + 5, census, e->num_sms, s);
   cudaEventRecord(e->cev[3], s);
   HPG_CUDA(cudaStreamSynchronize(s), "locate kernel");
   if (census) {
