@@ -317,6 +317,81 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   if (CENSUS && p.census) atomicAdd(p.census, (unsigned long long)sectors);
 }
 
+// Chain-only variant (the "split" form): lanes run only the vector searches,
+// with the smallest possible loop, and append every change point to the
+// device queue; a drain launch of batched_search_kernel then expands them.
+template <int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, BatchedParams p, int chunk) {
+  const uint32_t n_chains = 4u * p.n_reads;
+  uint32_t rs = 0;
+  const uint8_t* W = nullptr;
+  int len = 0;
+  uint32_t k = 0, l = 0, pk = 0, pl = 0;
+  int pos = 0, dir = 0;
+  uint32_t nb = 0;
+  bool active = false;
+  uint32_t next = 0, left = 0;
+  for (;;) {
+    while (!active) {
+      if (left == 0) {
+        next = claim(p.chain_ctr, (unsigned)chunk);
+        left = (unsigned)chunk;
+      }
+      if (next >= n_chains) break;
+      const uint32_t c = next++;
+      --left;
+      const uint32_t read = c >> 2;
+      const uint64_t b0 = p.offs[read];
+      const int L = (int)(p.offs[read + 1] - b0);
+      if (!p.ok[read] || L < 3 || L > 32767) continue;
+      rs = (read << 1) | ((c >> 1) & 1u);
+      W = p.codes + b0;
+      len = L;
+      k = 0;
+      l = X.top;
+      pk = 0;
+      pl = X.top;
+      dir = (c & 1u) ? 1 : -1;
+      pos = (c & 1u) ? 0 : L - 1;
+      nb = W[pos];
+      active = true;
+    }
+    if (!active) break;
+    const int stop = dir > 0 ? len - 1 : 0;
+    // next base, fetched alongside the gather instead of after it
+    const uint32_t nb_next = pos != stop ? W[pos + dir] : 0u;
+    {
+      const uint32_t strand = rs & 1u;
+      bw_step(X, View{(dir > 0 ? 1u : 0u) ^ strand, strand}, nb, k, l);
+    }
+    const int J = pos - dir, n = len - 1;
+    const int jlo = dir > 0 ? n / 2 - 1 : 2, jhi = dir > 0 ? n - 1 : n / 2;
+    const bool differ = (l - k) != (pl - pk);
+    if (differ && J >= jlo && J <= jhi) {
+      const uint32_t jt = (uint32_t)J | ((dir > 0 ? (J == n - 1 ? kBlkN : kCpFwd) : kCpBwd) << 16);
+      const unsigned s = claim(p.spill_tail, 1);
+      if (s < p.spill_cap) p.spill[s] = SpillEntry{pk, pl, rs, jt};
+      else atomicOr(p.status, kStatusSpillFull);
+    }
+    if (k <= l && pos != stop) {
+      pk = k;
+      pl = l;
+      pos += dir;
+      nb = nb_next;
+      continue;
+    }
+    if (dir < 0 && pos == 0) {
+      if (k <= l) emit_hit(p, rs, order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
+      if (differ) {
+        const unsigned s = claim(p.spill_tail, 1);
+        if (s < p.spill_cap) p.spill[s] = SpillEntry{pk, pl, rs, 1u | (kBlk1 << 16)};
+        else atomicOr(p.status, kStatusSpillFull);
+      }
+    }
+    active = false;
+  }
+}
+
 // ------------------------------------------------------------- finalize --
 
 __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const unsigned int* res_total,
@@ -464,6 +539,16 @@ __global__ void __launch_bounds__(kBlock)
   if (census) atomicAdd(census, (unsigned long long)sectors);
 }
 
+template <int MINB>
+void launch_chain_m(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, cudaStream_t s) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<MINB>, kBlock, 0);
+  if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+  if (per_sm < 1) per_sm = 1;
+  count_launches(1);
+  chain_kernel<MINB><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, t.chunk < 1 ? 1 : t.chunk);
+}
+
 template <int D, int MINB>
 void launch_search_dm(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                       cudaStream_t s) {
@@ -506,6 +591,17 @@ int occupancy_d(const BatchedTuning& t) {
 }  // namespace
 
 int batched_max_blocks_per_sm(const BatchedTuning& t) {
+  if (t.split) {
+    int per_sm = 0;
+    if (t.min_blocks >= 16)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<16>, kBlock, 0);
+    else if (t.min_blocks >= 12)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<12>, kBlock, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<1>, kBlock, 0);
+    if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+    return per_sm;
+  }
   if (t.stack <= 2) return occupancy_d<2>(t);
   if (t.stack <= 4) return occupancy_d<4>(t);
   return occupancy_d<8>(t);
@@ -513,6 +609,15 @@ int batched_max_blocks_per_sm(const BatchedTuning& t) {
 
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                            cudaStream_t s) {
+  if (t.split && !drain) {  // chains only; every change point goes to the queue
+    if (t.min_blocks >= 16)
+      launch_chain_m<16>(X, p, t, num_sms, s);
+    else if (t.min_blocks >= 12)
+      launch_chain_m<12>(X, p, t, num_sms, s);
+    else
+      launch_chain_m<1>(X, p, t, num_sms, s);
+    return;
+  }
   if (t.stack <= 2)
     launch_search_d<2>(X, p, t, num_sms, drain, s);
   else if (t.stack <= 4)

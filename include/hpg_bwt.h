@@ -151,14 +151,15 @@ void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
 /* Batched-form tuning: register bound (1 = compiler's choice, 12 or 16
  * resident 128-thread blocks per SM), resident blocks per SM actually
  * launched (0 = occupancy limit), change points per lane held in shared
- * memory (2, 4 or 8; more spill to the device queue), chains claimed per
- * refill (1..8).  get: {threads per block, blocks per SM, stack depth,
+ * memory (2, 4 or 8; more spill to the device queue; 0 = split form: a
+ * chain-only kernel queues every change point for the drain launch), chains
+ * claimed per refill (1..8).  get: {threads per block, blocks per SM, stack depth,
  * chains per claim, register bound}. */
 void bwt_gpu_set_tuning(bwt_index_t *index, int min_blocks, int blocks_per_sm, int stack_depth,
                         int chains_per_claim);
 void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
 /* Autotuner: times the batched search on a device-resident read batch for
- * every candidate setting (27) and keeps the fastest.  Optional table gets
+ * every candidate setting (36) and keeps the fastest.  Optional table gets
  * rows of {min_blocks, blocks_per_sm, stack, chains_per_claim, search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
