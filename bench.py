@@ -365,7 +365,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                           "stages_ms": [round(x, 3) for x in v["stages"]], "sectors_per_read": round(v["sectors"] / n, 2)}
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
-            "tuning": gi.get_tuning(),
+            "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }

@@ -256,6 +256,16 @@ void bwt_gpu_get_tuning(bwt_index_t* index, int* out5) {
   if (e && out5) engine_get_tuning(e, out5);
 }
 
+void bwt_gpu_set_load_mode(bwt_index_t* index, int mode) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_load_mode(e, mode);
+}
+
+int bwt_gpu_load_mode(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_load_mode(e) : -1;
+}
+
 int bwt_gpu_autotune(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int* table, int max_rows,
                      int* rows) {

@@ -257,6 +257,7 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   if ((ce = cudaMalloc(&en->d_err, 4)) != cudaSuccess) return fail("cudaMalloc(err)", ce);
   cudaMemset(en->d_err, 0, 4);
   en->X.err = en->d_err;
+  en->X.load_mode = 2;
 
   for (int b = 0; b < 4; ++b) {
     en->X.C[b] = h.C[b];
@@ -451,6 +452,9 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
   e->tuning.chunk = chunk < 1 ? 1 : (chunk > 8 ? 8 : chunk);
 }
 
+void engine_set_load_mode(Engine* e, int mode) { e->X.load_mode = (uint32_t)(mode < 0 ? 0 : (mode > 3 ? 3 : mode)); }
+int engine_load_mode(Engine* e) { return (int)e->X.load_mode; }
+
 void engine_get_tuning(Engine* e, int* out5) {
   out5[0] = e->tuning.block;
   out5[1] = batched_max_blocks_per_sm(e->tuning);
@@ -498,6 +502,32 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
         }
       }
   e->tuning = best;
+  // then the block-load form, with the chosen setting
+  uint32_t best_mode = e->X.load_mode;
+  for (int mode = 0; mode < 4; ++mode) {
+    e->X.load_mode = (uint32_t)mode;
+    float t = 0;
+    for (int rep = 0; rep < 2; ++rep) {
+      if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases, max_len,
+                               max_results, &r, err) != 0)
+        return -1;
+      t = e->stage_ms[kStageSearch];
+    }
+    if (table && rows < max_rows) {
+      int* row = table + 5 * rows;
+      row[0] = -1 - mode;  // load-mode rows are marked by a negative first column
+      row[1] = batched_max_blocks_per_sm(e->tuning);
+      row[2] = e->tuning.split ? 0 : e->tuning.stack;
+      row[3] = e->tuning.chunk;
+      row[4] = (int)(t * 1000.0f);
+    }
+    ++rows;
+    if (t < best_ms) {
+      best_ms = t;
+      best_mode = (uint32_t)mode;
+    }
+  }
+  e->X.load_mode = best_mode;
   if (rows_out) *rows_out = rows;
   return 0;
 }

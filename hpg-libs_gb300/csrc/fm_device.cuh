@@ -50,6 +50,7 @@ struct DevIndex {
   const uint64_t* kar_start;
   uint32_t kar_size;
   uint32_t* err;          // device error word (bit 0: LF walk exceeded n+1 steps)
+  uint32_t load_mode;     // how blocks are fetched, see load_block()
 };
 
 constexpr uint32_t kErrWalk = 1u;
@@ -70,14 +71,39 @@ __device__ __forceinline__ uint32_t sel4(const uint32_t (&a)[4], uint32_t p) {
   return (p & 2u) ? hi : lo;
 }
 
+// Block fetch.  mode 0: two 16-byte loads through L1; 1: one 32-byte load;
+// 2: one 32-byte load that skips L1 and asks L2 to keep the line (evict_last),
+// so the index outlives the streamed reads and outputs in L2; 3: 32-byte load
+// with the L2 hint only.  The mode is uniform across a launch.
+__device__ __forceinline__ void load_block_m(const OccBlock* p, uint32_t mode, uint32_t (&cnt)[4], uint4& bits) {
+  if (mode == 0) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+    const uint4 c = __ldg(q);
+    bits = __ldg(q + 1);
+    cnt[0] = c.x;
+    cnt[1] = c.y;
+    cnt[2] = c.z;
+    cnt[3] = c.w;
+  } else if (mode == 1) {
+    asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
+                   "=r"(bits.w)
+                 : "l"(p));
+  } else if (mode == 2) {
+    asm volatile("ld.global.nc.L1::no_allocate.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
+                   "=r"(bits.w)
+                 : "l"(p));
+  } else {
+    asm volatile("ld.global.nc.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
+                   "=r"(bits.w)
+                 : "l"(p));
+  }
+}
+
 __device__ __forceinline__ void load_block(const OccBlock* p, uint32_t (&cnt)[4], uint4& bits) {
-  const uint4* q = reinterpret_cast<const uint4*>(p);
-  uint4 c = __ldg(q);
-  bits = __ldg(q + 1);
-  cnt[0] = c.x;
-  cnt[1] = c.y;
-  cnt[2] = c.z;
-  cnt[3] = c.w;
+  load_block_m(p, 0, cnt, bits);
 }
 
 // One bit per row of the block: set where the row's code is p.
@@ -142,7 +168,7 @@ __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, u
   const bool a0 = (p == 0) && (q0 == (D.dollar >> 6));  // '$' block correction applies
   uint32_t cnt[4];
   uint4 bits;
-  load_block(D.occ + q0, cnt, bits);
+  load_block_m(D.occ + q0, X.load_mode, cnt, bits);
   uint64_t m = match_mask(bits, p);
   const uint32_t c0 = sel4(cnt, p);
   const uint32_t rk = c0 + (uint32_t)__popcll(m & prefix_mask(k & 63)) - ((a0 && k > D.dollar) ? 1u : 0u);
@@ -150,7 +176,7 @@ __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, u
   if (q1 == q0) {
     rl = c0 + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a0 && l >= D.dollar) ? 1u : 0u);
   } else {
-    load_block(D.occ + q1, cnt, bits);
+    load_block_m(D.occ + q1, X.load_mode, cnt, bits);
     m = match_mask(bits, p);
     const bool a1 = (p == 0) && (q1 == (D.dollar >> 6));
     rl = sel4(cnt, p) + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a1 && l >= D.dollar) ? 1u : 0u);
@@ -166,7 +192,7 @@ __device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, 
   const uint32_t q = i >> 6, r = i & 63;
   uint32_t cnt[4];
   uint4 bits;
-  load_block(D.occ + q, cnt, bits);
+  load_block_m(D.occ + q, X.load_mode, cnt, bits);
   const uint32_t lo = r < 32 ? bits.x : bits.y, hi = r < 32 ? bits.z : bits.w;
   const uint32_t b = ((lo >> (r & 31)) & 1u) | (((hi >> (r & 31)) & 1u) << 1);
   return sel4(X.C, b) + rank_block(D, q, b, r + 1, cnt, bits);

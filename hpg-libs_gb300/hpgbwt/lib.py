@@ -88,6 +88,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.bwt_gpu_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    lib.bwt_gpu_set_load_mode.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_load_mode.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
@@ -198,8 +200,15 @@ class GpuIndex:
         rows = ctypes.c_int()
         self._check(self.lib.bwt_gpu_autotune(self.handle, d_seqs, d_offs, n_reads, total_bases, max_len,
                                               max_results, table, 64, ctypes.byref(rows)))
+        rows.value = min(rows.value, 64)
         return [{"register_bound_blocks": table[5 * i], "blocks_per_sm": table[5 * i + 1], "stack": table[5 * i + 2],
                  "chains_per_claim": table[5 * i + 3], "search_us": table[5 * i + 4]} for i in range(rows.value)]
+
+    def set_load_mode(self, mode: int) -> None:
+        self.lib.bwt_gpu_set_load_mode(self.handle, mode)
+
+    def load_mode(self) -> int:
+        return int(self.lib.bwt_gpu_load_mode(self.handle))
 
     def index_bytes(self) -> int:
         return int(self.lib.bwt_gpu_index_bytes(self.handle))

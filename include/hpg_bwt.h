@@ -158,9 +158,16 @@ void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
 void bwt_gpu_set_tuning(bwt_index_t *index, int min_blocks, int blocks_per_sm, int stack_depth,
                         int chains_per_claim);
 void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
+/* How occurrence blocks are fetched by every kernel of this index: 0 two
+ * 16-byte loads; 1 one 32-byte load; 2 one 32-byte load that bypasses L1 and
+ * marks the line evict-last in L2 (default); 3 32-byte load, L2 hint only. */
+void bwt_gpu_set_load_mode(bwt_index_t *index, int mode);
+int bwt_gpu_load_mode(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
- * every candidate setting (36) and keeps the fastest.  Optional table gets
- * rows of {min_blocks, blocks_per_sm, stack, chains_per_claim, search us}. */
+ * every candidate setting (36), keeps the fastest, then picks the fastest
+ * block-load form for it (4 more runs).  Optional table gets rows of
+ * {min_blocks (or -1 - load mode), blocks_per_sm, stack, chains_per_claim,
+ * search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
                      int *rows);
