@@ -16,7 +16,7 @@ using namespace hpgbwt;
 
 namespace hpgbwt {
 int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s,
-                   std::string* err);
+                   std::string* err, uint32_t work);
 }
 
 namespace {
@@ -235,8 +235,16 @@ unsigned long long bwt_gpu_launch_count(void) { return launch_count(); }
 
 int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s) {
   std::string err;
-  if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err) != 0)
+  if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err, 0) != 0)
     return fail(err.empty() ? "bwt_gpu_gather_ceiling: null argument" : err);
+  return 0;
+}
+
+int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
+                         double* sectors_per_s) {
+  std::string err;
+  if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err, work) != 0)
+    return fail(err.empty() ? "bwt_gpu_gather_probe: null argument" : err);
   return 0;
 }
 

@@ -85,17 +85,17 @@ __device__ __forceinline__ void load_block_m(const OccBlock* p, uint32_t mode, u
     cnt[2] = c.z;
     cnt[3] = c.w;
   } else if (mode == 1) {
-    asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
                    "=r"(bits.w)
                  : "l"(p));
   } else if (mode == 2) {
-    asm volatile("ld.global.nc.L1::no_allocate.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.L1::no_allocate.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
                    "=r"(bits.w)
                  : "l"(p));
   } else {
-    asm volatile("ld.global.nc.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+    asm("ld.global.nc.L2::evict_last.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(cnt[0]), "=r"(cnt[1]), "=r"(cnt[2]), "=r"(cnt[3]), "=r"(bits.x), "=r"(bits.y), "=r"(bits.z),
                    "=r"(bits.w)
                  : "l"(p));

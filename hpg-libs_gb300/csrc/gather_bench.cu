@@ -33,7 +33,7 @@ __global__ void gather_fill_kernel(uint4* buf, uint64_t n16, uint32_t seed) {
 }
 
 __global__ void __launch_bounds__(128) gather_chain_kernel(const uint4* __restrict__ buf, uint32_t nsec,
-                                                            uint32_t steps, uint32_t seed,
+                                                            uint32_t steps, uint32_t seed, uint32_t work,
                                                             unsigned long long* sink) {
   const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t x = (uint32_t)(((uint64_t)mix32(tid ^ seed) * nsec) >> 32);
@@ -41,8 +41,10 @@ __global__ void __launch_bounds__(128) gather_chain_kernel(const uint4* __restri
   for (uint32_t s = 0; s < steps; ++s) {
     const uint4 a = __ldg(buf + 2ull * x);
     const uint4 b = __ldg(buf + 2ull * x + 1);
+    uint32_t h = a.x + s + b.z;
+    for (uint32_t w = 0; w < work; ++w) h = mix32(h);  // dependent ALU work between gathers
     acc += a.y ^ b.w;
-    x = (uint32_t)(((uint64_t)mix32(a.x + s + b.z) * nsec) >> 32);
+    x = (uint32_t)(((uint64_t)mix32(h) * nsec) >> 32);
   }
   if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
 }
@@ -50,9 +52,10 @@ __global__ void __launch_bounds__(128) gather_chain_kernel(const uint4* __restri
 }  // namespace
 
 // Sectors per second of dependent random 32-byte sector reads over a buffer
-// of `bytes`, with `blocks` x 128 threads each following `steps` hops.
+// of `bytes`, with `blocks` x 128 threads each following `steps` hops and
+// `work` dependent hash rounds between hops.
 int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s,
-                   std::string* err) {
+                   std::string* err, uint32_t work) {
   if (cudaSetDevice(device) != cudaSuccess) {
     *err = "cudaSetDevice failed";
     return -1;
@@ -77,9 +80,9 @@ int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, do
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  gather_chain_kernel<<<blocks, 128, 0, s>>>(buf, (uint32_t)nsec, steps / 4 + 1, 7u, sink);  // warm-up
+  gather_chain_kernel<<<blocks, 128, 0, s>>>(buf, (uint32_t)nsec, steps / 4 + 1, 7u, work, sink);  // warm-up
   cudaEventRecord(a, s);
-  gather_chain_kernel<<<blocks, 128, 0, s>>>(buf, (uint32_t)nsec, steps, 99u, sink);
+  gather_chain_kernel<<<blocks, 128, 0, s>>>(buf, (uint32_t)nsec, steps, 99u, work, sink);
   cudaEventRecord(b, s);
   cudaError_t ce = cudaStreamSynchronize(s);
   float ms = 0;

@@ -97,6 +97,7 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_index_bytes.restype = sz
     lib.bwt_gpu_index_bytes.argtypes = [vp]
     lib.bwt_gpu_gather_ceiling.argtypes = [ctypes.c_int, sz, u32, u32, ctypes.POINTER(ctypes.c_double)]
+    lib.bwt_gpu_gather_probe.argtypes = [ctypes.c_int, sz, u32, u32, u32, ctypes.POINTER(ctypes.c_double)]
     lib.hpg_bwt_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
                                         ctypes.c_char_p, ctypes.c_char_p, sz]
     _lib = lib
@@ -111,6 +112,14 @@ def gather_ceiling(device: int, nbytes: int, blocks: int, steps: int) -> float:
     lib = load()
     v = ctypes.c_double()
     if lib.bwt_gpu_gather_ceiling(device, nbytes, blocks, steps, ctypes.byref(v)) != 0:
+        raise RuntimeError(lib.bwt_gpu_last_error().decode())
+    return v.value
+
+
+def gather_probe(device: int, nbytes: int, blocks: int, steps: int, work: int) -> float:
+    lib = load()
+    v = ctypes.c_double()
+    if lib.bwt_gpu_gather_probe(device, nbytes, blocks, steps, work, ctypes.byref(v)) != 0:
         raise RuntimeError(lib.bwt_gpu_last_error().decode())
     return v.value
 

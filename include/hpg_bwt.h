@@ -178,6 +178,10 @@ size_t bwt_gpu_index_bytes(bwt_index_t *index);
 /* Measured ceiling of dependent random 32-byte sector reads over a buffer of
  * `bytes` on `device` (blocks x 128 threads, `steps` hops each), in sectors/s. */
 int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double *sectors_per_s);
+/* The same gather with `work` dependent hash rounds between hops (how much
+ * per-step arithmetic the memory system hides at a given occupancy). */
+int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
+                         double *sectors_per_s);
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
