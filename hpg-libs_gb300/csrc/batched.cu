@@ -27,25 +27,35 @@ __device__ __forceinline__ uint32_t order_key(uint32_t section, uint32_t t, uint
   return (section << 28) | (t << 8) | slot;
 }
 
-__device__ __forceinline__ void emit_hit(const BatchedParams& p, uint32_t rs, uint32_t key, uint32_t k, uint32_t l,
-                                         uint32_t meta) {
-  const uint32_t idx = atomicAdd(&p.rs_count[rs], 1u);
-  cg::coalesced_group g = cg::coalesced_threads();
-  unsigned base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(p.res_total, (unsigned)g.size());
-  base = g.shfl(base, 0) + g.thread_rank();
-  if (base < p.res_cap) {
+// Pool slots are reserved per lane in chunks, so an emission normally waits on
+// no atomic: the per-list arrival count is a fire-and-forget reduction and
+// the list position is assigned later by the scatter kernel.
+constexpr unsigned kResChunk = 8;
+
+__device__ __forceinline__ void write_hit(const BatchedParams& p, unsigned slot, uint32_t rs, uint32_t key,
+                                          uint32_t k, uint32_t l, uint32_t meta) {
+  atomicAdd(&p.rs_count[rs], 1u);  // result unused: compiles to a reduction
+  if (slot < p.res_cap) {
     PendingHit h;
     h.rs = rs;
     h.key = key;
     h.k = k;
     h.l = l;
     h.meta = meta;
-    h.idx = idx;
-    p.res[base] = h;
+    h.idx = 0;
+    p.res[slot] = h;
   } else {
     atomicOr(p.status, kStatusResFull);
   }
+}
+
+__device__ __forceinline__ void emit_hit(const BatchedParams& p, uint32_t rs, uint32_t key, uint32_t k, uint32_t l,
+                                         uint32_t meta) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(p.res_total, (unsigned)g.size());
+  base = g.shfl(base, 0) + g.thread_rank();
+  write_hit(p, base, rs, key, k, l, meta);
 }
 
 __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
@@ -53,6 +63,22 @@ __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
   unsigned base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(ctr, (unsigned)g.size() * n);
   return g.shfl(base, 0) + g.thread_rank() * n;
+}
+
+// Chunked pool slot for the calling lane (cold state c_res = next slot | left << 28).
+__device__ __forceinline__ unsigned res_slot(const BatchedParams& p, uint32_t& c_res) {
+  unsigned left = c_res >> 28;
+  if (left == 0) {
+    c_res = claim(p.res_total, kResChunk);
+    left = kResChunk;
+    if (c_res >= (1u << 28)) {  // beyond what the packed form holds: fall back to single slots
+      c_res = 0;
+      return claim(p.res_total, 1) | 0u;
+    }
+  }
+  const unsigned slot = c_res & 0x0FFFFFFFu;
+  c_res = (slot + 1) | ((left - 1) << 28);
+  return slot;
 }
 
 // Lane modes.
@@ -75,13 +101,13 @@ template <int D, int MINB, bool CENSUS>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
-  __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_next[kBlock], c_misc[kBlock];
+  __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_misc[kBlock], c_res[kBlock];
   const int tid = threadIdx.x;
   const uint32_t n_chains = 4u * p.n_reads;
   const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
   c_meta[tid] = 0;
   c_misc[tid] = 0;
-  c_next[tid] = 0;
+  c_res[tid] = 0;
 
   // hot state
   uint32_t rs = 0;                  // 2 * read + strand
@@ -93,6 +119,19 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   uint32_t nb = 0;                  // base of the pending step
   uint32_t mode = kNone;
   uint32_t sectors = 0;
+  // read-level work: the current read's next chain, and the next read claimed
+  // and its offsets fetched ahead of time (their loads complete while the
+  // current read is searched)
+  uint32_t cur_read = 0, chain = 4;
+  uint32_t nxt_read = drain ? 0xFFFFFFFFu : claim(p.chain_ctr, 1);
+  uint64_t nxt_b0 = 0, nxt_b1 = 0;
+  uint32_t nxt_ok = 0;
+  if (nxt_read < p.n_reads) {
+    nxt_b0 = p.offs[nxt_read];
+    nxt_b1 = p.offs[nxt_read + 1];
+    nxt_ok = p.ok[nxt_read];
+  }
+  (void)chunk;
 
   auto push = [&](uint32_t a, uint32_t b, uint32_t jt) {
     const uint32_t misc = c_misc[tid];
@@ -109,6 +148,12 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     }
   };
   // Result of a continuation search that matched to the read end.
+  auto emit = [&](uint32_t key, uint32_t a, uint32_t b, uint32_t meta) {
+    uint32_t r = c_res[tid];
+    const unsigned slot = res_slot(p, r);
+    c_res[tid] = r;
+    write_hit(p, slot, rs, key, a, b, meta);
+  };
   auto emit_cont = [&](uint32_t m) {
     const uint32_t ej = meta_j(m), sub = meta_sub(m);
     const bool bwd = meta_type(m) == kCpBwd;
@@ -118,9 +163,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     const uint32_t slot = sub == 0 ? 0u : (ins ? 1u + 2 * b : 2u + 2 * b);
     const uint32_t basev = sub == 0 ? 0xFFu : b;
     if (bwd)
-      emit_hit(p, rs, order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
+      emit(order_key(2, ej, slot), k, l, pack_meta(0, 1, kind, basev, (int32_t)ej - 1));
     else
-      emit_hit(p, rs, order_key(4, (uint32_t)(len - 1 - (int)ej), slot), k, l,
+      emit(order_key(4, (uint32_t)(len - 1 - (int)ej), slot), k, l,
                pack_meta(1, 1, kind, basev, (int32_t)ej + 1));
   };
 
@@ -141,9 +186,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         if (sub == 0) {
           if (blk) {  // the block's direct deletion result
             if (etype == kBlk1)
-              emit_hit(p, rs, order_key(1, 0, 0), c_ek[tid], c_el[tid], pack_meta(0, 1, 1, 0xFF, 0));
+              emit(order_key(1, 0, 0), c_ek[tid], c_el[tid], pack_meta(0, 1, 1, 0xFF, 0));
             else
-              emit_hit(p, rs, order_key(3, 0, 0), c_ek[tid], c_el[tid], pack_meta(1, 1, 1, 0xFF, end));
+              emit(order_key(3, 0, 0), c_ek[tid], c_el[tid], pack_meta(1, 1, 1, 0xFF, end));
             c_meta[tid] = m + (1u << 18);
             continue;
           }
@@ -211,28 +256,31 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         c_meta[tid] = make_meta(e.jtype & 0xFFFFu, e.jtype >> 16, 0, 0, true);
         continue;
       }
-      uint32_t left = misc >> 4, next = c_next[tid];
-      if (left == 0) {
-        next = claim(p.chain_ctr, (unsigned)chunk);
-        left = (unsigned)chunk;
+      if (chain >= 4) {  // next read: switch to the prefetched one, prefetch the one after
+        if (nxt_read >= p.n_reads) break;
+        cur_read = nxt_read;
+        const uint64_t b0 = nxt_b0;
+        const int L = (int)(nxt_b1 - nxt_b0);
+        const uint32_t okr = nxt_ok;
+        nxt_read = claim(p.chain_ctr, 1);
+        if (nxt_read < p.n_reads) {
+          nxt_b0 = p.offs[nxt_read];
+          nxt_b1 = p.offs[nxt_read + 1];
+          nxt_ok = p.ok[nxt_read];
+        }
+        if (!okr || L < 3 || L > 32767) continue;
+        W = p.codes + b0;
+        len = L;
+        chain = 0;
       }
-      if (next >= n_chains) break;
-      const uint32_t c = next;
-      c_next[tid] = next + 1;
-      c_misc[tid] = (left - 1) << 4;
-      const uint32_t read = c >> 2;
-      const uint64_t b0 = p.offs[read];
-      const int L = (int)(p.offs[read + 1] - b0);
-      if (!p.ok[read] || L < 3 || L > 32767) continue;
-      rs = (read << 1) | ((c >> 1) & 1u);
-      W = p.codes + b0;
-      len = L;
+      const uint32_t c = chain++;  // 0: '+' backward, 1: '+' forward, 2: '-' backward, 3: '-' forward
+      rs = (cur_read << 1) | (c >> 1);
       k = 0;
       l = X.top;
       pk = 0;
       pl = X.top;
-      dir = (c & 1u) ? 1 : -1;  // forward / backward vector search
-      pos = (c & 1u) ? 0 : L - 1;
+      dir = (c & 1u) ? 1 : -1;
+      pos = (c & 1u) ? 0 : len - 1;
       nb = W[pos];
       mode = kChain;
     }
@@ -263,7 +311,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         continue;
       }
       if (dir < 0 && pos == 0) {  // backward vector complete: exact hit, then the j = 1 block on vec[1]
-        if (k <= l) emit_hit(p, rs, order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
+        if (k <= l) emit(order_key(0, 0, 0), k, l, pack_meta(0, 0, 0, 0, 0));
         if (differ) push(pk, pl, 1u | (kBlk1 << 16));
       }
       mode = kNone;
@@ -292,9 +340,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
             const uint32_t w = etype == kBlk1 ? W[0] : W[end];
             if (b != w) {
               if (etype == kBlk1)
-                emit_hit(p, rs, order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)meta_bpos(m)));
+                emit(order_key(1, 0, 1 + 2 * b), k, l, pack_meta(0, 1, 2, b, (int32_t)meta_bpos(m)));
               else
-                emit_hit(p, rs, order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
+                emit(order_key(3, 0, 1 + 2 * b), k, l, pack_meta(1, 1, 2, b, end));
             }
           }
           c_meta[tid] = m + (1u << 18);
@@ -303,16 +351,22 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         uint32_t nm = m + (2u << 18);
         if (k <= l) {
           if (etype == kBlk1) {
-            emit_hit(p, rs, order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
+            emit(order_key(1, 0, 2 + 2 * b), k, l, pack_meta(0, 1, 3, 3, (int32_t)b));
             nm = (nm & ~(3u << 22)) | (b << 22);
           } else {
-            emit_hit(p, rs, order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, len - 1));
+            emit(order_key(3, 0, 2 + 2 * b), k, l, pack_meta(1, 1, 3, b, len - 1));
           }
         }
         c_meta[tid] = nm;
       }
       mode = kNone;
     }
+  }
+  {  // slots of this lane's last chunk that were reserved but not used
+    const uint32_t r = c_res[tid];
+    const unsigned left = r >> 28, slot = r & 0x0FFFFFFFu;
+    for (unsigned i = 0; i < left; ++i)
+      if (slot + i < p.res_cap) p.res[slot + i].rs = 0xFFFFFFFFu;
   }
   if (CENSUS && p.census) atomicAdd(p.census, (unsigned long long)sectors);
 }
@@ -396,11 +450,12 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
 
 __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const unsigned int* res_total,
                                     const uint64_t* __restrict__ seg_off, PendingHit* __restrict__ sorted,
-                                    uint32_t res_cap) {
+                                    uint32_t res_cap, uint32_t* __restrict__ cursor) {
   const uint32_t n = min(*res_total, res_cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const PendingHit h = res[i];
-    sorted[seg_off[h.rs] + h.idx] = h;
+    if (h.rs == 0xFFFFFFFFu) continue;  // reserved but never written (chunk tail)
+    sorted[seg_off[h.rs] + atomicAdd(&cursor[h.rs], 1u)] = h;
   }
 }
 
@@ -627,9 +682,9 @@ void launch_batched_search(const DevIndex& X, const BatchedParams& p, const Batc
 }
 
 void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
-                         PendingHit* sorted, uint32_t res_cap, cudaStream_t s) {
+                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s) {
   count_launches(1);
-  scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap);
+  scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap, cursor);
 }
 
 void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,

@@ -28,7 +28,7 @@ struct PendingHit {
   uint32_t key;   // emission order within the (read, strand) list
   uint32_t k, l;
   uint32_t meta;  // packed as pack_meta()
-  uint32_t idx;   // arrival index within the (read, strand) list
+  uint32_t idx;   // unused (list positions are assigned by the scatter kernel)
 };
 
 // A spilled change point.
@@ -79,7 +79,7 @@ int batched_max_blocks_per_sm(const BatchedTuning& t);
 // Finalize: scatter pending hits into (read, strand) segments, sort each by
 // key, truncate; kept counts to `kept`, truncation flags to `trunc`.
 void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
-                         PendingHit* sorted, uint32_t res_cap, cudaStream_t s);
+                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s);
 void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
                           uint32_t* kept, uint8_t* trunc, cudaStream_t s);
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
