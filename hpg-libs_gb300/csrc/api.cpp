@@ -8,6 +8,7 @@
 #include <string>
 
 #include "engine.hpp"
+#include "fm_device.cuh"
 #include "kernels.cuh"
 #include "hpg_bwt.h"
 #include "index_format.hpp"
@@ -15,6 +16,10 @@
 using namespace hpgbwt;
 
 namespace hpgbwt {
+int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_ascii, const uint64_t* d_offs,
+                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err);
+DevIndex engine_dev_index(void* engine);
+const uint8_t* engine_code_table(void* engine);
 int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s,
                    std::string* err, uint32_t work);
 }
@@ -245,6 +250,18 @@ int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t ste
   std::string err;
   if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err, work) != 0)
     return fail(err.empty() ? "bwt_gpu_gather_probe: null argument" : err);
+  return 0;
+}
+
+int bwt_gpu_fm_probe(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* d_offsets, size_t n_reads,
+                     uint32_t reps, float* ms) {
+  Engine* e = engine_of(index);
+  if (!e || !ms) return fail("bwt_gpu_fm_probe: null argument");
+  std::string err;
+  cudaSetDevice(engine_device(e));
+  if (fm_chain_probe(engine_dev_index(e), engine_code_table(e), d_seqs, d_offsets, (uint32_t)n_reads, reps, ms,
+                     &err) != 0)
+    return fail(err);
   return 0;
 }
 

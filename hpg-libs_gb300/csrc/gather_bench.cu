@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <string>
 
+#include "fm_device.cuh"
+
 namespace hpgbwt {
 
 namespace {
@@ -49,7 +51,64 @@ __global__ void __launch_bounds__(128) gather_chain_kernel(const uint4* __restri
   if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
 }
 
+// Pure FM steps: one thread per read runs the full backward search of the read
+// over the backward index (no vectors, no branching, no output but a
+// checksum).  Reads taken from the forward strand keep every lane busy for
+// the whole read, so this is the best case of the real access pattern.
+__global__ void __launch_bounds__(128) fm_chain_probe_kernel(DevIndex X, const uint8_t* __restrict__ ascii,
+                                                             const uint64_t* __restrict__ offs, uint32_t n_reads,
+                                                             const uint8_t* __restrict__ table, uint32_t reps,
+                                                             unsigned long long* sink) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_reads) return;
+  const uint64_t b = offs[r];
+  const int len = (int)(offs[r + 1] - b);
+  uint32_t acc = 0;
+  for (uint32_t rep = 0; rep < reps; ++rep) {
+    uint32_t k = 0, l = X.top;
+    for (int i = len - 1; i >= 0; --i) {
+      const uint32_t c = table[ascii[b + i]] & 3u;
+      bw_step(X, View{0, 0}, c, k, l);
+      if (k > l) break;
+    }
+    acc += k ^ l;
+  }
+  if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
+}
+
 }  // namespace
+
+// Rank steps per second of fm_chain_probe_kernel over device reads.
+int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_ascii, const uint64_t* d_offs,
+                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err) {
+  unsigned long long* sink = nullptr;
+  if (cudaMalloc(&sink, 8) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "out of device memory";
+    return -1;
+  }
+  cudaStream_t s;
+  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const unsigned grid = (n_reads + 127) / 128;
+  fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, 1, sink);
+  cudaEventRecord(a, s);
+  fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, reps, sink);
+  cudaEventRecord(b, s);
+  const cudaError_t ce = cudaStreamSynchronize(s);
+  cudaEventElapsedTime(ms_out, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamDestroy(s);
+  cudaFree(sink);
+  if (ce != cudaSuccess) {
+    *err = std::string("fm probe: ") + cudaGetErrorString(ce);
+    return -1;
+  }
+  return 0;
+}
 
 // Sectors per second of dependent random 32-byte sector reads over a buffer
 // of `bytes`, with `blocks` x 128 threads each following `steps` hops and

@@ -182,6 +182,11 @@ int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t s
  * per-step arithmetic the memory system hides at a given occupancy). */
 int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
                          double *sectors_per_s);
+/* Best case of the real access pattern: one thread per read runs only the
+ * full backward search over the backward index, `reps` times (device reads as
+ * for bwt_gpu_search_device); device time in *ms. */
+int bwt_gpu_fm_probe(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
+                     uint32_t reps, float *ms);
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
