@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         const unsigned s = claim(p.spill_head, 1);
         if (s >= spill_end) break;
         const SpillEntry e = p.spill[s];
+        if (e.rs == 0xFFFFFFFFu) continue;  // reserved but unused slot
         rs = e.rs;
         const uint32_t read = rs >> 1;
         const uint64_t b0 = p.offs[read];
@@ -443,6 +444,138 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
       }
     }
     active = false;
+  }
+}
+
+// Lockstep variant: one lane per read runs the read's four vector searches
+// together -- '+' backward over the backward index, '-' backward over the
+// forward index with complemented bases, both moving down the read, and the
+// two forward searches moving up -- so every lane spends about one read length
+// per read whatever the strand, and up to four independent gathers are in
+// flight per lane.  Change points go to the device queue for the drain launch.
+__device__ __forceinline__ void spill_push(const BatchedParams& p, uint32_t& chunk_state, uint32_t a, uint32_t b,
+                                           uint32_t rs, uint32_t jt) {
+  unsigned left = chunk_state >> 28;
+  if (left == 0) {
+    chunk_state = claim(p.spill_tail, kResChunk);
+    left = kResChunk;
+    if (chunk_state >= (1u << 28)) {
+      chunk_state = 0;
+      const unsigned s1 = claim(p.spill_tail, 1);
+      if (s1 < p.spill_cap) p.spill[s1] = SpillEntry{a, b, rs, jt};
+      else atomicOr(p.status, kStatusSpillFull);
+      return;
+    }
+  }
+  const unsigned slot = chunk_state & 0x0FFFFFFFu;
+  chunk_state = (slot + 1) | ((left - 1) << 28);
+  if (slot < p.spill_cap) p.spill[slot] = SpillEntry{a, b, rs, jt};
+  else atomicOr(p.status, kStatusSpillFull);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) chain4_kernel(DevIndex X, BatchedParams p) {
+  __shared__ uint32_t c_res[kBlock], c_spill[kBlock];
+  const int tid = threadIdx.x;
+  c_res[tid] = 0;
+  c_spill[tid] = 0;
+  uint32_t read = claim(p.chain_ctr, 1);
+  uint32_t nxt = read < p.n_reads ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
+  uint64_t nb0 = 0, nb1 = 0;
+  uint32_t nok = 0;
+  if (nxt < p.n_reads) {
+    nb0 = p.offs[nxt];
+    nb1 = p.offs[nxt + 1];
+    nok = p.ok[nxt];
+  }
+  uint64_t b0 = 0, b1 = 0;
+  uint32_t okr = 0;
+  if (read < p.n_reads) {
+    b0 = p.offs[read];
+    b1 = p.offs[read + 1];
+    okr = p.ok[read];
+  }
+  while (read < p.n_reads) {
+    const int len = (int)(b1 - b0);
+    if (okr && len >= 3 && len <= 32767) {
+      const uint8_t* W = p.codes + b0;
+      const int n = len - 1;
+      // chains: 0 '+' bwd, 1 '+' fwd, 2 '-' bwd, 3 '-' fwd
+      uint32_t k0 = 0, l0 = X.top, k1 = 0, l1 = X.top, k2 = 0, l2 = X.top, k3 = 0, l3 = X.top;
+      uint32_t pk0 = 0, pl0 = X.top, pk1 = 0, pl1 = X.top, pk2 = 0, pl2 = X.top, pk3 = 0, pl3 = X.top;
+      uint32_t alive = 0xFu;
+      for (int t = 0; t <= n; ++t) {
+        const int jb = n - t, jf = t;
+        const uint32_t bb = W[jb], bf = W[jf];
+        if (alive & 1u) bw_step(X, View{0, 0}, bb, k0, l0);
+        if (alive & 2u) bw_step(X, View{1, 0}, bf, k1, l1);
+        if (alive & 4u) bw_step(X, View{1, 1}, bb, k2, l2);
+        if (alive & 8u) bw_step(X, View{0, 1}, bf, k3, l3);
+        // backward chains: entry at jb vs entry at J = jb + 1; window [2, n/2], block at J = 1
+        // forward chains:  entry at jf vs entry at J = jf - 1; window [n/2 - 1, n - 2], block at n - 1
+        const int Jb = jb + 1, Jf = jf - 1;
+        const bool wb = Jb >= 2 && Jb <= n / 2;
+        const bool wf = Jf >= n / 2 - 1 && Jf <= n - 1 && jf >= 1;
+        const uint32_t tf = (uint32_t)Jf | ((Jf == n - 1 ? kBlkN : kCpFwd) << 16);
+        const uint32_t tb = (uint32_t)Jb | (kCpBwd << 16);
+#define HPG_CHAIN_TAIL(I, K, L, PK, PL, WIN, JT, STRAND, BWD)                                      \
+  if (alive & (1u << I)) {                                                                         \
+    const bool differ = (L - K) != (PL - PK);                                                      \
+    if (differ && WIN) {                                                                           \
+      uint32_t cs = c_spill[tid];                                                                  \
+      spill_push(p, cs, PK, PL, (read << 1) | STRAND, JT);                                         \
+      c_spill[tid] = cs;                                                                           \
+    }                                                                                              \
+    if (K > L || (BWD ? jb == 0 : jf == n)) {                                                      \
+      if (BWD && jb == 0) {                                                                        \
+        const uint32_t rs_ = (read << 1) | STRAND;                                                 \
+        if (K <= L) {                                                                              \
+          uint32_t r = c_res[tid];                                                                 \
+          const unsigned slot = res_slot(p, r);                                                    \
+          c_res[tid] = r;                                                                          \
+          write_hit(p, slot, rs_, order_key(0, 0, 0), K, L, pack_meta(0, 0, 0, 0, 0));             \
+        }                                                                                          \
+        if (differ) {                                                                              \
+          uint32_t cs = c_spill[tid];                                                              \
+          spill_push(p, cs, PK, PL, rs_, 1u | (kBlk1 << 16));                                      \
+          c_spill[tid] = cs;                                                                       \
+        }                                                                                          \
+      }                                                                                            \
+      alive &= ~(1u << I);                                                                         \
+    } else {                                                                                       \
+      PK = K;                                                                                      \
+      PL = L;                                                                                      \
+    }                                                                                              \
+  }
+        HPG_CHAIN_TAIL(0, k0, l0, pk0, pl0, wb, tb, 0u, true)
+        HPG_CHAIN_TAIL(1, k1, l1, pk1, pl1, wf, tf, 0u, false)
+        HPG_CHAIN_TAIL(2, k2, l2, pk2, pl2, wb, tb, 1u, true)
+        HPG_CHAIN_TAIL(3, k3, l3, pk3, pl3, wf, tf, 1u, false)
+#undef HPG_CHAIN_TAIL
+        if (!alive) break;
+      }
+    }
+    // next read: the prefetched one; prefetch the one after
+    read = nxt;
+    b0 = nb0;
+    b1 = nb1;
+    okr = nok;
+    if (read < p.n_reads) {
+      nxt = claim(p.chain_ctr, 1);
+      if (nxt < p.n_reads) {
+        nb0 = p.offs[nxt];
+        nb1 = p.offs[nxt + 1];
+        nok = p.ok[nxt];
+      }
+    }
+  }
+  {  // reserved but unused slots of the last chunks
+    const uint32_t r = c_res[tid];
+    for (unsigned i = 0, left = r >> 28, slot = r & 0x0FFFFFFFu; i < left; ++i)
+      if (slot + i < p.res_cap) p.res[slot + i].rs = 0xFFFFFFFFu;
+    const uint32_t q = c_spill[tid];
+    for (unsigned i = 0, left = q >> 28, slot = q & 0x0FFFFFFFu; i < left; ++i)
+      if (slot + i < p.spill_cap) p.spill[slot + i].rs = 0xFFFFFFFFu;
   }
 }
 
@@ -646,6 +779,17 @@ int occupancy_d(const BatchedTuning& t) {
 }  // namespace
 
 int batched_max_blocks_per_sm(const BatchedTuning& t) {
+  if (t.split == 2) {
+    int per_sm = 0;
+    if (t.min_blocks >= 16)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<16>, kBlock, 0);
+    else if (t.min_blocks >= 12)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<12>, kBlock, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<1>, kBlock, 0);
+    if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+    return per_sm;
+  }
   if (t.split) {
     int per_sm = 0;
     if (t.min_blocks >= 16)
@@ -664,6 +808,24 @@ int batched_max_blocks_per_sm(const BatchedTuning& t) {
 
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                            cudaStream_t s) {
+  if (t.split == 2 && !drain) {  // lockstep chains, one lane per read
+    int per_sm = 0;
+    if (t.min_blocks >= 16) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<16>, kBlock, 0);
+      count_launches(1);
+      chain4_kernel<16><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p);
+    } else if (t.min_blocks >= 12) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<12>, kBlock, 0);
+      count_launches(1);
+      chain4_kernel<12><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p);
+    } else {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain4_kernel<1>, kBlock, 0);
+      if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+      count_launches(1);
+      chain4_kernel<1><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p);
+    }
+    return;
+  }
   if (t.split && !drain) {  // chains only; every change point goes to the queue
     if (t.min_blocks >= 16)
       launch_chain_m<16>(X, p, t, num_sms, s);

@@ -66,7 +66,8 @@ struct BatchedTuning {
   int stack = 4;          // change points per lane kept in shared memory (2, 4 or 8)
   int chunk = 1;          // chains claimed per lane per refill (1, 2 or 4)
   int min_blocks = 1;     // register bound: 1 (compiler's choice), 12 or 16 resident blocks per SM
-  int split = 0;          // 1: chain-only kernel + drain of every change point; 0: fused (per-lane stacks)
+  int split = 0;          // 0: fused (per-lane stacks); 1: chain-only kernel + drain of every change point;
+                          // 2: lockstep kernel (4 chains of a read per lane) + drain
 };
 
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u;

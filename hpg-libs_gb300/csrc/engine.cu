@@ -338,7 +338,8 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     return -1;
   }
   if (e->b_res_cap < 4 * (size_t)n + 4096) e->b_res_cap = (uint32_t)std::min<size_t>(4 * (size_t)n + 4096, 0xFFFFFFF0u);
-  const size_t spill_want = e->tuning.split ? 4 * (size_t)n + 4096 : (size_t)n / 4 + 4096;
+  const size_t spill_want = e->tuning.split ? 4 * (size_t)n + 4096 + (size_t)e->num_sms * 16 * 128 * 8
+                                            : (size_t)n / 4 + 4096;
   if (e->b_spill_cap < spill_want) e->b_spill_cap = (uint32_t)std::min<size_t>(spill_want, 0xFFFFFFF0u);
   unsigned int* ctr = ptr<unsigned int>(e->b_ctr);  // [0] chains [1] spill head [2] spill tail [3] results [4] status [5] rows
   uint32_t status = 0, res_total = 0;
@@ -445,7 +446,8 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
 }  // namespace
 
 void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, int chunk) {
-  e->tuning.split = stack <= 0 ? 1 : 0;  // stack depth 0 selects the split (chain-only) form
+  // stack depth 0 selects the split (chain-only) form, -1 the lockstep form
+  e->tuning.split = stack == 0 ? 1 : (stack < 0 ? 2 : 0);
   if (stack <= 0) stack = 2;
   e->tuning.min_blocks = min_blocks >= 16 ? 16 : (min_blocks >= 12 ? 12 : 1);
   e->tuning.blocks_per_sm = blocks_per_sm;
@@ -459,7 +461,7 @@ int engine_load_mode(Engine* e) { return (int)e->X.load_mode; }
 void engine_get_tuning(Engine* e, int* out5) {
   out5[0] = e->tuning.block;
   out5[1] = batched_max_blocks_per_sm(e->tuning);
-  out5[2] = e->tuning.split ? 0 : e->tuning.stack;
+  out5[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
   out5[3] = e->tuning.chunk;
   out5[4] = e->tuning.min_blocks;
 }
@@ -471,7 +473,7 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
                     uint32_t max_len, uint32_t max_results, int* table, int max_rows, int* rows_out,
                     std::string* err) {
   static const int cand_minb[] = {1, 12, 16};
-  static const int cand_stack[] = {0, 2, 4, 8};  // 0: split form
+  static const int cand_stack[] = {-1, 0, 2, 4, 8};  // 0: split form, -1: lockstep form
   static const int cand_chunk[] = {1, 2, 4};
   BatchedTuning best = e->tuning;
   float best_ms = 1e30f;
@@ -518,7 +520,7 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
       int* row = table + 5 * rows;
       row[0] = -1 - mode;  // load-mode rows are marked by a negative first column
       row[1] = batched_max_blocks_per_sm(e->tuning);
-      row[2] = e->tuning.split ? 0 : e->tuning.stack;
+      row[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
       row[3] = e->tuning.chunk;
       row[4] = (int)(t * 1000.0f);
     }

@@ -152,8 +152,9 @@ void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
  * resident 128-thread blocks per SM), resident blocks per SM actually
  * launched (0 = occupancy limit), change points per lane held in shared
  * memory (2, 4 or 8; more spill to the device queue; 0 = split form: a
- * chain-only kernel queues every change point for the drain launch), chains
- * claimed per refill (1..8).  get: {threads per block, blocks per SM, stack depth,
+ * chain-only kernel queues every change point for the drain launch; -1 =
+ * lockstep form: one lane per read advances the read's four vector searches
+ * together and queues change points), chains claimed per refill (1..8).  get: {threads per block, blocks per SM, stack depth,
  * chains per claim, register bound}. */
 void bwt_gpu_set_tuning(bwt_index_t *index, int min_blocks, int blocks_per_sm, int stack_depth,
                         int chains_per_claim);
@@ -164,7 +165,7 @@ void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
 void bwt_gpu_set_load_mode(bwt_index_t *index, int mode);
 int bwt_gpu_load_mode(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
- * every candidate setting (36), keeps the fastest, then picks the fastest
+ * every candidate setting (45), keeps the fastest, then picks the fastest
  * block-load form for it (4 more runs).  Optional table gets rows of
  * {min_blocks (or -1 - load mode), blocks_per_sm, stack, chains_per_claim,
  * search us}. */

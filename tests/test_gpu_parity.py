@@ -78,7 +78,8 @@ def test_chunked_equals_single_pass(case_factory):
 
 
 @pytest.mark.parametrize("stack,chunk,per_sm,minb", [(2, 1, 0, 1), (4, 2, 0, 12), (8, 4, 0, 16), (2, 8, 1, 1),
-                                                     (4, 1, 3, 16), (0, 4, 0, 1), (0, 1, 2, 12)])
+                                                     (4, 1, 3, 16), (0, 4, 0, 1), (0, 1, 2, 12), (-1, 1, 0, 1),
+                                                     (-1, 1, 0, 12), (-1, 1, 2, 16)])
 def test_batched_tunings_agree(case_factory, stack, chunk, per_sm, minb):
     """Every autotuner setting gives the oracle's answer; depth 2 forces spills to the drain path."""
     c = case_factory("human_like", 200_000, 5, 5)
@@ -100,9 +101,9 @@ def test_autotuner_keeps_results(case_factory):
     with lib.GpuIndex(c.index) as g:
         table = g.autotune(d_seq.data_ptr(), d_off.data_ptr(), len(reads), int(reads.offsets[-1]),
                            int(np.diff(reads.offsets).max()), 64)
-        assert len(table) == 40 and all(r["search_us"] > 0 for r in table)
+        assert len(table) == 49 and all(r["search_us"] > 0 for r in table)
         chosen = g.get_tuning()
-        best = min(table[:36], key=lambda r: r["search_us"])
+        best = min(table[:45], key=lambda r: r["search_us"])
         assert (chosen["stack"], chosen["chains_per_claim"]) == (best["stack"], best["chains_per_claim"])
         got = g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED, max_results=64)
     _assert_same(got, want)
