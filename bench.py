@@ -251,7 +251,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             step()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
-        stage_sum = [0.0, 0.0, 0.0, 0.0]
+        stage_sum = [0.0, 0.0, 0.0, 0.0, 0.0]
         dist.barrier()
         torch.cuda.synchronize()
         l0 = lib.launch_count()
@@ -274,7 +274,11 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     total_reads = dist.sum(float(n))
     # autotune the batched form on this batch (untimed)
     table = []
-    if not args.no_autotune:
+    if args.tuning:
+        st, ch, mb, lm = (int(x) for x in args.tuning.split(","))
+        gi.set_tuning(0, st, ch, mb)
+        gi.set_load_mode(lm)
+    elif not args.no_autotune:
         t0 = time.time()
         table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
         log(f"[bench] autotune: {len(table)} settings in {time.time() - t0:.1f}s, "
@@ -359,7 +363,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "cpu_baseline": base,
             "clocks": clk_summary,
             "stages_ms": {"encode": round(per_step[0], 3), "search": round(per_step[1], 3),
-                          "finalize": round(per_step[2], 3), "locate": round(per_step[3], 3)},
+                          "of_which_drain": round(per_step[4], 3), "finalize": round(per_step[2], 3),
+                          "locate": round(per_step[3], 3)},
             "hits_per_step": n_hits, "located_rows_per_step": n_locs,
             "forms": {k: {"reads_per_s": round(v["value"], 1), "ms_per_step": round(v["ms"] / args.steps, 3),
                           "stages_ms": [round(x, 3) for x in v["stages"]], "sectors_per_read": round(v["sectors"] / n, 2)}
@@ -415,6 +420,8 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
+    ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
+                                                 "block_load_mode (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]

@@ -59,6 +59,8 @@ struct Engine {
   unsigned long long census_val = 0;
   cudaEvent_t ev[kStageCount + 1];
   cudaEvent_t cev[4];
+  cudaEvent_t dev_mid = nullptr;  // between the search and the drain launch
+  float drain_ms = 0;
   float stage_ms[kStageCount] = {0, 0, 0, 0};
   DeviceResult last;
 };
@@ -231,6 +233,7 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
     return fail("cudaStreamCreate", ce);
   for (int i = 0; i <= kStageCount; ++i) cudaEventCreate(&en->ev[i]);
   for (int i = 0; i < 4; ++i) cudaEventCreate(&en->cev[i]);
+  cudaEventCreate(&en->dev_mid);
   const SampledVec* S[2] = {&h.S, &h.Si};
   for (int d = 0; d < 2; ++d) {
     if ((ce = cudaMalloc(&en->d_occ[d], blk[d].size() * sizeof(OccBlock))) != cudaSuccess)
@@ -320,6 +323,7 @@ size_t engine_index_bytes(Engine* e) {
 
 void engine_stage_ms(Engine* e, float* out, int n) {
   for (int i = 0; i < n && i < kStageCount; ++i) out[i] = e->stage_ms[i];
+  if (n > kStageCount) out[kStageCount] = e->drain_ms;  // of the search stage: time in the drain launch
 }
 
 namespace {
@@ -372,6 +376,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.census = census;
     cudaEventRecord(e->cev[0], s);
     launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
+    cudaEventRecord(e->dev_mid, s);
     launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
     cudaEventRecord(e->cev[1], s);
     uint32_t h[5];
@@ -434,6 +439,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   float ms = 0;
   cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
   *t_search += ms;
+  cudaEventElapsedTime(&e->drain_ms, e->dev_mid, e->cev[1]);
   cudaEventElapsedTime(&ms, e->cev[1], e->cev[2]);
   *t_final += ms;
   cudaEventElapsedTime(&ms, e->cev[2], e->cev[3]);
@@ -592,6 +598,7 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
   size_t n_hits = 0, n_locs = 0;
   float t_search = 0, t_final = 0, t_loc = 0;
   cudaEvent_t a = e->cev[0], b = e->cev[1], c = e->cev[2], d = e->cev[3];
+  e->drain_ms = 0;
   if (form == kFormBatched) {
     if (run_batched(e, d_seqs, d_offs, n, max_results, census, &n_hits, &n_locs, &t_search, &t_final, &t_loc, err) !=
         0)

@@ -185,8 +185,9 @@ class GpuIndex:
         return self.lib.bwt_gpu_stream(self.handle)
 
     def stage_ms(self) -> list[float]:
-        a = (ctypes.c_float * 4)()
-        self.lib.bwt_gpu_stage_ms(self.handle, a, 4)
+        """encode, search, finalize, locate, and the drain launch's share of search."""
+        a = (ctypes.c_float * 5)()
+        self.lib.bwt_gpu_stage_ms(self.handle, a, 5)
         return list(a)
 
     def set_census(self, on: bool) -> None:

@@ -141,7 +141,8 @@ int bwt_gpu_copy_result(bwt_index_t *index, const hpg_result_set_t *dev, hpg_hit
 
 /* The CUDA stream (cudaStream_t) every kernel of this index runs on. */
 void *bwt_gpu_stream(bwt_index_t *index);
-/* Device times (ms) of the last call: encode, search, finalize, locate. */
+/* Device times (ms) of the last call: encode, search, finalize, locate and,
+ * as a fifth value, the part of search spent in the drain launch. */
 void bwt_gpu_stage_ms(bwt_index_t *index, float *out, int n);
 /* Count touched 32-byte index sectors during searches (for roofline figures). */
 void bwt_gpu_set_census(bwt_index_t *index, int on);
