@@ -185,8 +185,10 @@ int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t s
 int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
                          double *sectors_per_s);
 /* Best case of the real access pattern: one thread per read runs only the
- * full backward search over the backward index, `reps` times (device reads as
- * for bwt_gpu_search_device); device time in *ms. */
+ * full exact search, (reps & 0xFFFF) times (device reads as for
+ * bwt_gpu_search_device); reps >> 16 selects backward search on the backward
+ * index (0), forward search on the forward index (1) or half of each (2).
+ * Device time in *ms. */
 int bwt_gpu_fm_probe(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint32_t reps, float *ms);
 /* Message of the last failed call on this thread. */
