@@ -375,9 +375,12 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
 // Chain-only variant (the "split" form): lanes run only the vector searches,
 // with the smallest possible loop, and append every change point to the
 // device queue; a drain launch of batched_search_kernel then expands them.
+// `phase` 0 runs only the chains on the backward index ('+' backward and '-'
+// forward), 1 only those on the forward index ('+' forward, '-' backward), so
+// each launch keeps one direction's occurrence blocks hot in L2; 2 runs all.
 template <int MINB>
-__global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, BatchedParams p, int chunk) {
-  const uint32_t n_chains = 4u * p.n_reads;
+__global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, BatchedParams p, int chunk, int phase) {
+  const uint32_t n_chains = (phase == 2 ? 4u : 2u) * p.n_reads;
   uint32_t rs = 0;
   const uint8_t* W = nullptr;
   int len = 0;
@@ -385,7 +388,7 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
   int pos = 0, dir = 0;
   uint32_t nb = 0;
   bool active = false;
-  uint32_t next = 0, left = 0;
+  uint32_t next = 0, left = 0, sectors = 0;
   for (;;) {
     while (!active) {
       if (left == 0) {
@@ -395,19 +398,21 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
       if (next >= n_chains) break;
       const uint32_t c = next++;
       --left;
-      const uint32_t read = c >> 2;
+      const uint32_t read = phase == 2 ? c >> 2 : c >> 1;
       const uint64_t b0 = p.offs[read];
       const int L = (int)(p.offs[read + 1] - b0);
       if (!p.ok[read] || L < 3 || L > 32767) continue;
-      rs = (read << 1) | ((c >> 1) & 1u);
+      const uint32_t strand = phase == 2 ? (c >> 1) & 1u : c & 1u;
+      const bool fwd = phase == 2 ? (c & 1u) != 0 : ((strand ^ (uint32_t)phase) != 0);
+      rs = (read << 1) | strand;
       W = p.codes + b0;
       len = L;
       k = 0;
       l = X.top;
       pk = 0;
       pl = X.top;
-      dir = (c & 1u) ? 1 : -1;
-      pos = (c & 1u) ? 0 : L - 1;
+      dir = fwd ? 1 : -1;
+      pos = fwd ? 0 : L - 1;
       nb = W[pos];
       active = true;
     }
@@ -417,6 +422,7 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
     const uint32_t nb_next = pos != stop ? W[pos + dir] : 0u;
     {
       const uint32_t strand = rs & 1u;
+      if (p.census) sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
       bw_step(X, View{(dir > 0 ? 1u : 0u) ^ strand, strand}, nb, k, l);
     }
     const int J = pos - dir, n = len - 1;
@@ -445,6 +451,7 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
     }
     active = false;
   }
+  if (p.census) atomicAdd(p.census, (unsigned long long)sectors);
 }
 
 // Lockstep variant: one lane per read runs the read's four vector searches
@@ -645,24 +652,31 @@ __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const 
 // direction and len_calc (bwt.c:2025-2036), so that a lane starting a walk
 // needs a single 16-byte load.
 struct RowItem {
-  uint32_t row, hit, phys, len_calc;
+  uint32_t row, hit, out, phys_len;  // out: output index; phys_len: direction << 31 | len_calc
 };
 
+// Rows on the backward index fill the item array from the front, rows on the
+// forward index from the back, so walks claimed in order touch one direction
+// at a time.
 __global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
-                                   uint32_t n_hits, const uint64_t* __restrict__ read_offs,
-                                   RowItem* __restrict__ items) {
+                                   uint32_t n_hits, uint64_t n_locs, const uint64_t* __restrict__ read_offs,
+                                   RowItem* __restrict__ items, unsigned int* __restrict__ side) {
   for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x) {
     const hpg_hit_t x = hits[h];
+    const uint64_t b = loc_off[h], e = loc_off[h + 1];
+    if (e == b) continue;
     const uint64_t len = read_offs[x.read + 1] - read_offs[x.read];
     const uint32_t err = x.nm ? x.err_kind : 0u;
+    const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir, type = !strand
     RowItem it;
     it.hit = h;
-    it.phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir, type = !strand
-    it.len_calc = (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
-    const uint64_t b = loc_off[h], e = loc_off[h + 1];
-    for (uint64_t r = b; r < e; ++r) {
-      it.row = (uint32_t)((uint64_t)x.k + (r - b));
-      items[r] = it;
+    it.phys_len = (phys << 31) | (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
+    const unsigned cnt = (unsigned)(e - b);
+    const unsigned at = atomicAdd(&side[phys], cnt);
+    for (unsigned i = 0; i < cnt; ++i) {
+      it.row = (uint32_t)((uint64_t)x.k + i);
+      it.out = (uint32_t)(b + i);
+      items[phys ? n_locs - 1 - (at + i) : at + i] = it;
     }
   }
 }
@@ -692,8 +706,9 @@ __global__ void __launch_bounds__(kBlock)
       j = 0;
       active = true;
     }
+    const uint32_t phys = it.phys_len >> 31;
     if (!sampled_row(X, i)) {
-      i = lf_step(X, dir_of(X, it.phys), i);
+      i = lf_step(X, dir_of(X, phys), i);
       ++sectors;
       if (++j > X.walk_mod) {
         atomicOr(X.err, kErrWalk);
@@ -701,12 +716,12 @@ __global__ void __launch_bounds__(kBlock)
       }
       continue;
     }
-    const DevDir D = dir_of(X, it.phys);
+    const DevDir D = dir_of(X, phys);
     const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
     ++sectors;
     const uint32_t sa = (s + j) % X.walk_mod;
-    const uint64_t len_calc = it.len_calc;
-    const uint64_t key = it.phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
+    const uint64_t len_calc = it.phys_len & 0x7FFFFFFFu;
+    const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
     const uint32_t id = kar_search(X, key);
     hpg_loc_t o;
     o.key = key;
@@ -721,20 +736,21 @@ __global__ void __launch_bounds__(kBlock)
       o.chrom = 0;
       o.position = 0;
     }
-    out[r] = o;
+    out[it.out] = o;
     active = false;
   }
   if (census) atomicAdd(census, (unsigned long long)sectors);
 }
 
 template <int MINB>
-void launch_chain_m(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, cudaStream_t s) {
+void launch_chain_m(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, int phase,
+                    cudaStream_t s) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<MINB>, kBlock, 0);
   if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
   if (per_sm < 1) per_sm = 1;
   count_launches(1);
-  chain_kernel<MINB><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, t.chunk < 1 ? 1 : t.chunk);
+  chain_kernel<MINB><<<num_sms * per_sm, kBlock, 0, s>>>(X, p, t.chunk < 1 ? 1 : t.chunk, phase);
 }
 
 template <int D, int MINB>
@@ -827,12 +843,13 @@ void launch_batched_search(const DevIndex& X, const BatchedParams& p, const Batc
     return;
   }
   if (t.split && !drain) {  // chains only; every change point goes to the queue
+    const int phase = t.phase;
     if (t.min_blocks >= 16)
-      launch_chain_m<16>(X, p, t, num_sms, s);
+      launch_chain_m<16>(X, p, t, num_sms, phase, s);
     else if (t.min_blocks >= 12)
-      launch_chain_m<12>(X, p, t, num_sms, s);
+      launch_chain_m<12>(X, p, t, num_sms, phase, s);
     else
-      launch_chain_m<1>(X, p, t, num_sms, s);
+      launch_chain_m<1>(X, p, t, num_sms, phase, s);
     return;
   }
   if (t.stack <= 2)
@@ -868,8 +885,10 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
                               unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s) {
   if (!n_locs) return;
   RowItem* items = static_cast<RowItem*>(row_items);
+  unsigned int* side = row_ctr + 1;  // two counters after the row claim counter
+  cudaMemsetAsync(side, 0, 8, s);
   count_launches(1);
-  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(hits, loc_off, n_hits, read_offs, items);
+  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(hits, loc_off, n_hits, n_locs, read_offs, items, side);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
   if (per_sm < 1) per_sm = 1;

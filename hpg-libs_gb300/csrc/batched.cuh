@@ -68,6 +68,7 @@ struct BatchedTuning {
   int min_blocks = 1;     // register bound: 1 (compiler's choice), 12 or 16 resident blocks per SM
   int split = 0;          // 0: fused (per-lane stacks); 1: chain-only kernel + drain of every change point;
                           // 2: lockstep kernel (4 chains of a read per lane) + drain
+  int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
 };
 
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u;

@@ -345,7 +345,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   const size_t spill_want = e->tuning.split ? 4 * (size_t)n + 4096 + (size_t)e->num_sms * 16 * 128 * 8
                                             : (size_t)n / 4 + 4096;
   if (e->b_spill_cap < spill_want) e->b_spill_cap = (uint32_t)std::min<size_t>(spill_want, 0xFFFFFFF0u);
-  unsigned int* ctr = ptr<unsigned int>(e->b_ctr);  // [0] chains [1] spill head [2] spill tail [3] results [4] status [5] rows
+  unsigned int* ctr = ptr<unsigned int>(e->b_ctr);  // [0] chains [1] spill head [2] spill tail [3] results [4] status [5..7] locate [8] phase-1 chains
   uint32_t status = 0, res_total = 0;
   for (int attempt = 0; attempt < 8; ++attempt) {
     if (!ensure(e, e->b_res, (size_t)e->b_res_cap * sizeof(PendingHit)) ||
@@ -375,9 +375,25 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.status = ctr + 4;
     p.census = census;
     cudaEventRecord(e->cev[0], s);
-    launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
-    cudaEventRecord(e->dev_mid, s);
-    launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
+    if (e->tuning.split == 1) {
+      // one index direction at a time: chains on the backward index and their
+      // change points, then chains on the forward index and theirs
+      BatchedTuning t = e->tuning;
+      BatchedParams p1 = p;
+      p1.chain_ctr = ctr + 8;
+      t.phase = 0;
+      launch_batched_search(e->X, p, t, e->num_sms, false, s);
+      launch_batched_search(e->X, p, t, e->num_sms, true, s);
+      cudaMemcpyAsync(ctr + 1, ctr + 2, 4, cudaMemcpyDeviceToDevice, s);  // drain resumes at the queue tail
+      cudaEventRecord(e->dev_mid, s);
+      t.phase = 1;
+      launch_batched_search(e->X, p1, t, e->num_sms, false, s);
+      launch_batched_search(e->X, p1, t, e->num_sms, true, s);
+    } else {
+      launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
+      cudaEventRecord(e->dev_mid, s);
+      launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
+    }
     cudaEventRecord(e->cev[1], s);
     uint32_t h[5];
     HPG_CUDA(cudaMemcpyAsync(h, ctr, 20, cudaMemcpyDeviceToHost, s), "batched counters");
@@ -426,7 +442,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     return -1;
   }
   if (census) cudaMemsetAsync(census, 0, 8, s);
-  cudaMemsetAsync(ctr + 5, 0, 4, s);
+  cudaMemsetAsync(ctr + 5, 0, 12, s);  // row claim counter and the two direction counters
   launch_locate_persistent(e->X, ptr<hpg_hit_t>(e->hits), ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs,
                            ptr<hpg_loc_t>(e->locs), e->b_rowhit.p, ctr + 5, census, e->num_sms, s);
   cudaEventRecord(e->cev[3], s);
