@@ -1,6 +1,7 @@
 // batched.cu -- persistent work-queue search, ordered finalize and persistent
 // locate of the batched pipeline form.
 #include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
 #include <cuda_runtime.h>
 
 #include "batched.cuh"
@@ -586,6 +587,124 @@ __global__ void __launch_bounds__(kBlock, MINB) chain4_kernel(DevIndex X, Batche
   }
 }
 
+// Phased lockstep variant: one lane per read runs the two vector searches of
+// a phase together -- phase 0: '+' backward and '-' forward (both on the
+// backward index), phase 1: '-' backward and '+' forward (forward index).
+// Lanes then spend about one read length per read whatever the strand, the
+// next read is claimed and fetched ahead, and only one direction's blocks
+// are live in L2.  Change points go to the device queue for the drain launch.
+template <int MINB>
+__global__ void __launch_bounds__(kBlock, MINB) chain2_kernel(DevIndex X, BatchedParams p, int phase) {
+  __shared__ uint32_t c_res[kBlock], c_spill[kBlock];
+  const int tid = threadIdx.x;
+  c_res[tid] = 0;
+  c_spill[tid] = 0;
+  const uint32_t sA = (uint32_t)phase, sB = 1u - (uint32_t)phase;  // strands of the backward / forward chain
+  const View vA{(uint32_t)phase, sA}, vB{(uint32_t)phase, sB};
+  uint32_t read = claim(p.chain_ctr, 1);
+  uint32_t nxt = read < p.n_reads ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
+  uint64_t b0 = 0, b1 = 0, nb0 = 0, nb1 = 0;
+  uint32_t okr = 0, nok = 0;
+  if (read < p.n_reads) {
+    b0 = p.offs[read];
+    b1 = p.offs[read + 1];
+    okr = p.ok[read];
+  }
+  if (nxt < p.n_reads) {
+    nb0 = p.offs[nxt];
+    nb1 = p.offs[nxt + 1];
+    nok = p.ok[nxt];
+  }
+  uint32_t sectors = 0;
+  while (read < p.n_reads) {
+    const int len = (int)(b1 - b0);
+    if (okr && len >= 3 && len <= 32767) {
+      const uint8_t* W = p.codes + b0;
+      const int n = len - 1, half = n / 2;
+      uint32_t kA = 0, lA = X.top, pkA = 0, plA = X.top, kB = 0, lB = X.top, pkB = 0, plB = X.top;
+      bool aA = true, aB = true;
+      uint32_t bA = W[n], bB = W[0];
+      for (int t = 0; t <= n; ++t) {
+        const int jb = n - t, jf = t;
+        const uint32_t nbA = (aA && jb > 0) ? W[jb - 1] : 0u;  // next bases, fetched with this step's gathers
+        const uint32_t nbB = (aB && jf < n) ? W[jf + 1] : 0u;
+        if (p.census) sectors += (aA ? (((kA >> 6) == (lA >> 6)) ? 1u : 2u) : 0u) +
+                                 (aB ? (((kB >> 6) == (lB >> 6)) ? 1u : 2u) : 0u);
+        if (aA) bw_step(X, vA, bA, kA, lA);
+        if (aB) bw_step(X, vB, bB, kB, lB);
+        if (aA) {  // backward: entry at jb vs J = jb + 1; window [2, n/2], block at J = 1
+          const int J = jb + 1;
+          const bool differ = (lA - kA) != (plA - pkA);
+          if (differ && J >= 2 && J <= half) {
+            uint32_t cs = c_spill[tid];
+            spill_push(p, cs, pkA, plA, (read << 1) | sA, (uint32_t)J | (kCpBwd << 16));
+            c_spill[tid] = cs;
+          }
+          if (kA > lA || jb == 0) {
+            if (jb == 0) {
+              const uint32_t rs = (read << 1) | sA;
+              if (kA <= lA) {
+                uint32_t r = c_res[tid];
+                const unsigned slot = res_slot(p, r);
+                c_res[tid] = r;
+                write_hit(p, slot, rs, order_key(0, 0, 0), kA, lA, pack_meta(0, 0, 0, 0, 0));
+              }
+              if (differ) {
+                uint32_t cs = c_spill[tid];
+                spill_push(p, cs, pkA, plA, rs, 1u | (kBlk1 << 16));
+                c_spill[tid] = cs;
+              }
+            }
+            aA = false;
+          } else {
+            pkA = kA;
+            plA = lA;
+            bA = nbA;
+          }
+        }
+        if (aB) {  // forward: entry at jf vs J = jf - 1; window [n/2 - 1, n - 2], block at n - 1
+          const int J = jf - 1;
+          const bool differ = (lB - kB) != (plB - pkB);
+          if (differ && jf >= 1 && J >= half - 1 && J <= n - 1) {
+            uint32_t cs = c_spill[tid];
+            spill_push(p, cs, pkB, plB, (read << 1) | sB, (uint32_t)J | ((J == n - 1 ? kBlkN : kCpFwd) << 16));
+            c_spill[tid] = cs;
+          }
+          if (kB > lB || jf == n) {
+            aB = false;
+          } else {
+            pkB = kB;
+            plB = lB;
+            bB = nbB;
+          }
+        }
+        if (!aA && !aB) break;
+      }
+    }
+    read = nxt;
+    b0 = nb0;
+    b1 = nb1;
+    okr = nok;
+    if (read < p.n_reads) {
+      nxt = claim(p.chain_ctr, 1);
+      if (nxt < p.n_reads) {
+        nb0 = p.offs[nxt];
+        nb1 = p.offs[nxt + 1];
+        nok = p.ok[nxt];
+      }
+    }
+  }
+  {  // reserved but unused slots of the last chunks
+    const uint32_t r = c_res[tid];
+    for (unsigned i = 0, left = r >> 28, slot = r & 0x0FFFFFFFu; i < left; ++i)
+      if (slot + i < p.res_cap) p.res[slot + i].rs = 0xFFFFFFFFu;
+    const uint32_t q = c_spill[tid];
+    for (unsigned i = 0, left = q >> 28, slot = q & 0x0FFFFFFFu; i < left; ++i)
+      if (slot + i < p.spill_cap) p.spill[slot + i].rs = 0xFFFFFFFFu;
+  }
+  if (p.census) atomicAdd(p.census, (unsigned long long)sectors);
+}
+
 // ------------------------------------------------------------- finalize --
 
 __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const unsigned int* res_total,
@@ -672,7 +791,14 @@ __global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uin
     it.hit = h;
     it.phys_len = (phys << 31) | (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
     const unsigned cnt = (unsigned)(e - b);
-    const unsigned at = atomicAdd(&side[phys], cnt);
+    // one atomic per direction and warp: rows of the lanes sharing a direction are laid out by a scan
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group sub = cg::labeled_partition(g, phys);
+    const unsigned incl = cg::inclusive_scan(sub, cnt);
+    unsigned base = 0;
+    if (sub.thread_rank() == sub.size() - 1) base = atomicAdd(&side[phys], incl);
+    base = sub.shfl(base, sub.size() - 1);
+    const unsigned at = base + incl - cnt;
     for (unsigned i = 0; i < cnt; ++i) {
       it.row = (uint32_t)((uint64_t)x.k + i);
       it.out = (uint32_t)(b + i);
@@ -808,6 +934,16 @@ int batched_max_blocks_per_sm(const BatchedTuning& t) {
   }
   if (t.split) {
     int per_sm = 0;
+    if (t.split == 1) {
+      if (t.min_blocks >= 16)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<16>, kBlock, 0);
+      else if (t.min_blocks >= 12)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<12>, kBlock, 0);
+      else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<1>, kBlock, 0);
+      if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+      return per_sm;
+    }
     if (t.min_blocks >= 16)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain_kernel<16>, kBlock, 0);
     else if (t.min_blocks >= 12)
@@ -839,6 +975,24 @@ void launch_batched_search(const DevIndex& X, const BatchedParams& p, const Batc
       if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
       count_launches(1);
       chain4_kernel<1><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p);
+    }
+    return;
+  }
+  if (t.split == 1 && !drain && t.phase < 2) {  // phased lockstep: the phase's two chains per read
+    int per_sm = 0;
+    if (t.min_blocks >= 16) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<16>, kBlock, 0);
+      count_launches(1);
+      chain2_kernel<16><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p, t.phase);
+    } else if (t.min_blocks >= 12) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<12>, kBlock, 0);
+      count_launches(1);
+      chain2_kernel<12><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p, t.phase);
+    } else {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chain2_kernel<1>, kBlock, 0);
+      if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
+      count_launches(1);
+      chain2_kernel<1><<<num_sms * (per_sm > 0 ? per_sm : 1), kBlock, 0, s>>>(X, p, t.phase);
     }
     return;
   }
