@@ -103,8 +103,11 @@ def test_autotuner_keeps_results(case_factory):
                            int(np.diff(reads.offsets).max()), 64)
         assert len(table) == 49 and all(r["search_us"] > 0 for r in table)
         chosen = g.get_tuning()
-        best = min(table[:45], key=lambda r: r["search_us"])
-        assert (chosen["stack"], chosen["chains_per_claim"]) == (best["stack"], best["chains_per_claim"])
+        best_us = min(r["search_us"] for r in table[:45])
+        mine = [r["search_us"] for r in table[:45]
+                if (r["stack"], r["chains_per_claim"], r["register_bound_blocks"]) ==
+                (chosen["stack"], chosen["chains_per_claim"], chosen["register_bound_blocks"])]
+        assert mine and min(mine) <= best_us + 1  # the fastest setting (ties rounded to 1 us) was kept
         got = g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED, max_results=64)
     _assert_same(got, want)
 
