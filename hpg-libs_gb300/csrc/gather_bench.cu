@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128) fm_chain_probe_kernel(DevIndex X, const u
   if (r >= n_reads) return;
   const uint64_t b = offs[r];
   const int len = (int)(offs[r + 1] - b);
-  uint32_t acc = 0;
+  uint32_t acc = 0, steps = 0;
   for (uint32_t rep = 0; rep < reps; ++rep) {
     // variant 0: backward search on the backward index; 1: forward search on
     // the forward index; 2: odd reads do 0, even reads do 1 (both indexes live)
@@ -73,18 +73,20 @@ __global__ void __launch_bounds__(128) fm_chain_probe_kernel(DevIndex X, const u
       const int i = v ? t : len - 1 - t;
       const uint32_t c = table[ascii[b + i]] & 3u;
       bw_step(X, View{v, 0}, c, k, l);
+      ++steps;
       if (k > l) break;
     }
     acc += k ^ l;
   }
-  if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
+  atomicAdd(sink, (unsigned long long)steps + (acc == 0x9E3779B9u ? 1ull : 0ull));
 }
 
 }  // namespace
 
 // Rank steps per second of fm_chain_probe_kernel over device reads.
 int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_ascii, const uint64_t* d_offs,
-                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err) {
+                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err,
+                   unsigned long long* steps_out) {
   const uint32_t variant = reps >> 16;
   reps &= 0xFFFFu;
   unsigned long long* sink = nullptr;
@@ -100,11 +102,13 @@ int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_asc
   cudaEventCreate(&b);
   const unsigned grid = (n_reads + 127) / 128;
   fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, 1, variant, sink);
+  cudaMemsetAsync(sink, 0, 8, s);
   cudaEventRecord(a, s);
   fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, reps, variant, sink);
   cudaEventRecord(b, s);
   const cudaError_t ce = cudaStreamSynchronize(s);
   cudaEventElapsedTime(ms_out, a, b);
+  if (steps_out) cudaMemcpy(steps_out, sink, 8, cudaMemcpyDeviceToHost);
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaStreamDestroy(s);

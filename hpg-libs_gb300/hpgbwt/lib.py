@@ -88,7 +88,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.bwt_gpu_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
-    lib.bwt_gpu_fm_probe.argtypes = [vp, vp, vp, sz, u32, ctypes.POINTER(ctypes.c_float)]
+    lib.bwt_gpu_fm_probe.argtypes = [vp, vp, vp, sz, u32, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_ulonglong)]
     lib.bwt_gpu_set_load_mode.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_load_mode.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
@@ -215,10 +216,13 @@ class GpuIndex:
         return [{"register_bound_blocks": table[5 * i], "blocks_per_sm": table[5 * i + 1], "stack": table[5 * i + 2],
                  "chains_per_claim": table[5 * i + 3], "search_us": table[5 * i + 4]} for i in range(rows.value)]
 
-    def fm_probe(self, d_seqs: int, d_offs: int, n_reads: int, reps: int = 1) -> float:
+    def fm_probe(self, d_seqs: int, d_offs: int, n_reads: int, reps: int = 1) -> tuple[float, int]:
+        """(device ms, rank steps)"""
         ms = ctypes.c_float()
-        self._check(self.lib.bwt_gpu_fm_probe(self.handle, d_seqs, d_offs, n_reads, reps, ctypes.byref(ms)))
-        return ms.value
+        steps = ctypes.c_ulonglong()
+        self._check(self.lib.bwt_gpu_fm_probe(self.handle, d_seqs, d_offs, n_reads, reps, ctypes.byref(ms),
+                                              ctypes.byref(steps)))
+        return ms.value, int(steps.value)
 
     def set_load_mode(self, mode: int) -> None:
         self.lib.bwt_gpu_set_load_mode(self.handle, mode)

@@ -188,9 +188,9 @@ int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t ste
  * full exact search, (reps & 0xFFFF) times (device reads as for
  * bwt_gpu_search_device); reps >> 16 selects backward search on the backward
  * index (0), forward search on the forward index (1) or half of each (2).
- * Device time in *ms. */
+ * Device time in *ms, rank steps taken in *steps (may be NULL). */
 int bwt_gpu_fm_probe(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
-                     uint32_t reps, float *ms);
+                     uint32_t reps, float *ms, unsigned long long *steps);
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
