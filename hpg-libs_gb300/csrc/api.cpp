@@ -292,6 +292,16 @@ int bwt_gpu_load_mode(bwt_index_t* index) {
   return e ? engine_load_mode(e) : -1;
 }
 
+void bwt_gpu_set_graph(bwt_index_t* index, int on) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_graph(e, on);
+}
+
+int bwt_gpu_graph(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_graph(e) : -1;
+}
+
 int bwt_gpu_autotune(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int* table, int max_rows,
                      int* rows) {

@@ -101,10 +101,11 @@ __device__ __forceinline__ uint32_t make_meta(uint32_t j, uint32_t type, uint32_
 template <int D, int MINB, bool CENSUS>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
+  const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
   __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_misc[kBlock], c_res[kBlock];
   const int tid = threadIdx.x;
-  const uint32_t n_chains = 4u * p.n_reads;
+  const uint32_t n_chains = 4u * n_reads_;
   const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
   c_meta[tid] = 0;
   c_misc[tid] = 0;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   uint32_t nxt_read = drain ? 0xFFFFFFFFu : claim(p.chain_ctr, 1);
   uint64_t nxt_b0 = 0, nxt_b1 = 0;
   uint32_t nxt_ok = 0;
-  if (nxt_read < p.n_reads) {
+  if (nxt_read < n_reads_) {
     nxt_b0 = p.offs[nxt_read];
     nxt_b1 = p.offs[nxt_read + 1];
     nxt_ok = p.ok[nxt_read];
@@ -259,13 +260,13 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         continue;
       }
       if (chain >= 4) {  // next read: switch to the prefetched one, prefetch the one after
-        if (nxt_read >= p.n_reads) break;
+        if (nxt_read >= n_reads_) break;
         cur_read = nxt_read;
         const uint64_t b0 = nxt_b0;
         const int L = (int)(nxt_b1 - nxt_b0);
         const uint32_t okr = nxt_ok;
         nxt_read = claim(p.chain_ctr, 1);
-        if (nxt_read < p.n_reads) {
+        if (nxt_read < n_reads_) {
           nxt_b0 = p.offs[nxt_read];
           nxt_b1 = p.offs[nxt_read + 1];
           nxt_ok = p.ok[nxt_read];
@@ -381,7 +382,8 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
 // each launch keeps one direction's occurrence blocks hot in L2; 2 runs all.
 template <int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, BatchedParams p, int chunk, int phase) {
-  const uint32_t n_chains = (phase == 2 ? 4u : 2u) * p.n_reads;
+  const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
+  const uint32_t n_chains = (phase == 2 ? 4u : 2u) * n_reads_;
   uint32_t rs = 0;
   const uint8_t* W = nullptr;
   int len = 0;
@@ -483,27 +485,28 @@ __device__ __forceinline__ void spill_push(const BatchedParams& p, uint32_t& chu
 
 template <int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) chain4_kernel(DevIndex X, BatchedParams p) {
+  const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
   __shared__ uint32_t c_res[kBlock], c_spill[kBlock];
   const int tid = threadIdx.x;
   c_res[tid] = 0;
   c_spill[tid] = 0;
   uint32_t read = claim(p.chain_ctr, 1);
-  uint32_t nxt = read < p.n_reads ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
+  uint32_t nxt = read < n_reads_ ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
   uint64_t nb0 = 0, nb1 = 0;
   uint32_t nok = 0;
-  if (nxt < p.n_reads) {
+  if (nxt < n_reads_) {
     nb0 = p.offs[nxt];
     nb1 = p.offs[nxt + 1];
     nok = p.ok[nxt];
   }
   uint64_t b0 = 0, b1 = 0;
   uint32_t okr = 0;
-  if (read < p.n_reads) {
+  if (read < n_reads_) {
     b0 = p.offs[read];
     b1 = p.offs[read + 1];
     okr = p.ok[read];
   }
-  while (read < p.n_reads) {
+  while (read < n_reads_) {
     const int len = (int)(b1 - b0);
     if (okr && len >= 3 && len <= 32767) {
       const uint8_t* W = p.codes + b0;
@@ -568,9 +571,9 @@ __global__ void __launch_bounds__(kBlock, MINB) chain4_kernel(DevIndex X, Batche
     b0 = nb0;
     b1 = nb1;
     okr = nok;
-    if (read < p.n_reads) {
+    if (read < n_reads_) {
       nxt = claim(p.chain_ctr, 1);
-      if (nxt < p.n_reads) {
+      if (nxt < n_reads_) {
         nb0 = p.offs[nxt];
         nb1 = p.offs[nxt + 1];
         nok = p.ok[nxt];
@@ -595,6 +598,7 @@ __global__ void __launch_bounds__(kBlock, MINB) chain4_kernel(DevIndex X, Batche
 // are live in L2.  Change points go to the device queue for the drain launch.
 template <int MINB>
 __global__ void __launch_bounds__(kBlock, MINB) chain2_kernel(DevIndex X, BatchedParams p, int phase) {
+  const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
   __shared__ uint32_t c_res[kBlock], c_spill[kBlock];
   const int tid = threadIdx.x;
   c_res[tid] = 0;
@@ -602,21 +606,21 @@ __global__ void __launch_bounds__(kBlock, MINB) chain2_kernel(DevIndex X, Batche
   const uint32_t sA = (uint32_t)phase, sB = 1u - (uint32_t)phase;  // strands of the backward / forward chain
   const View vA{(uint32_t)phase, sA}, vB{(uint32_t)phase, sB};
   uint32_t read = claim(p.chain_ctr, 1);
-  uint32_t nxt = read < p.n_reads ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
+  uint32_t nxt = read < n_reads_ ? claim(p.chain_ctr, 1) : 0xFFFFFFFFu;
   uint64_t b0 = 0, b1 = 0, nb0 = 0, nb1 = 0;
   uint32_t okr = 0, nok = 0;
-  if (read < p.n_reads) {
+  if (read < n_reads_) {
     b0 = p.offs[read];
     b1 = p.offs[read + 1];
     okr = p.ok[read];
   }
-  if (nxt < p.n_reads) {
+  if (nxt < n_reads_) {
     nb0 = p.offs[nxt];
     nb1 = p.offs[nxt + 1];
     nok = p.ok[nxt];
   }
   uint32_t sectors = 0;
-  while (read < p.n_reads) {
+  while (read < n_reads_) {
     const int len = (int)(b1 - b0);
     if (okr && len >= 3 && len <= 32767) {
       const uint8_t* W = p.codes + b0;
@@ -685,9 +689,9 @@ __global__ void __launch_bounds__(kBlock, MINB) chain2_kernel(DevIndex X, Batche
     b0 = nb0;
     b1 = nb1;
     okr = nok;
-    if (read < p.n_reads) {
+    if (read < n_reads_) {
       nxt = claim(p.chain_ctr, 1);
-      if (nxt < p.n_reads) {
+      if (nxt < n_reads_) {
         nb0 = p.offs[nxt];
         nb1 = p.offs[nxt + 1];
         nok = p.ok[nxt];
@@ -709,7 +713,8 @@ __global__ void __launch_bounds__(kBlock, MINB) chain2_kernel(DevIndex X, Batche
 
 __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const unsigned int* res_total,
                                     const uint64_t* __restrict__ seg_off, PendingHit* __restrict__ sorted,
-                                    uint32_t res_cap, uint32_t* __restrict__ cursor) {
+                                    uint32_t res_cap, uint32_t* __restrict__ cursor, const unsigned* gate) {
+  if (gate && *gate) return;  // a pool overflowed: the graph's host reruns the batch
   const uint32_t n = min(*res_total, res_cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const PendingHit h = res[i];
@@ -720,9 +725,11 @@ __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const un
 
 __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
                                      uint32_t n_rs, uint32_t max_results, uint32_t* __restrict__ kept,
-                                     uint8_t* __restrict__ trunc) {
+                                     uint8_t* __restrict__ trunc, const uint32_t* max_dev, const unsigned* gate) {
   const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
   if (rs >= n_rs) return;
+  if (gate && *gate) return;
+  if (max_dev) max_results = *max_dev;
   const uint64_t b = seg_off[rs], e = seg_off[rs + 1];
   // insertion sort by key (lists are short; keys are unique within a list)
   for (uint64_t i = b + 1; i < e; ++i) {
@@ -741,9 +748,11 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
 
 __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
                                    const uint64_t* __restrict__ hit_off, const uint32_t* __restrict__ kept,
-                                   uint32_t n_rs, hpg_hit_t* __restrict__ hits, uint32_t* __restrict__ rows) {
+                                   uint32_t n_rs, hpg_hit_t* __restrict__ hits, uint32_t* __restrict__ rows,
+                                   const unsigned* gate) {
   const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
   if (rs >= n_rs) return;
+  if (gate && *gate) return;
   const uint32_t m = kept[rs];
   const uint64_t b = seg_off[rs], o = hit_off[rs];
   for (uint32_t i = 0; i < m; ++i) {
@@ -779,7 +788,16 @@ struct RowItem {
 // at a time.
 __global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
                                    uint32_t n_hits, uint64_t n_locs, const uint64_t* __restrict__ read_offs,
-                                   RowItem* __restrict__ items, unsigned int* __restrict__ side) {
+                                   RowItem* __restrict__ items, unsigned int* __restrict__ side, LocateSizes z) {
+  if (z.status) {  // graph form: sizes from device memory, rows checked against the item capacity
+    if (*z.status) return;
+    n_hits = (uint32_t)*z.n_hits;
+    n_locs = *z.n_locs;
+    if (n_locs > z.locs_cap) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(z.status, kStatusLocFull);
+      return;
+    }
+  }
   for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x) {
     const hpg_hit_t x = hits[h];
     const uint64_t b = loc_off[h], e = loc_off[h + 1];
@@ -811,7 +829,12 @@ constexpr unsigned kRowsPerClaim = 4;
 
 __global__ void __launch_bounds__(kBlock)
     locate_persistent_kernel(DevIndex X, const RowItem* __restrict__ items, uint64_t n_locs,
-                             hpg_loc_t* __restrict__ out, unsigned int* row_ctr, unsigned long long* census) {
+                             hpg_loc_t* __restrict__ out, unsigned int* row_ctr, unsigned long long* census,
+                             LocateSizes z) {
+  if (z.status) {
+    if (*z.status) return;  // includes an item capacity overflow found by expand_rows_kernel
+    n_locs = *z.n_locs;
+  }
   uint32_t r = 0, left = 0;
   uint32_t i = 0, j = 0;
   RowItem it{0, 0, 0, 0};
@@ -1015,34 +1038,40 @@ void launch_batched_search(const DevIndex& X, const BatchedParams& p, const Batc
 }
 
 void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
-                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s) {
+                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s, const unsigned* gate) {
   count_launches(1);
-  scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap, cursor);
+  scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap, cursor, gate);
 }
 
 void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
-                          uint32_t* kept, uint8_t* trunc, cudaStream_t s) {
+                          uint32_t* kept, uint8_t* trunc, cudaStream_t s, const uint32_t* max_dev,
+                          const unsigned* gate) {
   if (!n_rs) return;
   count_launches(1);
-  sort_truncate_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, n_rs, max_results, kept, trunc);
+  sort_truncate_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, n_rs, max_results, kept, trunc, max_dev,
+                                                          gate);
 }
 
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
-                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s) {
+                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
+                        const unsigned* gate) {
   if (!n_rs) return;
   count_launches(1);
-  expand_hits_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, hit_off, kept, n_rs, hits, rows);
+  expand_hits_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, hit_off, kept, n_rs, hits, rows, gate);
 }
 
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
                               uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, void* row_items,
-                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s) {
+                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s,
+                              const LocateSizes& z) {
   if (!n_locs) return;
   RowItem* items = static_cast<RowItem*>(row_items);
   unsigned int* side = row_ctr + 1;  // two counters after the row claim counter
   cudaMemsetAsync(side, 0, 8, s);
   count_launches(1);
-  expand_rows_kernel<<<(n_hits + 255) / 256, 256, 0, s>>>(hits, loc_off, n_hits, n_locs, read_offs, items, side);
+  const uint64_t hit_grid = z.status ? 4ull * num_sms : (n_hits + 255) / 256;  // graph form: grid-stride over hits
+  expand_rows_kernel<<<(unsigned)(hit_grid ? hit_grid : 1), 256, 0, s>>>(hits, loc_off, n_hits, n_locs, read_offs,
+                                                                         items, side, z);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
@@ -1050,7 +1079,7 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
   const uint64_t need = (n_locs + kBlock * kRowsPerClaim - 1) / (kBlock * kRowsPerClaim);
   if (need < blocks) blocks = need;
   count_launches(1);
-  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, items, n_locs, out, row_ctr, census);
+  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, items, n_locs, out, row_ctr, census, z);
 }
 
 size_t locate_row_item_bytes() { return sizeof(RowItem); }

@@ -44,6 +44,7 @@ struct BatchedParams {
   const uint64_t* offs;
   const uint8_t* ok;
   uint32_t n_reads;
+  const uint32_t* n_reads_dev;  // when set, the read count is read from device memory (graph replays)
   uint32_t max_results;
   // work queues
   unsigned int* chain_ctr;   // next chain id
@@ -71,7 +72,17 @@ struct BatchedTuning {
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
 };
 
-constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u;
+constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u;
+
+// Locate sizes of the graph form: with `status` set, the hit and row counts
+// are read from device memory, rows beyond `locs_cap` raise kStatusLocFull,
+// and a nonzero status skips the stage.
+struct LocateSizes {
+  unsigned* status = nullptr;
+  const uint64_t* n_hits = nullptr;
+  const uint64_t* n_locs = nullptr;
+  uint64_t locs_cap = 0;
+};
 
 // Search kernels: `drain` empties the spill queue instead of pulling chains.
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
@@ -80,17 +91,24 @@ int batched_max_blocks_per_sm(const BatchedTuning& t);
 
 // Finalize: scatter pending hits into (read, strand) segments, sort each by
 // key, truncate; kept counts to `kept`, truncation flags to `trunc`.
+// In the graph form `gate` (the search status word) skips the stage after a
+// pool overflow and `max_dev` holds max_results.
 void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
-                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s);
+                         PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s,
+                         const unsigned* gate = nullptr);
 void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
-                          uint32_t* kept, uint8_t* trunc, cudaStream_t s);
+                          uint32_t* kept, uint8_t* trunc, cudaStream_t s, const uint32_t* max_dev = nullptr,
+                          const unsigned* gate = nullptr);
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
-                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s);
+                        const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
+                        const unsigned* gate = nullptr);
 
-// Persistent locate: lanes pull rows from a counter and refill when their walk ends.
+// Persistent locate: lanes pull rows from a counter and refill when their walk
+// ends.  In the graph form n_hits / n_locs are capacities and `z` the sizes.
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
                               uint64_t n_locs, const uint64_t* read_offs, hpg_loc_t* out, void* row_items,
-                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s);
+                              unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s,
+                              const LocateSizes& z = LocateSizes());
 size_t locate_row_item_bytes();
 
 }  // namespace hpgbwt

@@ -8,92 +8,11 @@
 #include <cstring>
 #include <vector>
 
-#include "batched.cuh"
-#include "engine.hpp"
-#include "fm_device.cuh"
-#include "kernels.cuh"
+#include "engine_internal.hpp"
 
 namespace hpgbwt {
 
 namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-};
-
-#define HPG_CUDA(call, msg)                                                        \
-  do {                                                                             \
-    cudaError_t _e = (call);                                                       \
-    if (_e != cudaSuccess) {                                                       \
-      if (err) *err = std::string(msg) + ": " + cudaGetErrorString(_e);            \
-      return -1;                                                                   \
-    }                                                                              \
-  } while (0)
-
-}  // namespace
-
-struct Engine {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  DevIndex X{};
-  OccBlock* d_occ[2] = {nullptr, nullptr};
-  uint32_t* d_S[2] = {nullptr, nullptr};
-  uint64_t* d_kar_off = nullptr;
-  uint64_t* d_kar_start = nullptr;
-  uint8_t* d_table = nullptr;
-  uint32_t* d_err = nullptr;
-  uint8_t h_table[256];
-
-  // workspace
-  DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
-      loc_off, locs, census;
-  // batched form
-  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit;
-  uint32_t b_res_cap = 0, b_spill_cap = 0;
-  BatchedTuning tuning;
-  int num_sms = 0;
-  uint32_t ovf_cap = 0;
-  size_t chunk = 0;  // reads per chunk, 0 = automatic
-  bool census_on = false;
-  unsigned long long census_val = 0;
-  cudaEvent_t ev[kStageCount + 1];
-  cudaEvent_t cev[4];
-  cudaEvent_t dev_mid = nullptr;  // between the search and the drain launch
-  float drain_ms = 0;
-  float stage_ms[kStageCount] = {0, 0, 0, 0};
-  DeviceResult last;
-};
-
-namespace {
-
-// Grow-only device buffer; `keep` preserves the old contents.
-bool ensure(Engine* e, DevBuf& b, size_t bytes, bool keep = false) {
-  if (bytes <= b.cap) return true;
-  size_t want = std::max(bytes, b.cap + b.cap / 2);
-  void* p = nullptr;
-  if (cudaMalloc(&p, want) != cudaSuccess) {
-    cudaGetLastError();
-    want = bytes;
-    if (cudaMalloc(&p, want) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-  }
-  if (keep && b.p && b.cap) cudaMemcpyAsync(p, b.p, b.cap, cudaMemcpyDeviceToDevice, e->stream);
-  if (b.p) {
-    cudaStreamSynchronize(e->stream);
-    cudaFree(b.p);
-  }
-  b.p = p;
-  b.cap = want;
-  return true;
-}
-
-template <typename T>
-T* ptr(DevBuf& b) {
-  return static_cast<T*>(b.p);
-}
 
 // Code of row t (0..63) of a block (bit-plane layout).
 uint32_t block_code(const OccBlock& B, int t) {
@@ -285,6 +204,7 @@ void engine_destroy(Engine* e) {
   if (!e) return;
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
+  graph_plans_destroy(e);
   for (int d = 0; d < 2; ++d) {
     cudaFree(e->d_occ[d]);
     cudaFree(e->d_S[d]);
@@ -362,6 +282,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.offs = d_offs;
     p.ok = ptr<uint8_t>(e->ok);
     p.n_reads = n;
+    p.n_reads_dev = nullptr;
     p.max_results = max_results;
     p.chain_ctr = ctr + 0;
     p.spill_head = ctr + 1;
@@ -501,6 +422,14 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
   float best_ms = 1e30f;
   int rows = 0;
   DeviceResult r;
+  // candidates run in the direct form (same kernels and grids; no capture per candidate)
+  const bool graph_was = e->use_graph;
+  e->use_graph = false;
+  struct Restore {
+    Engine* e;
+    bool on;
+    ~Restore() { e->use_graph = on; }
+  } restore{e, graph_was};
   for (int mb : cand_minb)
     for (int st : cand_stack)
       for (int ch : cand_chunk) {
@@ -557,6 +486,30 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
   return 0;
 }
 
+namespace {
+
+// Batched form from the captured graph, then the walk-error check every form makes.
+int finish_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, uint64_t total,
+                 uint32_t max_results, DeviceResult* out, std::string* err) {
+  DeviceResult r;
+  if (run_batched_graph(e, seqs, offs, n, total, max_results, &r, err) != 0) return -1;
+  uint32_t derr = 0;
+  HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+  if (derr) {
+    cudaMemset(e->d_err, 0, 4);
+    *err = "corrupt index: suffix-array walk did not reach a sampled row";
+    return -1;
+  }
+  e->last = r;
+  *out = r;
+  return 0;
+}
+
+}  // namespace
+
+void engine_set_graph(Engine* e, int on) { e->use_graph = on != 0; }
+int engine_graph(Engine* e) { return e->use_graph ? 1 : 0; }
+
 int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
                          uint64_t total_bases, uint32_t max_len, uint32_t max_results, DeviceResult* out,
                          std::string* err) {
@@ -581,6 +534,7 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
   cudaStream_t s = e->stream;
   const uint32_t n = (uint32_t)n_reads;
   const uint32_t len_cap = std::max<uint32_t>(max_len, 3);
+  if (form == kFormBatched && e->use_graph) return finish_graph(e, d_seqs, d_offs, n, total_bases, max_results, out, err);
 
   if (!ensure(e, e->codes, total_bases + 16) || !ensure(e, e->ok, n + 16) || !ensure(e, e->rs_count, 8ull * n + 16) ||
       !ensure(e, e->rs_trunc, 2ull * n + 16) || !ensure(e, e->census, 16) || !ensure(e, e->ovf_count, 16)) {
@@ -757,6 +711,25 @@ int engine_copy_result(Engine* e, const DeviceResult& r, hpg_hit_t* hits, hpg_lo
   return 0;
 }
 
+namespace {
+
+int host_result(Engine* e, const DeviceResult& r, size_t n_reads, hpg_result_set_t* out, std::string* err) {
+  out->n_reads = n_reads;
+  out->n_hits = r.n_hits;
+  out->n_locs = r.n_locs;
+  out->hits = (hpg_hit_t*)std::malloc((r.n_hits + 1) * sizeof(hpg_hit_t));
+  out->locs = (hpg_loc_t*)std::malloc((r.n_locs + 1) * sizeof(hpg_loc_t));
+  out->rs_count = (uint32_t*)std::malloc((2 * n_reads + 1) * 4);
+  out->rs_truncated = (uint8_t*)std::malloc(2 * n_reads + 1);
+  if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
+    *err = "out of host memory";
+    return -1;
+  }
+  return engine_copy_result(e, r, out->hits, out->locs, out->rs_count, out->rs_truncated, err);
+}
+
+}  // namespace
+
 int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
                        uint32_t max_results, hpg_result_set_t* out, std::string* err) {
   std::memset(out, 0, sizeof(*out));
@@ -782,24 +755,22 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
   std::vector<uint64_t> rel(n_reads + 1);
   for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
   cudaStream_t s = e->stream;
+  if (form == kFormBatched && mode == HPG_BWT_MODE_SEARCH1 && e->use_graph) {
+    if (n_reads >= (1ull << 31)) {
+      *err = "too many reads in one batch";
+      return -1;
+    }
+    DeviceResult r;
+    if (finish_graph(e, seqs + offs[0], rel.data(), (uint32_t)n_reads, total, max_results, &r, err) != 0) return -1;
+    return host_result(e, r, n_reads, out, err);
+  }
   if (total) HPG_CUDA(cudaMemcpyAsync(e->seqs.p, seqs + offs[0], total, cudaMemcpyHostToDevice, s), "upload reads");
   HPG_CUDA(cudaMemcpyAsync(e->offs.p, rel.data(), (n_reads + 1) * 8, cudaMemcpyHostToDevice, s), "upload offsets");
   DeviceResult r;
   if (engine_search_device(e, mode, form, ptr<uint8_t>(e->seqs), ptr<uint64_t>(e->offs), n_reads, total, max_len,
                            max_results, &r, err) != 0)
     return -1;
-  out->n_reads = n_reads;
-  out->n_hits = r.n_hits;
-  out->n_locs = r.n_locs;
-  out->hits = (hpg_hit_t*)std::malloc((r.n_hits + 1) * sizeof(hpg_hit_t));
-  out->locs = (hpg_loc_t*)std::malloc((r.n_locs + 1) * sizeof(hpg_loc_t));
-  out->rs_count = (uint32_t*)std::malloc((2 * n_reads + 1) * 4);
-  out->rs_truncated = (uint8_t*)std::malloc(2 * n_reads + 1);
-  if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
-    *err = "out of host memory";
-    return -1;
-  }
-  return engine_copy_result(e, r, out->hits, out->locs, out->rs_count, out->rs_truncated, err);
+  return host_result(e, r, n_reads, out, err);
 }
 
 }  // namespace hpgbwt

@@ -63,6 +63,10 @@ size_t engine_index_bytes(Engine* e);
 void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, int chunk);
 void engine_get_tuning(Engine* e, int* out5);
 void engine_set_load_mode(Engine* e, int mode);
+// Batched form from the captured CUDA graph (1, the default) or launched
+// stage by stage with host-read sizes (0).
+void engine_set_graph(Engine* e, int on);
+int engine_graph(Engine* e);
 int engine_load_mode(Engine* e);
 int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads, uint64_t total_bases,
                     uint32_t max_len, uint32_t max_results, int* table, int max_rows, int* rows_out,

@@ -1,0 +1,107 @@
+// engine_internal.hpp -- the Engine context shared by the pipeline
+// orchestration (engine.cu), the CUDA-graph form (graph.cu) and the request
+// loop (serve.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+
+#include "batched.cuh"
+#include "engine.hpp"
+#include "fm_device.cuh"
+#include "kernels.cuh"
+
+namespace hpgbwt {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+#define HPG_CUDA(call, msg)                                                        \
+  do {                                                                             \
+    cudaError_t _e = (call);                                                       \
+    if (_e != cudaSuccess) {                                                       \
+      if (err) *err = std::string(msg) + ": " + cudaGetErrorString(_e);            \
+      return -1;                                                                   \
+    }                                                                              \
+  } while (0)
+
+struct GraphPlan;
+
+struct Engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevIndex X{};
+  OccBlock* d_occ[2] = {nullptr, nullptr};
+  uint32_t* d_S[2] = {nullptr, nullptr};
+  uint64_t* d_kar_off = nullptr;
+  uint64_t* d_kar_start = nullptr;
+  uint8_t* d_table = nullptr;
+  uint32_t* d_err = nullptr;
+  uint8_t h_table[256];
+
+  // workspace
+  DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
+      loc_off, locs, census;
+  // batched form
+  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit;
+  uint32_t b_res_cap = 0, b_spill_cap = 0;
+  BatchedTuning tuning;
+  int num_sms = 0;
+  uint32_t ovf_cap = 0;
+  size_t chunk = 0;  // reads per chunk, 0 = automatic
+  bool census_on = false;
+  unsigned long long census_val = 0;
+  cudaEvent_t ev[kStageCount + 1];
+  cudaEvent_t cev[4];
+  cudaEvent_t dev_mid = nullptr;  // between the search and the drain launch
+  float drain_ms = 0;
+  float stage_ms[kStageCount] = {0, 0, 0, 0};
+  DeviceResult last;
+  // batched form replayed from a captured CUDA graph (graph.cu)
+  GraphPlan** plans = nullptr;  // by power-of-two read capacity
+  bool use_graph = true;
+};
+
+// Grow-only device buffer; `keep` preserves the old contents.
+inline bool ensure(Engine* e, DevBuf& b, size_t bytes, bool keep = false) {
+  if (bytes <= b.cap) return true;
+  size_t want = std::max(bytes, b.cap + b.cap / 2);
+  void* p = nullptr;
+  if (cudaMalloc(&p, want) != cudaSuccess) {
+    cudaGetLastError();
+    want = bytes;
+    if (cudaMalloc(&p, want) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  if (keep && b.p && b.cap) cudaMemcpyAsync(p, b.p, b.cap, cudaMemcpyDeviceToDevice, e->stream);
+  if (b.p) {
+    cudaStreamSynchronize(e->stream);
+    cudaFree(b.p);
+  }
+  b.p = p;
+  b.cap = want;
+  return true;
+}
+
+template <typename T>
+inline T* ptr(DevBuf& b) {
+  return static_cast<T*>(b.p);
+}
+
+
+// Graph form of the batched pipeline (graph.cu).
+int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, uint64_t total,
+                      uint32_t max_results, DeviceResult* out, std::string* err);
+void graph_plan_destroy(GraphPlan* g);
+void graph_plans_destroy(Engine* e);
+// The plan serving batches of n reads and `total` bases (captured on demand).
+GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
+                          std::string* err);
+
+}  // namespace hpgbwt

@@ -22,10 +22,16 @@ constexpr uint32_t kSlotCap = 8;  // hits kept in place per (read, strand); the 
 // Kernels launched by this library since load (the benchmark's launch count).
 unsigned long long launch_count();
 void count_launches(unsigned n);
+void uncount_launches(unsigned long long n);  // launches recorded while capturing a graph
 
 // ASCII -> 2-bit codes (0xFF outside the alphabet) and a per-read validity flag.
 void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, uint32_t n_reads,
                    const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
+
+// Graph form of launch_encode: n_reads read from device memory, byte count
+// offs[n] (at most bases_cap), flags cleared over n_cap reads.
+void launch_encode_dev(const uint8_t* ascii, uint64_t bases_cap, const uint64_t* offs, const uint32_t* n_dev,
+                       uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
 
 // Exact backward search on both strands (mode EXACT), one thread per (read, strand).
 void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,

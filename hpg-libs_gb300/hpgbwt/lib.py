@@ -92,6 +92,8 @@ def load() -> ctypes.CDLL:
                                      ctypes.POINTER(ctypes.c_ulonglong)]
     lib.bwt_gpu_set_load_mode.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_load_mode.argtypes = [vp]
+    lib.bwt_gpu_set_graph.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_graph.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
@@ -229,6 +231,13 @@ class GpuIndex:
 
     def load_mode(self) -> int:
         return int(self.lib.bwt_gpu_load_mode(self.handle))
+
+    def set_graph(self, on: bool) -> None:
+        """Batched form from the captured CUDA graph (default) or launched stage by stage."""
+        self.lib.bwt_gpu_set_graph(self.handle, 1 if on else 0)
+
+    def graph(self) -> bool:
+        return bool(self.lib.bwt_gpu_graph(self.handle))
 
     def index_bytes(self) -> int:
         return int(self.lib.bwt_gpu_index_bytes(self.handle))

@@ -165,6 +165,12 @@ void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
  * marks the line evict-last in L2 (default); 3 32-byte load, L2 hint only. */
 void bwt_gpu_set_load_mode(bwt_index_t *index, int mode);
 int bwt_gpu_load_mode(bwt_index_t *index);
+/* Batched form launch: 1 (default) replays a CUDA graph captured once per
+ * power-of-two read capacity (all sizes read from device memory, one host
+ * synchronize per batch); 0 launches stage by stage with sizes read back to
+ * the host between stages.  Results are identical. */
+void bwt_gpu_set_graph(bwt_index_t *index, int on);
+int bwt_gpu_graph(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
  * every candidate setting (45), keeps the fastest, then picks the fastest
  * block-load form for it (4 more runs).  Optional table gets rows of
