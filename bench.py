@@ -121,7 +121,7 @@ def prepare(wl: dict, rank: int, dist):
     dist.barrier()
     reads = synth.reads_fast(genome, wl["reads"], 2 + rank, wl["read_len"], wl["edits"])
     log(f"[bench] rank {rank}: genome+index+reads ready in {time.time() - t0:.1f}s")
-    return str(base / "index"), reads
+    return str(base / "index"), reads, genome
 
 
 class ClockSampler:
@@ -218,12 +218,131 @@ def cpu_baseline(index_dir: str, reads, seconds: float = 12.0) -> dict:
                       f"({dt:.1f}s)"}
 
 
+def _pct(v: list[float], q: float) -> float:
+    if not v:
+        return float("nan")
+    s = sorted(v)
+    return s[min(len(s) - 1, max(0, int(round(q / 100.0 * (len(s) - 1)))))]
+
+
+def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: float | None, seconds: float,
+              rng: np.random.Generator, sat: float | None = None, burst: int = 48) -> dict:
+    """One serving measurement through bwt_gpu_server_*: with load None a burst
+    of requests submitted at once (saturated throughput); else Poisson arrivals
+    offering `load` x `sat` reads/s for `seconds`.  Requests are slices of a
+    pinned read pool; latency is submit (scheduled arrival, when the submitter
+    lags) to results readable in host memory."""
+    import ctypes
+    import queue
+    from hpgbwt import lib
+    L = gi.lib
+    srv = lib.Server(gi, max_batch_reads=1 << 20, max_results=MAX_RESULTS)
+    st0 = srv.stats()
+    pend: queue.Queue = queue.Queue()
+    lat: list[float] = []
+    done_reads = [0]
+    t_done = [0.0]
+
+    def waiter():
+        rs = lib.ResultSetC()
+        lt = ctypes.c_double()
+        while True:
+            item = pend.get()
+            if item is None:
+                return
+            tk, n, lag = item
+            if L.bwt_gpu_server_wait(srv.handle, tk, ctypes.byref(rs), ctypes.byref(lt), -1) != 0:
+                raise RuntimeError(L.bwt_gpu_last_error().decode())
+            lat.append(lt.value + lag)
+            done_reads[0] += n
+            t_done[0] = time.perf_counter()
+            L.bwt_gpu_server_release(srv.handle, tk)
+
+    def submit(n: int) -> int:
+        start = int(rng.integers(0, pool_n - n + 1))
+        t = ctypes.c_uint64()
+        if L.bwt_gpu_server_submit(srv.handle, seq_ptr, off_ptr + 8 * start, n, ctypes.byref(t)) != 0:
+            raise RuntimeError(L.bwt_gpu_last_error().decode())
+        return t.value
+
+    th = threading.Thread(target=waiter, daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    offered = None
+    n_req = 0
+    if load is None:
+        for _ in range(burst):
+            n = draw_size()
+            pend.put((submit(n), n, 0.0))
+            n_req += 1
+    else:
+        mean_n = float(np.mean([draw_size() for _ in range(4096)]))
+        rate = load * sat / mean_n  # requests per second
+        offered = load * sat
+        t_next = t0
+        while t_next - t0 < seconds:
+            t_next += rng.exponential(1.0 / rate)
+            while True:
+                now = time.perf_counter()
+                if now >= t_next:
+                    break
+                time.sleep(min(t_next - now, 0.0005))
+            n = draw_size()
+            tk = submit(n)
+            pend.put((tk, n, max(0.0, time.perf_counter() - t_next) * 1e3))
+            n_req += 1
+    pend.put(None)
+    th.join()
+    st = srv.stats()
+    srv.close()
+    span = t_done[0] - t0
+    nb = st["batches"] - st0["batches"]
+    out = {"requests": n_req, "reads": done_reads[0], "achieved_reads_per_s": round(done_reads[0] / span, 1),
+           "p50_ms": round(_pct(lat, 50), 3), "p99_ms": round(_pct(lat, 99), 3), "max_ms": round(max(lat), 3),
+           "mean_ms": round(float(np.mean(lat)), 3), "batches": int(nb),
+           "mean_batch_reads": round(st["reads"] / max(1, st["batches"]), 1),
+           "mean_batch_requests": round(st["requests"] / max(1, st["batches"]), 2),
+           "max_batch_requests": int(st["max_batch_requests"]), "pool_regrowths": int(st["regrowths"]),
+           "plan_hbm_bytes": int(st["plan_bytes"]), "hbm_budget_bytes": int(st["hbm_budget"])}
+    if offered is not None:
+        out = {"offered_load": load, "offered_reads_per_s": round(offered, 1), **out}
+    return out
+
+
+def serving(gi, reads, genome, log) -> dict:
+    """The serving form at 70 % offered load: 64k x 100 bp requests (the batch
+    read model), and requests of log-uniform 1k-256k reads of 50-300 bp."""
+    import torch
+    from hpgbwt import synth
+    rng = np.random.default_rng(7)
+    res = {}
+    pin_seq = torch.from_numpy(reads.seq).pin_memory()
+    pin_off = torch.from_numpy(reads.offsets.view(np.int64)).pin_memory()
+    t = time.time()
+    mix = synth.reads_fast_var(genome, 600_000, 11, 50, 300, "subst_capped")
+    mix_seq = torch.from_numpy(mix.seq).pin_memory()
+    mix_off = torch.from_numpy(mix.offsets.view(np.int64)).pin_memory()
+    log(f"[bench] serving read pools ready ({time.time() - t:.1f}s)")
+    cases = [("requests_64k_100bp", pin_seq, pin_off, len(reads), lambda: 65536),
+             ("requests_1k_256k_50_300bp", mix_seq, mix_off, len(mix),
+              lambda: int(np.exp(rng.uniform(np.log(1024), np.log(262144)))))]
+    for name, sq, of, pn, draw in cases:
+        serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)  # captures the plans it needs
+        sat = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)
+        loaded = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, 0.7, 2.0, rng,
+                           sat=sat["achieved_reads_per_s"])
+        res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "at_70pct_load": loaded}
+        log(f"[bench] serving {name}: saturated {sat['achieved_reads_per_s'] / 1e6:.1f} M reads/s; at 70% "
+            f"p50 {loaded['p50_ms']} ms p99 {loaded['p99_ms']} ms, {loaded['mean_batch_requests']} req/batch")
+    return res
+
+
 def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     import torch
     from hpgbwt import lib
     dev = dist.local
     torch.cuda.set_device(dev)
-    index_dir, reads = prepare(wl, dist.rank, dist)
+    index_dir, reads, genome = prepare(wl, dist.rank, dist)
     gi = lib.GpuIndex(index_dir, device=dev)
     n = len(reads)
     total = int(reads.offsets[-1])
@@ -316,6 +435,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             e2e_t.append(dt)
         e_hits, e_locs = int(rsc.n_hits), int(rsc.n_locs)
         gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rsc))
+    serve = serving(gi, reads, genome, log) if not args.no_serving else None
     e2e_s = dist.max(sum(e2e_t))
     e2e_value = total_reads * args.steps / e2e_s
     h2d = total + 8 * (n + 1)
@@ -370,6 +490,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                           "stages_ms": [round(x, 3) for x in v["stages"]], "sectors_per_read": round(v["sectors"] / n, 2)}
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
+            "serving": serve,
             "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
@@ -381,7 +502,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
 def run_reference(args, wl: dict, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
-    index_dir, reads = prepare(wl, 0, dist)
+    index_dir, reads, _ = prepare(wl, 0, dist)
     from oracle.pyoracle import PortOracle
     ora = PortOracle(index_dir)
     threads = os.cpu_count() or 1
@@ -420,6 +541,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
                                                  "block_load_mode (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()

@@ -12,6 +12,7 @@
 #include "kernels.cuh"
 #include "hpg_bwt.h"
 #include "index_format.hpp"
+#include "serve.hpp"
 
 using namespace hpgbwt;
 
@@ -313,6 +314,49 @@ int bwt_gpu_autotune(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* 
     return fail(err);
   return 0;
 }
+
+bwt_gpu_server_t* bwt_gpu_server_new(bwt_index_t* index, size_t max_batch_reads, uint64_t max_batch_bases,
+                                     uint64_t hbm_budget_bytes, uint32_t max_results) {
+  Engine* e = engine_of(index);
+  if (!e) {
+    fail("bwt_gpu_server_new: null index");
+    return nullptr;
+  }
+  std::string err;
+  Server* s = server_create(e, max_batch_reads, max_batch_bases, hbm_budget_bytes, max_results, &err);
+  if (!s) fail(err);
+  return reinterpret_cast<bwt_gpu_server_t*>(s);
+}
+
+int bwt_gpu_server_submit(bwt_gpu_server_t* server, const char* seqs, const uint64_t* offsets, size_t n_reads,
+                          uint64_t* ticket) {
+  if (!server || !ticket) return fail("bwt_gpu_server_submit: null argument");
+  std::string err;
+  if (server_submit(reinterpret_cast<Server*>(server), seqs, offsets, n_reads, ticket, &err) != 0) return fail(err);
+  return 0;
+}
+
+int bwt_gpu_server_wait(bwt_gpu_server_t* server, uint64_t ticket, hpg_result_set_t* view, double* latency_ms,
+                        int timeout_ms) {
+  if (!server) return fail("bwt_gpu_server_wait: null server");
+  std::string err;
+  const int rc = server_wait(reinterpret_cast<Server*>(server), ticket, view, latency_ms, timeout_ms, &err);
+  if (rc < 0) return fail(err);
+  return rc;
+}
+
+int bwt_gpu_server_release(bwt_gpu_server_t* server, uint64_t ticket) {
+  if (!server) return fail("bwt_gpu_server_release: null server");
+  std::string err;
+  if (server_release(reinterpret_cast<Server*>(server), ticket, &err) != 0) return fail(err);
+  return 0;
+}
+
+void bwt_gpu_server_stats(bwt_gpu_server_t* server, double* out, int n) {
+  if (server && out) server_stats(reinterpret_cast<Server*>(server), out, n);
+}
+
+void bwt_gpu_server_free(bwt_gpu_server_t* server) { server_destroy(reinterpret_cast<Server*>(server)); }
 
 void bwt_gpu_set_chunk(bwt_index_t* index, size_t reads) {
   Engine* e = engine_of(index);

@@ -7,6 +7,7 @@
 
 #include <algorithm>
 #include <string>
+#include <vector>
 
 #include "batched.cuh"
 #include "engine.hpp"
@@ -29,7 +30,51 @@ struct DevBuf {
     }                                                                              \
   } while (0)
 
-struct GraphPlan;
+// The batched pipeline captured for one capacity class (graph.cu).
+struct GraphPlan {
+  // capacity class and the settings baked into the capture
+  uint32_t n_cap = 0;
+  uint64_t bases_cap = 0;
+  uint32_t res_cap = 0, spill_cap = 0;
+  uint64_t locs_cap = 0;
+  BatchedTuning tuning;
+  uint32_t load_mode = 0;
+  bool census = false;
+  // device buffers
+  uint8_t* seqs = nullptr;
+  uint64_t* offs = nullptr;
+  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results
+  uint8_t* codes = nullptr;
+  uint8_t* ok = nullptr;
+  unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
+                            // [5..7] locate [8] phase-1 chains
+  uint32_t* arr = nullptr;  // arrivals per (read, strand)
+  uint64_t* seg = nullptr;
+  uint64_t* hit_off = nullptr;
+  uint32_t* kept = nullptr;
+  uint8_t* trunc = nullptr;
+  uint64_t* part = nullptr;
+  PendingHit* res = nullptr;
+  PendingHit* sorted = nullptr;
+  SpillEntry* spill = nullptr;
+  hpg_hit_t* hits = nullptr;
+  uint32_t* rows = nullptr;
+  uint64_t* loc_off = nullptr;
+  void* items = nullptr;
+  hpg_loc_t* locs = nullptr;
+  unsigned long long* census_d = nullptr;
+  uint64_t* summary_d = nullptr;
+  // pinned host words
+  uint64_t* h_summary = nullptr;  // [0] status | results << 32, [1] spill tail, [2] hits, [3] rows, [4] census
+  uint32_t* h_hdr = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long kernels = 0;  // kernel nodes per replay
+  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  std::vector<void*> allocs;
+  uint64_t bytes = 0;  // device bytes held
+};
+
 
 struct Engine {
   int device = 0;
@@ -100,6 +145,12 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
                       uint32_t max_results, DeviceResult* out, std::string* err);
 void graph_plan_destroy(GraphPlan* g);
 void graph_plans_destroy(Engine* e);
+// Asynchronous halves of run_batched_graph for a batch already staged in the
+// plan's input buffers: launch (header + replay), then collect (synchronize,
+// read the summary; returns 1 with `grow` filled when a pool overflowed, the
+// batch then has to run again through run_batched_graph).
+int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err);
+int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceResult* out, std::string* err);
 // The plan serving batches of n reads and `total` bases (captured on demand).
 GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
                           std::string* err);

@@ -21,48 +21,6 @@
 
 namespace hpgbwt {
 
-struct GraphPlan {
-  // capacity class and the settings baked into the capture
-  uint32_t n_cap = 0;
-  uint64_t bases_cap = 0;
-  uint32_t res_cap = 0, spill_cap = 0;
-  uint64_t locs_cap = 0;
-  BatchedTuning tuning;
-  uint32_t load_mode = 0;
-  bool census = false;
-  // device buffers
-  uint8_t* seqs = nullptr;
-  uint64_t* offs = nullptr;
-  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results
-  uint8_t* codes = nullptr;
-  uint8_t* ok = nullptr;
-  unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
-                            // [5..7] locate [8] phase-1 chains
-  uint32_t* arr = nullptr;  // arrivals per (read, strand)
-  uint64_t* seg = nullptr;
-  uint64_t* hit_off = nullptr;
-  uint32_t* kept = nullptr;
-  uint8_t* trunc = nullptr;
-  uint64_t* part = nullptr;
-  PendingHit* res = nullptr;
-  PendingHit* sorted = nullptr;
-  SpillEntry* spill = nullptr;
-  hpg_hit_t* hits = nullptr;
-  uint32_t* rows = nullptr;
-  uint64_t* loc_off = nullptr;
-  void* items = nullptr;
-  hpg_loc_t* locs = nullptr;
-  unsigned long long* census_d = nullptr;
-  uint64_t* summary_d = nullptr;
-  // pinned host words
-  uint64_t* h_summary = nullptr;  // [0] status | results << 32, [1] spill tail, [2] hits, [3] rows, [4] census
-  uint32_t* h_hdr = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  unsigned long long kernels = 0;  // kernel nodes per replay
-  cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  std::vector<void*> allocs;
-};
 
 namespace {
 
@@ -98,6 +56,7 @@ bool grab(GraphPlan* g, T** p, size_t bytes) {
     return false;
   }
   g->allocs.push_back(q);
+  g->bytes += bytes ? bytes : 16;
   *p = static_cast<T*>(q);
   return true;
 }
@@ -301,6 +260,50 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   return g;
 }
 
+int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err) {
+  cudaStream_t s = e->stream;
+  g->h_hdr[0] = n;
+  g->h_hdr[1] = max_results;
+  HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 8, cudaMemcpyHostToDevice, s), "batch header");
+  HPG_CUDA(cudaGraphLaunch(g->exec, s), "graph launch");
+  count_launches((unsigned)g->kernels);
+  return 0;
+}
+
+int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceResult* out, std::string* err) {
+  HPG_CUDA(cudaStreamSynchronize(e->stream), "batched pipeline");
+  const uint64_t* h = g->h_summary;
+  const uint32_t status = (uint32_t)h[0];
+  if (status) {
+    grow->res_cap = g->res_cap;
+    grow->spill_cap = g->spill_cap;
+    grow->locs_cap = g->locs_cap;
+    if (status & kStatusResFull) grow->res_cap = (uint32_t)std::min<uint64_t>((h[0] >> 32) * 2 + 4096, 0xFFFFFFF0u);
+    if (status & kStatusSpillFull) grow->spill_cap = (uint32_t)std::min<uint64_t>(h[1] * 2 + 4096, 0xFFFFFFF0u);
+    if (status & kStatusLocFull) grow->locs_cap = h[3] + h[3] / 4 + 4096;
+    return 1;
+  }
+  e->census_val = g->census ? h[4] : 0;
+  float ms = 0;
+  cudaEventElapsedTime(&e->stage_ms[kStageEncode], g->ev[0], g->ev[1]);
+  cudaEventElapsedTime(&e->stage_ms[kStageSearch], g->ev[1], g->ev[3]);
+  cudaEventElapsedTime(&e->drain_ms, g->ev[2], g->ev[3]);
+  cudaEventElapsedTime(&ms, g->ev[3], g->ev[4]);
+  e->stage_ms[kStageFinalize] = ms;
+  cudaEventElapsedTime(&ms, g->ev[4], g->ev[5]);
+  e->stage_ms[kStageLocate] = ms;
+  DeviceResult r;
+  r.n_reads = n;
+  r.n_hits = h[2];
+  r.hits = g->hits;
+  r.n_locs = h[3];
+  r.locs = g->locs;
+  r.rs_count = g->kept;
+  r.rs_truncated = g->trunc;
+  *out = r;
+  return 0;
+}
+
 int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, uint64_t total,
                       uint32_t max_results, DeviceResult* out, std::string* err) {
   cudaStream_t s = e->stream;
@@ -320,43 +323,10 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
     if (total && seqs != g->seqs) HPG_CUDA(cudaMemcpyAsync(g->seqs, seqs, total, cudaMemcpyDefault, s), "reads");
     if (offs != g->offs)
       HPG_CUDA(cudaMemcpyAsync(g->offs, offs, ((size_t)n + 1) * 8, cudaMemcpyDefault, s), "read offsets");
-    g->h_hdr[0] = n;
-    g->h_hdr[1] = max_results;
-    HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 8, cudaMemcpyHostToDevice, s), "batch header");
-    HPG_CUDA(cudaGraphLaunch(g->exec, s), "graph launch");
-    count_launches((unsigned)g->kernels);
-    HPG_CUDA(cudaStreamSynchronize(s), "batched pipeline");
-    const uint64_t* h = g->h_summary;
-    const uint32_t status = (uint32_t)h[0];
-    if (status) {
-      grow.res_cap = g->res_cap;
-      grow.spill_cap = g->spill_cap;
-      grow.locs_cap = g->locs_cap;
-      if (status & kStatusResFull)
-        grow.res_cap = (uint32_t)std::min<uint64_t>((h[0] >> 32) * 2 + 4096, 0xFFFFFFF0u);
-      if (status & kStatusSpillFull) grow.spill_cap = (uint32_t)std::min<uint64_t>(h[1] * 2 + 4096, 0xFFFFFFF0u);
-      if (status & kStatusLocFull) grow.locs_cap = h[3] + h[3] / 4 + 4096;
-      continue;
-    }
-    e->census_val = g->census ? h[4] : 0;
-    float ms = 0;
-    cudaEventElapsedTime(&e->stage_ms[kStageEncode], g->ev[0], g->ev[1]);
-    cudaEventElapsedTime(&e->stage_ms[kStageSearch], g->ev[1], g->ev[3]);
-    cudaEventElapsedTime(&e->drain_ms, g->ev[2], g->ev[3]);
-    cudaEventElapsedTime(&ms, g->ev[3], g->ev[4]);
-    e->stage_ms[kStageFinalize] = ms;
-    cudaEventElapsedTime(&ms, g->ev[4], g->ev[5]);
-    e->stage_ms[kStageLocate] = ms;
-    DeviceResult r;
-    r.n_reads = n;
-    r.n_hits = h[2];
-    r.hits = g->hits;
-    r.n_locs = h[3];
-    r.locs = g->locs;
-    r.rs_count = g->kept;
-    r.rs_truncated = g->trunc;
-    *out = r;
-    return 0;
+    if (graph_launch(e, g, n, max_results, err) != 0) return -1;
+    const int rc = graph_collect(e, g, n, &grow, out, err);
+    if (rc < 0) return -1;
+    if (rc == 0) return 0;
   }
   *err = "batched search pools kept overflowing";
   return -1;

@@ -1,0 +1,583 @@
+// serve.cu -- the serving form: a request loop with continuous batching over
+// the graph-replayed batched pipeline.
+//
+// Clients submit read sets of any size (up to the batch capacity) at any
+// time.  One worker thread owns the index's stream.  Each iteration it admits,
+// in arrival order, every waiting request that fits the batch's read, base and
+// HBM budgets (frontier pools and hit lists estimated from the hit and row
+// rates of earlier batches), stages them side by side in the capacity plan's
+// device buffers (one copy per request straight from the client's memory), and
+// replays the captured pipeline once for all of them: the requests' reads share
+// the persistent search and locate kernels.  While a batch runs the worker
+// already forms the next one from whatever arrived meanwhile, so a request
+// waits at most for the batch in flight.  Results are rebased to each
+// request's own read and hit numbering on the device and copied to pinned host
+// buffers, which clients read in place until they release the request.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "engine_internal.hpp"
+#include "serve.hpp"
+
+namespace hpgbwt {
+
+namespace {
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Per batch: segment s holds the reads [seg_read0[s], seg_read0[s+1]).  Hit
+// read ids and located-row hit ids become segment-relative; bounds[2s] and
+// bounds[2s+1] get the first hit and first row of each segment (s = n_seg is
+// the end).
+__global__ void serve_rebase_kernel(hpg_hit_t* __restrict__ hits, uint64_t n_hits, hpg_loc_t* __restrict__ locs,
+                                    uint64_t n_locs, const uint64_t* __restrict__ hit_off,
+                                    const uint64_t* __restrict__ loc_off, const uint32_t* __restrict__ seg_read0,
+                                    uint32_t n_seg, uint64_t* __restrict__ bounds) {
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t s = tid; s <= n_seg; s += stride) {
+    const uint64_t h0 = hit_off[2ull * seg_read0[s]];
+    bounds[2 * s] = h0;
+    bounds[2 * s + 1] = loc_off[h0];
+  }
+  for (uint64_t i = tid; i < n_hits; i += stride) {
+    const uint32_t r = hits[i].read;
+    uint32_t lo = 0, hi = n_seg;  // last segment starting at or before r
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (seg_read0[mid] <= r) lo = mid;
+      else hi = mid;
+    }
+    hits[i].read = r - seg_read0[lo];
+  }
+  for (uint64_t j = tid; j < n_locs; j += stride) {
+    const uint64_t h = locs[j].hit;
+    uint32_t lo = 0, hi = n_seg;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (hit_off[2ull * seg_read0[mid]] <= h) lo = mid;
+      else hi = mid;
+    }
+    locs[j].hit = (uint32_t)(h - hit_off[2ull * seg_read0[lo]]);
+  }
+}
+
+struct ServeReq {
+  uint64_t ticket = 0;
+  const char* seqs = nullptr;  // client memory, read when the request's batch is staged
+  const uint64_t* offs = nullptr;
+  uint32_t n = 0;
+  uint64_t bases = 0;
+  double t_submit = 0, t_done = 0;
+  int state = 0;  // 0 queued, 1 in a batch, 2 done, 3 failed
+  std::string err;
+  int set = -1;
+  uint64_t hit0 = 0, nh = 0, loc0 = 0, nl = 0, read0 = 0;
+};
+
+// Pinned host buffers one batch's results land in; requests point into them.
+struct ResultBuf {
+  hpg_hit_t* hits = nullptr;
+  size_t hits_cap = 0;
+  hpg_loc_t* locs = nullptr;
+  size_t locs_cap = 0;
+  uint32_t* cnt = nullptr;
+  uint8_t* trunc = nullptr;
+  size_t rs_cap = 0;
+  uint64_t* bounds = nullptr;
+  size_t seg_cap = 0;
+  int refs = 0;
+  cudaEvent_t done = nullptr;
+};
+
+struct Batch {
+  std::vector<ServeReq*> reqs;
+  uint32_t n = 0;
+  uint64_t bases = 0;
+  int slot = 0;  // staging slot of its offsets and segment table
+  GraphPlan* g = nullptr;
+  double t_launch = 0;
+};
+
+constexpr int kSets = 3;
+
+template <typename T>
+bool pinned_grow(T** p, size_t* cap, size_t want) {
+  if (want <= *cap) return true;
+  const size_t n = std::max(want, *cap + *cap / 2);
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  if (cudaHostAlloc(reinterpret_cast<void**>(p), n * sizeof(T) + 64, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return false;
+  }
+  *cap = n;
+  return true;
+}
+
+}  // namespace
+
+struct Server {
+  Engine* e = nullptr;
+  size_t max_reads = 0;
+  uint64_t max_bases = 0;
+  uint64_t budget = 0;
+  uint32_t max_results = 0;
+  size_t max_segs = 4096;
+
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_sets;
+  std::deque<ServeReq*> queue;
+  std::unordered_map<uint64_t, ServeReq*> reqs;
+  uint64_t next_ticket = 1;
+  bool stop = false;
+  std::thread worker;
+
+  ResultBuf sets[kSets];
+  int next_set = 0;
+  uint64_t* h_offs[2] = {nullptr, nullptr};
+  uint32_t* h_seg[2] = {nullptr, nullptr};
+  uint32_t* d_seg = nullptr;
+  uint64_t* d_bounds = nullptr;
+
+  // admission estimates, updated from finished batches
+  double hits_per_read = 4.0, rows_per_read = 16.0;
+
+  // statistics
+  uint64_t batches = 0, requests = 0, reads = 0, regrows = 0, max_batch_reads = 0, max_batch_reqs = 0;
+  uint64_t plan_bytes = 0;
+  double gpu_ms = 0;
+  std::string fatal;
+
+  // HBM bytes a batch of n reads and `bases` bases is expected to hold.
+  double est_bytes(uint64_t n, uint64_t bases) const {
+    const double per_read = 9.0 + 2 * 25.0 + hits_per_read * 1.25 * (2 * 24 + 32 + 4 + 8) +
+                            rows_per_read * 1.25 * (16 + 32) + 4.0;
+    return 2.0 * (double)bases + per_read * (double)n;
+  }
+
+  // Take waiting requests in arrival order while they fit (called with mu held).
+  void form(Batch* b) {
+    b->reqs.clear();
+    b->n = 0;
+    b->bases = 0;
+    double bytes = 0;
+    while (!queue.empty() && b->reqs.size() < max_segs) {
+      ServeReq* q = queue.front();
+      const double add = est_bytes(q->n, q->bases);
+      if (!b->reqs.empty() && ((size_t)b->n + q->n > max_reads || b->bases + q->bases > max_bases ||
+                               bytes + add > (double)budget))
+        break;
+      queue.pop_front();
+      q->state = 1;
+      b->reqs.push_back(q);
+      b->n += q->n;
+      b->bases += q->bases;
+      bytes += add;
+    }
+  }
+
+  // Offsets and segment table of a batch into its pinned staging slot.
+  void prepare(Batch* b) {
+    uint64_t* o = h_offs[b->slot];
+    uint32_t* sg = h_seg[b->slot];
+    uint64_t base = 0;
+    uint32_t r = 0;
+    for (size_t s = 0; s < b->reqs.size(); ++s) {
+      const ServeReq* q = b->reqs[s];
+      sg[s] = r;
+      const uint64_t o0 = q->offs[0];
+      for (uint32_t i = 0; i < q->n; ++i) o[r + i] = base + (q->offs[i] - o0);
+      r += q->n;
+      base += q->bases;
+    }
+    o[r] = base;
+    sg[b->reqs.size()] = r;
+  }
+
+  int launch(Batch* b, std::string* err) {
+    cudaStream_t s = e->stream;
+    b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err);
+    if (!b->g) return -1;
+    uint64_t at = 0;
+    for (const ServeReq* q : b->reqs) {
+      if (q->bases)
+        HPG_CUDA(cudaMemcpyAsync(b->g->seqs + at, q->seqs + q->offs[0], q->bases, cudaMemcpyDefault, s),
+                 "stage reads");
+      at += q->bases;
+    }
+    HPG_CUDA(cudaMemcpyAsync(b->g->offs, h_offs[b->slot], ((size_t)b->n + 1) * 8, cudaMemcpyHostToDevice, s),
+             "stage offsets");
+    b->t_launch = now_ms();
+    return graph_launch(e, b->g, b->n, max_results, err);
+  }
+
+  ResultBuf* take_set(size_t hits, size_t locs, size_t rs, size_t segs, std::string* err) {
+    int pick = -1;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_sets.wait(lk, [&] {
+        for (int k = 0; k < kSets; ++k)
+          if (sets[(next_set + k) % kSets].refs == 0) return true;
+        return false;
+      });
+      for (int k = 0; k < kSets && pick < 0; ++k)
+        if (sets[(next_set + k) % kSets].refs == 0) pick = (next_set + k) % kSets;
+      next_set = (pick + 1) % kSets;
+    }
+    ResultBuf& rb = sets[pick];
+    if (!pinned_grow(&rb.hits, &rb.hits_cap, hits + 1) || !pinned_grow(&rb.locs, &rb.locs_cap, locs + 1) ||
+        !pinned_grow(&rb.bounds, &rb.seg_cap, 2 * segs + 2)) {
+      *err = "out of pinned host memory (serving results)";
+      return nullptr;
+    }
+    if (rs > rb.rs_cap) {
+      size_t c1 = rb.rs_cap, c2 = rb.rs_cap;
+      if (!pinned_grow(&rb.cnt, &c1, rs + 1) || !pinned_grow(&rb.trunc, &c2, rs + 1)) {
+        *err = "out of pinned host memory (serving results)";
+        return nullptr;
+      }
+      rb.rs_cap = std::min(c1, c2);
+    }
+    return &rb;
+  }
+
+  void fail(Batch* b, const std::string& why) {
+    std::lock_guard<std::mutex> lk(mu);
+    for (ServeReq* q : b->reqs) {
+      q->state = 3;
+      q->err = why;
+      q->t_done = now_ms();
+    }
+    b->reqs.clear();
+    cv_done.notify_all();
+  }
+
+  // Wait for a launched batch, rebase and copy its results, publish them.
+  int finish(Batch* b, Batch* next, bool have_next, bool* next_launched, std::string* err) {
+    cudaStream_t s = e->stream;
+    DeviceResult r;
+    GraphPlan grow;
+    int rc = graph_collect(e, b->g, b->n, &grow, &r, err);
+    if (rc == 1) {  // a pool overflowed: grow it and run the batch again (staged inputs carried over)
+      ++regrows;
+      if (run_batched_graph(e, b->g->seqs, b->g->offs, b->n, b->bases, max_results, &r, err) != 0) return -1;
+      b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err);
+      if (!b->g) return -1;
+    } else if (rc < 0) {
+      return -1;
+    }
+    gpu_ms += now_ms() - b->t_launch;
+    uint32_t derr = 0;
+    HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+    if (derr) {
+      cudaMemset(e->d_err, 0, 4);
+      *err = "corrupt index: suffix-array walk did not reach a sampled row";
+      return -1;
+    }
+    const size_t nseg = b->reqs.size();
+    ResultBuf* rb = take_set(r.n_hits, r.n_locs, 2ull * b->n, nseg, err);
+    if (!rb) return -1;
+    HPG_CUDA(cudaMemcpyAsync(d_seg, h_seg[b->slot], (nseg + 1) * 4, cudaMemcpyHostToDevice, s), "segments");
+    const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(r.n_hits, r.n_locs), nseg + 1);
+    const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
+    count_launches(1);
+    serve_rebase_kernel<<<grid, 256, 0, s>>>(b->g->hits, r.n_hits, b->g->locs, r.n_locs, b->g->hit_off,
+                                             b->g->loc_off, d_seg, (uint32_t)nseg, d_bounds);
+    if (r.n_hits)
+      HPG_CUDA(cudaMemcpyAsync(rb->hits, b->g->hits, r.n_hits * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
+               "copy hits");
+    if (r.n_locs)
+      HPG_CUDA(cudaMemcpyAsync(rb->locs, b->g->locs, r.n_locs * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, s),
+               "copy rows");
+    if (b->n) {
+      HPG_CUDA(cudaMemcpyAsync(rb->cnt, r.rs_count, 2ull * b->n * 4, cudaMemcpyDeviceToHost, s), "copy counts");
+      HPG_CUDA(cudaMemcpyAsync(rb->trunc, r.rs_truncated, 2ull * b->n, cudaMemcpyDeviceToHost, s), "copy flags");
+    }
+    HPG_CUDA(cudaMemcpyAsync(rb->bounds, d_bounds, (nseg + 1) * 16, cudaMemcpyDeviceToHost, s), "copy bounds");
+    HPG_CUDA(cudaEventRecord(rb->done, s), "result event");
+    // the next batch goes to the GPU behind these copies
+    if (have_next) {
+      std::string e2;
+      if (launch(next, &e2) != 0) fail(next, e2);
+      else *next_launched = true;
+    }
+    HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
+    HPG_CUDA(cudaGetLastError(), "rebase kernel");
+    const double t = now_ms();
+    std::lock_guard<std::mutex> lk(mu);
+    for (size_t k = 0; k < nseg; ++k) {
+      ServeReq* q = b->reqs[k];
+      q->set = (int)(rb - sets);
+      q->read0 = h_seg[b->slot][k];
+      q->hit0 = rb->bounds[2 * k];
+      q->nh = rb->bounds[2 * k + 2] - q->hit0;
+      q->loc0 = rb->bounds[2 * k + 1];
+      q->nl = rb->bounds[2 * k + 3] - q->loc0;
+      q->state = 2;
+      q->t_done = t;
+      rb->refs++;
+    }
+    ++batches;
+    requests += nseg;
+    reads += b->n;
+    max_batch_reads = std::max<uint64_t>(max_batch_reads, b->n);
+    max_batch_reqs = std::max<uint64_t>(max_batch_reqs, nseg);
+    if (b->n >= 1024) {  // smoothed, biased up: admission must not undershoot
+      const double hpr = (double)r.n_hits / b->n, rpr = (double)r.n_locs / b->n;
+      hits_per_read = std::max(hpr, 0.8 * hits_per_read + 0.2 * hpr);
+      rows_per_read = std::max(rpr, 0.8 * rows_per_read + 0.2 * rpr);
+    }
+    plan_bytes = 0;
+    for (int i = 0; i < 33; ++i)
+      if (e->plans && e->plans[i]) plan_bytes += e->plans[i]->bytes;
+    b->reqs.clear();
+    cv_done.notify_all();
+    return 0;
+  }
+
+  void run() {
+    cudaSetDevice(e->device);
+    Batch cur, nxt;
+    int slot = 0;
+    bool have_cur = false;
+    for (;;) {
+      if (!have_cur) {
+        {
+          std::unique_lock<std::mutex> lk(mu);
+          cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+          if (queue.empty()) return;  // stopping with nothing left
+          cur.slot = slot;
+          slot ^= 1;
+          form(&cur);
+        }
+        prepare(&cur);
+        std::string err;
+        if (launch(&cur, &err) != 0) {
+          fail(&cur, err);
+          continue;
+        }
+        have_cur = true;
+      }
+      bool have_next = false;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!queue.empty()) {
+          nxt.slot = slot;
+          form(&nxt);
+          have_next = !nxt.reqs.empty();
+        }
+      }
+      if (have_next) {
+        slot ^= 1;
+        prepare(&nxt);  // host work overlapping the batch in flight
+      }
+      std::string err;
+      bool next_launched = false;
+      if (finish(&cur, &nxt, have_next, &next_launched, &err) != 0) {
+        fail(&cur, err);
+        if (have_next && !next_launched) fail(&nxt, "batch before it failed: " + err);
+        std::lock_guard<std::mutex> lk(mu);
+        fatal = err;
+      }
+      std::swap(cur, nxt);
+      have_cur = next_launched;
+    }
+  }
+};
+
+Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_bases, uint64_t hbm_budget,
+                      uint32_t max_results, std::string* err) {
+  if (max_batch_reads == 0 || max_batch_reads >= (1ull << 30)) {
+    *err = "batch capacity must be 1 .. 2^30-1 reads";
+    return nullptr;
+  }
+  if (cudaSetDevice(e->device) != cudaSuccess) {
+    *err = "cudaSetDevice failed";
+    return nullptr;
+  }
+  Server* S = new Server();
+  S->e = e;
+  S->max_reads = max_batch_reads;
+  S->max_bases = max_batch_bases ? max_batch_bases : (uint64_t)max_batch_reads * 320;
+  S->max_results = max_results;
+  if (hbm_budget == 0) {  // a quarter of what is free now
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    hbm_budget = fr / 4;
+  }
+  S->budget = hbm_budget;
+  bool ok = true;
+  for (int k = 0; k < 2 && ok; ++k) {
+    ok = cudaHostAlloc(reinterpret_cast<void**>(&S->h_offs[k]), (max_batch_reads + 1) * 8, 0) == cudaSuccess &&
+         cudaHostAlloc(reinterpret_cast<void**>(&S->h_seg[k]), (S->max_segs + 1) * 4, 0) == cudaSuccess;
+  }
+  ok = ok && cudaMalloc(&S->d_seg, (S->max_segs + 1) * 4) == cudaSuccess &&
+       cudaMalloc(&S->d_bounds, (S->max_segs + 1) * 16) == cudaSuccess;
+  for (int k = 0; k < kSets && ok; ++k) ok = cudaEventCreateWithFlags(&S->sets[k].done, cudaEventDisableTiming) ==
+                                            cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    *err = "out of memory (serving buffers)";
+    server_destroy(S);
+    return nullptr;
+  }
+  S->worker = std::thread([S] { S->run(); });
+  return S;
+}
+
+void server_destroy(Server* S) {
+  if (!S) return;
+  if (S->worker.joinable()) {
+    {
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->stop = true;
+    }
+    S->cv_work.notify_all();
+    S->worker.join();
+  }
+  cudaStreamSynchronize(S->e->stream);
+  for (ResultBuf& rb : S->sets) {
+    cudaFreeHost(rb.hits);
+    cudaFreeHost(rb.locs);
+    cudaFreeHost(rb.cnt);
+    cudaFreeHost(rb.trunc);
+    cudaFreeHost(rb.bounds);
+    if (rb.done) cudaEventDestroy(rb.done);
+  }
+  for (int k = 0; k < 2; ++k) {
+    cudaFreeHost(S->h_offs[k]);
+    cudaFreeHost(S->h_seg[k]);
+  }
+  cudaFree(S->d_seg);
+  cudaFree(S->d_bounds);
+  for (auto& kv : S->reqs) delete kv.second;
+  delete S;
+}
+
+int server_submit(Server* S, const char* seqs, const uint64_t* offs, size_t n, uint64_t* ticket, std::string* err) {
+  if (n > S->max_reads) {
+    *err = "request has more reads than the batch capacity";
+    return -1;
+  }
+  if (n && (!seqs || !offs)) {
+    *err = "null reads";
+    return -1;
+  }
+  for (size_t i = 0; i < n; ++i) {
+    if (offs[i + 1] < offs[i] || offs[i + 1] - offs[i] > 32767) {
+      *err = "read offsets must be non-decreasing and reads at most 32767 bases";
+      return -1;
+    }
+  }
+  const uint64_t bases = n ? offs[n] - offs[0] : 0;
+  if (bases > S->max_bases) {
+    *err = "request has more bases than the batch capacity";
+    return -1;
+  }
+  ServeReq* q = new ServeReq();
+  static const uint64_t zero = 0;
+  q->seqs = seqs;
+  q->offs = n ? offs : &zero;
+  q->n = (uint32_t)n;
+  q->bases = bases;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) {
+      delete q;
+      *err = "server is stopping";
+      return -1;
+    }
+    q->ticket = S->next_ticket++;
+    q->t_submit = now_ms();
+    S->reqs[q->ticket] = q;
+    S->queue.push_back(q);
+  }
+  S->cv_work.notify_one();
+  *ticket = q->ticket;
+  return 0;
+}
+
+int server_wait(Server* S, uint64_t ticket, hpg_result_set_t* view, double* latency_ms, int timeout_ms,
+                std::string* err) {
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) {
+    *err = "unknown or released ticket";
+    return -1;
+  }
+  ServeReq* q = it->second;
+  auto done = [&] { return q->state >= 2; };
+  if (timeout_ms < 0) {
+    S->cv_done.wait(lk, done);
+  } else if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) {
+    return 1;
+  }
+  if (q->state == 3) {
+    *err = q->err;
+    return -1;
+  }
+  const ResultBuf& rb = S->sets[q->set];
+  if (view) {
+    view->n_reads = q->n;
+    view->n_hits = q->nh;
+    view->hits = rb.hits + q->hit0;
+    view->n_locs = q->nl;
+    view->locs = rb.locs + q->loc0;
+    view->rs_count = rb.cnt + 2 * q->read0;
+    view->rs_truncated = rb.trunc + 2 * q->read0;
+  }
+  if (latency_ms) *latency_ms = q->t_done - q->t_submit;
+  return 0;
+}
+
+int server_release(Server* S, uint64_t ticket, std::string* err) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) {
+    *err = "unknown or released ticket";
+    return -1;
+  }
+  ServeReq* q = it->second;
+  if (q->state < 2) {
+    *err = "request still in flight";
+    return -1;
+  }
+  if (q->state == 2) S->sets[q->set].refs--;
+  S->reqs.erase(it);
+  delete q;
+  S->cv_sets.notify_all();
+  return 0;
+}
+
+void server_stats(Server* S, double* out, int n) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  const uint64_t plan_bytes = S->plan_bytes;
+  const double v[] = {(double)S->batches,
+                      (double)S->requests,
+                      (double)S->reads,
+                      S->batches ? (double)S->reads / S->batches : 0.0,
+                      S->gpu_ms,
+                      (double)S->regrows,
+                      (double)plan_bytes,
+                      (double)S->budget,
+                      (double)S->max_batch_reads,
+                      (double)S->max_batch_reqs,
+                      (double)S->queue.size(),
+                      S->hits_per_read,
+                      S->rows_per_read};
+  for (int i = 0; i < n && i < (int)(sizeof(v) / sizeof(v[0])); ++i) out[i] = v[i];
+}
+
+}  // namespace hpgbwt

@@ -92,6 +92,14 @@ def load() -> ctypes.CDLL:
                                      ctypes.POINTER(ctypes.c_ulonglong)]
     lib.bwt_gpu_set_load_mode.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_load_mode.argtypes = [vp]
+    lib.bwt_gpu_server_new.restype = vp
+    lib.bwt_gpu_server_new.argtypes = [vp, sz, u64, u64, u32]
+    lib.bwt_gpu_server_submit.argtypes = [vp, vp, vp, sz, ctypes.POINTER(ctypes.c_uint64)]
+    lib.bwt_gpu_server_wait.argtypes = [vp, u64, ctypes.POINTER(ResultSetC), ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_int]
+    lib.bwt_gpu_server_release.argtypes = [vp, u64]
+    lib.bwt_gpu_server_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    lib.bwt_gpu_server_free.argtypes = [vp]
     lib.bwt_gpu_set_graph.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_graph.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
@@ -244,3 +252,69 @@ class GpuIndex:
 
     def set_chunk(self, reads: int) -> None:
         self.lib.bwt_gpu_set_chunk(self.handle, reads)
+
+
+SERVER_STATS = ("batches", "requests", "reads", "mean_batch_reads", "batch_wall_ms", "regrowths", "plan_bytes",
+                "hbm_budget", "max_batch_reads", "max_batch_requests", "queued", "hits_per_read", "rows_per_read")
+
+
+class Server:
+    """The serving form of an index (bwt_gpu_server_*): submit read sets from
+    any thread, wait for each; results of a request equal a lone search of it."""
+
+    def __init__(self, index: GpuIndex, max_batch_reads: int, max_batch_bases: int = 0, hbm_budget: int = 0,
+                 max_results: int = 1 << 16):
+        self.lib = index.lib
+        self.handle = self.lib.bwt_gpu_server_new(index.handle, max_batch_reads, max_batch_bases, hbm_budget,
+                                                  max_results)
+        if not self.handle:
+            raise RuntimeError(self.lib.bwt_gpu_last_error().decode())
+        self._held = {}  # submitted arrays stay alive until their request is released
+
+    def submit(self, seq: np.ndarray, offsets: np.ndarray) -> int:
+        seq = np.ascontiguousarray(seq, dtype=np.uint8)
+        offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+        t = ctypes.c_uint64()
+        rc = self.lib.bwt_gpu_server_submit(self.handle, seq.ctypes.data, offsets.ctypes.data, len(offsets) - 1,
+                                            ctypes.byref(t))
+        if rc != 0:
+            raise RuntimeError(self.lib.bwt_gpu_last_error().decode())
+        self._held[t.value] = (seq, offsets)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1, copy: bool = True, release: bool = True):
+        """(Result or None if timed out, latency ms).  With copy the view is copied out and released."""
+        rs = ResultSetC()
+        lat = ctypes.c_double()
+        rc = self.lib.bwt_gpu_server_wait(self.handle, ticket, ctypes.byref(rs), ctypes.byref(lat), timeout_ms)
+        if rc < 0:
+            self._held.pop(ticket, None)
+            raise RuntimeError(self.lib.bwt_gpu_last_error().decode())
+        if rc == 1:
+            return None, None
+        res = result_from_c(rs, rs.n_reads) if copy else rs
+        if copy and release:
+            self.release(ticket)
+        return res, lat.value
+
+    def release(self, ticket: int) -> None:
+        self._held.pop(ticket, None)
+        if self.lib.bwt_gpu_server_release(self.handle, ticket) != 0:
+            raise RuntimeError(self.lib.bwt_gpu_last_error().decode())
+
+    def stats(self) -> dict:
+        a = (ctypes.c_double * len(SERVER_STATS))()
+        self.lib.bwt_gpu_server_stats(self.handle, a, len(SERVER_STATS))
+        return dict(zip(SERVER_STATS, list(a)))
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.bwt_gpu_server_free(self.handle)
+            self.handle = None
+            self._held.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -147,6 +147,9 @@ def _edit_plan(kind: str, n: int, lens: np.ndarray, rng: np.random.Generator) ->
         has = rng.random(n) < p_any
         which = rng.choice(3, size=n, p=np.array([p_s, p_i, p_d]) / (p_s + p_i + p_d)) + 1
         return np.where(has, which, 0).astype(np.int8)
+    if kind == "subst_capped":  # 0.5 % substitution per base, at most one
+        has = rng.random(n) < 1.0 - (1.0 - 0.005) ** lens
+        return np.where(has, 1, 0).astype(np.int8)
     if kind == "mix_30_50_20":  # 30 % exact, 50 % one substitution, 20 % one indel
         u = rng.random(n)
         e = np.zeros(n, dtype=np.int8)
@@ -253,3 +256,44 @@ def from_strings(seqs: list[bytes]) -> ReadSet:
     seq = np.frombuffer(b"".join(seqs), dtype=np.uint8).copy()
     z = np.zeros(len(seqs), dtype=np.int64)
     return ReadSet(seq, offs, z, z.astype(np.int8), z.astype(np.int8))
+
+
+def reads_fast_var(g: np.ndarray, n: int, seed: int, lo: int, hi: int, edits: str = "none",
+                   chunk: int = 200_000) -> ReadSet:
+    """Vectorised sampler for reads of uniform length in [lo, hi] (large read
+    sets): the same models as reads(), drawn row-wise over fixed-width tiles."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(lo, hi + 1, size=n)
+    plan = _edit_plan(edits, n, lens, rng)
+    pos = (rng.random(n) * (len(g) - lens - 1)).astype(np.int64)
+    strand = (rng.random(n) < 0.5).astype(np.int8)
+    cut = (rng.random(n) * (lens - 1)).astype(np.int64) + 1          # deletion: in [1, L)
+    at = (rng.random(n) * np.maximum(lens - 2, 1)).astype(np.int64) + 1  # insertion: in [1, L-1)
+    ins_base = rng.integers(0, 4, size=n, dtype=np.uint8)
+    sat = (rng.random(n) * lens).astype(np.int64)                     # substitution: in [0, L)
+    sdelta = rng.integers(1, 4, size=n, dtype=np.uint8)
+    offs = np.zeros(n + 1, dtype=np.uint64)
+    np.cumsum(lens, out=offs[1:])
+    out = np.empty(int(offs[-1]), dtype=np.uint8)
+    W = hi + 1
+    col = np.arange(hi)[None, :]
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        L = lens[a:b, None]
+        frag = g[np.minimum(pos[a:b, None] + np.arange(W)[None, :], len(g) - 1)]  # rows x (hi + 1); past L unused
+        src = col.repeat(b - a, axis=0)
+        d = np.nonzero(plan[a:b] == 3)[0]
+        src[d] = np.where(col >= cut[a:b][d, None], col + 1, col)
+        ii = np.nonzero(plan[a:b] == 2)[0]
+        src[ii] = np.where(col > at[a:b][ii, None], col - 1, col)
+        base = np.take_along_axis(frag, src, axis=1)
+        base[ii, at[a:b][ii]] = ins_base[a:b][ii]
+        rows = np.nonzero(plan[a:b] == 1)[0]
+        base[rows, sat[a:b][rows]] = (base[rows, sat[a:b][rows]] + sdelta[a:b][rows]) % 4
+        rc = np.nonzero(strand[a:b] == 1)[0]
+        if len(rc):
+            ridx = np.clip(L[rc] - 1 - col, 0, hi - 1)
+            base[rc] = _COMP[np.take_along_axis(base[rc], ridx, axis=1)]
+        keep = col < L
+        out[offs[a]:offs[b]] = _ASCII[base[keep]]
+    return ReadSet(out, offs, pos, strand, plan)

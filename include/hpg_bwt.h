@@ -239,6 +239,39 @@ size_t bwt_gpu_noalloc_scratch_bytes(void);
 /* Message of the last failed bwt_gpu_search1_noalloc call on this thread. */
 const char *bwt_gpu_noalloc_last_error(void);
 
+/* ---- Serving form (no reference counterpart: the reference maps each batch
+ * synchronously in the caller's thread, bwt.c:1097-1160).  A server owns the
+ * index's stream until freed; other calls on that index meanwhile race.
+ *
+ * Requests of any size up to max_batch_reads / max_batch_bases are submitted
+ * from any thread and mapped with BWSearch1 exactly as bwt_gpu_search_batch
+ * maps them (HPG_BWT_MODE_SEARCH1, batched form, max_results per (read,
+ * strand)): the result of a request is the same alone and in any mix.  A
+ * worker thread admits waiting requests in arrival order while they fit the
+ * batch capacity and the HBM budget (0 = a quarter of the device memory free
+ * at creation), runs them as one graph replay, and forms the next batch from
+ * new arrivals while a batch is on the GPU.
+ *
+ * submit: the reads stay in the caller's memory (pinned memory copies fastest)
+ * until wait returns for the ticket.  wait: 0 done, 1 timed out (timeout_ms
+ * >= 0), -1 failed (bwt_gpu_last_error); `view` then points into the server's
+ * pinned result buffers, read and hit ids relative to the request, valid until
+ * release.  Unreleased requests hold their batch's buffers (three in turn).
+ * stats: {batches, requests, reads, mean reads per batch, batch wall ms (sum),
+ * pool regrowths, device bytes of the captured plans, HBM budget, largest
+ * batch (reads), largest batch (requests), queued requests, hits per read,
+ * rows per read}. */
+typedef struct bwt_gpu_server bwt_gpu_server_t;
+bwt_gpu_server_t *bwt_gpu_server_new(bwt_index_t *index, size_t max_batch_reads, uint64_t max_batch_bases,
+                                     uint64_t hbm_budget_bytes, uint32_t max_results);
+int bwt_gpu_server_submit(bwt_gpu_server_t *server, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                          uint64_t *ticket);
+int bwt_gpu_server_wait(bwt_gpu_server_t *server, uint64_t ticket, hpg_result_set_t *view, double *latency_ms,
+                        int timeout_ms);
+int bwt_gpu_server_release(bwt_gpu_server_t *server, uint64_t ticket);
+void bwt_gpu_server_stats(bwt_gpu_server_t *server, double *out, int n);
+void bwt_gpu_server_free(bwt_gpu_server_t *server);
+
 #ifdef __cplusplus
 }
 #endif

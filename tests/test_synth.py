@@ -37,3 +37,30 @@ def test_error_free_reads_come_from_the_genome():
     for i in range(len(r)):
         s = r.read(i)
         assert s in text or s in rc
+
+
+def test_reads_fast_var_models():
+    """The vectorised variable-length sampler draws the same edit models as reads()."""
+    g = synth.genome("iid", 50_000, 3)
+    for edits in ("none", "mix_30_50_20", "subst_capped"):
+        rs = synth.reads_fast_var(g, 3000, 11, 50, 300, edits)
+        lens = np.diff(rs.offsets.astype(np.int64))
+        assert lens.min() >= 50 and lens.max() <= 300 and len(rs.seq) == lens.sum()
+        comp = {ord("A"): 3, ord("C"): 2, ord("G"): 1, ord("T"): 0}
+        code = {ord("A"): 0, ord("C"): 1, ord("G"): 2, ord("T"): 3}
+        for i in range(0, 3000, 7):
+            r = rs.seq[rs.offsets[i]:rs.offsets[i + 1]]
+            c = np.array([comp[x] for x in r[::-1]] if rs.truth_strand[i] else [code[x] for x in r], np.uint8)
+            p, L, e = int(rs.truth_pos[i]), len(c), int(rs.edit[i])
+            if e == 0:
+                assert np.array_equal(c, g[p:p + L])
+            elif e == 1:
+                assert int((c != g[p:p + L]).sum()) == 1
+            elif e == 3:  # one genome base left out
+                f = g[p:p + L + 1]
+                assert any(np.array_equal(c, np.delete(f, k)) for k in range(1, L))
+            else:  # one base inserted
+                f = g[p:p + L - 1]
+                k = next(k for k in range(L) if k >= L - 1 or c[k] != f[k])
+                assert np.array_equal(np.delete(c, k), f) or any(
+                    np.array_equal(np.delete(c, j), f) for j in range(1, L - 1))
