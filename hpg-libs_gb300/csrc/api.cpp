@@ -13,6 +13,7 @@
 #include "hpg_bwt.h"
 #include "index_format.hpp"
 #include "serve.hpp"
+#include "host_pool.hpp"
 
 using namespace hpgbwt;
 
@@ -174,10 +175,10 @@ int bwt_gpu_search_batch(bwt_index_t* index, int mode, int form, const char* seq
 
 void bwt_gpu_result_free(hpg_result_set_t* out) {
   if (!out) return;
-  std::free(out->hits);
-  std::free(out->locs);
-  std::free(out->rs_count);
-  std::free(out->rs_truncated);
+  host_pool_free(out->hits);
+  host_pool_free(out->locs);
+  host_pool_free(out->rs_count);
+  host_pool_free(out->rs_truncated);
   std::memset(out, 0, sizeof(*out));
 }
 

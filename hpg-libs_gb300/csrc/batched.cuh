@@ -72,7 +72,7 @@ struct BatchedTuning {
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
 };
 
-constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u;
+constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u, kStatusBadInput = 8u;
 
 // Locate sizes of the graph form: with `status` set, the hit and row counts
 // are read from device memory, rows beyond `locs_cap` raise kStatusLocFull,

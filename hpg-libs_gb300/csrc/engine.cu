@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine_internal.hpp"
+#include "host_pool.hpp"
 
 namespace hpgbwt {
 
@@ -717,10 +718,10 @@ int host_result(Engine* e, const DeviceResult& r, size_t n_reads, hpg_result_set
   out->n_reads = n_reads;
   out->n_hits = r.n_hits;
   out->n_locs = r.n_locs;
-  out->hits = (hpg_hit_t*)std::malloc((r.n_hits + 1) * sizeof(hpg_hit_t));
-  out->locs = (hpg_loc_t*)std::malloc((r.n_locs + 1) * sizeof(hpg_loc_t));
-  out->rs_count = (uint32_t*)std::malloc((2 * n_reads + 1) * 4);
-  out->rs_truncated = (uint8_t*)std::malloc(2 * n_reads + 1);
+  out->hits = (hpg_hit_t*)host_pool_alloc((r.n_hits + 1) * sizeof(hpg_hit_t));
+  out->locs = (hpg_loc_t*)host_pool_alloc((r.n_locs + 1) * sizeof(hpg_loc_t));
+  out->rs_count = (uint32_t*)host_pool_alloc((2 * n_reads + 1) * 4);
+  out->rs_truncated = (uint8_t*)host_pool_alloc(2 * n_reads + 1);
   if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
     *err = "out of host memory";
     return -1;
@@ -734,7 +735,36 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
                        uint32_t max_results, hpg_result_set_t* out, std::string* err) {
   std::memset(out, 0, sizeof(*out));
   HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  if (n_reads && offs[n_reads] < offs[0]) {
+    *err = "read offsets must be non-decreasing";
+    return -1;
+  }
   const uint64_t total = n_reads ? offs[n_reads] - offs[0] : 0;
+  cudaStream_t s = e->stream;
+  std::vector<uint64_t> rel;
+  if (form == kFormBatched && mode == HPG_BWT_MODE_SEARCH1 && e->use_graph) {
+    // the graph checks every read's offsets on the device (no host pass over them)
+    if (n_reads >= (1ull << 31)) {
+      *err = "too many reads in one batch";
+      return -1;
+    }
+    if (total > (1ull << 40)) {
+      *err = "batch too large";
+      return -1;
+    }
+    const uint64_t* o = offs;
+    if (n_reads && offs[0] != 0) {
+      rel.resize(n_reads + 1);
+      for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
+      o = rel.data();
+    }
+    static const uint64_t zero = 0;
+    DeviceResult r;
+    if (finish_graph(e, seqs + (n_reads ? offs[0] : 0), n_reads ? o : &zero, (uint32_t)n_reads, total, max_results,
+                     &r, err) != 0)
+      return -1;
+    return host_result(e, r, n_reads, out, err);
+  }
   uint32_t max_len = 0;
   for (size_t i = 0; i < n_reads; ++i) {
     if (offs[i + 1] < offs[i]) {
@@ -752,18 +782,8 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
     *err = "out of device memory (reads)";
     return -1;
   }
-  std::vector<uint64_t> rel(n_reads + 1);
+  rel.resize(n_reads + 1);
   for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
-  cudaStream_t s = e->stream;
-  if (form == kFormBatched && mode == HPG_BWT_MODE_SEARCH1 && e->use_graph) {
-    if (n_reads >= (1ull << 31)) {
-      *err = "too many reads in one batch";
-      return -1;
-    }
-    DeviceResult r;
-    if (finish_graph(e, seqs + offs[0], rel.data(), (uint32_t)n_reads, total, max_results, &r, err) != 0) return -1;
-    return host_result(e, r, n_reads, out, err);
-  }
   if (total) HPG_CUDA(cudaMemcpyAsync(e->seqs.p, seqs + offs[0], total, cudaMemcpyHostToDevice, s), "upload reads");
   HPG_CUDA(cudaMemcpyAsync(e->offs.p, rel.data(), (n_reads + 1) * 8, cudaMemcpyHostToDevice, s), "upload offsets");
   DeviceResult r;

@@ -107,6 +107,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   cudaMemsetAsync(g->rows, 0, (size_t)g->res_cap * 4, s);
   if (census) cudaMemsetAsync(census, 0, 8, s);
   launch_encode_dev(g->seqs, g->bases_cap, g->offs, g->hdr, g->n_cap, e->d_table, g->codes, g->ok, s);
+  launch_check_offsets(g->offs, g->hdr, g->n_cap, g->bases_cap, g->ok, status, s);
   record(g->ev[1], s);
 
   BatchedParams p;
@@ -274,6 +275,10 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
   HPG_CUDA(cudaStreamSynchronize(e->stream), "batched pipeline");
   const uint64_t* h = g->h_summary;
   const uint32_t status = (uint32_t)h[0];
+  if (status & kStatusBadInput) {
+    *err = "read offsets must be non-decreasing and reads at most 32767 bases";
+    return -1;
+  }
   if (status) {
     grow->res_cap = g->res_cap;
     grow->spill_cap = g->spill_cap;

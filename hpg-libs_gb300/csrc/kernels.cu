@@ -3,6 +3,7 @@
 // device-wide scan, ordered hit gather and the locate pass.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.cuh"
@@ -369,6 +370,33 @@ void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, u
   const unsigned grid = (unsigned)(chunks < 152ull * 32 * 8 ? (chunks + 255) / 256 : 152ull * 32);
   count_launches(1);
   encode_kernel<<<grid, 256, 0, s>>>(ascii, total, offs, n_reads, d_table, codes, ok, nullptr);
+}
+
+namespace {
+
+// Graph form: read offsets checked on the device (non-decreasing, reads at
+// most 32767 bases, inside the staged bases).  A bad read is switched off so
+// no kernel reads past its buffers, and the status word reports the batch.
+__global__ void check_offsets_kernel(const uint64_t* __restrict__ offs, const uint32_t* __restrict__ n_dev,
+                                     uint64_t bases_cap, uint8_t* __restrict__ ok, unsigned* status) {
+  const uint32_t n = *n_dev;
+  const uint64_t end = offs[n];
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const uint64_t b0 = offs[r], b1 = offs[r + 1];
+    if (b1 < b0 || b1 - b0 > 32767 || b1 > end || end > bases_cap) {
+      ok[r] = 0;
+      atomicOr(status, 8u);
+    }
+  }
+}
+
+}  // namespace
+
+void launch_check_offsets(const uint64_t* offs, const uint32_t* n_dev, uint32_t n_cap, uint64_t bases_cap,
+                          uint8_t* ok, unsigned* status, cudaStream_t s) {
+  const unsigned grid = (unsigned)std::min<uint64_t>((n_cap + 255) / 256, 152ull * 8);
+  count_launches(1);
+  check_offsets_kernel<<<grid ? grid : 1, 256, 0, s>>>(offs, n_dev, bases_cap, ok, status);
 }
 
 void launch_encode_dev(const uint8_t* ascii, uint64_t bases_cap, const uint64_t* offs, const uint32_t* n_dev,

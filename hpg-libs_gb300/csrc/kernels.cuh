@@ -33,6 +33,11 @@ void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, u
 void launch_encode_dev(const uint8_t* ascii, uint64_t bases_cap, const uint64_t* offs, const uint32_t* n_dev,
                        uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
 
+// Graph form: reads whose offsets are decreasing, longer than 32767 bases or
+// past the staged bases get ok = 0 and set bit 8 of *status.
+void launch_check_offsets(const uint64_t* offs, const uint32_t* n_dev, uint32_t n_cap, uint64_t bases_cap,
+                          uint8_t* ok, unsigned* status, cudaStream_t s);
+
 // Exact backward search on both strands (mode EXACT), one thread per (read, strand).
 void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,
                   uint32_t nr, uint4* slots, uint32_t* rs_count, uint8_t* rs_trunc,

@@ -122,8 +122,9 @@ int hpg_bwt_build_index(const char *ref_file, const char *output_dir, unsigned i
  * Reads: seqs[offsets[i] .. offsets[i+1]) in ASCII, n_reads + 1 offsets.
  * Reads shorter than 3 bases, or with characters outside the index alphabet
  * (undefined in the reference), get no hits.
- * Output: host arrays malloc'ed by the library; release with
- * bwt_gpu_result_free.  Returns 0, or -1 (see bwt_gpu_last_error). */
+ * Output: host arrays allocated by the library (large ones page-locked and
+ * reused across calls); release with bwt_gpu_result_free only.  Returns 0, or
+ * -1 (see bwt_gpu_last_error). */
 int bwt_gpu_search_batch(bwt_index_t *index, int mode, int form, const char *seqs, const uint64_t *offsets,
                          size_t n_reads, uint32_t max_results, hpg_result_set_t *out);
 void bwt_gpu_result_free(hpg_result_set_t *out);

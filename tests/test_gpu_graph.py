@@ -104,3 +104,24 @@ def test_graph_replay_launches_counted(case_factory):
         per_replay = lib.launch_count() - n0
         g.search(reads, form=lib.FORM_BATCHED)
         assert lib.launch_count() - n0 == 2 * per_replay and per_replay >= 10
+
+
+def test_graph_rejects_bad_offsets(case_factory):
+    """The graph checks read offsets on the device: bad reads are switched off
+    before any kernel reads them and the call fails; the next call is clean."""
+    c = case_factory("repeats", 300_000, 3, 3)
+    good = synth.reads(c.genome, 500, 81, length=100)
+    want = PortOracle(c.index).search(good, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
+    seq = np.frombuffer(b"ACGT" * 20000, dtype=np.uint8)
+    bad_sets = [np.array([0, 100, 50, 150], dtype=np.uint64),        # decreasing inside the batch
+                np.array([0, 40_000, 40_100], dtype=np.uint64)]      # a read longer than 32767 bases
+
+    class RS:
+        pass
+    with lib.GpuIndex(c.index) as g:
+        for offs in bad_sets:
+            rs = RS()
+            rs.seq, rs.offsets = seq, offs
+            with pytest.raises(RuntimeError, match="non-decreasing"):
+                g.search(rs, form=lib.FORM_BATCHED)
+            _same(g.search(good, form=lib.FORM_BATCHED), want)
