@@ -776,13 +776,6 @@ __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const 
 
 // --------------------------------------------------------------- locate --
 
-// One locate work item per SA row: the row, the owning hit, the physical
-// direction and len_calc (bwt.c:2025-2036), so that a lane starting a walk
-// needs a single 16-byte load.
-struct RowItem {
-  uint32_t row, hit, out, phys_len;  // out: output index; phys_len: direction << 31 | len_calc
-};
-
 // Rows on the backward index fill the item array from the front, rows on the
 // forward index from the back, so walks claimed in order touch one direction
 // at a time.
@@ -1080,6 +1073,21 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
   if (need < blocks) blocks = need;
   count_launches(1);
   locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, items, n_locs, out, row_ctr, census, z);
+}
+
+void launch_locate_items(const DevIndex& X, const RowItem* items, uint64_t n_items, hpg_loc_t* out,
+                         unsigned int* row_ctr, int num_sms, cudaStream_t s) {
+  if (!n_items) return;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t blocks = (uint64_t)num_sms * per_sm;
+  const uint64_t need = (n_items + kBlock * kRowsPerClaim - 1) / (kBlock * kRowsPerClaim);
+  if (need < blocks) blocks = need;
+  cudaMemsetAsync(row_ctr, 0, 4, s);
+  count_launches(1);
+  locate_persistent_kernel<<<(unsigned)blocks, kBlock, 0, s>>>(X, items, n_items, out, row_ctr, nullptr,
+                                                               LocateSizes());
 }
 
 size_t locate_row_item_bytes() { return sizeof(RowItem); }

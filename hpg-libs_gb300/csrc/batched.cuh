@@ -72,6 +72,13 @@ struct BatchedTuning {
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
 };
 
+// One locate work item per SA row: the row, the owning hit (or request), the
+// output index, and the physical direction with len_calc (bwt.c:2025-2036), so
+// that a lane starting a walk needs a single 16-byte load.
+struct RowItem {
+  uint32_t row, hit, out, phys_len;  // phys_len: direction << 31 | len_calc
+};
+
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u, kStatusBadInput = 8u;
 
 // Locate sizes of the graph form: with `status` set, the hit and row counts
@@ -110,5 +117,8 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
                               unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s,
                               const LocateSizes& z = LocateSizes());
 size_t locate_row_item_bytes();
+// Locate caller-built rows (device array of n_items RowItem); out[item.out] per row.
+void launch_locate_items(const DevIndex& X, const RowItem* items, uint64_t n_items, hpg_loc_t* out,
+                         unsigned int* row_ctr, int num_sms, cudaStream_t s);
 
 }  // namespace hpgbwt

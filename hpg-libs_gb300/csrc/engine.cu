@@ -353,9 +353,11 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   }
   launch_expand_hits(ptr<PendingHit>(e->b_sorted), ptr<uint64_t>(e->b_seg), ptr<uint64_t>(e->hit_off),
                      ptr<uint32_t>(e->rs_count), (uint32_t)T, ptr<hpg_hit_t>(e->hits), ptr<uint32_t>(e->rows), s);
-  launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
   uint64_t l_tot = 0;
-  HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
+  if (!e->skip_locate) {
+    launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
+    HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
+  }
   HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
   cudaEventRecord(e->cev[2], s);
   if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t)) ||

@@ -72,4 +72,20 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
                     uint32_t max_len, uint32_t max_results, int* table, int max_rows, int* rows_out,
                     std::string* err);
 
+// ---- device passes of the alignment-list layer (map_device.cu) ----
+// Host reads in (ASCII + n+1 offsets).  kl gets per read {k+, l+, k-, l-}:
+// the '+' backward search over backward and the '-' forward search over
+// forward_rev of bwt_map_exact_seq, where each stopped (k = l + 1 if a base failed).
+int engine_exact_api(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t* kl, std::string* err);
+// For the listed reads: per chain {good steps, k, l, 0} of the four vector searches.
+int engine_anchor_scan(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* reads, size_t m,
+                       uint32_t* out, std::string* err);
+struct MapRow {
+  uint32_t row, phys, len_calc;  // SA row, physical index direction (0 backward, 1 forward), located length
+};
+int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, std::string* err);
+// Batched form: hits only, no located rows.
+void engine_set_skip_locate(Engine* e, int on);
+uint32_t engine_sa_top(Engine* e);  // last SA row (n)
+
 }  // namespace hpgbwt

@@ -40,6 +40,7 @@ struct GraphPlan {
   BatchedTuning tuning;
   uint32_t load_mode = 0;
   bool census = false;
+  bool skip_locate = false;  // hits only (the alignment-list layer locates the rows it needs)
   // device buffers
   uint8_t* seqs = nullptr;
   uint64_t* offs = nullptr;
@@ -109,6 +110,7 @@ struct Engine {
   // batched form replayed from a captured CUDA graph (graph.cu)
   GraphPlan** plans = nullptr;  // by power-of-two read capacity
   bool use_graph = true;
+  bool skip_locate = false;  // batched form: hits only, no located rows
 };
 
 // Grow-only device buffer; `keep` preserves the old contents.

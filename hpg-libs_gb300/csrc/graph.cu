@@ -66,7 +66,7 @@ bool same_settings(const GraphPlan* g, const Engine* e) {
   const BatchedTuning& b = e->tuning;
   return a.block == b.block && a.blocks_per_sm == b.blocks_per_sm && a.stack == b.stack && a.chunk == b.chunk &&
          a.min_blocks == b.min_blocks && a.split == b.split && g->load_mode == e->X.load_mode &&
-         g->census == e->census_on;
+         g->census == e->census_on && g->skip_locate == e->skip_locate;
 }
 
 void record(cudaEvent_t ev, cudaStream_t s) { cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal); }
@@ -163,8 +163,9 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   z.n_hits = g->hit_off + T;
   z.n_locs = g->loc_off + g->res_cap;
   z.locs_cap = g->locs_cap;
-  launch_locate_persistent(e->X, g->hits, g->loc_off, g->res_cap, g->locs_cap, g->offs, g->locs, g->items, ctr + 5,
-                           census, e->num_sms, s, z);
+  if (!g->skip_locate)
+    launch_locate_persistent(e->X, g->hits, g->loc_off, g->res_cap, g->locs_cap, g->offs, g->locs, g->items,
+                             ctr + 5, census, e->num_sms, s, z);
   record(g->ev[5], s);
   count_launches(1);
   graph_summary_kernel<<<1, 1, 0, s>>>(ctr, z.n_hits, z.n_locs, census, g->summary_d);
@@ -244,6 +245,7 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   g->tuning = e->tuning;
   g->load_mode = e->X.load_mode;
   g->census = e->census_on;
+  g->skip_locate = e->skip_locate;
   if (old) cudaStreamSynchronize(e->stream);
   if (capture(e, g, err) != 0) {
     graph_plan_destroy(g);
@@ -301,7 +303,7 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
   r.n_reads = n;
   r.n_hits = h[2];
   r.hits = g->hits;
-  r.n_locs = h[3];
+  r.n_locs = g->skip_locate ? 0 : h[3];
   r.locs = g->locs;
   r.rs_count = g->kept;
   r.rs_truncated = g->trunc;

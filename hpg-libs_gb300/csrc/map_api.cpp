@@ -1,0 +1,647 @@
+// map_api.cpp -- the alignment-list entry points of c/src/aligners/bwt/bwt.c
+// (bwt_map_exact_*, bwt_map_inexact_*), served by the GPU passes of the engine.
+//
+// Every call maps its reads as one batch: the search on the device (the exact
+// pair of bwt_map_exact_seq, or BWSearch1 with hits only), then the host picks
+// the suffix-array rows the reference would locate (interval cap, mapping
+// filter), one device pass locates them, and the alignment records are built
+// here with the reference's field values, order and quirks.  Anchors
+// (bwt.c:1822-1869) take one more scan and locate pass for the reads that end
+// without alignments in a list flagged 1.
+#include <cinttypes>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.hpp"
+#include "hpg_bwt_api.h"
+
+using namespace hpgbwt;
+
+namespace {
+
+std::mutex g_mu;  // the engine's stream and workspace serve one call at a time
+
+[[noreturn]] void fatal(const std::string& what) {
+  // the reference's fatal path (bwt_commons.h:48-70): report and exit
+  std::fprintf(stderr, "[hpgbwt] %s\n", what.c_str());
+  std::exit(EXIT_FAILURE);
+}
+
+Engine* engine_for(bwt_index_t* idx) {
+  Engine* e = idx ? static_cast<Engine*>(idx->gpu_) : nullptr;
+  if (!e) fatal("bwt_map: the index has no GPU context (load it with bwt_index_new)");
+  return e;
+}
+
+char* dup_bytes(const char* s, size_t n) {
+  char* p = static_cast<char*>(std::malloc(n + 1));
+  if (!p) fatal("out of host memory");
+  if (n) std::memcpy(p, s, n);
+  p[n] = '\0';
+  return p;
+}
+
+char* dup_str(const char* s) { return dup_bytes(s, std::strlen(s)); }
+
+char* fmt(const char* f, unsigned long v) {
+  char buf[48];
+  std::snprintf(buf, sizeof buf, f, v);
+  return dup_str(buf);
+}
+
+// Reads of one call, concatenated for the device passes.
+struct Reads {
+  std::string seq;
+  std::vector<uint64_t> offs{0};
+  void add(const char* s, size_t n) {
+    seq.append(s, n);
+    offs.push_back(seq.size());
+  }
+  size_t n() const { return offs.size() - 1; }
+  size_t len(size_t i) const { return offs[i + 1] - offs[i]; }
+};
+
+// alignment_init_single_end (alignment.c:12-42) on a zeroed alignment_new().
+alignment_t* new_alignment(char* qname, char* seq, char* qual, int strand, unsigned chrom, int pos, char* cigar,
+                           int ncigar, int mapq, int mapped, int secondary) {
+  alignment_t* a = alignment_new();
+  if (!a) fatal("out of host memory");
+  a->query_name = qname;
+  a->sequence = seq;
+  a->quality = qual;
+  a->cigar = cigar;
+  a->chromosome = chrom;
+  a->position = pos;
+  a->mate_position = -1;
+  a->mate_chromosome = -1;
+  a->template_length = 0;
+  a->map_quality = mapq;
+  a->num_cigar_operations = ncigar;
+  a->is_paired_end = 0;
+  a->is_paired_end_mapped = 0;
+  a->is_seq_mapped = (uint8_t)mapped;
+  a->is_mate_mapped = 0;
+  a->seq_strand = (uint8_t)strand;
+  a->mate_strand = 0;
+  a->pair_num = 0;
+  a->secondary_alignment = (uint8_t)secondary;
+  a->fails_quality_check = 0;
+  a->pc_optical_duplicate = 0;
+  a->optional_fields = nullptr;
+  a->optional_fields_length = 0;
+  a->map_len = 0;
+  a->alig_data = nullptr;
+  return a;
+}
+
+// get_to_first_blank (commons/string_utils.c:400-428): skip a leading '@',
+// stop at ' ' or '/' or after `length` bytes.
+char* first_blank(const char* s, size_t length) {
+  char* out = static_cast<char*>(std::malloc(length + 2));
+  if (!out) fatal("out of host memory");
+  size_t i = s[0] == '@' ? 1 : 0, o = 0;
+  while (i < length && s[i] != ' ' && s[i] != '/') out[o++] = s[i++];
+  out[o] = '\0';
+  return out;
+}
+
+// ----------------------------------------------------------------- exact --
+
+// bwt_map_exact_seq (bwt.c:889-981) for every read: alignments in the
+// reference's order, '+' first.
+std::vector<std::vector<alignment_t*>> exact_alignments(Engine* e, const Reads& R, const bwt_optarg_t* opt) {
+  const size_t n = R.n();
+  std::string err;
+  std::vector<uint32_t> kl(4 * n + 4);
+  if (engine_exact_api(e, R.seq.data(), R.offs.data(), n, kl.data(), &err) != 0) fatal(err);
+  const size_t filter = (size_t)(long)opt->filter_read_mappings;
+  const uint64_t top = engine_sa_top(e);
+  struct Span {
+    size_t k, l;
+  };
+  std::vector<Span> span(2 * n);
+  std::vector<uint8_t> rc(n, 0);
+  std::vector<MapRow> rows;
+  for (size_t r = 0; r < n; ++r) {
+    size_t k_aux = 0, l_aux = 0;
+    for (int type = 1; type >= 0; --type) {
+      const size_t k = type ? kl[4 * r] : kl[4 * r + 2], l = type ? kl[4 * r + 1] : kl[4 * r + 3];
+      if (type == 0) rc[r] = (l_aux - k_aux + 1 < filter) ? 1 : 0;  // tested on the '+' interval (bwt.c:936)
+      k_aux = k;
+      l_aux = l;
+      if (l_aux - k_aux + 1 >= filter) l_aux = k_aux + 1;  // bwt.c:945-947
+      span[2 * r + (type ? 0 : 1)] = Span{k_aux, l_aux};
+      for (size_t j = k_aux; j <= l_aux && j <= top; ++j)  // rows past the array are not read
+        rows.push_back(MapRow{(uint32_t)j, 0u, (uint32_t)R.len(r)});
+    }
+  }
+  std::vector<hpg_loc_t> loc(rows.size() + 1);
+  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  std::vector<std::vector<alignment_t*>> out(n);
+  size_t at = 0;
+  for (size_t r = 0; r < n; ++r) {
+    const size_t len = R.len(r);
+    std::string strand_seq(R.seq.data() + R.offs[r], len);
+    unsigned num = 0;
+    for (int type = 1; type >= 0; --type) {
+      if (type == 0 && rc[r]) seq_reverse_complementary(&strand_seq[0], (unsigned)len);
+      const Span sp = span[2 * r + (type ? 0 : 1)];
+      for (size_t j = sp.k; j <= sp.l && j <= top; ++j, ++at) {
+        const hpg_loc_t& L = loc[at];
+        if (!L.valid) continue;
+        out[r].push_back(new_alignment(nullptr, dup_bytes(strand_seq.data(), len), nullptr, !type, L.chrom,
+                                       (int)(unsigned)L.position, fmt("%lu=", (unsigned long)len), 1, 254, 1,
+                                       num > 0));
+        ++num;
+      }
+    }
+  }
+  return out;
+}
+
+void announce(size_t n) {  // bwt.c:894 prints one line per mapped sequence
+  for (size_t i = 0; i < n; ++i) std::fputs("\tIn function ...\n", stdout);
+}
+
+// --------------------------------------------------------------- inexact --
+
+struct InexactRead {
+  const char* id;
+  const char* seq;
+  size_t len;
+  const char* revcomp;  // may be null: computed here
+  const char* quality;
+};
+
+// The output list of one read: the caller's array_list_t, or a fresh list
+// (batch forms) whose items the caller collects.
+struct OutList {
+  array_list_t* list = nullptr;
+  std::vector<void*> fresh;
+  int fresh_flag = 0;
+  size_t size() { return list ? array_list_size(list) : fresh.size(); }
+  void* get(size_t i) { return list ? array_list_get(i, list) : fresh[i]; }
+  void insert(void* p) {
+    if (list) array_list_insert(p, list);
+    else fresh.push_back(p);
+  }
+  int flag() { return list ? array_list_get_flag(list) : fresh_flag; }
+  void set_flag(int f) {
+    if (list) array_list_set_flag(f, list);
+    else fresh_flag = f;
+  }
+};
+
+// bwt_cigar_cpy (bwt.c:501-547): the read quality, reversed on the '-' strand.
+void quality_copy(alignment_t* a, const char* quality) {
+  const size_t n = std::strlen(quality);
+  std::free(a->quality);
+  a->quality = static_cast<char*>(std::malloc(n + 1));
+  if (!a->quality) fatal("out of host memory");
+  if (a->seq_strand == 0) {
+    std::memcpy(a->quality, quality, n);
+    a->quality[n] = '\0';
+  } else {
+    reverse_str(const_cast<char*>(quality), a->quality, n);
+  }
+}
+
+// add_optional_fields (bwt.c:3065-3100): AS, NH and NM as 3-byte tags with
+// 4-byte values; map quality becomes 255.
+void optional_fields(alignment_t* a, size_t n_mappings, int read_length) {
+  const int distance = a->map_quality;
+  int as = (int)(read_length * 1 - distance * 0.4);
+  as = as * 100 / read_length;
+  char* f = static_cast<char*>(std::calloc(100, 1));
+  if (!f) fatal("out of host memory");
+  const uint32_t nh = (uint32_t)n_mappings;
+  std::memcpy(f, "ASi", 3);
+  std::memcpy(f + 3, &as, 4);
+  std::memcpy(f + 7, "NHi", 3);
+  std::memcpy(f + 10, &nh, 4);
+  std::memcpy(f + 14, "NMi", 3);
+  std::memcpy(f + 17, &distance, 4);
+  a->map_quality = 255;
+  std::free(a->optional_fields);
+  a->optional_fields = reinterpret_cast<uint8_t*>(f);
+  a->optional_fields_length = 21;
+}
+
+// Per read after the search: what the reference locates, strand by strand.
+struct InexactPlan {
+  int exceeded_type = -1;          // strand (type) whose rows passed the filter, or -1
+  bool has_minus_results = false;  // the '-' helper returned results (bwt.c:2003-2006)
+  size_t row0[2] = {0, 0};         // first located row of each type's exact hits
+  std::vector<uint32_t> hits[2];   // included exact hits (indices into the hit array) per type
+};
+
+struct InexactOutcome {
+  size_t added = 0;       // alignments this call put in the list
+  bool anchors = false;   // list ended empty with flag 1
+};
+
+// Alignments of one read into its list (bwt.c:1896-2289, without the anchors).
+InexactOutcome assemble_inexact(const InexactRead& rd, const InexactPlan& P, const hpg_hit_t* hits,
+                                const hpg_loc_t* loc, OutList& L) {
+  InexactOutcome res;
+  const size_t len = rd.len;
+  if (len < 5) {  // bwt.c:1900-1917
+    L.insert(new_alignment(nullptr, dup_bytes(rd.seq, len), fmt("%lu", 0), 0, (unsigned)-1, -1,
+                           fmt("%luX", (unsigned long)len), 1, 0, 0, 0));
+    res.added = 1;
+    return res;
+  }
+  std::string rc_store;
+  const char* strand_seq = rd.seq;
+  size_t num = 0;
+  for (int type = 1; type >= 0; --type) {
+    if (type == 0 && P.has_minus_results) {
+      if (rd.revcomp) {
+        strand_seq = rd.revcomp;
+      } else {
+        rc_store.assign(rd.seq, len);
+        seq_reverse_complementary(&rc_store[0], (unsigned)len);
+        strand_seq = rc_store.data();
+      }
+    }
+    if (P.exceeded_type == type) {  // bwt.c:2180-2184
+      L.set_flag(2);
+      break;
+    }
+    std::vector<alignment_t*> tmp;
+    size_t at = P.row0[type];
+    for (uint32_t h : P.hits[type]) {
+      const hpg_hit_t& x = hits[h];
+      for (int64_t j = x.k; j <= x.l; ++j, ++at) {
+        const hpg_loc_t& q = loc[at];
+        if (!q.valid) continue;
+        tmp.push_back(new_alignment(dup_str(rd.id), dup_bytes(strand_seq, len), fmt("%lu", 0), !type, q.chrom,
+                                    (int)q.position, fmt("%luM", (unsigned long)len), 1, 0, 1, num > 0));
+      }
+    }
+    // alignments closer than 10 bp on one chromosome (bwt.c:2190-2221)
+    const int nm = (int)tmp.size();
+    std::vector<uint8_t> del(nm, 0);
+    for (int a1 = nm - 1; a1 >= 1; --a1) {
+      if (del[a1]) continue;
+      for (int a2 = a1 - 1; a2 >= 0; --a2) {
+        const size_t dist = (size_t)std::abs(tmp[a1]->position - tmp[a2]->position);
+        if (tmp[a1]->chromosome == tmp[a2]->chromosome && dist < 10 && !del[a2]) {
+          if (tmp[a1]->num_cigar_operations < tmp[a2]->num_cigar_operations) del[a2] = 1;
+          else del[a1] = 1;
+        }
+      }
+    }
+    bool primary_delete = false;
+    for (int m = nm - 1; m >= 0; --m) {  // taken from the back, appended (bwt.c:2223-2235)
+      alignment_t* a = tmp[m];
+      if (del[m]) {
+        if (!a->secondary_alignment) primary_delete = true;
+        alignment_free(a);
+      } else {
+        L.insert(a);
+        a->secondary_alignment = num > 0;
+        ++num;
+      }
+    }
+    if (primary_delete) static_cast<alignment_t*>(L.get(0))->secondary_alignment = 0;
+  }
+  res.added = num;
+  if (L.size() == 0) {
+    res.anchors = L.flag() == 1;
+  } else {
+    for (size_t i = 0; i < L.size(); ++i) {
+      alignment_t* a = static_cast<alignment_t*>(L.get(i));
+      quality_copy(a, rd.quality);
+      optional_fields(a, num, (int)len);
+    }
+    L.set_flag(0);
+  }
+  return res;
+}
+
+// Maps reads into their lists; returns per read what was added.
+std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead>& rds, const bwt_optarg_t* opt,
+                                        std::vector<OutList*>& lists) {
+  const size_t n = rds.size();
+  std::string err;
+  const int fr = opt->filter_read_mappings;
+  const size_t filter = (size_t)(long)fr;
+  // 1. BWSearch1 hits (result lists of capacity filter_read_mappings) for reads of 5+ bases
+  Reads R;
+  std::vector<uint32_t> gidx(n, UINT32_MAX);
+  for (size_t i = 0; i < n; ++i)
+    if (rds[i].len >= 5) {
+      gidx[i] = (uint32_t)R.n();
+      R.add(rds[i].seq, rds[i].len);
+    }
+  hpg_result_set_t rs;
+  std::memset(&rs, 0, sizeof rs);
+  if (R.n()) {
+    engine_set_skip_locate(e, 1);
+    const int rc = engine_search_host(e, HPG_BWT_MODE_SEARCH1, kFormBatched, R.seq.data(), R.offs.data(), R.n(),
+                                      fr > 0 ? (uint32_t)fr : 0u, &rs, &err);
+    engine_set_skip_locate(e, 0);
+    if (rc != 0) fatal(err);
+  }
+  std::vector<uint64_t> hit0(2 * R.n() + 1, 0);
+  for (size_t t = 0; t < 2 * R.n(); ++t) hit0[t + 1] = hit0[t] + rs.rs_count[t];
+  // 2. rows the reference locates: exact hits until a strand passes the filter
+  std::vector<InexactPlan> plan(n);
+  std::vector<MapRow> rows;
+  for (size_t i = 0; i < n; ++i) {
+    if (gidx[i] == UINT32_MAX) continue;
+    InexactPlan& P = plan[i];
+    const size_t g = gidx[i];
+    P.has_minus_results = rs.rs_count[2 * g + 1] > 0;
+    size_t tot = 0;  // rows counted over both strands (bwt.c:1978, 2148-2149)
+    for (int type = 1; type >= 0 && P.exceeded_type < 0; --type) {
+      const size_t t = 2 * g + (type ? 0 : 1);
+      P.row0[type] = rows.size();
+      const size_t mark = rows.size();
+      for (uint64_t h = hit0[t]; h < hit0[t + 1]; ++h) {
+        const hpg_hit_t& x = rs.hits[h];
+        if (x.nm) continue;
+        tot += (size_t)(x.l - x.k);
+        if (tot > filter) {
+          P.exceeded_type = type;
+          P.hits[type].clear();
+          rows.resize(mark);  // that strand's alignments are dropped
+          break;
+        }
+        P.hits[type].push_back((uint32_t)h);
+        const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)(type ? 0 : 1);  // direction = type ? dir : !dir
+        for (int64_t j = x.k; j <= x.l; ++j) rows.push_back(MapRow{(uint32_t)j, phys, (uint32_t)rds[i].len});
+      }
+    }
+  }
+  std::vector<hpg_loc_t> loc(rows.size() + 1);
+  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  // 3. alignment records, read by read in order
+  std::vector<InexactOutcome> out(n);
+  for (size_t i = 0; i < n; ++i) out[i] = assemble_inexact(rds[i], plan[i], rs.hits, loc.data(), *lists[i]);
+  bwt_gpu_result_free(&rs);
+  // 4. anchors for reads left without alignments in a list flagged 1 (bwt.c:2243-2273)
+  std::vector<uint32_t> need;
+  Reads A;
+  for (size_t i = 0; i < n; ++i)
+    if (out[i].anchors) {
+      need.push_back((uint32_t)A.n());
+      A.add(rds[i].seq, rds[i].len);
+    }
+  if (need.empty()) return out;
+  std::vector<uint32_t> ends(16 * need.size());
+  if (engine_anchor_scan(e, A.seq.data(), A.offs.data(), A.n(), need.data(), need.size(), ends.data(), &err) != 0)
+    fatal(err);
+  struct Want {
+    size_t read;
+    int type, kind;
+    uint32_t nt;
+  };
+  std::vector<Want> wants;
+  rows.clear();
+  size_t a = 0;
+  for (size_t i = 0; i < n; ++i) {
+    if (!out[i].anchors) continue;
+    for (int c = 0; c < 4; ++c) {  // '+' BACKWARD, '+' FORWARD, '-' BACKWARD, '-' FORWARD
+      const uint32_t* v = &ends[16 * a + 4 * c];
+      const uint32_t nt = v[0];
+      const size_t k = v[1], l = v[2];
+      const int kind = (c == 0 || c == 2) ? BACKWARD_ANCHOR : FORWARD_ANCHOR;
+      if (nt == 0 || !(l - k < 50)) continue;  // at most 50 rows (bwt.c:1851)
+      for (size_t j = k; j <= l; ++j) {
+        rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt});
+        wants.push_back(Want{i, c < 2 ? 1 : 0, kind, nt});
+      }
+    }
+    ++a;
+  }
+  loc.assign(rows.size() + 1, hpg_loc_t{});
+  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  for (size_t w = 0; w < wants.size(); ++w) {
+    if (!loc[w].valid) continue;
+    const Want& W = wants[w];
+    lists[W.read]->insert(bwt_anchor_new(!W.type, (int)loc[w].chrom, loc[w].position + 1,
+                                         loc[w].position + W.nt, W.kind));
+  }
+  return out;
+}
+
+InexactRead read_of(const fastq_read_t* r) {
+  return InexactRead{r->id, r->sequence, std::strlen(r->sequence), r->revcomp, r->quality};
+}
+
+}  // namespace
+
+extern "C" {
+
+bwt_anchor_t* bwt_anchor_new(int strand, int chromosome, size_t start, size_t end, int type) {
+  bwt_anchor_t* a = static_cast<bwt_anchor_t*>(std::malloc(sizeof(bwt_anchor_t)));
+  if (!a) fatal("out of host memory");
+  a->strand = strand;
+  a->chromosome = chromosome;
+  a->start = start;
+  a->end = end;
+  a->type = type;
+  return a;
+}
+
+void bwt_anchor_free(bwt_anchor_t* a) { std::free(a); }
+
+void seq_reverse_complementary(char* seq, unsigned int len) {
+  for (unsigned i = 0, j = len ? len - 1 : 0; len && i <= j; ++i, --j) {
+    auto comp = [](char c) -> char {
+      switch (c) {
+        case 'A': case 'a': return 'T';
+        case 'C': case 'c': return 'G';
+        case 'G': case 'g': return 'C';
+        case 'T': case 't': return 'A';
+        default: return 'N';
+      }
+    };
+    const char a = comp(seq[i]), b = comp(seq[j]);
+    seq[i] = b;
+    seq[j] = a;
+    if (j == 0) break;
+  }
+}
+
+char* reverse_str(char* src, char* dsp, size_t length) {
+  for (size_t i = 0; i < length; ++i) dsp[i] = src[length - 1 - i];
+  dsp[length] = '\0';
+  return dsp;
+}
+
+size_t bwt_map_exact_seq(char* seq, bwt_optarg_t* opt, bwt_index_t* index, array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  announce(1);
+  Reads R;
+  R.add(seq, std::strlen(seq));
+  auto al = exact_alignments(e, R, opt);
+  for (alignment_t* a : al[0]) array_list_insert(a, mapping_list);
+  return al[0].size();
+}
+
+size_t bwt_map_exact_read(fastq_read_t* read, bwt_optarg_t* opt, bwt_index_t* index, array_list_t* mapping_list) {
+  const size_t padding = array_list_size(mapping_list);
+  const size_t n = bwt_map_exact_seq(read->sequence, opt, index, mapping_list);
+  const size_t qlen = std::strlen(read->quality) + 1;  // bwt.c:1014-1024, terminator included
+  for (size_t i = 0; i < n; ++i) {
+    alignment_t* m = static_cast<alignment_t*>(array_list_get(i + padding, mapping_list));
+    if (!m) continue;
+    m->query_name = first_blank(read->id, std::strlen(read->id) + 1);
+    m->quality = static_cast<char*>(std::malloc(qlen + 1));
+    if (!m->quality) fatal("out of host memory");
+    if (m->seq_strand == 0) std::memcpy(m->quality, read->quality, qlen);
+    else reverse_str(read->quality, m->quality, qlen);  // reverses the terminator to the front, as bwt.c does
+    m->quality[qlen - 1] = '\0';
+  }
+  return n;
+}
+
+size_t bwt_map_exact_seqs(char** seqs, size_t num_reads, bwt_optarg_t* opt, bwt_index_t* index, char* out_status,
+                          array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  announce(num_reads);
+  Reads R;
+  for (size_t i = 0; i < num_reads; ++i) R.add(seqs[i], std::strlen(seqs[i]));
+  auto al = exact_alignments(e, R, opt);
+  for (size_t i = 0; i < num_reads; ++i) {
+    out_status[i] = al[i].empty() ? 0 : 1;
+    for (alignment_t* a : al[i]) array_list_insert(a, mapping_list);
+  }
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_exact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_t* index,
+                           fastq_batch_t* unmapped_batch, array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  const size_t n = batch->num_reads;
+  announce(n);
+  Reads R;
+  for (size_t i = 0; i < n; ++i) {
+    const char* s = batch->seq + batch->data_indices[i];
+    R.add(s, std::strlen(s));
+  }
+  auto al = exact_alignments(e, R, opt);
+  // bwt.c:1134-1172: names and qualities from the batch, unmapped reads copied out
+  size_t u = 0;
+  unmapped_batch->header_indices[0] = 0;
+  unmapped_batch->data_indices[0] = 0;
+  for (size_t i = 0; i < n; ++i) {
+    const size_t hlen = (size_t)(batch->header_indices[i + 1] - batch->header_indices[i]);
+    const size_t qlen = (size_t)(batch->data_indices[i + 1] - batch->data_indices[i]);
+    if (!al[i].empty()) {
+      for (alignment_t* m : al[i]) {
+        m->query_name = first_blank(batch->header + batch->header_indices[i], hlen);
+        m->quality = static_cast<char*>(std::malloc(qlen + 1));
+        if (!m->quality) fatal("out of host memory");
+        std::memcpy(m->quality, batch->quality + batch->data_indices[i], qlen);
+        m->quality[qlen] = '\0';
+        array_list_insert(m, mapping_list);
+      }
+    } else {
+      ++u;
+      std::memcpy(unmapped_batch->header + unmapped_batch->header_indices[u - 1],
+                  batch->header + batch->header_indices[i], hlen);
+      std::memcpy(unmapped_batch->seq + unmapped_batch->data_indices[u - 1], batch->seq + batch->data_indices[i],
+                  qlen);
+      std::memcpy(unmapped_batch->quality + unmapped_batch->data_indices[u - 1],
+                  batch->quality + batch->data_indices[i], qlen);
+      unmapped_batch->data_indices[u] = unmapped_batch->data_indices[u - 1] + (int)qlen;
+      unmapped_batch->header_indices[u] = unmapped_batch->header_indices[u - 1] + (int)hlen;
+    }
+  }
+  unmapped_batch->num_reads = u;
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_inexact_read(fastq_read_t* read, bwt_optarg_t* opt, bwt_index_t* index, array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  std::vector<InexactRead> rds{read_of(read)};
+  OutList L;
+  L.list = mapping_list;
+  std::vector<OutList*> lists{&L};
+  map_inexact(e, rds, opt, lists);
+  if (rds[0].len < 5) return 1;  // bwt.c:1917
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_t* index,
+                             fastq_batch_t* unmapped_batch, array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  const size_t n = batch->num_reads;
+  std::vector<std::string> rc(n);
+  std::vector<InexactRead> rds(n);
+  for (size_t i = 0; i < n; ++i) {
+    const char* s = batch->seq + batch->data_indices[i];
+    rds[i] = InexactRead{batch->header + batch->header_indices[i], s, std::strlen(s), nullptr,
+                         batch->quality + batch->data_indices[i]};
+  }
+  std::vector<OutList> L(n);
+  std::vector<OutList*> lists(n);
+  for (size_t i = 0; i < n; ++i) lists[i] = &L[i];
+  map_inexact(e, rds, opt, lists);
+  size_t u = 0;
+  unmapped_batch->header_indices[0] = 0;
+  unmapped_batch->data_indices[0] = 0;
+  for (size_t i = 0; i < n; ++i) {
+    bool mapped = false;
+    for (void* p : L[i].fresh) {
+      array_list_insert(p, mapping_list);
+      mapped = mapped || static_cast<alignment_t*>(p)->is_seq_mapped;
+    }
+    if (mapped) continue;
+    const size_t hlen = (size_t)(batch->header_indices[i + 1] - batch->header_indices[i]);
+    const size_t qlen = (size_t)(batch->data_indices[i + 1] - batch->data_indices[i]);
+    ++u;
+    std::memcpy(unmapped_batch->header + unmapped_batch->header_indices[u - 1], batch->header + batch->header_indices[i],
+                hlen);
+    std::memcpy(unmapped_batch->seq + unmapped_batch->data_indices[u - 1], batch->seq + batch->data_indices[i], qlen);
+    std::memcpy(unmapped_batch->quality + unmapped_batch->data_indices[u - 1], batch->quality + batch->data_indices[i],
+                qlen);
+    unmapped_batch->data_indices[u] = unmapped_batch->data_indices[u - 1] + (int)qlen;
+    unmapped_batch->header_indices[u] = unmapped_batch->header_indices[u - 1] + (int)hlen;
+  }
+  unmapped_batch->num_reads = u;
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_inexact_array_list(array_list_t* reads, bwt_optarg_t* opt, bwt_index_t* index, array_list_t** lists,
+                                  size_t* num_unmapped, size_t* unmapped_indices) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  const size_t n = array_list_size(reads);
+  std::vector<InexactRead> rds(n);
+  std::vector<OutList> L(n);
+  std::vector<OutList*> out(n);
+  std::vector<size_t> before(n);
+  for (size_t i = 0; i < n; ++i) {
+    rds[i] = read_of(static_cast<fastq_read_t*>(array_list_get(i, reads)));
+    L[i].list = lists[i];
+    out[i] = &L[i];
+    before[i] = array_list_size(lists[i]);
+  }
+  auto res = map_inexact(e, rds, opt, out);
+  size_t total = 0;
+  *num_unmapped = 0;
+  for (size_t i = 0; i < n; ++i) {
+    bool mapped = false;
+    for (size_t j = before[i]; j < array_list_size(lists[i]) && j < before[i] + res[i].added; ++j)
+      mapped = mapped || static_cast<alignment_t*>(array_list_get(j, lists[i]))->is_seq_mapped;
+    total += res[i].added;
+    if (!mapped) unmapped_indices[(*num_unmapped)++] = i;
+  }
+  return total;
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+/*
+ * hpg_bwt_api.h -- the alignment-list entry points of hpg-libs' FM-index mapper
+ * (c/src/aligners/bwt/bwt.h), served from the GPU.
+ *
+ * A caller built against hpg-libs keeps its own containers and bioformats
+ * (array_list_t, alignment_t, fastq_read_t, fastq_batch_t): the types below
+ * have the same layout and are skipped when the hpg-libs headers were
+ * included first (their include guards).  The library creates alignments with
+ * alignment_new() and appends them with array_list_insert(), resolved at load
+ * time to the caller's hpg-libs; processes without hpg-libs get the
+ * library's own definitions of those container functions (same behaviour).
+ *
+ * Searches run as one GPU batch per call (a per-read call is a batch of one):
+ * exact backward search or BWSearch1 on the device, then the SA rows the
+ * reference would locate, then the alignment records on the host, following
+ * bwt.c's rules and observable quirks (listed per function).
+ */
+#ifndef HPG_BWT_API_H
+#define HPG_BWT_API_H
+
+#include <pthread.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "hpg_bwt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- hpg-libs types (c/src/containers/array_list.h:29-43,
+ * c/src/bioformats/bam/alignment.h:39-69, c/src/bioformats/fastq/fastq_read.h:27-42,
+ * c/src/bioformats/fastq/fastq_batch.h:24-34, c/src/aligners/bwt/bwt.h:173-179) ---- */
+#ifndef ARRAY_LIST_H
+#define ARRAY_LIST_H
+#ifndef COLLECTION_MODE_SYNCHRONIZED
+#define COLLECTION_MODE_SYNCHRONIZED 1
+#define COLLECTION_MODE_ASYNCHRONIZED 2
+#endif
+typedef struct array_list {
+  size_t capacity;
+  size_t size;
+  float realloc_factor;
+  int mode;
+  int flag;
+  int (*compare_fn)(const void *, const void *);
+  pthread_mutex_t lock;
+  pthread_cond_t condition;
+  void **items;
+} array_list_t;
+array_list_t *array_list_new(size_t initial_capacity, float realloc_factor, int SYNC_MODE);
+void array_list_free(array_list_t *array_list_p, void (*data_callback)(void *));
+int array_list_insert(void *item_p, array_list_t *array_list_p);
+size_t array_list_size(array_list_t *array_list_p);
+void *array_list_get(size_t index, array_list_t *array_list_p);
+void *array_list_remove_at(size_t index, array_list_t *array_list_p);
+int array_list_clear(array_list_t *array_list_p, void (*data_callback)(void *));
+void array_list_set_flag(int flag, array_list_t *array_list_p);
+int array_list_get_flag(array_list_t *array_list_p);
+#endif
+
+#ifndef ALIGNMENTS_H
+#define ALIGNMENTS_H
+typedef struct alignment {
+  int optional_fields_length;
+  unsigned int chromosome;
+  int position;
+  int mate_position;
+  int mate_chromosome;
+  int template_length;
+  int map_quality;
+  int mapq;
+  int num_cigar_operations;
+  int map_len;
+  uint8_t is_paired_end;
+  uint8_t is_paired_end_mapped;
+  uint8_t is_seq_mapped;
+  uint8_t is_mate_mapped;
+  uint8_t seq_strand;
+  uint8_t mate_strand;
+  uint8_t pair_num;
+  uint8_t secondary_alignment;
+  uint8_t fails_quality_check;
+  uint8_t pc_optical_duplicate;
+  char *query_name;
+  char *sequence;
+  char *quality;
+  char *cigar;
+  uint8_t *optional_fields;
+  void *alig_data;
+} alignment_t;
+alignment_t *alignment_new(void);
+void alignment_free(alignment_t *alignment_p);
+#endif
+
+#ifndef FASTQ_READ_H
+#define FASTQ_READ_H
+typedef struct fastq_read {
+  char *id;
+  char *sequence;
+  char *revcomp;
+  char *quality;
+  char *rev_quality;
+  char *adapter;
+  char *adapter_revcomp;
+  char *adapter_quality;
+  int length;
+  int adapter_length;
+  int adapter_strand;
+} fastq_read_t;
+#endif
+
+#ifndef FASTQ_BATCH_H
+#define FASTQ_BATCH_H
+typedef struct fastq_batch {
+  unsigned long num_reads;
+  unsigned long data_indices_size;
+  unsigned long data_size;
+  int source_id;
+  int *header_indices;
+  char *header;
+  int *data_indices;
+  char *seq;
+  char *quality;
+} fastq_batch_t;
+#endif
+
+#ifndef HPG_BWT_ANCHOR_DEFINED
+#define HPG_BWT_ANCHOR_DEFINED
+#define BACKWARD_ANCHOR 0
+#define FORWARD_ANCHOR 1
+typedef struct bwt_anchor {
+  int strand;
+  int chromosome;
+  size_t start;
+  size_t end;
+  int type;
+} bwt_anchor_t;
+#endif
+
+/* bwt.h:181-182 */
+bwt_anchor_t *bwt_anchor_new(int strand, int chromosome, size_t start, size_t end, int type);
+void bwt_anchor_free(bwt_anchor_t *bwt_anchor);
+/* bwt.h:326,330: reverse complement in place (non-ACGT -> 'N'); reverse `length` bytes into dsp and
+ * terminate it at dsp[length]. */
+void seq_reverse_complementary(char *seq, unsigned int len);
+char *reverse_str(char *src, char *dsp, size_t length);
+
+/* ---- exact mapping (bwt.c:889-1163) ----
+ * Per read: '+' is BWExactSearchBackward over the backward index; '-' is
+ * BWExactSearchForward over forward_rev (so it rarely finds the reverse
+ * strand), both located on the backward suffix array; an interval of at least
+ * filter_read_mappings rows is cut to its first two rows; every valid row
+ * becomes an alignment with cigar "<len>=", map quality 254, the first one
+ * primary.  bwt_map_exact_seq prints "\tIn function ...\n" per read, like the
+ * reference.  bwt_map_exact_seqs appends in read order (the reference's order
+ * depends on its OpenMP schedule; with one thread they agree). */
+size_t bwt_map_exact_seq(char *seq, bwt_optarg_t *bwt_optarg, bwt_index_t *index, array_list_t *mapping_list);
+size_t bwt_map_exact_read(fastq_read_t *read, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                          array_list_t *mapping_list);
+size_t bwt_map_exact_seqs(char **seqs, size_t num_reads, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                          char *out_status, array_list_t *mapping_list);
+size_t bwt_map_exact_batch(fastq_batch_t *batch, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                           fastq_batch_t *unmapped_batch, array_list_t *mapping_list);
+
+/* ---- inexact mapping (bwt.c:1879-2310) ----
+ * BWSearch1 on both strands with filter_read_mappings as the result-list
+ * capacity; only the exact hits become alignments (cigar "<len>M", 0-based
+ * positions); a strand whose hits span more than filter_read_mappings rows
+ * drops every alignment of the call from that strand on and sets the list
+ * flag to 2; alignments closer than 10 bp on one chromosome are merged; the
+ * read quality and the AS/NH/NM optional fields are added; reads shorter than
+ * 5 bases get one unmapped record.  When the list ends empty with flag 1, the
+ * longest exact prefix/suffix matches of the four vector searches are located
+ * as bwt_anchor_t items (at most 50 rows each). */
+size_t bwt_map_inexact_read(fastq_read_t *read, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                            array_list_t *mapping_list);
+/* Batch forms declared by bwt.h:362-366,519-524 (their reference bodies are
+ * commented out): every read is mapped as bwt_map_inexact_read maps it into a
+ * fresh list.  _batch appends the alignments in read order and copies reads
+ * without any to unmapped_batch; _array_list maps reads[i] (fastq_read_t *)
+ * into lists[i] (whose flag the caller sets, 1 asking for anchors) and lists
+ * the reads that got no alignment in unmapped_indices. */
+size_t bwt_map_inexact_batch(fastq_batch_t *batch, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                             fastq_batch_t *unmapped_batch, array_list_t *mapping_list);
+size_t bwt_map_inexact_array_list(array_list_t *reads, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                                  array_list_t **lists, size_t *num_unmapped, size_t *unmapped_indices);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HPG_BWT_API_H */

@@ -75,6 +75,11 @@ class RefOracle:
         self.lib.ref_search.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_uint32, ctypes.POINTER(ResultSetC)]
         self.lib.ref_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
+        self.lib.ref_map_api.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                         ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                         ctypes.POINTER(ctypes.c_size_t)]
+        self.lib.ref_blob_free.argtypes = [ctypes.c_void_p]
         self.h = self.lib.ref_index_load(index_dir.encode()) if index_dir else None
 
     def build_index(self, fasta: str, outdir: str, ratio: int = 16) -> None:
@@ -91,6 +96,18 @@ class RefOracle:
             return result_from_c(rs, n)
         finally:
             self.lib.ref_result_free(ctypes.byref(rs))
+
+    def map_api(self, api: int, fq, filter_read_mappings: int, flag: int = 0) -> bytes:
+        """The reference's alignment-list functions on a fastq set (see ref_map_api), serialised."""
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        self.lib.ref_map_api(self.h, api, fq.seq.ctypes.data, fq.qual.ctypes.data, fq.offs.ctypes.data,
+                             fq.ids.ctypes.data, fq.id_offs.ctypes.data, fq.n, filter_read_mappings, flag,
+                             ctypes.byref(p), ctypes.byref(n))
+        try:
+            return ctypes.string_at(p.value, n.value) if n.value else b""
+        finally:
+            self.lib.ref_blob_free(p)
 
     def close(self) -> None:
         if self.h:

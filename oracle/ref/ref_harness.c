@@ -13,8 +13,12 @@
  *                        mode SEARCH1: the four vector searches of bwt.c:1940-1950,
  *                                      BWSearch1VectorHelper per type (bwt.c:1989-2002)
  *                        then, for every hit, the locate loop of bwt.c:2158-2166.
- *   ref_map_inexact   -> bwt_map_inexact_read (bwt.c:1879) per read, flattened.
- *   ref_map_exact     -> bwt_map_exact_read (bwt.c:994) per read, flattened.
+ *   ref_map_api       -> the alignment-list entry points themselves:
+ *                        0 bwt_map_exact_read per read (bwt.c:994), fresh list each
+ *                        1 bwt_map_exact_seqs over all reads, one thread (bwt.c:1040)
+ *                        2 bwt_map_exact_batch over all reads (bwt.c:1097)
+ *                        3 bwt_map_inexact_read per read (bwt.c:1879), fresh list with `flag`
+ *                        serialised as described at ref_map_api.
  */
 #include <fcntl.h>
 #include <unistd.h>
@@ -215,3 +219,181 @@ void ref_result_free(hpg_result_set_t *out) {
   free(out->rs_truncated);
   memset(out, 0, sizeof(*out));
 }
+
+/* ---- alignment lists, serialised (little endian) ----
+ * per list:  u32 items, i32 list flag, u64 return value, u8 items-are-anchors,
+ *            then per item an alignment or an anchor:
+ * alignment: u32 chromosome, i32 position, i32 map_quality, i32 num_cigar_operations,
+ *            u8 seq_strand, u8 is_seq_mapped, u8 secondary_alignment,
+ *            i32 mate_position, i32 mate_chromosome, i32 template_length,
+ *            str query_name, str sequence, str quality (at most the read's quality
+ *            length: strand-0 qualities are not terminated, bwt.c:540), str cigar,
+ *            i32 optional_fields_length + those bytes
+ * anchor:    i32 strand, i32 chromosome, u64 start, u64 end, i32 type
+ * str:       u32 length (0xFFFFFFFF for NULL) + bytes
+ * api 1 appends u8 out_status per read; api 2 appends u32 unmapped reads and
+ * per unmapped read str header, str seq, str quality (raw index ranges). */
+typedef struct {
+  uint8_t *p;
+  size_t n, cap;
+} blob_t;
+
+static void put(blob_t *b, const void *v, size_t n) {
+  if (b->n + n > b->cap) {
+    b->cap = (b->n + n) * 2 + 1024;
+    b->p = (uint8_t *)realloc(b->p, b->cap);
+  }
+  memcpy(b->p + b->n, v, n);
+  b->n += n;
+}
+static void put_u8(blob_t *b, uint8_t v) { put(b, &v, 1); }
+static void put_u32(blob_t *b, uint32_t v) { put(b, &v, 4); }
+static void put_i32(blob_t *b, int32_t v) { put(b, &v, 4); }
+static void put_u64(blob_t *b, uint64_t v) { put(b, &v, 8); }
+static void put_str(blob_t *b, const char *s, size_t maxlen) {
+  if (!s) {
+    put_u32(b, 0xFFFFFFFFu);
+    return;
+  }
+  size_t n = strnlen(s, maxlen);
+  put_u32(b, (uint32_t)n);
+  put(b, s, n);
+}
+static void put_raw(blob_t *b, const char *s, size_t n) {
+  put_u32(b, (uint32_t)n);
+  put(b, s, n);
+}
+
+static void put_list(blob_t *b, array_list_t *list, size_t ret, int anchors, size_t qmax) {
+  size_t n = array_list_size(list);
+  put_u32(b, (uint32_t)n);
+  put_i32(b, array_list_get_flag(list));
+  put_u64(b, ret);
+  put_u8(b, (uint8_t)anchors);
+  for (size_t i = 0; i < n; i++) {
+    if (anchors) {
+      bwt_anchor_t *a = (bwt_anchor_t *)array_list_get(i, list);
+      put_i32(b, a->strand);
+      put_i32(b, a->chromosome);
+      put_u64(b, a->start);
+      put_u64(b, a->end);
+      put_i32(b, a->type);
+    } else {
+      alignment_t *a = (alignment_t *)array_list_get(i, list);
+      put_u32(b, a->chromosome);
+      put_i32(b, a->position);
+      put_i32(b, a->map_quality);
+      put_i32(b, a->num_cigar_operations);
+      put_u8(b, a->seq_strand);
+      put_u8(b, a->is_seq_mapped);
+      put_u8(b, a->secondary_alignment);
+      put_i32(b, a->mate_position);
+      put_i32(b, a->mate_chromosome);
+      put_i32(b, a->template_length);
+      put_str(b, a->query_name, (size_t)-1);
+      put_str(b, a->sequence, (size_t)-1);
+      put_str(b, a->quality, qmax);
+      put_str(b, a->cigar, (size_t)-1);
+      put_i32(b, a->optional_fields_length);
+      if (a->optional_fields_length > 0 && a->optional_fields) put(b, a->optional_fields, a->optional_fields_length);
+    }
+  }
+}
+
+static void free_list(array_list_t *list, int anchors) {
+  size_t n = array_list_size(list);
+  for (size_t i = 0; i < n; i++) {
+    void *p = array_list_get(i, list);
+    if (anchors) bwt_anchor_free((bwt_anchor_t *)p);
+    else alignment_free((alignment_t *)p);
+  }
+  array_list_free(list, NULL);
+}
+
+/* Reads: sequences and qualities as NUL-terminated strings (seqs + offs[i],
+ * length offs[i+1]-offs[i]-1), ids likewise with id_offs. */
+int ref_map_api(void *vidx, int api, const char *seqs, const char *quals, const uint64_t *offs, const char *ids,
+                const uint64_t *id_offs, size_t n, int filter, int flag, uint8_t **out, size_t *out_len) {
+  bwt_index_t *index = (bwt_index_t *)vidx;
+  bwt_optarg_t *opt = bwt_optarg_new(api == 3 ? 1 : 0, 1, filter, filter);
+  blob_t b = {0};
+  int q = quiet_begin(); /* bwt_map_exact_seq prints a line per read */
+  if (api == 0 || api == 3) {
+    for (size_t i = 0; i < n; i++) {
+      fastq_read_t r;
+      memset(&r, 0, sizeof(r));
+      r.id = (char *)ids + id_offs[i];
+      r.sequence = (char *)seqs + offs[i];
+      r.quality = (char *)quals + offs[i];
+      size_t len = offs[i + 1] - offs[i] - 1;
+      char *rc = strdup(r.sequence);
+      seq_reverse_complementary(rc, (unsigned)len);
+      r.revcomp = rc;
+      r.length = (int)len;
+      array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_ASYNCHRONIZED);
+      array_list_set_flag(api == 3 ? flag : 0, list);
+      size_t ret = api == 0 ? bwt_map_exact_read(&r, opt, index, list) : bwt_map_inexact_read(&r, opt, index, list);
+      int anchors = api == 3 && len >= 5 && array_list_get_flag(list) == 1;
+      put_list(&b, list, ret, anchors, len);
+      free_list(list, anchors);
+      free(rc);
+    }
+  } else if (api == 1) {
+    char **ss = (char **)malloc(n * sizeof(char *) + 1);
+    char *status = (char *)malloc(n + 1);
+    for (size_t i = 0; i < n; i++) ss[i] = (char *)seqs + offs[i];
+    array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_SYNCHRONIZED);
+    size_t ret = bwt_map_exact_seqs(ss, n, opt, index, status, list);
+    put_list(&b, list, ret, 0, (size_t)-1);
+    for (size_t i = 0; i < n; i++) put_u8(&b, (uint8_t)status[i]);
+    free_list(list, 0);
+    free(ss);
+    free(status);
+  } else if (api == 2) {
+    fastq_batch_t batch, unmapped;
+    memset(&batch, 0, sizeof(batch));
+    memset(&unmapped, 0, sizeof(unmapped));
+    batch.num_reads = n;
+    batch.header_indices = (int *)malloc((n + 1) * sizeof(int));
+    batch.data_indices = (int *)malloc((n + 1) * sizeof(int));
+    for (size_t i = 0; i <= n; i++) {
+      batch.header_indices[i] = (int)id_offs[i];
+      batch.data_indices[i] = (int)offs[i];
+    }
+    batch.header = (char *)ids;
+    batch.seq = (char *)seqs;
+    batch.quality = (char *)quals;
+    unmapped.header_indices = (int *)calloc(n + 1, sizeof(int));
+    unmapped.data_indices = (int *)calloc(n + 1, sizeof(int));
+    unmapped.header = (char *)calloc(id_offs[n] + 1, 1);
+    unmapped.seq = (char *)calloc(offs[n] + 1, 1);
+    unmapped.quality = (char *)calloc(offs[n] + 1, 1);
+    array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_SYNCHRONIZED);
+    size_t ret = bwt_map_exact_batch(&batch, opt, index, &unmapped, list);
+    put_list(&b, list, ret, 0, (size_t)-1);
+    put_u32(&b, (uint32_t)unmapped.num_reads);
+    for (size_t u = 0; u < unmapped.num_reads; u++) {
+      put_raw(&b, unmapped.header + unmapped.header_indices[u],
+              (size_t)(unmapped.header_indices[u + 1] - unmapped.header_indices[u]));
+      put_raw(&b, unmapped.seq + unmapped.data_indices[u],
+              (size_t)(unmapped.data_indices[u + 1] - unmapped.data_indices[u]));
+      put_raw(&b, unmapped.quality + unmapped.data_indices[u],
+              (size_t)(unmapped.data_indices[u + 1] - unmapped.data_indices[u]));
+    }
+    free_list(list, 0);
+    free(batch.header_indices);
+    free(batch.data_indices);
+    free(unmapped.header_indices);
+    free(unmapped.data_indices);
+    free(unmapped.header);
+    free(unmapped.seq);
+    free(unmapped.quality);
+  }
+  quiet_end(q);
+  bwt_optarg_free(opt);
+  *out = b.p;
+  *out_len = b.n;
+  return 0;
+}
+
+void ref_blob_free(uint8_t *p) { free(p); }

@@ -28,8 +28,33 @@ ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT / "hpg-libs_gb300"))
 sys.path.insert(0, str(ROOT))
 
+sys.path.insert(0, str(ROOT / "tests"))
 from hpgbwt import synth  # noqa: E402
 from oracle.pyoracle import RefOracle, ref_available  # noqa: E402
+import api_lists  # noqa: E402
+
+# Alignment-list entry points recorded per case: (api, filter_read_mappings, list flag).
+API_RUNS = [(api_lists.API_EXACT_READ, 200, 0), (api_lists.API_EXACT_READ, 2, 0),
+            (api_lists.API_EXACT_SEQS, 200, 0), (api_lists.API_EXACT_BATCH, 200, 0),
+            (api_lists.API_INEXACT_READ, 200, 0), (api_lists.API_INEXACT_READ, 3, 0),
+            (api_lists.API_INEXACT_READ, 200, 1), (api_lists.API_INEXACT_READ, 3, 1),
+            (api_lists.API_INEXACT_READ, 0, 1)]
+API_READS = 400  # first reads of each case taken through the entry points
+
+
+def api_read_set(seq: np.ndarray, offs: np.ndarray) -> list[bytes]:
+    """Reads the entry points are recorded on: upper-case A/C/G/T only (other
+    characters index an uninitialised table in the reference, bwt_commons.c:60-92)
+    and at least 4 bases (shorter reads overflow the reference's cigar buffer,
+    bwt.c:960-961)."""
+    out = []
+    for i in range(len(offs) - 1):
+        s = seq[offs[i]:offs[i + 1]].tobytes()
+        if len(s) >= 4 and not s.strip(b"ACGT"):
+            out.append(s)
+        if len(out) == API_READS:
+            break
+    return out
 
 CASES = [
     # name, genome kind, length, seed, chromosome lengths, reads: (n, seed, length, edits), max_results list
@@ -93,6 +118,12 @@ def main() -> int:
                     arrays[f"{tag}_locs"] = r.locs
                     arrays[f"{tag}_count"] = r.rs_count
                     arrays[f"{tag}_trunc"] = r.rs_truncated
+            edge = synth.from_strings(edge_reads(g, cl))
+            fq = api_lists.FastqSet(api_read_set(seq, offs)[:API_READS - 20] + api_read_set(edge.seq, edge.offsets))
+            arrays["api_seq"] = np.frombuffer(b"".join(fq.seqs), dtype=np.uint8)
+            arrays["api_offs"] = np.cumsum([0] + [len(x) for x in fq.seqs]).astype(np.uint64)
+            for api, filt, flag in API_RUNS:
+                arrays[f"api{api}_f{filt}_g{flag}"] = np.frombuffer(ro.map_api(api, fq, filt, flag), dtype=np.uint8)
             ro.close()
         np.savez_compressed(HERE / f"{name}.npz", **arrays)
         manifest[name] = {"kind": kind, "length": n, "seed": seed, "chrom_lengths": cl, "sa_ratio": 16,

@@ -36,6 +36,24 @@ class GoldenCase:
         return lib.Result(a[f"{tag}_hits"].view(lib.HIT_DTYPE) if a[f"{tag}_hits"].dtype != lib.HIT_DTYPE
                           else a[f"{tag}_hits"], a[f"{tag}_locs"], a[f"{tag}_count"], a[f"{tag}_trunc"])
 
+    def api_runs(self):
+        """(api, filter_read_mappings, flag) of the recorded alignment-list runs."""
+        out = []
+        for k in self.arrays:
+            if k.startswith("api") and "_f" in k:
+                a, f, g = k[3:].split("_")
+                out.append((int(a), int(f[1:]), int(g[1:])))
+        return sorted(out)
+
+    def api_fastq(self):
+        import api_lists
+        s, o = self.arrays["api_seq"], self.arrays["api_offs"]
+        return api_lists.FastqSet([s[o[i]:o[i + 1]].tobytes() for i in range(len(o) - 1)])
+
+    def api_expected(self, api: int, filt: int, flag: int, n_reads: int):
+        import api_lists
+        return api_lists.parse_blob(api, self.arrays[f"api{api}_f{filt}_g{flag}"].tobytes(), n_reads)
+
     def build(self, tmp: Path) -> str:
         fa = tmp / "genome.fa"
         synth.write_fasta(str(fa), self.genome, self.chrom_lengths)
