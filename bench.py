@@ -70,41 +70,53 @@ def log(*a):
 
 
 class Dist:
-    def __init__(self, gpus: int):
+    """Ranks of a torchrun launch: one replica per GPU, reads sharded by rank
+    (each rank draws its own seeded batch), no collective on the data path --
+    only the timing barrier and max/sum of scalars.  NCCL on GPUs; gloo where
+    no GPU is visible (the CPU tests of this logic)."""
+
+    def __init__(self, gpus: int, backend: str | None = None):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
+        self.device = "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            backend = backend or ("nccl" if torch.cuda.is_available() else "gloo")
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+                self.device = f"cuda:{self.local}"
+                dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            else:
+                dist.init_process_group("gloo")
             self.pg = dist
 
     def barrier(self):
         if self.pg:
             self.pg.barrier()
 
-    def max(self, v: float) -> float:
-        if not self.pg:
-            return v
+    def _reduce(self, v: float, op) -> float:
         import torch
-        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{self.local}")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        self.pg.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, v: float) -> float:
+        return self._reduce(v, self.pg.ReduceOp.MAX) if self.pg else v
+
     def sum(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{self.local}")
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
+        return self._reduce(v, self.pg.ReduceOp.SUM) if self.pg else v
 
     def close(self):
         if self.pg:
             self.pg.destroy_process_group()
+
+
+def read_seed(rank: int) -> int:
+    """Each rank's read batch: the same generator, its own seed (weak scaling)."""
+    return 2 + rank
 
 
 def prepare(wl: dict, rank: int, dist):
@@ -119,7 +131,7 @@ def prepare(wl: dict, rank: int, dist):
         synth.write_fasta(str(base / "genome.fa"), genome)
         lib.build_index(str(base / "genome.fa"), str(base / "index"), SA_RATIO)
     dist.barrier()
-    reads = synth.reads_fast(genome, wl["reads"], 2 + rank, wl["read_len"], wl["edits"])
+    reads = synth.reads_fast(genome, wl["reads"], read_seed(rank), wl["read_len"], wl["edits"])
     log(f"[bench] rank {rank}: genome+index+reads ready in {time.time() - t0:.1f}s")
     return str(base / "index"), reads, genome
 
