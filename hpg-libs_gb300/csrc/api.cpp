@@ -299,6 +299,11 @@ void bwt_gpu_set_graph(bwt_index_t* index, int on) {
   if (e) engine_set_graph(e, on);
 }
 
+void bwt_gpu_set_pipeline_chunk(bwt_index_t* index, size_t reads) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_pipeline_chunk(e, reads);
+}
+
 int bwt_gpu_graph(bwt_index_t* index) {
   Engine* e = engine_of(index);
   return e ? engine_graph(e) : -1;

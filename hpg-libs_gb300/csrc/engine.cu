@@ -10,6 +10,7 @@
 
 #include "engine_internal.hpp"
 #include "host_pool.hpp"
+#include "hpg_bwt.h"
 
 namespace hpgbwt {
 
@@ -206,6 +207,11 @@ void engine_destroy(Engine* e) {
   cudaSetDevice(e->device);
   if (e->stream) cudaStreamSynchronize(e->stream);
   graph_plans_destroy(e);
+  for (cudaStream_t& x : e->xs)
+    if (x) cudaStreamDestroy(x);
+  if (e->pev_made)
+    for (auto& row : e->pev)
+      for (cudaEvent_t ev : row) cudaEventDestroy(ev);
   for (int d = 0; d < 2; ++d) {
     cudaFree(e->d_occ[d]);
     cudaFree(e->d_S[d]);
@@ -511,6 +517,7 @@ int finish_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, 
 }  // namespace
 
 void engine_set_graph(Engine* e, int on) { e->use_graph = on != 0; }
+void engine_set_pipeline_chunk(Engine* e, size_t reads) { e->pipe_chunk = reads; }
 int engine_graph(Engine* e) { return e->use_graph ? 1 : 0; }
 
 int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads,
@@ -759,6 +766,24 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
       rel.resize(n_reads + 1);
       for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
       o = rel.data();
+    }
+    // Pipelined on request only: on GB300 the copies slow the latency-bound
+    // search by about as long as they take, so overlapping them gains nothing.
+    const size_t pchunk = e->pipe_chunk;
+    if (pchunk && pchunk != SIZE_MAX && n_reads >= 2 * pchunk && !e->census_on) {
+      if (run_graph_pipelined(e, seqs, offs, n_reads, total, max_results, out, err) != 0) {
+        bwt_gpu_result_free(out);
+        return -1;
+      }
+      uint32_t derr = 0;
+      HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+      if (derr) {
+        cudaMemset(e->d_err, 0, 4);
+        bwt_gpu_result_free(out);
+        *err = "corrupt index: suffix-array walk did not reach a sampled row";
+        return -1;
+      }
+      return 0;
     }
     static const uint64_t zero = 0;
     DeviceResult r;

@@ -66,6 +66,8 @@ void engine_set_load_mode(Engine* e, int mode);
 // Batched form from the captured CUDA graph (1, the default) or launched
 // stage by stage with host-read sizes (0).
 void engine_set_graph(Engine* e, int on);
+// Host-buffer batches of at least two chunks run pipelined; reads per chunk (0 automatic, SIZE_MAX off).
+void engine_set_pipeline_chunk(Engine* e, size_t reads);
 int engine_graph(Engine* e);
 int engine_load_mode(Engine* e);
 int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads, uint64_t total_bases,

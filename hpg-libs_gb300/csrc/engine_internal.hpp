@@ -108,7 +108,12 @@ struct Engine {
   float stage_ms[kStageCount] = {0, 0, 0, 0};
   DeviceResult last;
   // batched form replayed from a captured CUDA graph (graph.cu)
-  GraphPlan** plans = nullptr;  // by power-of-two read capacity
+  GraphPlan** plans = nullptr;  // two per power-of-two read capacity
+  cudaStream_t xs[2] = {nullptr, nullptr};  // host-to-device and device-to-host copy streams (pipelined calls)
+  cudaEvent_t pev[3][2];                    // per plan slot: inputs copied, replay done, results copied
+  bool pev_made = false;
+  double hits_per_read = 2.0, rows_per_read = 2.0;  // result sizing of pipelined calls (running estimate)
+  size_t pipe_chunk = 0;  // reads per pipelined chunk: 0 automatic, SIZE_MAX never pipelined
   bool use_graph = true;
   bool skip_locate = false;  // batched form: hits only, no located rows
 };
@@ -154,7 +159,12 @@ void graph_plans_destroy(Engine* e);
 int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err);
 int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceResult* out, std::string* err);
 // The plan serving batches of n reads and `total` bases (captured on demand).
+// `pslot` (0/1) picks one of the two plans of a capacity class.
 GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
-                          std::string* err);
+                          std::string* err, int pslot = 0);
+// Host reads in, host records out, in chunks whose copies overlap the
+// neighbouring chunks' replays (graph.cu).
+int run_graph_pipelined(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint64_t total,
+                        uint32_t max_results, hpg_result_set_t* out, std::string* err);
 
 }  // namespace hpgbwt

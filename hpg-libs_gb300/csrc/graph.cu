@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "engine_internal.hpp"
+#include "host_pool.hpp"
 
 namespace hpgbwt {
 
@@ -25,6 +26,7 @@ namespace hpgbwt {
 namespace {
 
 constexpr int kMaxPlans = 33;  // one per power-of-two read capacity
+constexpr int kPlanSlots = 2;  // two plans per capacity: chunks of one batch alternate between them
 
 __global__ void graph_summary_kernel(const unsigned* __restrict__ ctr, const uint64_t* __restrict__ n_hits,
                                      const uint64_t* __restrict__ n_locs, const unsigned long long* census,
@@ -198,7 +200,9 @@ void graph_plan_destroy(GraphPlan* g) {
 void graph_plans_destroy(Engine* e) {
   if (!e->plans) return;
   cudaStreamSynchronize(e->stream);
-  for (int i = 0; i < kMaxPlans; ++i) graph_plan_destroy(e->plans[i]);
+  for (cudaStream_t x : e->xs)
+    if (x) cudaStreamSynchronize(x);
+  for (int i = 0; i < kMaxPlans * kPlanSlots; ++i) graph_plan_destroy(e->plans[i]);
   delete[] e->plans;
   e->plans = nullptr;
 }
@@ -209,13 +213,17 @@ void graph_plans_destroy(Engine* e) {
 // With `carry` the batch already staged in the old plan's input buffers (n
 // reads, `total` bases) is copied into the new plan's.
 GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
-                          std::string* err) {
+                          std::string* err, int pslot) {
   if (!e->plans) {
-    e->plans = new GraphPlan*[kMaxPlans];
-    for (int i = 0; i < kMaxPlans; ++i) e->plans[i] = nullptr;
+    e->plans = new GraphPlan*[kMaxPlans * kPlanSlots];
+    for (int i = 0; i < kMaxPlans * kPlanSlots; ++i) e->plans[i] = nullptr;
+  }
+  if (n >= (1u << 31) || total > (1ull << 40)) {
+    *err = "batch too large for one graph plan";
+    return nullptr;
   }
   const uint64_t n_cap = pow2_at_least(n, 4096);
-  const int slot = log2_of(n_cap);
+  const int slot = log2_of(n_cap) * kPlanSlots + (pslot & 1);
   GraphPlan* g = e->plans[slot];
   const uint64_t bases_cap = pow2_at_least(total, n_cap * 128);
   uint32_t res_cap = (uint32_t)std::min<uint64_t>(4 * n_cap + 4096, 0xFFFFFFF0u);
@@ -246,7 +254,11 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   g->load_mode = e->X.load_mode;
   g->census = e->census_on;
   g->skip_locate = e->skip_locate;
-  if (old) cudaStreamSynchronize(e->stream);
+  if (old) {  // no stream may still read the old plan's buffers
+    cudaStreamSynchronize(e->stream);
+    for (cudaStream_t x : e->xs)
+      if (x) cudaStreamSynchronize(x);
+  }
   if (capture(e, g, err) != 0) {
     graph_plan_destroy(g);
     return nullptr;
@@ -311,16 +323,207 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
   return 0;
 }
 
+namespace {
+
+// Read and hit ids of one chunk made batch-wide.
+__global__ void chunk_rebase_kernel(hpg_hit_t* __restrict__ hits, uint64_t n_hits, uint32_t r0,
+                                    hpg_loc_t* __restrict__ locs, uint64_t n_locs, uint32_t h0) {
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = tid; i < n_hits; i += stride) hits[i].read += r0;
+  for (uint64_t j = tid; j < n_locs; j += stride) locs[j].hit += h0;
+}
+
+// A result array that grows (page-locked blocks) while chunks land in it.
+template <typename T>
+bool reserve(T** p, size_t* cap, size_t used, size_t want, cudaStream_t copies) {
+  if (want <= *cap) return true;
+  const size_t n = std::max(want, *cap + *cap / 2);
+  T* q = static_cast<T*>(host_pool_alloc(n * sizeof(T)));
+  if (!q) return false;
+  if (*p) {
+    cudaStreamSynchronize(copies);  // earlier chunks must have landed
+    if (used) std::memcpy(q, *p, used * sizeof(T));
+    host_pool_free(*p);
+  }
+  *p = q;
+  *cap = n;
+  return true;
+}
+
+}  // namespace
+
+int run_graph_pipelined(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint64_t total,
+                        uint32_t max_results, hpg_result_set_t* out, std::string* err) {
+  (void)total;
+  const size_t chunk = e->pipe_chunk ? e->pipe_chunk : std::max<size_t>(262144, (n + 3) / 4);
+  if (chunk == 0 || n == 0) return -1;
+  const size_t K = (n + chunk - 1) / chunk;
+  if (!e->xs[0]) {
+    HPG_CUDA(cudaStreamCreateWithFlags(&e->xs[0], cudaStreamNonBlocking), "copy stream");
+    HPG_CUDA(cudaStreamCreateWithFlags(&e->xs[1], cudaStreamNonBlocking), "copy stream");
+  }
+  if (!e->pev_made) {
+    for (auto& row : e->pev)
+      for (cudaEvent_t& ev : row) HPG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "pipeline events");
+    e->pev_made = true;
+  }
+  cudaStream_t cs = e->stream, h2d = e->xs[0], d2h = e->xs[1];
+  cudaEvent_t* ev_in = e->pev[0];
+  cudaEvent_t* ev_run = e->pev[1];
+  cudaEvent_t* ev_out = e->pev[2];
+  // page-locked staging of each slot's chunk offsets
+  std::vector<uint64_t*> stage(2, nullptr);
+  for (int s = 0; s < 2; ++s) {
+    stage[s] = static_cast<uint64_t*>(host_pool_alloc((chunk + 1) * 8));
+    if (!stage[s]) {
+      *err = "out of host memory (chunk offsets)";
+      return -1;
+    }
+  }
+  auto release = [&]() {
+    for (uint64_t* p : stage) host_pool_free(p);
+  };
+  // result arrays, sized from the hit and row rates of the previous call
+  std::memset(out, 0, sizeof(*out));
+  out->n_reads = n;
+  out->rs_count = static_cast<uint32_t*>(host_pool_alloc((2 * n + 1) * 4));
+  out->rs_truncated = static_cast<uint8_t*>(host_pool_alloc(2 * n + 1));
+  size_t hcap = 0, lcap = 0;
+  const size_t hguess = (size_t)(e->hits_per_read * 1.25 * (double)n) + 1024;
+  const size_t lguess = (size_t)(e->rows_per_read * 1.25 * (double)n) + 1024;
+  if (!out->rs_count || !out->rs_truncated || !reserve(&out->hits, &hcap, 0, hguess, d2h) ||
+      !reserve(&out->locs, &lcap, 0, lguess, d2h)) {
+    release();
+    *err = "out of host memory (results)";
+    return -1;
+  }
+  std::vector<GraphPlan*> plan(K, nullptr);
+  std::vector<uint32_t> nr(K);
+  float st[kStageCount + 1] = {0, 0, 0, 0, 0};
+  auto issue = [&](size_t i) -> int {
+    const int s = (int)(i & 1);
+    const size_t r0 = i * chunk, r1 = std::min(n, r0 + chunk);
+    nr[i] = (uint32_t)(r1 - r0);
+    if (offs[r1] < offs[r0]) {
+      *err = "read offsets must be non-decreasing and reads at most 32767 bases";
+      return -1;
+    }
+    const uint64_t b0 = offs[r0], bases = offs[r1] - b0;
+    GraphPlan* g = graph_plan_for(e, nr[i], bases, nullptr, false, err, s);
+    if (!g) return -1;
+    plan[i] = g;
+    HPG_CUDA(cudaEventSynchronize(ev_in[s]), "chunk staging");  // the slot's previous offsets were sent
+    for (size_t r = r0; r <= r1; ++r) stage[s][r - r0] = offs[r] - b0;
+    // inputs once the slot's previous replay has finished with them
+    HPG_CUDA(cudaStreamWaitEvent(h2d, ev_run[s], 0), "pipeline order");
+    if (bases) HPG_CUDA(cudaMemcpyAsync(g->seqs, seqs + b0, bases, cudaMemcpyDefault, h2d), "chunk reads");
+    HPG_CUDA(cudaMemcpyAsync(g->offs, stage[s], (nr[i] + 1) * 8, cudaMemcpyHostToDevice, h2d), "chunk offsets");
+    HPG_CUDA(cudaEventRecord(ev_in[s], h2d), "pipeline order");
+    // replay once the inputs are in and the slot's previous results are out
+    HPG_CUDA(cudaStreamWaitEvent(cs, ev_in[s], 0), "pipeline order");
+    HPG_CUDA(cudaStreamWaitEvent(cs, ev_out[s], 0), "pipeline order");
+    if (graph_launch(e, g, nr[i], max_results, err) != 0) return -1;
+    HPG_CUDA(cudaEventRecord(ev_run[s], cs), "pipeline order");
+    return 0;
+  };
+  size_t h0 = 0, l0 = 0;
+  auto collect = [&](size_t i) -> int {
+    const int s = (int)(i & 1);
+    GraphPlan* g = plan[i];
+    HPG_CUDA(cudaEventSynchronize(ev_run[s]), "chunk replay");
+    const uint64_t* h = g->h_summary;
+    if ((uint32_t)h[0] & kStatusBadInput) {
+      *err = "read offsets must be non-decreasing and reads at most 32767 bases";
+      return -1;
+    }
+    if ((uint32_t)h[0]) {  // a pool overflowed: grow it and rerun this chunk alone
+      HPG_CUDA(cudaStreamSynchronize(h2d), "pipeline drain");
+      HPG_CUDA(cudaStreamSynchronize(d2h), "pipeline drain");
+      HPG_CUDA(cudaStreamSynchronize(cs), "pipeline drain");
+      const size_t r0 = i * chunk;
+      DeviceResult r;
+      if (run_batched_graph(e, g->seqs, g->offs, nr[i], offs[r0 + nr[i]] - offs[r0], max_results, &r, err) != 0)
+        return -1;
+      g = plan[i] = graph_plan_for(e, nr[i], offs[r0 + nr[i]] - offs[r0], nullptr, false, err, s);
+      if (!g) return -1;
+      h = g->h_summary;  // the rerun's summary, in the grown plan
+      HPG_CUDA(cudaEventRecord(ev_run[s], cs), "pipeline order");
+    }
+    const uint64_t nh = h[2], nl = g->skip_locate ? 0 : h[3];
+    if (!reserve(&out->hits, &hcap, h0, h0 + nh + 1, d2h) || !reserve(&out->locs, &lcap, l0, l0 + nl + 1, d2h)) {
+      *err = "out of host memory (results)";
+      return -1;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, g->ev[0], g->ev[1]);
+    st[kStageEncode] += ms;
+    cudaEventElapsedTime(&ms, g->ev[1], g->ev[3]);
+    st[kStageSearch] += ms;
+    cudaEventElapsedTime(&ms, g->ev[2], g->ev[3]);
+    st[kStageCount] += ms;
+    cudaEventElapsedTime(&ms, g->ev[3], g->ev[4]);
+    st[kStageFinalize] += ms;
+    cudaEventElapsedTime(&ms, g->ev[4], g->ev[5]);
+    st[kStageLocate] += ms;
+    const size_t r0 = i * chunk;
+    HPG_CUDA(cudaStreamWaitEvent(d2h, ev_run[s], 0), "pipeline order");
+    if ((r0 || h0) && (nh || nl)) {
+      const uint64_t work = std::max<uint64_t>(nh, nl);
+      count_launches(1);
+      chunk_rebase_kernel<<<(unsigned)std::min<uint64_t>((work + 255) / 256, 1216), 256, 0, d2h>>>(
+          g->hits, nh, (uint32_t)r0, g->locs, nl, (uint32_t)h0);
+    }
+    if (nh) HPG_CUDA(cudaMemcpyAsync(out->hits + h0, g->hits, nh * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, d2h),
+                     "copy hits");
+    if (nl) HPG_CUDA(cudaMemcpyAsync(out->locs + l0, g->locs, nl * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, d2h),
+                     "copy rows");
+    HPG_CUDA(cudaMemcpyAsync(out->rs_count + 2 * r0, g->kept, 2ull * nr[i] * 4, cudaMemcpyDeviceToHost, d2h),
+             "copy counts");
+    HPG_CUDA(cudaMemcpyAsync(out->rs_truncated + 2 * r0, g->trunc, 2ull * nr[i], cudaMemcpyDeviceToHost, d2h),
+             "copy flags");
+    HPG_CUDA(cudaEventRecord(ev_out[s], d2h), "pipeline order");
+    h0 += nh;
+    l0 += nl;
+    return 0;
+  };
+  int rc = 0;
+  for (size_t i = 0; i < K && rc == 0; ++i) {
+    rc = issue(i);
+    if (rc == 0 && i >= 1) rc = collect(i - 1);
+  }
+  if (rc == 0) rc = collect(K - 1);
+  cudaError_t ce = cudaStreamSynchronize(d2h);
+  release();
+  if (rc != 0) return -1;
+  if (ce != cudaSuccess) {
+    *err = std::string("result copies: ") + cudaGetErrorString(ce);
+    return -1;
+  }
+  out->n_hits = h0;
+  out->n_locs = l0;
+  for (int k = 0; k < kStageCount; ++k) e->stage_ms[k] = st[k];
+  e->drain_ms = st[kStageCount];
+  if (n >= 1024) {
+    e->hits_per_read = 0.5 * e->hits_per_read + 0.5 * (double)h0 / n;
+    e->rows_per_read = 0.5 * e->rows_per_read + 0.5 * (double)l0 / n;
+  }
+  return 0;
+}
+
 int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, uint64_t total,
                       uint32_t max_results, DeviceResult* out, std::string* err) {
   cudaStream_t s = e->stream;
   GraphPlan grow;
   const GraphPlan* staged_in = nullptr;  // plan whose own buffers hold the batch
+  int pslot = 0;
   if (e->plans)
-    for (int i = 0; i < kMaxPlans; ++i)
-      if (e->plans[i] && seqs == e->plans[i]->seqs && offs == e->plans[i]->offs) staged_in = e->plans[i];
+    for (int i = 0; i < kMaxPlans * kPlanSlots; ++i)
+      if (e->plans[i] && seqs == e->plans[i]->seqs && offs == e->plans[i]->offs) {
+        staged_in = e->plans[i];
+        pslot = i % kPlanSlots;
+      }
   for (int attempt = 0; attempt < 8; ++attempt) {
-    GraphPlan* g = graph_plan_for(e, n, total, attempt ? &grow : nullptr, staged_in != nullptr, err);
+    GraphPlan* g = graph_plan_for(e, n, total, attempt ? &grow : nullptr, staged_in != nullptr, err, pslot);
     if (!g) return -1;
     if (staged_in) {  // follow the batch into a replacement plan
       seqs = g->seqs;

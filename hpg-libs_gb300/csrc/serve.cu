@@ -340,7 +340,7 @@ struct Server {
       rows_per_read = std::max(rpr, 0.8 * rows_per_read + 0.2 * rpr);
     }
     plan_bytes = 0;
-    for (int i = 0; i < 33; ++i)
+    for (int i = 0; i < 66; ++i)
       if (e->plans && e->plans[i]) plan_bytes += e->plans[i]->bytes;
     b->reqs.clear();
     cv_done.notify_all();

@@ -102,6 +102,7 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_server_free.argtypes = [vp]
     lib.bwt_gpu_set_graph.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_graph.argtypes = [vp]
+    lib.bwt_gpu_set_pipeline_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
@@ -243,6 +244,10 @@ class GpuIndex:
     def set_graph(self, on: bool) -> None:
         """Batched form from the captured CUDA graph (default) or launched stage by stage."""
         self.lib.bwt_gpu_set_graph(self.handle, 1 if on else 0)
+
+    def set_pipeline_chunk(self, reads: int) -> None:
+        """Reads per chunk of pipelined host batches (0 or -1: not pipelined, the default)."""
+        self.lib.bwt_gpu_set_pipeline_chunk(self.handle, reads if reads >= 0 else (1 << 64) - 1)
 
     def graph(self) -> bool:
         return bool(self.lib.bwt_gpu_graph(self.handle))

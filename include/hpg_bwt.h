@@ -172,6 +172,12 @@ int bwt_gpu_load_mode(bwt_index_t *index);
  * the host between stages.  Results are identical. */
 void bwt_gpu_set_graph(bwt_index_t *index, int on);
 int bwt_gpu_graph(bwt_index_t *index);
+/* With a chunk size set, bwt_gpu_search_batch of at least two chunks (batched
+ * form, graph on) runs as a pipeline: chunk i+1's reads go in and chunk i-1's
+ * records come out while chunk i is searched.  reads per chunk: 0 or SIZE_MAX
+ * never (the default: on GB300 the copies slow the search by about their own
+ * duration, so the overlap gains nothing). */
+void bwt_gpu_set_pipeline_chunk(bwt_index_t *index, size_t reads);
 /* Autotuner: times the batched search on a device-resident read batch for
  * every candidate setting (45), keeps the fastest, then picks the fastest
  * block-load form for it (4 more runs).  Optional table gets rows of

@@ -125,3 +125,36 @@ def test_graph_rejects_bad_offsets(case_factory):
             with pytest.raises(RuntimeError, match="non-decreasing"):
                 g.search(rs, form=lib.FORM_BATCHED)
             _same(g.search(good, form=lib.FORM_BATCHED), want)
+
+
+def test_pipelined_host_batches(tmp_path_factory):
+    """Host batches of 2+ chunks run with their copies overlapping other chunks'
+    replays; a chunk whose pools overflow (read-dense repeat copies) is grown and
+    rerun inside the pipeline.  Equal to the stage-by-stage form and the oracle."""
+    rng = np.random.default_rng(18)
+    g0 = synth.genome("repeats", 400_000, 61)
+    elem = rng.integers(0, 4, 300, dtype=np.uint8)
+    for k in range(150):
+        cp = elem.copy()
+        m = rng.random(300) < 0.02
+        cp[m] = rng.integers(0, 4, int(m.sum()), dtype=np.uint8)
+        g0[200_000 + k * 300: 200_000 + (k + 1) * 300] = cp
+    d = tmp_path_factory.mktemp("pipe")
+    synth.write_fasta(str(d / "g.fa"), g0, [200_000, 200_000])
+    lib.build_index(str(d / "g.fa"), str(d / "idx"), 16)
+    normal = synth.reads_fast(g0[:190_000], 480_000, 71, 100, "per_base_capped")
+    heavy = synth.reads(g0[200_000:245_000], 60_000, 72, length=(60, 100), edits="mix_30_50_20")
+    seqs = [normal.seq[:int(normal.offsets[300_000])], heavy.seq, normal.seq[int(normal.offsets[300_000]):]]
+    offs = np.concatenate([normal.offsets[:300_001],
+                           heavy.offsets[1:] + normal.offsets[300_000],
+                           normal.offsets[300_001:] - normal.offsets[300_000] + normal.offsets[300_000]
+                           + heavy.offsets[-1]]).astype(np.uint64)
+    reads = synth.ReadSet(np.concatenate(seqs), offs, np.zeros(1), np.zeros(1), np.zeros(1))
+    assert len(reads) == 540_000
+    want = PortOracle(str(d / "idx")).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=16)
+    with lib.GpuIndex(str(d / "idx")) as g:
+        g.set_pipeline_chunk(262144)  # 3 chunks
+        for _ in range(2):  # the second call reuses grown plans and result sizing
+            _same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+        g.set_graph(False)
+        _same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
