@@ -406,9 +406,12 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     # autotune the batched form on this batch (untimed)
     table = []
     if args.tuning:
-        st, ch, mb, lm = (int(x) for x in args.tuning.split(","))
+        vals = [int(x) for x in args.tuning.split(",")]
+        st, ch, mb, lm = vals[:4]
         gi.set_tuning(0, st, ch, mb)
         gi.set_load_mode(lm)
+        if len(vals) > 4:
+            gi.set_start_table(vals[4])
     elif not args.no_autotune:
         t0 = time.time()
         table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
@@ -503,7 +506,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "serving": serve,
-            "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode()),
+            "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }
@@ -555,7 +558,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
-                                                 "block_load_mode (stack 0 = split, -1 = lockstep)")
+                                                 "block_load_mode[,start_table] (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]

@@ -299,6 +299,19 @@ void bwt_gpu_set_graph(bwt_index_t* index, int on) {
   if (e) engine_set_graph(e, on);
 }
 
+int bwt_gpu_set_start_table(bwt_index_t* index, int symbols) {
+  Engine* e = engine_of(index);
+  if (!e) return fail("bwt_gpu_set_start_table: null index");
+  std::string err;
+  if (engine_set_kmer(e, symbols, &err) != 0) return fail(err);
+  return 0;
+}
+
+int bwt_gpu_start_table(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_kmer(e) : -1;
+}
+
 void bwt_gpu_set_pipeline_chunk(bwt_index_t* index, size_t reads) {
   Engine* e = engine_of(index);
   if (e) engine_set_pipeline_chunk(e, reads);

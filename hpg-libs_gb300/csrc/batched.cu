@@ -83,7 +83,7 @@ __device__ __forceinline__ unsigned res_slot(const BatchedParams& p, uint32_t& c
 }
 
 // Lane modes.
-enum : uint32_t { kNone = 0, kChain = 1, kCont = 2, kSingle = 3 };
+enum : uint32_t { kNone = 0, kChain = 1, kCont = 2, kSingle = 3, kKmer = 4 };
 
 // Cold lane state lives in shared memory (one word per lane and field), so
 // that the registers hold only what every step touches.
@@ -284,8 +284,23 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       pl = X.top;
       dir = (c & 1u) ? 1 : -1;
       pos = (c & 1u) ? 0 : len - 1;
-      nb = W[pos];
-      mode = kChain;
+      const uint32_t L = X.kmer_len;
+      if (L && len >= 2 * (int)L + 2) {
+        // The first L steps of a chain from the full interval never reach a
+        // branching position (J stays above n/2 backward, below n/2 - 1
+        // forward): one table lookup stands for them.
+        const uint32_t strand = rs & 1u;
+        uint32_t code = 0;
+        for (uint32_t i = 0; i < L; ++i) {
+          const uint32_t b = W[dir > 0 ? (int)i : len - 1 - (int)i];
+          code = (code << 2) | (strand ? sel4(X.comp, b) : b);
+        }
+        nb = code;
+        mode = kKmer;
+      } else {
+        nb = W[pos];
+        mode = kChain;
+      }
     }
     if (mode == kNone) break;
 
@@ -293,10 +308,29 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
     {
       const uint32_t strand = rs & 1u;
       const uint32_t vsel = dir > 0 ? 1u : 0u;  // forward searches use the strand's forward view
-      if (CENSUS) sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
-      bw_step(X, View{vsel ^ strand, strand}, nb, k, l);
+      if (mode == kKmer) {
+        if (CENSUS) sectors += 1u;
+        const uint2 t = __ldg(((vsel ^ strand) ? X.kmer[1] : X.kmer[0]) + nb);
+        k = t.x;
+        l = t.y;
+      } else {
+        if (CENSUS) sectors += ((k >> 6) == (l >> 6)) ? 1u : 2u;
+        bw_step(X, View{vsel ^ strand, strand}, nb, k, l);
+      }
     }
     const int stop = dir > 0 ? len - 1 : 0;
+    if (mode == kKmer) {
+      if (k > l) {  // failed within the first L steps: no change point, no hit
+        mode = kNone;
+        continue;
+      }
+      pk = k;
+      pl = l;
+      pos = dir > 0 ? (int)X.kmer_len : len - 1 - (int)X.kmer_len;
+      nb = W[pos];
+      mode = kChain;
+      continue;
+    }
     if (mode == kChain) {
       // (k,l) = vector entry at pos, (pk,pl) = entry at J = pos - dir.  The helper
       // branches at J in [2, n/2] (backward, block at 1) and [n/2 - 1, n - 2]
@@ -917,6 +951,8 @@ void launch_search_d(const DevIndex& X, const BatchedParams& p, const BatchedTun
     launch_search_dm<D, 16>(X, p, t, num_sms, drain, s);
   else if (t.min_blocks >= 12)
     launch_search_dm<D, 12>(X, p, t, num_sms, drain, s);
+  else if (t.min_blocks >= 10)
+    launch_search_dm<D, 10>(X, p, t, num_sms, drain, s);
   else
     launch_search_dm<D, 1>(X, p, t, num_sms, drain, s);
 }
@@ -928,6 +964,8 @@ int occupancy_d(const BatchedTuning& t) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 16, false>, kBlock, 0);
   else if (t.min_blocks >= 12)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 12, false>, kBlock, 0);
+  else if (t.min_blocks >= 10)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 10, false>, kBlock, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_search_kernel<D, 1, false>, kBlock, 0);
   if (t.blocks_per_sm > 0 && t.blocks_per_sm < per_sm) per_sm = t.blocks_per_sm;
@@ -1091,5 +1129,28 @@ void launch_locate_items(const DevIndex& X, const RowItem* items, uint64_t n_ite
 }
 
 size_t locate_row_item_bytes() { return sizeof(RowItem); }
+
+namespace {
+
+// One thread per string of L symbols: the search from the full interval over
+// them on physical direction d, stopped where it fails.
+__global__ void build_kmer_kernel(DevIndex X, uint32_t d, uint32_t L, uint2* __restrict__ out) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (1u << (2 * L))) return;
+  uint32_t k = 0, l = X.top;
+  for (uint32_t i = 0; i < L; ++i) {
+    bw_step(X, View{d, 0}, (c >> (2 * (L - 1 - i))) & 3u, k, l);
+    if (k > l) break;
+  }
+  out[c] = make_uint2(k, l);
+}
+
+}  // namespace
+
+void launch_build_kmer(const DevIndex& X, uint32_t d, uint32_t L, uint2* out, cudaStream_t s) {
+  const uint32_t n = 1u << (2 * L);
+  count_launches(1);
+  build_kmer_kernel<<<(n + 255) / 256, 256, 0, s>>>(X, d, L, out);
+}
 
 }  // namespace hpgbwt

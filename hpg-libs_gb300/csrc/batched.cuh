@@ -117,6 +117,8 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
                               unsigned int* row_ctr, unsigned long long* census, int num_sms, cudaStream_t s,
                               const LocateSizes& z = LocateSizes());
 size_t locate_row_item_bytes();
+// Start table of physical direction d for strings of L symbols (4^L entries).
+void launch_build_kmer(const DevIndex& X, uint32_t d, uint32_t L, uint2* out, cudaStream_t s);
 // Locate caller-built rows (device array of n_items RowItem); out[item.out] per row.
 void launch_locate_items(const DevIndex& X, const RowItem* items, uint64_t n_items, hpg_loc_t* out,
                          unsigned int* row_ctr, int num_sms, cudaStream_t s);

@@ -182,6 +182,8 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   cudaMemset(en->d_err, 0, 4);
   en->X.err = en->d_err;
   en->X.load_mode = 2;
+  en->X.kmer_len = 0;
+  en->X.kmer[0] = en->X.kmer[1] = nullptr;
 
   for (int b = 0; b < 4; ++b) {
     en->X.C[b] = h.C[b];
@@ -199,6 +201,14 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   en->X.kar_size = (uint32_t)nk;
   cudaDeviceGetAttribute(&en->num_sms, cudaDevAttrMultiProcessorCount, device);
   if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return fail("index upload", ce);
+  {
+    std::string kerr;
+    if (engine_set_kmer(en, kDefaultKmer, &kerr) != 0) {
+      *err = kerr;
+      engine_destroy(en);
+      return nullptr;
+    }
+  }
   return en;
 }
 
@@ -220,6 +230,8 @@ void engine_destroy(Engine* e) {
   cudaFree(e->d_kar_start);
   cudaFree(e->d_table);
   cudaFree(e->d_err);
+  cudaFree(e->d_kmer[0]);
+  cudaFree(e->d_kmer[1]);
   DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
                     &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
                     &e->census, &e->b_ctr, &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg,
@@ -401,7 +413,7 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
   // stack depth 0 selects the split (chain-only) form, -1 the lockstep form
   e->tuning.split = stack == 0 ? 1 : (stack < 0 ? 2 : 0);
   if (stack <= 0) stack = 2;
-  e->tuning.min_blocks = min_blocks >= 16 ? 16 : (min_blocks >= 12 ? 12 : 1);
+  e->tuning.min_blocks = min_blocks >= 16 ? 16 : (min_blocks >= 12 ? 12 : (min_blocks >= 10 ? 10 : 1));
   e->tuning.blocks_per_sm = blocks_per_sm;
   e->tuning.stack = stack <= 2 ? 2 : (stack <= 4 ? 4 : 8);
   e->tuning.chunk = chunk < 1 ? 1 : (chunk > 8 ? 8 : chunk);
@@ -424,7 +436,7 @@ void engine_get_tuning(Engine* e, int* out5) {
 int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, size_t n_reads, uint64_t total_bases,
                     uint32_t max_len, uint32_t max_results, int* table, int max_rows, int* rows_out,
                     std::string* err) {
-  static const int cand_minb[] = {1, 12, 16};
+  static const int cand_minb[] = {1, 10, 12, 16};  // 10: fused form only (the others take 1)
   static const int cand_stack[] = {-1, 0, 2, 4, 8};  // 0: split form, -1: lockstep form
   static const int cand_chunk[] = {1, 2, 4};
   BatchedTuning best = e->tuning;
@@ -491,6 +503,32 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
     }
   }
   e->X.load_mode = best_mode;
+  // then the start-table length (rows marked by a first column of -100 - L)
+  int best_kmer = (int)e->X.kmer_len;
+  for (int L : {0, 8, 10, 11}) {
+    if (engine_set_kmer(e, L, err) != 0) return -1;
+    float t = 0;
+    for (int rep = 0; rep < 2; ++rep) {
+      if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases, max_len,
+                               max_results, &r, err) != 0)
+        return -1;
+      t = e->stage_ms[kStageSearch];
+    }
+    if (table && rows < max_rows) {
+      int* row = table + 5 * rows;
+      row[0] = -100 - L;
+      row[1] = batched_max_blocks_per_sm(e->tuning);
+      row[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
+      row[3] = e->tuning.chunk;
+      row[4] = (int)(t * 1000.0f);
+    }
+    ++rows;
+    if (t < best_ms) {
+      best_ms = t;
+      best_kmer = L;
+    }
+  }
+  if (engine_set_kmer(e, best_kmer, err) != 0) return -1;
   if (rows_out) *rows_out = rows;
   return 0;
 }
@@ -515,6 +553,40 @@ int finish_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, 
 }
 
 }  // namespace
+
+int engine_set_kmer(Engine* e, int L, std::string* err) {
+  if (L < 0 || L > 12) {
+    *err = "start table length must be 0..12 symbols";
+    return -1;
+  }
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  if ((uint32_t)L == e->X.kmer_len) return 0;
+  HPG_CUDA(cudaStreamSynchronize(e->stream), "start table");
+  for (uint2*& t : e->d_kmer) {
+    cudaFree(t);
+    t = nullptr;
+  }
+  e->X.kmer[0] = e->X.kmer[1] = nullptr;
+  e->X.kmer_len = 0;
+  if (L > 0) {
+    const size_t bytes = ((size_t)1 << (2 * L)) * sizeof(uint2);
+    for (int d = 0; d < 2; ++d) {
+      if (cudaMalloc(&e->d_kmer[d], bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *err = "out of device memory (start table)";
+        return -1;
+      }
+      launch_build_kmer(e->X, (uint32_t)d, (uint32_t)L, e->d_kmer[d], e->stream);
+    }
+    HPG_CUDA(cudaStreamSynchronize(e->stream), "start table");
+    e->X.kmer[0] = e->d_kmer[0];
+    e->X.kmer[1] = e->d_kmer[1];
+    e->X.kmer_len = (uint32_t)L;
+  }
+  return 0;
+}
+
+int engine_kmer(Engine* e) { return (int)e->X.kmer_len; }
 
 void engine_set_graph(Engine* e, int on) { e->use_graph = on != 0; }
 void engine_set_pipeline_chunk(Engine* e, size_t reads) { e->pipe_chunk = reads; }

@@ -66,6 +66,11 @@ void engine_set_load_mode(Engine* e, int mode);
 // Batched form from the captured CUDA graph (1, the default) or launched
 // stage by stage with host-read sizes (0).
 void engine_set_graph(Engine* e, int on);
+// Start table of the batched search: chains of reads of 2L+2 or more bases
+// begin with one lookup instead of their first L steps (0 = no table).
+constexpr int kDefaultKmer = 0;
+int engine_set_kmer(Engine* e, int L, std::string* err);
+int engine_kmer(Engine* e);
 // Host-buffer batches of at least two chunks run pipelined; reads per chunk (0 automatic, SIZE_MAX off).
 void engine_set_pipeline_chunk(Engine* e, size_t reads);
 int engine_graph(Engine* e);

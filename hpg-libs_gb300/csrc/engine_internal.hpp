@@ -41,6 +41,8 @@ struct GraphPlan {
   uint32_t load_mode = 0;
   bool census = false;
   bool skip_locate = false;  // hits only (the alignment-list layer locates the rows it needs)
+  uint32_t kmer_len = 0;     // start table captured with the kernels (length and address)
+  const void* kmer0 = nullptr;
   // device buffers
   uint8_t* seqs = nullptr;
   uint64_t* offs = nullptr;
@@ -87,6 +89,7 @@ struct Engine {
   uint64_t* d_kar_start = nullptr;
   uint8_t* d_table = nullptr;
   uint32_t* d_err = nullptr;
+  uint2* d_kmer[2] = {nullptr, nullptr};  // start tables of the batched search (X.kmer_len symbols)
   uint8_t h_table[256];
 
   // workspace

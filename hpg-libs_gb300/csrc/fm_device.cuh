@@ -22,6 +22,8 @@
 // instead, so no table is copied.
 #pragma once
 
+#include <vector_types.h>
+
 #include <cstdint>
 
 namespace hpgbwt {
@@ -51,6 +53,13 @@ struct DevIndex {
   uint32_t kar_size;
   uint32_t* err;          // device error word (bit 0: LF walk exceeded n+1 steps)
   uint32_t load_mode;     // how blocks are fetched, see load_block()
+  // Start table of the batched search: for every string of kmer_len symbols
+  // (first symbol in the top bits, in search order) the interval the search
+  // reaches from the full interval after those steps on that physical
+  // direction, or the failing interval (k > l) where it stopped.  kmer_len 0:
+  // no table.
+  const uint2* kmer[2];
+  uint32_t kmer_len;
 };
 
 constexpr uint32_t kErrWalk = 1u;

@@ -68,7 +68,8 @@ bool same_settings(const GraphPlan* g, const Engine* e) {
   const BatchedTuning& b = e->tuning;
   return a.block == b.block && a.blocks_per_sm == b.blocks_per_sm && a.stack == b.stack && a.chunk == b.chunk &&
          a.min_blocks == b.min_blocks && a.split == b.split && g->load_mode == e->X.load_mode &&
-         g->census == e->census_on && g->skip_locate == e->skip_locate;
+         g->census == e->census_on && g->skip_locate == e->skip_locate && g->kmer_len == e->X.kmer_len &&
+         g->kmer0 == (const void*)e->X.kmer[0];
 }
 
 void record(cudaEvent_t ev, cudaStream_t s) { cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal); }
@@ -254,6 +255,8 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   g->load_mode = e->X.load_mode;
   g->census = e->census_on;
   g->skip_locate = e->skip_locate;
+  g->kmer_len = e->X.kmer_len;
+  g->kmer0 = e->X.kmer[0];
   if (old) {  // no stream may still read the old plan's buffers
     cudaStreamSynchronize(e->stream);
     for (cudaStream_t x : e->xs)

@@ -103,6 +103,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_graph.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_graph.argtypes = [vp]
     lib.bwt_gpu_set_pipeline_chunk.argtypes = [vp, sz]
+    lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_start_table.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
     lib.bwt_gpu_last_error.restype = ctypes.c_char_p
@@ -219,11 +221,11 @@ class GpuIndex:
 
     def autotune(self, d_seqs: int, d_offs: int, n_reads: int, total_bases: int, max_len: int,
                  max_results: int = 1 << 16) -> list[dict]:
-        table = (ctypes.c_int * (5 * 64))()
+        table = (ctypes.c_int * (5 * 128))()
         rows = ctypes.c_int()
         self._check(self.lib.bwt_gpu_autotune(self.handle, d_seqs, d_offs, n_reads, total_bases, max_len,
-                                              max_results, table, 64, ctypes.byref(rows)))
-        rows.value = min(rows.value, 64)
+                                              max_results, table, 128, ctypes.byref(rows)))
+        rows.value = min(rows.value, 128)
         return [{"register_bound_blocks": table[5 * i], "blocks_per_sm": table[5 * i + 1], "stack": table[5 * i + 2],
                  "chains_per_claim": table[5 * i + 3], "search_us": table[5 * i + 4]} for i in range(rows.value)]
 
@@ -244,6 +246,13 @@ class GpuIndex:
     def set_graph(self, on: bool) -> None:
         """Batched form from the captured CUDA graph (default) or launched stage by stage."""
         self.lib.bwt_gpu_set_graph(self.handle, 1 if on else 0)
+
+    def set_start_table(self, symbols: int) -> None:
+        """Start-table length of the batched search (0 = none)."""
+        self._check(self.lib.bwt_gpu_set_start_table(self.handle, symbols))
+
+    def start_table(self) -> int:
+        return int(self.lib.bwt_gpu_start_table(self.handle))
 
     def set_pipeline_chunk(self, reads: int) -> None:
         """Reads per chunk of pipelined host batches (0 or -1: not pipelined, the default)."""

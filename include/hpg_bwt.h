@@ -150,8 +150,8 @@ void bwt_gpu_set_census(bwt_index_t *index, int on);
 unsigned long long bwt_gpu_census(bwt_index_t *index);
 /* Reads per internal chunk of the plain form (0 = automatic). */
 void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
-/* Batched-form tuning: register bound (1 = compiler's choice, 12 or 16
- * resident 128-thread blocks per SM), resident blocks per SM actually
+/* Batched-form tuning: register bound (1 = compiler's choice, 10 (fused form
+ * only), 12 or 16 resident 128-thread blocks per SM), resident blocks per SM actually
  * launched (0 = occupancy limit), change points per lane held in shared
  * memory (2, 4 or 8; more spill to the device queue; 0 = split form: a
  * chain-only kernel queues every change point for the drain launch; -1 =
@@ -178,10 +178,18 @@ int bwt_gpu_graph(bwt_index_t *index);
  * never (the default: on GB300 the copies slow the search by about their own
  * duration, so the overlap gains nothing). */
 void bwt_gpu_set_pipeline_chunk(bwt_index_t *index, size_t reads);
+/* Start table of the batched search (fused form): a chain of a read of at
+ * least 2L+2 bases starts with one lookup of its first L symbols in a table of
+ * 4^L intervals per index direction (8 MB each at L = 10) instead of L
+ * dependent steps.  0 = no table (the default; the autotuner tries 8, 10, 11),
+ * at most 12.  Results are identical. */
+int bwt_gpu_set_start_table(bwt_index_t *index, int symbols);
+int bwt_gpu_start_table(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
- * every candidate setting (45), keeps the fastest, then picks the fastest
- * block-load form for it (4 more runs).  Optional table gets rows of
- * {min_blocks (or -1 - load mode), blocks_per_sm, stack, chains_per_claim,
+ * every candidate setting (60), keeps the fastest, then picks the fastest
+ * block-load form for it (4 more runs), then the start-table length among
+ * 0, 8, 10, 11 (4 more).  Optional table gets rows of {min_blocks (or -1 - load
+ * mode, or -100 - table length), blocks_per_sm, stack, chains_per_claim,
  * search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
