@@ -412,6 +412,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
         gi.set_load_mode(lm)
         if len(vals) > 4:
             gi.set_start_table(vals[4])
+        if len(vals) > 5:
+            gi.set_direction_split(vals[5])
     elif not args.no_autotune:
         t0 = time.time()
         table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
@@ -506,7 +508,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "serving": serve,
-            "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table()),
+            "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table(),
+                           direction_split=gi.direction_split()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }
@@ -558,7 +561,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
-                                                 "block_load_mode[,start_table] (stack 0 = split, -1 = lockstep)")
+                                                 "block_load_mode[,start_table[,direction_split]] (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]

@@ -299,6 +299,16 @@ void bwt_gpu_set_graph(bwt_index_t* index, int on) {
   if (e) engine_set_graph(e, on);
 }
 
+void bwt_gpu_set_direction_split(bwt_index_t* index, int mode) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_dir_split(e, mode);
+}
+
+int bwt_gpu_direction_split(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_dir_split(e) : -1;
+}
+
 int bwt_gpu_set_start_table(bwt_index_t* index, int symbols) {
   Engine* e = engine_of(index);
   if (!e) return fail("bwt_gpu_set_start_table: null index");

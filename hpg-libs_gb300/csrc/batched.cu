@@ -66,6 +66,22 @@ __device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
   return g.shfl(base, 0) + g.thread_rank() * n;
 }
 
+// Next read of a chain set (part 0: the chains on the backward index, 1: those
+// on the forward index, 2: all four), aggregated per warp and per set.
+__device__ __forceinline__ unsigned claim_part(const BatchedParams& p, uint32_t part) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  cg::coalesced_group sub = cg::labeled_partition(g, part);
+  unsigned base = 0;
+  if (sub.thread_rank() == 0) base = atomicAdd(part == 1 ? p.chain_ctr2 : p.chain_ctr, (unsigned)sub.size());
+  return sub.shfl(base, 0) + sub.thread_rank();
+}
+
+__device__ __forceinline__ uint32_t sm_id() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+
 // Chunked pool slot for the calling lane (cold state c_res = next slot | left << 28).
 __device__ __forceinline__ unsigned res_slot(const BatchedParams& p, uint32_t& c_res) {
   unsigned left = c_res >> 28;
@@ -103,7 +119,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
                                                                       int chunk) {
   const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
-  __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_misc[kBlock], c_res[kBlock];
+  __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_misc[kBlock], c_res[kBlock], c_part[kBlock];
   const int tid = threadIdx.x;
   const uint32_t n_chains = 4u * n_reads_;
   const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
@@ -124,8 +140,33 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   // read-level work: the current read's next chain, and the next read claimed
   // and its offsets fetched ahead of time (their loads complete while the
   // current read is searched)
+  // With the direction split, SMs of the first half take the two chains of a
+  // read that run on the backward index ('+' backward, '-' forward) and the
+  // others the two on the forward index ('+' forward, '-' backward): every
+  // chain and its branches stay on one index direction, so each half's L2
+  // holds one direction's blocks.  A half that runs out takes the other's reads.
+  // (claim state in shared memory, touched once per read: bits 0-1 the chain
+  // set being claimed, bit 2 set once it moved to the other half's reads,
+  // bits 3-4 the set of the current read, bits 5-6 that of the prefetched one)
+  {
+    const uint32_t part0 = p.dir_split == 1 ? (sm_id() >= p.num_sms / 2 ? 1u : 0u)
+                                             : (p.dir_split == 2 ? 0u : (p.dir_split == 3 ? 1u : 2u));
+    c_part[tid] = part0 | (part0 << 3) | (part0 << 5);
+  }
   uint32_t cur_read = 0, chain = 4;
-  uint32_t nxt_read = drain ? 0xFFFFFFFFu : claim(p.chain_ctr, 1);
+  auto next_claim = [&]() -> uint32_t {
+    uint32_t st = c_part[tid];
+    for (;;) {
+      const uint32_t part = st & 3u;
+      const uint32_t r = claim_part(p, part);
+      if (r < n_reads_ || part == 2u || (st & 4u) || p.dir_split != 1) {
+        c_part[tid] = (st & ~(3u << 5)) | (part << 5);
+        return r;
+      }
+      st = (st & ~3u) | (part ^ 1u) | 4u;
+    }
+  };
+  uint32_t nxt_read = drain ? 0xFFFFFFFFu : next_claim();
   uint64_t nxt_b0 = 0, nxt_b1 = 0;
   uint32_t nxt_ok = 0;
   if (nxt_read < n_reads_) {
@@ -259,24 +300,35 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         c_meta[tid] = make_meta(e.jtype & 0xFFFFu, e.jtype >> 16, 0, 0, true);
         continue;
       }
-      if (chain >= 4) {  // next read: switch to the prefetched one, prefetch the one after
+      if (chain >= ((((c_part[tid] >> 3) & 3u) == 2u) ? 4u : 2u)) {
+        // next read: switch to the prefetched one, prefetch the one after
         if (nxt_read >= n_reads_) break;
         cur_read = nxt_read;
+        {
+          const uint32_t st = c_part[tid];
+          c_part[tid] = (st & ~(3u << 3)) | (((st >> 5) & 3u) << 3);
+        }
         const uint64_t b0 = nxt_b0;
         const int L = (int)(nxt_b1 - nxt_b0);
         const uint32_t okr = nxt_ok;
-        nxt_read = claim(p.chain_ctr, 1);
+        nxt_read = next_claim();
         if (nxt_read < n_reads_) {
           nxt_b0 = p.offs[nxt_read];
           nxt_b1 = p.offs[nxt_read + 1];
           nxt_ok = p.ok[nxt_read];
         }
-        if (!okr || L < 3 || L > 32767) continue;
+        if (!okr || L < 3 || L > 32767) {
+          chain = 4;  // no chains for this read
+          continue;
+        }
         W = p.codes + b0;
         len = L;
         chain = 0;
       }
-      const uint32_t c = chain++;  // 0: '+' backward, 1: '+' forward, 2: '-' backward, 3: '-' forward
+      const uint32_t ci = chain++;
+      const uint32_t cur_part = (c_part[tid] >> 3) & 3u;
+      // 0: '+' backward, 1: '+' forward, 2: '-' backward, 3: '-' forward
+      const uint32_t c = cur_part == 2u ? ci : (cur_part == 0u ? (ci ? 3u : 0u) : (ci ? 2u : 1u));
       rs = (cur_read << 1) | (c >> 1);
       k = 0;
       l = X.top;

@@ -47,7 +47,12 @@ struct BatchedParams {
   const uint32_t* n_reads_dev;  // when set, the read count is read from device memory (graph replays)
   uint32_t max_results;
   // work queues
-  unsigned int* chain_ctr;   // next chain id
+  unsigned int* chain_ctr;   // next chain id (next read in the fused form)
+  unsigned int* chain_ctr2;  // fused form with direction split: next read for the forward-index chains
+  uint32_t dir_split;        // fused form: 1 = SMs of the first half run the chains on the backward index,
+                             // the others those on the forward index (each half then takes the rest);
+                             // 2 / 3 = this launch runs only the backward / forward-index chains
+  uint32_t num_sms;
   unsigned int* spill_head;  // next spill entry to drain
   unsigned int* spill_tail;  // spill entries written
   SpillEntry* spill;
@@ -70,6 +75,7 @@ struct BatchedTuning {
   int split = 0;          // 0: fused (per-lane stacks); 1: chain-only kernel + drain of every change point;
                           // 2: lockstep kernel (4 chains of a read per lane) + drain
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
+  int dir_split = 0;      // fused form: 0 mixed, 1 direction by SM half, 2 one launch per direction
 };
 
 // One locate work item per SA row: the row, the owning hit (or request), the

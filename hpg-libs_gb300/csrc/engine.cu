@@ -304,6 +304,9 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.n_reads_dev = nullptr;
     p.max_results = max_results;
     p.chain_ctr = ctr + 0;
+    p.chain_ctr2 = ctr + 9;
+    p.dir_split = e->tuning.split == 0 ? (uint32_t)e->tuning.dir_split : 0u;
+    p.num_sms = (uint32_t)e->num_sms;
     p.spill_head = ctr + 1;
     p.spill_tail = ctr + 2;
     p.spill = ptr<SpillEntry>(e->b_spill);
@@ -329,6 +332,13 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
       t.phase = 1;
       launch_batched_search(e->X, p1, t, e->num_sms, false, s);
       launch_batched_search(e->X, p1, t, e->num_sms, true, s);
+    } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
+      launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
+      BatchedParams p1 = p;
+      p1.dir_split = 3;
+      launch_batched_search(e->X, p1, e->tuning, e->num_sms, false, s);
+      cudaEventRecord(e->dev_mid, s);
+      launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
     } else {
       launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
       cudaEventRecord(e->dev_mid, s);
@@ -419,6 +429,9 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
   e->tuning.chunk = chunk < 1 ? 1 : (chunk > 8 ? 8 : chunk);
 }
 
+void engine_set_dir_split(Engine* e, int mode) { e->tuning.dir_split = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+int engine_dir_split(Engine* e) { return e->tuning.dir_split; }
+
 void engine_set_load_mode(Engine* e, int mode) { e->X.load_mode = (uint32_t)(mode < 0 ? 0 : (mode > 3 ? 3 : mode)); }
 int engine_load_mode(Engine* e) { return (int)e->X.load_mode; }
 
@@ -503,6 +516,35 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
     }
   }
   e->X.load_mode = best_mode;
+  // then the direction split of the fused form (rows marked by -50 - mode)
+  if (e->tuning.split == 0) {
+    const int was = e->tuning.dir_split;
+    int best_split = was;
+    for (int on = 0; on < 3; ++on) {
+      e->tuning.dir_split = on;
+      float t = 0;
+      for (int rep = 0; rep < 2; ++rep) {
+        if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases,
+                                 max_len, max_results, &r, err) != 0)
+          return -1;
+        t = e->stage_ms[kStageSearch];
+      }
+      if (table && rows < max_rows) {
+        int* row = table + 5 * rows;
+        row[0] = -50 - on;
+        row[1] = batched_max_blocks_per_sm(e->tuning);
+        row[2] = e->tuning.stack;
+        row[3] = e->tuning.chunk;
+        row[4] = (int)(t * 1000.0f);
+      }
+      ++rows;
+      if (t < best_ms) {
+        best_ms = t;
+        best_split = on;
+      }
+    }
+    e->tuning.dir_split = best_split;
+  }
   // then the start-table length (rows marked by a first column of -100 - L)
   int best_kmer = (int)e->X.kmer_len;
   for (int L : {0, 8, 10, 11}) {

@@ -63,6 +63,11 @@ size_t engine_index_bytes(Engine* e);
 void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, int chunk);
 void engine_get_tuning(Engine* e, int* out5);
 void engine_set_load_mode(Engine* e, int mode);
+// Fused form, index direction of the chains: 0 any lane any chain; 1 SMs of the
+// first half the backward-index chains, the rest the forward-index ones; 2 one
+// launch per direction.
+void engine_set_dir_split(Engine* e, int mode);
+int engine_dir_split(Engine* e);
 // Batched form from the captured CUDA graph (1, the default) or launched
 // stage by stage with host-read sizes (0).
 void engine_set_graph(Engine* e, int on);

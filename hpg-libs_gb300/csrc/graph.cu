@@ -67,7 +67,8 @@ bool same_settings(const GraphPlan* g, const Engine* e) {
   const BatchedTuning& a = g->tuning;
   const BatchedTuning& b = e->tuning;
   return a.block == b.block && a.blocks_per_sm == b.blocks_per_sm && a.stack == b.stack && a.chunk == b.chunk &&
-         a.min_blocks == b.min_blocks && a.split == b.split && g->load_mode == e->X.load_mode &&
+         a.min_blocks == b.min_blocks && a.split == b.split && a.dir_split == b.dir_split &&
+         g->load_mode == e->X.load_mode &&
          g->census == e->census_on && g->skip_locate == e->skip_locate && g->kmer_len == e->X.kmer_len &&
          g->kmer0 == (const void*)e->X.kmer[0];
 }
@@ -121,6 +122,9 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   p.n_reads_dev = g->hdr;
   p.max_results = 0;  // truncation happens in the finalize, from the header
   p.chain_ctr = ctr + 0;
+  p.chain_ctr2 = ctr + 9;
+  p.dir_split = g->tuning.split == 0 ? (uint32_t)g->tuning.dir_split : 0u;
+  p.num_sms = (uint32_t)e->num_sms;
   p.spill_head = ctr + 1;
   p.spill_tail = ctr + 2;
   p.spill = g->spill;
@@ -143,6 +147,13 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
     t.phase = 1;
     launch_batched_search(e->X, p1, t, e->num_sms, false, s);
     launch_batched_search(e->X, p1, t, e->num_sms, true, s);
+  } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
+    launch_batched_search(e->X, p, g->tuning, e->num_sms, false, s);
+    BatchedParams p1 = p;
+    p1.dir_split = 3;
+    launch_batched_search(e->X, p1, g->tuning, e->num_sms, false, s);
+    record(g->ev[2], s);
+    launch_batched_search(e->X, p, g->tuning, e->num_sms, true, s);
   } else {
     launch_batched_search(e->X, p, g->tuning, e->num_sms, false, s);
     record(g->ev[2], s);

@@ -104,6 +104,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_graph.argtypes = [vp]
     lib.bwt_gpu_set_pipeline_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_direction_split.argtypes = [vp]
     lib.bwt_gpu_start_table.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
@@ -246,6 +248,13 @@ class GpuIndex:
     def set_graph(self, on: bool) -> None:
         """Batched form from the captured CUDA graph (default) or launched stage by stage."""
         self.lib.bwt_gpu_set_graph(self.handle, 1 if on else 0)
+
+    def set_direction_split(self, mode: int) -> None:
+        """Fused batched search: 0 mixed, 1 index direction by SM half, 2 one launch per direction."""
+        self.lib.bwt_gpu_set_direction_split(self.handle, int(mode))
+
+    def direction_split(self) -> int:
+        return int(self.lib.bwt_gpu_direction_split(self.handle))
 
     def set_start_table(self, symbols: int) -> None:
         """Start-table length of the batched search (0 = none)."""

@@ -178,6 +178,15 @@ int bwt_gpu_graph(bwt_index_t *index);
  * never (the default: on GB300 the copies slow the search by about their own
  * duration, so the overlap gains nothing). */
 void bwt_gpu_set_pipeline_chunk(bwt_index_t *index, size_t reads);
+/* Direction split of the batched search (fused form).  Every chain of a read
+ * and its branches run on one index direction ('+' backward and '-' forward
+ * on the backward index, the other two on the forward index).  0 (default):
+ * any lane runs any chain; 1: SMs of the first half run the backward-index
+ * chains and the other SMs the forward-index ones (a half that runs out takes
+ * the other's reads); 2: one launch per direction, so the whole L2 holds one
+ * direction's occurrence blocks at a time.  Results are identical. */
+void bwt_gpu_set_direction_split(bwt_index_t *index, int mode);
+int bwt_gpu_direction_split(bwt_index_t *index);
 /* Start table of the batched search (fused form): a chain of a read of at
  * least 2L+2 bases starts with one lookup of its first L symbols in a table of
  * 4^L intervals per index direction (8 MB each at L = 10) instead of L
@@ -187,10 +196,10 @@ int bwt_gpu_set_start_table(bwt_index_t *index, int symbols);
 int bwt_gpu_start_table(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
  * every candidate setting (60), keeps the fastest, then picks the fastest
- * block-load form for it (4 more runs), then the start-table length among
- * 0, 8, 10, 11 (4 more).  Optional table gets rows of {min_blocks (or -1 - load
- * mode, or -100 - table length), blocks_per_sm, stack, chains_per_claim,
- * search us}. */
+ * block-load form for it (4 more runs), then the direction split (3 more, fused
+ * form only), then the start-table length among 0, 8, 10, 11 (4 more).
+ * Optional table gets rows of {min_blocks (or -1 - load mode, -50 - split,
+ * -100 - table length), blocks_per_sm, stack, chains_per_claim, search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
                      int *rows);
