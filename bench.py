@@ -55,6 +55,10 @@ WORKLOADS = {
     "c2_profile": dict(desc="profiling size of c2: the same 100 Mbp genome and index, 200k x 100 bp reads",
                        genome="repeats", genome_bp=100_000_000, reads=200_000, read_len=100,
                        edits="per_base_capped"),
+    "c3": dict(desc="100 Mbp genome (as c2); 4M reads of 36-250 bp per GPU (uniform), 30% exact, 50% one "
+                    "substitution, 20% one 1-bp indel; BWSearch1 + locate",
+               genome="repeats", genome_bp=100_000_000, reads=4_000_000, read_len=(36, 250),
+               edits="mix_30_50_20"),
     "c1": dict(desc="4 Mbp i.i.d. genome; 200k x 100 bp error-free reads; BWSearch1 + locate",
                genome="iid", genome_bp=4_000_000, reads=200_000, read_len=100, edits="none"),
     "small": dict(desc="2 Mbp genome (repeats); 100k x 100 bp reads; BWSearch1 + locate (smoke-size)",
@@ -131,7 +135,11 @@ def prepare(wl: dict, rank: int, dist):
         synth.write_fasta(str(base / "genome.fa"), genome)
         lib.build_index(str(base / "genome.fa"), str(base / "index"), SA_RATIO)
     dist.barrier()
-    reads = synth.reads_fast(genome, wl["reads"], read_seed(rank), wl["read_len"], wl["edits"])
+    if isinstance(wl["read_len"], tuple):
+        lo, hi = wl["read_len"]
+        reads = synth.reads_fast_var(genome, wl["reads"], read_seed(rank), lo, hi, wl["edits"])
+    else:
+        reads = synth.reads_fast(genome, wl["reads"], read_seed(rank), wl["read_len"], wl["edits"])
     log(f"[bench] rank {rank}: genome+index+reads ready in {time.time() - t0:.1f}s")
     return str(base / "index"), reads, genome
 
@@ -321,7 +329,7 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
     return out
 
 
-def serving(gi, reads, genome, log) -> dict:
+def serving(gi, reads, genome, log, read_label: str = "100bp") -> dict:
     """The serving form at 70 % offered load: 64k x 100 bp requests (the batch
     read model), and requests of log-uniform 1k-256k reads of 50-300 bp."""
     import torch
@@ -335,7 +343,7 @@ def serving(gi, reads, genome, log) -> dict:
     mix_seq = torch.from_numpy(mix.seq).pin_memory()
     mix_off = torch.from_numpy(mix.offsets.view(np.int64)).pin_memory()
     log(f"[bench] serving read pools ready ({time.time() - t:.1f}s)")
-    cases = [("requests_64k_100bp", pin_seq, pin_off, len(reads), lambda: 65536),
+    cases = [(f"requests_64k_{read_label}", pin_seq, pin_off, len(reads), lambda: 65536),
              ("requests_1k_256k_50_300bp", mix_seq, mix_off, len(mix),
               lambda: int(np.exp(rng.uniform(np.log(1024), np.log(262144)))))]
     for name, sq, of, pn, draw in cases:
@@ -452,7 +460,9 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             e2e_t.append(dt)
         e_hits, e_locs = int(rsc.n_hits), int(rsc.n_locs)
         gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rsc))
-    serve = serving(gi, reads, genome, log) if not args.no_serving else None
+    rl = wl["read_len"]
+    serve = serving(gi, reads, genome, log, f"{rl[0]}_{rl[1]}bp" if isinstance(rl, tuple) else f"{rl}bp") \
+        if not args.no_serving else None
     e2e_s = dist.max(sum(e2e_t))
     e2e_value = total_reads * args.steps / e2e_s
     h2d = total + 8 * (n + 1)
@@ -491,7 +501,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "config": {"workload": wl["desc"], "genome_bp": wl["genome_bp"], "reads_per_gpu": n,
                        "read_len": wl["read_len"], "max_results": MAX_RESULTS, "sa_ratio": SA_RATIO,
                        "o_ratio": 64, "form": "batched", "l2": "flushed (256 MiB write) before every step; "
-                       "reads 200 MB > L2", "parallelism": f"replica x{dist.world} (reads sharded)"},
+                       f"reads {total / 1e6:.0f} MB > L2", "parallelism": f"replica x{dist.world} (reads sharded)"},
             "e2e": {"value": round(e2e_value, 1), "unit": "reads/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "bwt_gpu_search_batch"},
             "gpu_launches": int(launches),
