@@ -11,6 +11,7 @@
 //   R[p/ratio]  = ISA[p]  for text positions p with p % ratio == 0
 // which are the values the reference's walk stores.  Both directions are
 // built concurrently.
+#include <cuda_runtime.h>
 #include <omp.h>
 #include <sys/stat.h>
 
@@ -22,6 +23,7 @@
 #include <string>
 #include <vector>
 
+#include "gpu_sa.hpp"
 #include "index_format.hpp"
 #include "sais.hpp"
 
@@ -97,11 +99,10 @@ struct Direction {
   SampledVec S, R;
 };
 
+// Every table of one direction from its suffix array (n+1 entries, sa[0] == n).
 template <typename I>
-void build_direction(const std::vector<uint8_t>& X, uint32_t ratio, Direction* d) {
+void tables_from_sa(const std::vector<uint8_t>& X, const std::vector<I>& sa, uint32_t ratio, Direction* d) {
   const int64_t n = (int64_t)X.size();
-  std::vector<I> sa;
-  suffix_array_dna<I>(X.data(), n, sa);
   const int64_t rows = n + 1;
 
   d->bwt.resize((size_t)rows);
@@ -156,11 +157,27 @@ void build_direction(const std::vector<uint8_t>& X, uint32_t ratio, Direction* d
   }
 }
 
+template <typename I>
+void build_direction(const std::vector<uint8_t>& X, uint32_t ratio, Direction* d) {
+  std::vector<I> sa;
+  suffix_array_dna<I>(X.data(), (int64_t)X.size(), sa);
+  tables_from_sa<I>(X, sa, ratio, d);
+}
+
 void build_direction_any(const std::vector<uint8_t>& X, uint32_t ratio, Direction* d) {
   if ((int64_t)X.size() + 1 < ((int64_t)1 << 31))
     build_direction<int32_t>(X, ratio, d);
   else
     build_direction<int64_t>(X, ratio, d);
+}
+
+// The same with the suffix array built on a GPU.
+std::string build_direction_gpu(const std::vector<uint8_t>& X, uint32_t ratio, int device, Direction* d) {
+  std::vector<uint32_t> sa(X.size() + 1);
+  std::string e;
+  if (gpu_suffix_array(X.data(), X.size(), device, sa.data(), &e) != 0) return e;
+  tables_from_sa<uint32_t>(X, sa, ratio, d);
+  return "";
 }
 
 // BWT without the '$' row, as dbwt writes it into B.vec (dbwt.c:732-763).
@@ -180,7 +197,7 @@ std::string mkdir_p(const std::string& dir) {
 }  // namespace
 
 std::string build_index(const std::string& fasta, const std::string& outdir, uint32_t ratio, bool duplicate_strand,
-                        const std::string& bases) {
+                        const std::string& bases, int device) {
   if (ratio == 0) return "sampling ratio must be positive";
   Alphabet a;
   std::string e;
@@ -218,12 +235,17 @@ std::string build_index(const std::string& fasta, const std::string& outdir, uin
 
   std::vector<uint8_t> Xi(X.rbegin(), X.rend());
   Direction fw, bw;
+  if (device >= 0) {  // suffix arrays on the GPU, one direction after the other
+    if (!(e = build_direction_gpu(X, ratio, device, &bw)).empty()) return e;
+    if (!(e = build_direction_gpu(Xi, ratio, device, &fw)).empty()) return e;
+  } else {
 #pragma omp parallel sections num_threads(2)
-  {
+    {
 #pragma omp section
-    build_direction_any(X, ratio, &bw);
+      build_direction_any(X, ratio, &bw);
 #pragma omp section
-    build_direction_any(Xi, ratio, &fw);
+      build_direction_any(Xi, ratio, &fw);
+    }
   }
 
   // C counts symbols of B only (preprocess.c:44-72); both directions load it.
@@ -265,20 +287,32 @@ std::string build_index(const std::string& fasta, const std::string& outdir, uin
 extern "C" {
 
 // Status-returning builder: 0 on success, -1 with a message in errbuf.
-int hpg_bwt_build_index(const char* ref_file, const char* output_dir, unsigned int s_ratio, int duplicate_strand,
-                        const char* bases, char* errbuf, size_t errlen) {
+int hpg_bwt_build_index_on(const char* ref_file, const char* output_dir, unsigned int s_ratio,
+                           int duplicate_strand, const char* bases, int device, char* errbuf, size_t errlen) {
   std::string e = hpgbwt::build_index(ref_file ? ref_file : "", output_dir ? output_dir : "", s_ratio,
-                                      duplicate_strand != 0, bases ? bases : "ACGT");
+                                      duplicate_strand != 0, bases ? bases : "ACGT", device);
   if (e.empty()) return 0;
   if (errbuf && errlen) std::snprintf(errbuf, errlen, "%s", e.c_str());
   return -1;
 }
 
+int hpg_bwt_build_index(const char* ref_file, const char* output_dir, unsigned int s_ratio, int duplicate_strand,
+                        const char* bases, char* errbuf, size_t errlen) {
+  return hpg_bwt_build_index_on(ref_file, output_dir, s_ratio, duplicate_strand, bases, -1, errbuf, errlen);
+}
+
 // bwt.h:287-289.  Like the reference, an unrecoverable error ends the process.
+// The suffix arrays are built on GPU 0 when one is visible, else on the host.
 void bwt_generate_index_files(char* ref_file, char* output_dir, unsigned int s_ratio, bool duplicate_strand,
                               char* bases) {
   char err[512];
-  if (hpg_bwt_build_index(ref_file, output_dir, s_ratio, duplicate_strand ? 1 : 0, bases, err, sizeof err) != 0) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess) {
+    cudaGetLastError();
+    ndev = 0;
+  }
+  if (hpg_bwt_build_index_on(ref_file, output_dir, s_ratio, duplicate_strand ? 1 : 0, bases, ndev > 0 ? 0 : -1, err,
+                             sizeof err) != 0) {
     std::fprintf(stderr, "bwt_generate_index_files: %s\n", err);
     std::exit(EXIT_FAILURE);
   }

@@ -117,6 +117,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_gather_probe.argtypes = [ctypes.c_int, sz, u32, u32, u32, ctypes.POINTER(ctypes.c_double)]
     lib.hpg_bwt_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
                                         ctypes.c_char_p, ctypes.c_char_p, sz]
+    lib.hpg_bwt_build_index_on.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
+                                           ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, sz]
     _lib = lib
     return lib
 
@@ -141,10 +143,11 @@ def gather_probe(device: int, nbytes: int, blocks: int, steps: int, work: int) -
     return v.value
 
 
-def build_index(fasta: str, outdir: str, ratio: int = 16, bases: str = "ACGT") -> None:
+def build_index(fasta: str, outdir: str, ratio: int = 16, bases: str = "ACGT", device: int = -1) -> None:
+    """Write the reference's index files for a FASTA; suffix arrays on the host, or on CUDA device `device`."""
     lib = load()
     err = ctypes.create_string_buffer(1024)
-    if lib.hpg_bwt_build_index(fasta.encode(), outdir.encode(), ratio, 0, bases.encode(), err, 1024) != 0:
+    if lib.hpg_bwt_build_index_on(fasta.encode(), outdir.encode(), ratio, 0, bases.encode(), device, err, 1024) != 0:
         raise RuntimeError(err.value.decode())
 
 

@@ -95,14 +95,23 @@ bwt_optarg_t *bwt_optarg_new(const size_t num_errors, const size_t num_threads, 
 /* bwt.h:268 (bwt.c:449-453) */
 void bwt_optarg_free(bwt_optarg_t *optarg);
 
-/* bwt.h:287-289 (bwt.c:744-819): writes the reference on-disk index format.
- * Ends the process on error, like the reference. */
+/* bwt.h:287-289 (bwt.c:744-819): writes the reference on-disk index format,
+ * byte for byte.  The suffix arrays are built on GPU 0 when one is visible
+ * (prefix doubling with a device radix sort), else on the host (SA-IS); the
+ * files are the same either way.  Ends the process on error, like the
+ * reference. */
 void bwt_generate_index_files(char *ref_file, char *output_dir, unsigned int s_ratio, bool duplicate_strand,
                               char *bases);
 
-/* Status-returning builder (0 ok, -1 with errbuf).  No reference counterpart. */
+/* Status-returning builder (0 ok, -1 with errbuf), suffix arrays on the host.
+ * No reference counterpart. */
 int hpg_bwt_build_index(const char *ref_file, const char *output_dir, unsigned int s_ratio, int duplicate_strand,
                         const char *bases, char *errbuf, size_t errlen);
+/* The same with the suffix arrays built on CUDA device `device` (-1: on the
+ * host).  A 3.1 Gbp genome needs about 100 GB of device memory.  No reference
+ * counterpart. */
+int hpg_bwt_build_index_on(const char *ref_file, const char *output_dir, unsigned int s_ratio,
+                           int duplicate_strand, const char *bases, int device, char *errbuf, size_t errlen);
 
 /* ------------------------------------------------ GPU batch search ---- */
 
