@@ -59,6 +59,11 @@ WORKLOADS = {
                     "substitution, 20% one 1-bp indel; BWSearch1 + locate",
                genome="repeats", genome_bp=100_000_000, reads=4_000_000, read_len=(36, 250),
                edits="mix_30_50_20"),
+    "c4": dict(desc="3.1 Gbp human-like genome (GC 41%; 10% 300 bp and 17% 6 kbp element copies at 80-98% "
+                    "identity, 18% perfect tandem runs of 1-6 bp units, 20-149 bp long); 20M x 150 bp reads per "
+                    "GPU at 1% per-base substitution (uncapped, <=1 edit searched); BWSearch1 + locate; index "
+                    "built with the GPU builder",
+               genome="large", genome_bp=3_100_000_000, reads=20_000_000, read_len=150, edits="subst_1pct"),
     "c1": dict(desc="4 Mbp i.i.d. genome; 200k x 100 bp error-free reads; BWSearch1 + locate",
                genome="iid", genome_bp=4_000_000, reads=200_000, read_len=100, edits="none"),
     "small": dict(desc="2 Mbp genome (repeats); 100k x 100 bp reads; BWSearch1 + locate (smoke-size)",
@@ -129,18 +134,29 @@ def prepare(wl: dict, rank: int, dist):
     key = f"{wl['genome']}_{wl['genome_bp']}_r{SA_RATIO}"
     base = Path(os.environ.get("HPG_BENCH_CACHE", tempfile.gettempdir())) / "hpgbwt_bench" / key
     t0 = time.time()
-    genome = synth.genome(wl["genome"], wl["genome_bp"], 1)
+    large = wl["genome"] == "large"
+    if large:
+        genome = synth.genome_large(wl["genome_bp"], 1)
+    else:
+        genome = synth.genome(wl["genome"], wl["genome_bp"], 1)
+    t_gen = time.time() - t0
     if rank == 0 and not (base / "index" / "Si.vec").exists():
         base.mkdir(parents=True, exist_ok=True)
         synth.write_fasta(str(base / "genome.fa"), genome)
-        lib.build_index(str(base / "genome.fa"), str(base / "index"), SA_RATIO)
+        t1 = time.time()
+        # the 3.1 Gbp genome is indexed on this rank's GPU (the host builder takes tens of minutes)
+        lib.build_index(str(base / "genome.fa"), str(base / "index"), SA_RATIO, device=dist.local if large else -1)
+        log(f"[bench] index of {wl['genome_bp'] // 1_000_000} Mbp built in {time.time() - t1:.1f}s "
+            f"({'GPU' if large else 'host'} suffix arrays)")
     dist.barrier()
-    if isinstance(wl["read_len"], tuple):
+    if wl["edits"] == "subst_1pct":
+        reads = synth.reads_large(genome, wl["reads"], read_seed(rank), wl["read_len"], 0.01)
+    elif isinstance(wl["read_len"], tuple):
         lo, hi = wl["read_len"]
         reads = synth.reads_fast_var(genome, wl["reads"], read_seed(rank), lo, hi, wl["edits"])
     else:
         reads = synth.reads_fast(genome, wl["reads"], read_seed(rank), wl["read_len"], wl["edits"])
-    log(f"[bench] rank {rank}: genome+index+reads ready in {time.time() - t0:.1f}s")
+    log(f"[bench] rank {rank}: genome ({t_gen:.1f}s) + index + reads ready in {time.time() - t0:.1f}s")
     return str(base / "index"), reads, genome
 
 
@@ -600,6 +616,7 @@ def main():
 class _Rank0:
     """Rank 0 of a reference-arm run: no process group, nothing to wait for."""
     rank = 0
+    local = 0
     world = int(os.environ.get("WORLD_SIZE", "1"))
 
     def barrier(self):

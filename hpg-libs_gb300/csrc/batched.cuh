@@ -85,6 +85,11 @@ struct RowItem {
   uint32_t row, hit, out, phys_len;  // phys_len: direction << 31 | len_calc
 };
 
+// Located rows of one batched call: row items carry 32-bit output indices and
+// rows are claimed through a 32-bit counter that may run a few claims past the
+// end, so a batch stays well below 2^32 rows (the plain form has no such limit).
+constexpr uint64_t kMaxLocateRows = 0xF0000000ull;
+
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u, kStatusBadInput = 8u;
 
 // Locate sizes of the graph form: with `status` set, the hit and row counts

@@ -388,9 +388,15 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   }
   HPG_CUDA(cudaStreamSynchronize(s), "locate scan");
   cudaEventRecord(e->cev[2], s);
+  if (l_tot > kMaxLocateRows) {
+    *err = "too many located rows in one batched call (" + std::to_string(l_tot) + ", limit " +
+           std::to_string(kMaxLocateRows) + "): split the batch or use the plain form";
+    return -1;
+  }
   if (!ensure(e, e->locs, (l_tot + 1) * sizeof(hpg_loc_t)) ||
       !ensure(e, e->b_rowhit, (l_tot + 1) * locate_row_item_bytes())) {
-    *err = "out of device memory (locate output)";
+    *err = oom_message(("locate output, " + std::to_string(l_tot) + " rows of " + std::to_string(h_tot) + " hits").c_str(),
+                       (l_tot + 1) * (sizeof(hpg_loc_t) + locate_row_item_bytes()));
     return -1;
   }
   if (census) cudaMemsetAsync(census, 0, 8, s);
@@ -772,7 +778,8 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
     if (census) cudaMemsetAsync(census, 0, 8, s);
     cudaEventRecord(c, s);
     if (!ensure(e, e->locs, (n_locs + l_tot + 1) * sizeof(hpg_loc_t), true)) {
-      *err = "out of device memory (locate output)";
+      *err = oom_message(("locate output, " + std::to_string(n_locs + l_tot) + " rows").c_str(),
+                         (n_locs + l_tot + 1) * sizeof(hpg_loc_t));
       return -1;
     }
     launch_locate(e->X, hits, ptr<uint64_t>(e->loc_off), (uint32_t)h_tot, l_tot, d_offs, (uint32_t)n_hits,

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -142,6 +143,18 @@ inline bool ensure(Engine* e, DevBuf& b, size_t bytes, bool keep = false) {
   b.p = p;
   b.cap = want;
   return true;
+}
+
+// "out of device memory (<what>: <bytes> requested, <bytes> free)": the sizes
+// say whether the batch or the device is the problem.
+inline std::string oom_message(const char* what, size_t requested) {
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  cudaGetLastError();
+  char buf[192];
+  snprintf(buf, sizeof buf, "out of device memory (%s: %.2f GB requested, %.2f GB free of %.2f GB)", what,
+           requested / 1e9, free_b / 1e9, total_b / 1e9);
+  return buf;
 }
 
 template <typename T>

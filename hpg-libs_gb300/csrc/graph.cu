@@ -241,7 +241,7 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   uint32_t res_cap = (uint32_t)std::min<uint64_t>(4 * n_cap + 4096, 0xFFFFFFF0u);
   uint32_t spill_cap = (uint32_t)std::min<uint64_t>(
       e->tuning.split ? 4 * n_cap + 4096 + (uint64_t)e->num_sms * 16 * 128 * 8 : n_cap / 4 + 4096, 0xFFFFFFF0u);
-  uint64_t locs_cap = 8 * n_cap + 4096;
+  uint64_t locs_cap = std::min<uint64_t>(8 * n_cap + 4096, kMaxLocateRows);
   if (g) {  // keep what earlier batches of this class needed
     res_cap = std::max(res_cap, g->res_cap);
     spill_cap = std::max(spill_cap, g->spill_cap);
@@ -313,7 +313,14 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
     grow->locs_cap = g->locs_cap;
     if (status & kStatusResFull) grow->res_cap = (uint32_t)std::min<uint64_t>((h[0] >> 32) * 2 + 4096, 0xFFFFFFF0u);
     if (status & kStatusSpillFull) grow->spill_cap = (uint32_t)std::min<uint64_t>(h[1] * 2 + 4096, 0xFFFFFFF0u);
-    if (status & kStatusLocFull) grow->locs_cap = h[3] + h[3] / 4 + 4096;
+    if (status & kStatusLocFull) {
+      if (h[3] > kMaxLocateRows) {
+        *err = "too many located rows in one batched call (" + std::to_string(h[3]) + ", limit " +
+               std::to_string(kMaxLocateRows) + "): split the batch or use the plain form";
+        return -1;
+      }
+      grow->locs_cap = std::min<uint64_t>(h[3] + h[3] / 4 + 4096, kMaxLocateRows);
+    }
     return 1;
   }
   e->census_val = g->census ? h[4] : 0;

@@ -51,7 +51,8 @@ class Result:
 def _arr(ptr: int | None, n: int, dt: np.dtype) -> np.ndarray:
     if n == 0 or not ptr:
         return np.zeros(0, dtype=dt)
-    return np.frombuffer(ctypes.string_at(ptr, n * dt.itemsize), dtype=dt).copy()
+    # a ctypes array view, not ctypes.string_at, whose size argument is a C int (wraps past 2 GiB)
+    return np.frombuffer((ctypes.c_uint8 * (n * dt.itemsize)).from_address(ptr), dtype=dt).copy()
 
 
 def result_from_c(rs: ResultSetC, n_reads: int) -> Result:

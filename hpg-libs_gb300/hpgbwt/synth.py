@@ -297,3 +297,76 @@ def reads_fast_var(g: np.ndarray, n: int, seed: int, lo: int, hi: int, edits: st
         keep = col < L
         out[offs[a]:offs[b]] = _ASCII[base[keep]]
     return ReadSet(out, offs, pos, strand, plan)
+
+
+def genome_large(n: int, seed: int, chunk: int = 1 << 26) -> np.ndarray:
+    """Human-like genome of n bases built in bounded memory (about 1.2 n bytes
+    at peak): GC 41 % background, 10 % copies of 300 bp elements and 17 % of
+    6 kbp elements at 80-98 % identity, 18 % tandem repeats of 1-6 bp units
+    (perfect runs of 20-149 bp, each closed at both ends by a base that breaks
+    its period, so that no two runs of one unit merge into a stretch as long as
+    a 150 bp read: a read lying inside a longer run of a 1-6 bp unit matches
+    every window of every such run with up to max_results indel variants of
+    that interval, millions of rows per read at 3.1 Gbp).
+    Deterministic for (n, seed); meant for the 3.1 Gbp shapes, where genome()
+    would need tens of GB of temporaries."""
+    rng = np.random.default_rng(seed)
+    g = np.empty(n, dtype=np.uint8)
+    cum = np.cumsum([0.295, 0.205, 0.205])
+    for a in range(0, n, chunk):
+        u = rng.random(min(chunk, n - a))
+        g[a:a + len(u)] = np.searchsorted(cum, u, side="right").astype(np.uint8)
+    for frac, L, fams, batch in ((0.10, 300, 64, 100_000), (0.17, 6000, 32, 5_000)):
+        elems = np.stack([background(L, rng, 0.41) for _ in range(fams)])
+        copies = int(frac * n) // L
+        col = np.arange(L)
+        for b0 in range(0, copies, batch):
+            b = min(batch, copies - b0)
+            fam = rng.integers(0, fams, size=b)
+            starts = rng.integers(0, n - L, size=b)
+            ident = rng.uniform(0.80, 0.98, size=b)
+            mat = elems[fam]
+            m = rng.random((b, L)) > ident[:, None]
+            mat[m] = (mat[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
+            g[starts[:, None] + col[None, :]] = mat
+    target, done = int(0.18 * n), 0
+    j = np.arange(-1, 151)  # run bases 0..rlen-1, breakers at -1 and rlen
+    while done < target:
+        b = 200_000
+        units = rng.integers(0, 4, size=(b, 6), dtype=np.uint8)
+        ulen = rng.integers(1, 7, size=b)
+        rlen = rng.integers(20, 150, size=b)
+        starts = rng.integers(1, n - 151, size=b)
+        keep = (j[None, :] >= -1) & (j[None, :] <= rlen[:, None])
+        vals = np.take_along_axis(units, (j[None, :] % ulen[:, None]), axis=1)
+        ends = (j[None, :] == -1) | (j[None, :] == rlen[:, None])
+        vals[ends] = (vals[ends] + rng.integers(1, 4, size=int(ends.sum()), dtype=np.uint8)) % 4
+        g[(starts[:, None] + j[None, :])[keep]] = vals[keep]
+        done += int(rlen.sum())
+    return g
+
+
+def reads_large(g: np.ndarray, n: int, seed: int, length: int, subst_rate: float, chunk: int = 1_000_000) -> ReadSet:
+    """n reads of `length` bases from uniform positions on either strand with
+    independent per-base substitutions at subst_rate (uncapped), generated in
+    chunks so that memory stays near the output size."""
+    rng = np.random.default_rng(seed)
+    L = int(length)
+    offs = np.arange(n + 1, dtype=np.uint64) * np.uint64(L)
+    out = np.empty(n * L, dtype=np.uint8)
+    pos_all = np.empty(n, dtype=np.int64)
+    strand_all = np.empty(n, dtype=np.int8)
+    col = np.arange(L)
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        pos = (rng.random(b - a) * (len(g) - L)).astype(np.int64)
+        strand = (rng.random(b - a) < 0.5).astype(np.int8)
+        frag = g[pos[:, None] + col[None, :]]
+        m = rng.random(frag.shape) < subst_rate
+        frag[m] = (frag[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
+        rc = np.nonzero(strand)[0]
+        frag[rc] = _COMP[frag[rc][:, ::-1]]
+        out[a * L:b * L] = _ASCII[frag].reshape(-1)
+        pos_all[a:b] = pos
+        strand_all[a:b] = strand
+    return ReadSet(out, offs, pos_all, strand_all, np.zeros(n, dtype=np.int8))

@@ -105,7 +105,7 @@ class RefOracle:
                              fq.ids.ctypes.data, fq.id_offs.ctypes.data, fq.n, filter_read_mappings, flag,
                              ctypes.byref(p), ctypes.byref(n))
         try:
-            return ctypes.string_at(p.value, n.value) if n.value else b""
+            return bytes((ctypes.c_uint8 * n.value).from_address(p.value)) if n.value else b""
         finally:
             self.lib.ref_blob_free(p)
 

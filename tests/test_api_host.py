@@ -84,3 +84,13 @@ def test_recorded_lists_parse():
         anchors = sum(it[0] == "anchor" for x in gc.api_expected(al.API_INEXACT_READ, 200, 1, fq.n)
                       for it in x["items"])
         assert anchors > 0 and (2 in flags or name == "iid_1chr")
+
+
+def test_result_arrays_past_2gib():
+    """Result arrays above 2 GiB come back whole (ctypes.string_at would wrap the size)."""
+    from hpgbwt.lib import _arr, LOC_DTYPE
+    n = (1 << 31) // LOC_DTYPE.itemsize + 1000
+    buf = np.zeros(n, dtype=LOC_DTYPE)
+    buf["hit"][-1] = 7
+    out = _arr(buf.ctypes.data, n, LOC_DTYPE)
+    assert len(out) == n and out["hit"][-1] == 7
