@@ -809,6 +809,9 @@ __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const un
   }
 }
 
+constexpr uint32_t kLongList = 32;  // longer lists are sorted by a whole block (sort_long_lists_kernel)
+constexpr int kRankTpb = 512, kRankTile = 2048;
+
 __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
                                      uint32_t n_rs, uint32_t max_results, uint32_t* __restrict__ kept,
                                      uint8_t* __restrict__ trunc, const uint32_t* max_dev, const unsigned* gate) {
@@ -817,7 +820,12 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
   if (gate && *gate) return;
   if (max_dev) max_results = *max_dev;
   const uint64_t b = seg_off[rs], e = seg_off[rs + 1];
-  // insertion sort by key (lists are short; keys are unique within a list)
+  const uint64_t cnt = e - b;
+  const uint32_t keep = (uint32_t)(cnt < max_results ? cnt : max_results);
+  kept[rs] = keep;
+  trunc[rs] = cnt > max_results ? 1 : 0;
+  if (keep == 0 || cnt > kLongList) return;
+  // insertion sort by key (short list; keys are unique within a list)
   for (uint64_t i = b + 1; i < e; ++i) {
     const PendingHit x = sorted[i];
     uint64_t j = i;
@@ -827,9 +835,54 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
     }
     sorted[j] = x;
   }
-  const uint64_t cnt = e - b;
-  kept[rs] = (uint32_t)(cnt < max_results ? cnt : max_results);
-  trunc[rs] = cnt > max_results ? 1 : 0;
+}
+
+// Lists longer than kLongList (low-complexity reads emit thousands of pending
+// hits), one list at a time per block: the rank of an entry is the number of
+// entries of its list with a smaller (key, position) pair, counted against
+// tiles of the list's keys in shared memory; entries ranked below the kept
+// count are written to `scratch` (the unsorted pending array, dead after the
+// scatter) at their rank and copied back.  O(m^2 / 512) per list of m entries.
+__global__ void __launch_bounds__(kRankTpb)
+    sort_long_lists_kernel(PendingHit* __restrict__ sorted, PendingHit* __restrict__ scratch,
+                           const uint64_t* __restrict__ seg_off, uint32_t n_rs, const uint32_t* __restrict__ kept,
+                           const unsigned* gate) {
+  if (gate && *gate) return;
+  __shared__ uint64_t tile[kRankTile];
+  __shared__ uint32_t longs[kRankTpb];
+  __shared__ uint32_t n_long;
+  for (uint64_t base = (uint64_t)blockIdx.x * kRankTpb; base < n_rs; base += (uint64_t)gridDim.x * kRankTpb) {
+    if (threadIdx.x == 0) n_long = 0;
+    __syncthreads();
+    const uint64_t rs = base + threadIdx.x;
+    if (rs < n_rs && seg_off[rs + 1] - seg_off[rs] > kLongList && kept[rs] > 0)
+      longs[atomicAdd(&n_long, 1u)] = (uint32_t)rs;
+    __syncthreads();
+    const uint32_t nl = n_long;
+    for (uint32_t q = 0; q < nl; ++q) {
+      const uint32_t r = longs[q];
+      const uint64_t b = seg_off[r];
+      const uint32_t m = (uint32_t)(seg_off[r + 1] - b), keep = kept[r];
+      for (uint32_t i0 = 0; i0 < m; i0 += kRankTpb) {
+        const uint32_t i = i0 + threadIdx.x;
+        const uint64_t mine = i < m ? ((uint64_t)sorted[b + i].key << 32 | i) : ~0ull;
+        uint32_t rank = 0;
+        for (uint32_t t0 = 0; t0 < m; t0 += kRankTile) {
+          const uint32_t tn = min((uint32_t)kRankTile, m - t0);
+          __syncthreads();  // the previous tile is no longer read
+          for (uint32_t t = threadIdx.x; t < tn; t += kRankTpb)
+            tile[t] = (uint64_t)sorted[b + t0 + t].key << 32 | (t0 + t);
+          __syncthreads();
+          for (uint32_t t = 0; t < tn; ++t) rank += tile[t] < mine ? 1u : 0u;
+        }
+        if (i < m && rank < keep) scratch[b + rank] = sorted[b + i];
+      }
+      __syncthreads();  // every rank written before the copy back
+      for (uint32_t i = threadIdx.x; i < keep; i += kRankTpb) sorted[b + i] = scratch[b + i];
+      __syncthreads();  // the list is final before the next one reuses the tile
+    }
+    __syncthreads();  // n_long and longs are read before they are reset
+  }
 }
 
 __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
@@ -1126,13 +1179,17 @@ void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, c
   scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap, cursor, gate);
 }
 
-void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
-                          uint32_t* kept, uint8_t* trunc, cudaStream_t s, const uint32_t* max_dev,
-                          const unsigned* gate) {
+void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_t* seg_off, uint32_t n_rs,
+                          uint32_t max_results, uint32_t* kept, uint8_t* trunc, int num_sms, cudaStream_t s,
+                          const uint32_t* max_dev, const unsigned* gate) {
   if (!n_rs) return;
   count_launches(1);
   sort_truncate_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, n_rs, max_results, kept, trunc, max_dev,
                                                           gate);
+  uint64_t blocks = ((uint64_t)n_rs + kRankTpb - 1) / kRankTpb;
+  if (blocks > 2ull * (uint64_t)num_sms) blocks = 2ull * (uint64_t)num_sms;
+  count_launches(1);
+  sort_long_lists_kernel<<<(unsigned)blocks, kRankTpb, 0, s>>>(sorted, scratch, seg_off, n_rs, kept, gate);
 }
 
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,

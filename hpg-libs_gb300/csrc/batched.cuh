@@ -114,9 +114,12 @@ int batched_max_blocks_per_sm(const BatchedTuning& t);
 void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, const uint64_t* seg_off,
                          PendingHit* sorted, uint32_t res_cap, uint32_t* cursor, cudaStream_t s,
                          const unsigned* gate = nullptr);
-void launch_sort_truncate(PendingHit* sorted, const uint64_t* seg_off, uint32_t n_rs, uint32_t max_results,
-                          uint32_t* kept, uint8_t* trunc, cudaStream_t s, const uint32_t* max_dev = nullptr,
-                          const unsigned* gate = nullptr);
+// Sorts every (read, strand) list by emission key and keeps the first max_results
+// (from max_dev when given); `scratch` holds at least as many entries as
+// `sorted` and its contents are overwritten (the scatter's input is dead by then).
+void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_t* seg_off, uint32_t n_rs,
+                          uint32_t max_results, uint32_t* kept, uint8_t* trunc, int num_sms, cudaStream_t s,
+                          const uint32_t* max_dev = nullptr, const unsigned* gate = nullptr);
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
                         const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
                         const unsigned* gate = nullptr);

@@ -368,8 +368,8 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   cudaMemsetAsync(e->hit_off.p, 0, T * 4, s);  // per-list cursors (hit_off is rewritten below)
   launch_scatter_hits(ptr<PendingHit>(e->b_res), ctr + 3, ptr<uint64_t>(e->b_seg), ptr<PendingHit>(e->b_sorted),
                       e->b_res_cap, ptr<uint32_t>(e->hit_off), s);
-  launch_sort_truncate(ptr<PendingHit>(e->b_sorted), ptr<uint64_t>(e->b_seg), (uint32_t)T, max_results,
-                       ptr<uint32_t>(e->rs_count), ptr<uint8_t>(e->rs_trunc), s);
+  launch_sort_truncate(ptr<PendingHit>(e->b_sorted), ptr<PendingHit>(e->b_res), ptr<uint64_t>(e->b_seg), (uint32_t)T,
+                       max_results, ptr<uint32_t>(e->rs_count), ptr<uint8_t>(e->rs_trunc), e->num_sms, s);
   launch_scan(ptr<uint32_t>(e->rs_count), T, ptr<uint64_t>(e->hit_off), ptr<uint64_t>(e->scan_part), s);
   uint64_t h_tot = 0;
   HPG_CUDA(cudaMemcpyAsync(&h_tot, ptr<uint64_t>(e->hit_off) + T, 8, cudaMemcpyDeviceToHost, s), "hit count");

@@ -166,7 +166,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   cudaMemsetAsync(g->hit_off, 0, T * 4, s);  // per-list cursors (hit_off is rewritten below)
   launch_scatter_hits(g->res, ctr + 3, g->seg, g->sorted, g->res_cap, reinterpret_cast<uint32_t*>(g->hit_off), s,
                       status);
-  launch_sort_truncate(g->sorted, g->seg, (uint32_t)T, 0, g->kept, g->trunc, s, g->hdr + 1, status);
+  launch_sort_truncate(g->sorted, g->res, g->seg, (uint32_t)T, 0, g->kept, g->trunc, e->num_sms, s, g->hdr + 1,
+                       status);
   launch_scan(g->kept, T, g->hit_off, g->part, s);
   launch_expand_hits(g->sorted, g->seg, g->hit_off, g->kept, (uint32_t)T, g->hits, g->rows, s, status);
   launch_scan(g->rows, g->res_cap, g->loc_off, g->part, s);
