@@ -309,6 +309,16 @@ int bwt_gpu_direction_split(bwt_index_t* index) {
   return e ? engine_dir_split(e) : -1;
 }
 
+void bwt_gpu_set_locate_limit(bwt_index_t* index, uint64_t max_rows) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_locate_limit(e, max_rows);
+}
+
+uint64_t bwt_gpu_locate_limit(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_locate_limit(e) : 0;
+}
+
 int bwt_gpu_set_start_table(bwt_index_t* index, int symbols) {
   Engine* e = engine_of(index);
   if (!e) return fail("bwt_gpu_set_start_table: null index");

@@ -383,6 +383,8 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
                      ptr<uint32_t>(e->rs_count), (uint32_t)T, ptr<hpg_hit_t>(e->hits), ptr<uint32_t>(e->rows), s);
   uint64_t l_tot = 0;
   if (!e->skip_locate) {
+    launch_limit_rows(ptr<uint64_t>(e->hit_off), ptr<uint32_t>(e->rows), (uint32_t)T, e->locate_limit, nullptr,
+                      ptr<uint8_t>(e->rs_trunc), s);
     launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
     HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");
   }
@@ -437,6 +439,8 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
 
 void engine_set_dir_split(Engine* e, int mode) { e->tuning.dir_split = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
 int engine_dir_split(Engine* e) { return e->tuning.dir_split; }
+void engine_set_locate_limit(Engine* e, uint64_t max_rows) { e->locate_limit = max_rows; }
+uint64_t engine_locate_limit(Engine* e) { return e->locate_limit; }
 
 void engine_set_load_mode(Engine* e, int mode) { e->X.load_mode = (uint32_t)(mode < 0 ? 0 : (mode > 3 ? 3 : mode)); }
 int engine_load_mode(Engine* e) { return (int)e->X.load_mode; }
@@ -771,6 +775,8 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
       return -1;
     }
     launch_hit_rows(hits, (uint32_t)h_tot, ptr<uint32_t>(e->rows), s);
+    launch_limit_rows(ptr<uint64_t>(e->hit_off), ptr<uint32_t>(e->rows), (uint32_t)T, e->locate_limit, nullptr,
+                      ptr<uint8_t>(e->rs_trunc) + 2 * r0, s);
     launch_scan(ptr<uint32_t>(e->rows), h_tot, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
     uint64_t l_tot = 0;
     HPG_CUDA(cudaMemcpyAsync(&l_tot, ptr<uint64_t>(e->loc_off) + h_tot, 8, cudaMemcpyDeviceToHost, s), "loc count");

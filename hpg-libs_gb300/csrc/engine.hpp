@@ -68,6 +68,8 @@ void engine_set_load_mode(Engine* e, int mode);
 // launch per direction.
 void engine_set_dir_split(Engine* e, int mode);
 int engine_dir_split(Engine* e);
+void engine_set_locate_limit(Engine* e, uint64_t max_rows);
+uint64_t engine_locate_limit(Engine* e);
 // Batched form from the captured CUDA graph (1, the default) or launched
 // stage by stage with host-read sizes (0).
 void engine_set_graph(Engine* e, int on);

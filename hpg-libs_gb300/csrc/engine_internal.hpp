@@ -47,7 +47,7 @@ struct GraphPlan {
   // device buffers
   uint8_t* seqs = nullptr;
   uint64_t* offs = nullptr;
-  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results
+  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results, [2..3] locate limit (u64)
   uint8_t* codes = nullptr;
   uint8_t* ok = nullptr;
   unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
@@ -120,6 +120,7 @@ struct Engine {
   size_t pipe_chunk = 0;  // reads per pipelined chunk: 0 automatic, SIZE_MAX never pipelined
   bool use_graph = true;
   bool skip_locate = false;  // batched form: hits only, no located rows
+  uint64_t locate_limit = 0;  // rows per (read, strand) list beyond which the list is not located; 0 = none
 };
 
 // Grow-only device buffer; `keep` preserves the old contents.

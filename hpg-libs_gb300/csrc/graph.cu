@@ -170,6 +170,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
                        status);
   launch_scan(g->kept, T, g->hit_off, g->part, s);
   launch_expand_hits(g->sorted, g->seg, g->hit_off, g->kept, (uint32_t)T, g->hits, g->rows, s, status);
+  launch_limit_rows(g->hit_off, g->rows, (uint32_t)T, 0, reinterpret_cast<const uint64_t*>(g->hdr + 2), g->trunc, s,
+                    status);
   launch_scan(g->rows, g->res_cap, g->loc_off, g->part, s);
   record(g->ev[4], s);
 
@@ -294,7 +296,9 @@ int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std:
   cudaStream_t s = e->stream;
   g->h_hdr[0] = n;
   g->h_hdr[1] = max_results;
-  HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 8, cudaMemcpyHostToDevice, s), "batch header");
+  const uint64_t limit = e->skip_locate ? 0 : e->locate_limit;  // hits-only calls locate nothing anyway
+  std::memcpy(g->h_hdr + 2, &limit, 8);
+  HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 16, cudaMemcpyHostToDevice, s), "batch header");
   HPG_CUDA(cudaGraphLaunch(g->exec, s), "graph launch");
   count_launches((unsigned)g->kernels);
   return 0;

@@ -299,6 +299,22 @@ __global__ void hit_rows_kernel(const hpg_hit_t* __restrict__ hits, uint32_t n, 
   rows[i] = k <= l ? (uint32_t)(l - k + 1) : 0u;
 }
 
+__global__ void limit_rows_kernel(const uint64_t* __restrict__ list_off, uint32_t* __restrict__ rows,
+                                  uint32_t n_lists, uint64_t limit, const uint64_t* limit_dev,
+                                  uint8_t* __restrict__ trunc, const unsigned* gate) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_lists) return;
+  if (gate && *gate) return;
+  if (limit_dev) limit = *limit_dev;
+  if (limit == 0) return;
+  const uint64_t b = list_off[t], e = list_off[t + 1];
+  uint64_t sum = 0;
+  for (uint64_t h = b; h < e; ++h) sum += rows[h];
+  if (sum <= limit) return;
+  for (uint64_t h = b; h < e; ++h) rows[h] = 0;
+  trunc[t] |= 2;
+}
+
 // ---------------------------------------------------------------- locate --
 
 __global__ void __launch_bounds__(kTpb)
@@ -460,6 +476,13 @@ void launch_hit_rows(const hpg_hit_t* hits, uint32_t n_hits, uint32_t* rows, cud
   if (!n_hits) return;
   count_launches(1);
   hit_rows_kernel<<<grid_for(n_hits, 256), 256, 0, s>>>(hits, n_hits, rows);
+}
+
+void launch_limit_rows(const uint64_t* list_off, uint32_t* rows, uint32_t n_lists, uint64_t limit,
+                       const uint64_t* limit_dev, uint8_t* trunc, cudaStream_t s, const unsigned* gate) {
+  if (!n_lists || (!limit_dev && limit == 0)) return;
+  count_launches(1);
+  limit_rows_kernel<<<grid_for(n_lists, 256), 256, 0, s>>>(list_off, rows, n_lists, limit, limit_dev, trunc, gate);
 }
 
 void launch_locate(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,

@@ -62,6 +62,12 @@ void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t*
 // Rows per hit (l - k + 1 or 0).
 void launch_hit_rows(const hpg_hit_t* hits, uint32_t n_hits, uint32_t* rows, cudaStream_t s);
 
+// Locate limit: a list (read, strand) whose hits list_off[t]..list_off[t+1]
+// cover more than `limit` rows (read from limit_dev when given; 0 = no limit)
+// has its rows set to 0, so nothing of it is located, and trunc[t] |= 2.
+void launch_limit_rows(const uint64_t* list_off, uint32_t* rows, uint32_t n_lists, uint64_t limit,
+                       const uint64_t* limit_dev, uint8_t* trunc, cudaStream_t s, const unsigned* gate = nullptr);
+
 // Locate every row of every hit (bwt.c:2158-2166); hit ids are offset by hit_base.
 void launch_locate(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,
                    uint64_t n_locs, const uint64_t* read_offs, uint32_t hit_base, hpg_loc_t* out,

@@ -107,6 +107,9 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_direction_split.argtypes = [vp]
+    lib.bwt_gpu_set_locate_limit.argtypes = [vp, u64]
+    lib.bwt_gpu_locate_limit.argtypes = [vp]
+    lib.bwt_gpu_locate_limit.restype = u64
     lib.bwt_gpu_start_table.argtypes = [vp]
     lib.bwt_gpu_autotune.argtypes = [vp, vp, vp, sz, u64, u32, u32, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
                                      ctypes.POINTER(ctypes.c_int)]
@@ -259,6 +262,13 @@ class GpuIndex:
 
     def direction_split(self) -> int:
         return int(self.lib.bwt_gpu_direction_split(self.handle))
+
+    def set_locate_limit(self, max_rows: int) -> None:
+        """Lists (read, strand) covering more than max_rows rows are not located (rs_truncated bit 1); 0 = none."""
+        self.lib.bwt_gpu_set_locate_limit(self.handle, int(max_rows))
+
+    def locate_limit(self) -> int:
+        return int(self.lib.bwt_gpu_locate_limit(self.handle))
 
     def set_start_table(self, symbols: int) -> None:
         """Start-table length of the batched search (0 = none)."""

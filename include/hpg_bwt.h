@@ -196,6 +196,16 @@ void bwt_gpu_set_pipeline_chunk(bwt_index_t *index, size_t reads);
  * direction's occurrence blocks at a time.  Results are identical. */
 void bwt_gpu_set_direction_split(bwt_index_t *index, int mode);
 int bwt_gpu_direction_split(bwt_index_t *index);
+/* Locate limit of bwt_gpu_search_batch / _device and the serving form (no
+ * counterpart in the reference's search layer, which locates every row; its
+ * bwt_map_inexact_read drops repetitive strands with filter_read_mappings,
+ * bwt.c:2148-2149, for the same reason).  A (read, strand) list whose kept
+ * hits cover more than max_rows suffix-array rows keeps its hits but gets no
+ * located rows, and bit 1 (value 2) of its rs_truncated entry is set.  Low-
+ * complexity reads (a 50 bp read inside a homopolymer run of a 3 Gbp genome)
+ * cover millions of rows each.  0, the default, locates every row. */
+void bwt_gpu_set_locate_limit(bwt_index_t *index, uint64_t max_rows);
+uint64_t bwt_gpu_locate_limit(bwt_index_t *index);
 /* Start table of the batched search (fused form): a chain of a read of at
  * least 2L+2 bases starts with one lookup of its first L symbols in a table of
  * 4^L intervals per index direction (8 MB each at L = 10) instead of L

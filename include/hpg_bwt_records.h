@@ -72,7 +72,8 @@ typedef struct {
   size_t n_locs;
   hpg_loc_t *locs;
   uint32_t *rs_count;    /* [2*n_reads] hits kept per (read, strand) */
-  uint8_t *rs_truncated; /* [2*n_reads] 1 when the helper overflowed max_results */
+  uint8_t *rs_truncated; /* [2*n_reads] bit 0: the helper overflowed max_results;
+                          bit 1: rows not located (over the locate limit) */
 } hpg_result_set_t;
 
 #ifdef __cplusplus

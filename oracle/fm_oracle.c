@@ -507,8 +507,19 @@ static void locate(const fmo_index_t *ix, sink_t *s, uint32_t hid, int64_t k, in
 
 /* ------------------------------------------------------------ per read -- */
 
+/* Rows of a list's kept hits, and whether a locate limit leaves them unlocated
+ * (the product's bwt_gpu_set_locate_limit: lists over the limit keep their hits,
+ * get no located rows and bit 1 of their truncation flag). */
+static int over_limit(const hpg_hit_t *h, uint32_t n, uint64_t limit) {
+  if (!limit) return 0;
+  uint64_t rows = 0;
+  for (uint32_t t = 0; t < n; t++)
+    if (h[t].k <= h[t].l) rows += (uint64_t)(h[t].l - h[t].k + 1);
+  return rows > limit;
+}
+
 static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *seq, size_t len, uint32_t max_results,
-                     sink_t *s, hpg_hit_t *lbuf, uint8_t *code, int64_t *vecs, uint32_t *rs_count,
+                     uint64_t limit, sink_t *s, hpg_hit_t *lbuf, uint8_t *code, int64_t *vecs, uint32_t *rs_count,
                      uint8_t *rs_trunc) {
   if (len < 3 || len > 32767) return;
   for (size_t i = 0; i < len; i++) {
@@ -532,6 +543,10 @@ static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *s
         uint32_t hid = (uint32_t)s->n_hits;
         sink_hit(s, &h);
         rs_count[2 * (size_t)rd + !type] = 1;
+        if (over_limit(&h, 1, limit)) {
+          rs_trunc[2 * (size_t)rd + !type] |= 2;
+          continue;
+        }
         locate(ix, s, hid, c.k, c.l, type ? 0 : 1, len);
       }
     }
@@ -548,12 +563,14 @@ static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *s
     list_t L = {lbuf, 0, max_results, rd, (uint8_t)!type};
     int over = type ? search1_helper(code, start, end, k1, l1, ki1, li1, &ix->bw, &ix->fw, &L)
                     : search1_helper(code, start, end, ki0, li0, k0, l0, &ix->fw_rev, &ix->bw_rev, &L);
-    rs_trunc[2 * (size_t)rd + !type] = (uint8_t)over;
+    const int skip = over_limit(lbuf, L.n, limit);
+    rs_trunc[2 * (size_t)rd + !type] = (uint8_t)(over | (skip ? 2 : 0));
     rs_count[2 * (size_t)rd + !type] = L.n;
     for (uint32_t t = 0; t < L.n; t++) {
       const hpg_hit_t *h = &lbuf[t];
       uint32_t hid = (uint32_t)s->n_hits;
       sink_hit(s, h);
+      if (skip) continue;
       uint8_t err = h->nm ? h->err_kind : 0;
       int direction = type ? h->dir : !h->dir;
       uint64_t len_calc = len;
@@ -566,8 +583,8 @@ static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *s
 
 /* Batch driver: reads are split into chunks processed by `threads` OpenMP
  * threads (dynamic schedule, as bwt.c:1134), then merged in read order. */
-int fmo_search(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
-               uint32_t max_results, int threads, hpg_result_set_t *out) {
+int fmo_search_limit(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                     uint32_t max_results, uint64_t locate_limit, int threads, hpg_result_set_t *out) {
   memset(out, 0, sizeof *out);
   out->n_reads = n_reads;
   out->rs_count = (uint32_t *)calloc(2 * n_reads + 1, sizeof(uint32_t));
@@ -591,7 +608,7 @@ int fmo_search(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t
       size_t r0 = ch * 256, r1 = r0 + 256 < n_reads ? r0 + 256 : n_reads;
       for (size_t r = r0; r < r1; r++)
         one_read(ix, mode, (uint32_t)r, seqs + offsets[r], (size_t)(offsets[r + 1] - offsets[r]), max_results,
-                 &sinks[ch],
+                 locate_limit, &sinks[ch],
                  lbuf, code, vecs, out->rs_count, out->rs_truncated);
     }
     free(lbuf);
@@ -622,6 +639,11 @@ int fmo_search(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t
   out->n_hits = nh;
   out->n_locs = nl;
   return 0;
+}
+
+int fmo_search(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
+               uint32_t max_results, int threads, hpg_result_set_t *out) {
+  return fmo_search_limit(ix, mode, seqs, offsets, n_reads, max_results, 0, threads, out);
 }
 
 void fmo_result_free(hpg_result_set_t *out) {

@@ -34,6 +34,9 @@ class PortOracle:
         self.lib.fmo_index_free.argtypes = [ctypes.c_void_p]
         self.lib.fmo_search.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_size_t, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(ResultSetC)]
+        self.lib.fmo_search_limit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                              ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
+                                              ctypes.POINTER(ResultSetC)]
         self.lib.fmo_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
         self.lib.fmo_max_threads.restype = ctypes.c_int
         self.h = self.lib.fmo_index_load(index_dir.encode())
@@ -43,13 +46,14 @@ class PortOracle:
     def max_threads(self) -> int:
         return int(self.lib.fmo_max_threads())
 
-    def search(self, reads, mode: int = 1, max_results: int = 1 << 16, threads: int = 1) -> Result:
+    def search(self, reads, mode: int = 1, max_results: int = 1 << 16, threads: int = 1,
+               locate_limit: int = 0) -> Result:
         seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
         offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
         n = len(offs) - 1
         rs = ResultSetC()
-        self.lib.fmo_search(self.h, mode, seq.ctypes.data, offs.ctypes.data, n, max_results, threads,
-                            ctypes.byref(rs))
+        self.lib.fmo_search_limit(self.h, mode, seq.ctypes.data, offs.ctypes.data, n, max_results, locate_limit,
+                                  threads, ctypes.byref(rs))
         try:
             return result_from_c(rs, n)
         finally:

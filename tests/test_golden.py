@@ -53,3 +53,24 @@ def test_golden_cases_exercise_edges():
             seen_quirk |= bool(((e.hits["err_kind"] == 3) & (e.hits["err_base"] == 3) & (e.hits["dir"] == 0)).any())
             seen_multi |= bool(((e.hits["l"] - e.hits["k"]) > 0).any())
     assert seen_trunc and seen_invalid and seen_quirk and seen_multi
+
+
+def test_oracle_locate_limit(tmp_path):
+    """The oracle's locate limit: hits, counts and overflow bits unchanged; lists
+    whose kept hits cover more rows than the limit lose exactly their located rows
+    and get truncation bit 1."""
+    from low_complexity import low_complexity_case
+    index, reads = low_complexity_case(tmp_path)
+    ora = PortOracle(index)
+    full = ora.search(reads, mode=1, max_results=100, threads=4)
+    lim = ora.search(reads, mode=1, max_results=100, threads=4, locate_limit=5000)
+    assert np.array_equal(full.hits, lim.hits) and np.array_equal(full.rs_count, lim.rs_count)
+    assert np.array_equal(full.rs_truncated, lim.rs_truncated & 1)
+    sz = np.maximum(full.hits["l"] - full.hits["k"] + 1, 0).astype(np.int64)
+    lst = 2 * full.hits["read"].astype(np.int64) + full.hits["strand"]
+    rows = np.bincount(lst, weights=sz, minlength=2 * len(reads.offsets) - 2)
+    over = rows > 5000
+    assert over.any() and not over.all()
+    assert np.array_equal((lim.rs_truncated & 2) != 0, over)
+    keep = ~over[lst[full.locs["hit"]]]
+    assert np.array_equal(lim.locs, full.locs[keep])

@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 from hpgbwt import lib, synth
+from low_complexity import low_complexity_case
 from oracle.pyoracle import PortOracle
 
 pytestmark = pytest.mark.gpu
@@ -174,35 +175,12 @@ def test_direction_split_agrees(case_factory, split, stack, minb):
         _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
 
 
-def _low_complexity_case(tmp):
-    """300 kbp i.i.d. genome with a 1.5 kbp G run, 100 scattered 170 bp G runs and
-    (AC)/(AGT) tandem runs: reads drawn from them hit thousands of rows per interval
-    and fill the result list (indel variants of one homopolymer interval)."""
-    rng = np.random.default_rng(5)
-    g = rng.integers(0, 4, size=300_000, dtype=np.uint8)
-    g[10_000:11_500] = 2
-    g[50_000:52_000] = np.resize(np.array([0, 1], dtype=np.uint8), 2000)
-    g[90_000:91_800] = np.resize(np.array([0, 2, 3], dtype=np.uint8), 1800)
-    for s in rng.integers(100_000, 290_000, size=100):
-        g[s:s + 170] = 2
-    fasta = str(tmp / "genome.fa")
-    synth.write_fasta(fasta, g, [150_000, 150_000])
-    index = str(tmp / "index")
-    lib.build_index(fasta, index, 16)
-    seqs = [b"G" * 150, b"C" * 150, b"G" * 120, b"G" * 149 + b"A", b"T" + b"G" * 99, b"AC" * 75, b"CA" * 60,
-            b"AGT" * 50, b"ACT" * 40, b"G" * 60 + b"T" + b"G" * 60]
-    A = np.frombuffer(b"ACGT", dtype=np.uint8)
-    for s in rng.integers(0, 299_800, size=100):
-        seqs.append(A[g[s:s + 120]].tobytes())
-    return index, synth.from_strings(seqs)
-
-
 @pytest.mark.parametrize("form", [lib.FORM_PLAIN, lib.FORM_BATCHED])
 @pytest.mark.parametrize("max_results", [100, 1024])
 def test_large_intervals_match_oracle(tmp_path_factory, form, max_results):
     """Every row of every hit is located when intervals hold thousands of rows and
     the hit lists are cut at max_results (low-complexity reads)."""
-    index, reads = _low_complexity_case(tmp_path_factory.mktemp(f"lowcx_{form}_{max_results}"))
+    index, reads = low_complexity_case(tmp_path_factory.mktemp(f"lowcx_{form}_{max_results}"))
     ora = PortOracle(index)
     with lib.GpuIndex(index) as g:
         got = g.search(reads, mode=lib.MODE_SEARCH1, form=form, max_results=max_results)
@@ -211,3 +189,22 @@ def test_large_intervals_match_oracle(tmp_path_factory, form, max_results):
     assert sz.max() > 1000 and len(want.locs) == int(sz.sum())
     assert want.rs_truncated.any() or max_results > 100
     _assert_same(got, want)
+
+
+@pytest.mark.parametrize("form,graph", [(lib.FORM_PLAIN, True), (lib.FORM_BATCHED, True), (lib.FORM_BATCHED, False)])
+def test_locate_limit_matches_oracle(tmp_path_factory, form, graph):
+    """With a locate limit, lists covering more rows keep their hits, lose their
+    located rows and carry truncation bit 1, exactly as the oracle's limit."""
+    index, reads = low_complexity_case(tmp_path_factory.mktemp(f"lowcx_limit_{form}_{graph}"))
+    ora = PortOracle(index)
+    with lib.GpuIndex(index) as g:
+        g.set_graph(graph)
+        g.set_locate_limit(5000)
+        assert g.locate_limit() == 5000
+        got = g.search(reads, mode=lib.MODE_SEARCH1, form=form, max_results=100)
+        g.set_locate_limit(0)
+        again = g.search(reads, mode=lib.MODE_SEARCH1, form=form, max_results=100)
+    want = ora.search(reads, mode=lib.MODE_SEARCH1, max_results=100, threads=8, locate_limit=5000)
+    assert (want.rs_truncated & 2).any() and len(want.locs) > 0
+    _assert_same(got, want)
+    _assert_same(again, ora.search(reads, mode=lib.MODE_SEARCH1, max_results=100, threads=8))

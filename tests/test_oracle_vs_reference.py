@@ -46,3 +46,4 @@ def test_builder_equals_reference_builder_at_other_ratios(tmp_path, ratio):
     for p in sorted((tmp_path / "ref").iterdir()):
         q = tmp_path / "mine" / p.name
         assert hashlib.sha256(p.read_bytes()).digest() == hashlib.sha256(q.read_bytes()).digest(), p.name
+
