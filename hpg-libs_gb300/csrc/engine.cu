@@ -189,6 +189,7 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
     en->X.C[b] = h.C[b];
     en->X.C1[b] = h.C1[b];
     en->X.comp[b] = a.comp[b];
+    en->X.comp_packed |= (a.comp[b] & 3u) << (2 * b);
   }
   en->X.ratio = h.S.ratio;
   en->X.ratio_shift = 0xFFFFFFFFu;

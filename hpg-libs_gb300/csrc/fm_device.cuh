@@ -44,6 +44,7 @@ struct DevIndex {
   DevDir dir[2];
   uint32_t C[4], C1[4];   // C counts symbols < b without '$'; C1 = C + 1
   uint32_t comp[4];       // complement of each code
+  uint32_t comp_packed;   // the same, 2 bits per code: comp[b] = (comp_packed >> 2b) & 3
   uint32_t ratio;         // SA sampling ratio
   uint32_t ratio_shift;   // log2(ratio) when ratio is a power of two, else 0xFFFFFFFF
   uint32_t walk_mod;      // O.siz - 1 = n + 1: modulus of the SA walk (csafm.h:233)
@@ -166,32 +167,45 @@ __device__ __forceinline__ DevDir dir_of(const DevIndex& X, uint32_t d) {
   return D;
 }
 
+// The first r rows of a block (r in 0..64) as a bit mask.  PTX clamps a
+// shift amount above the width to the width, so r = 64 gives all ones.
+__device__ __forceinline__ uint64_t row_mask(uint32_t r) {
+  uint64_t m;
+  asm("shl.b64 %0, %1, %2;" : "=l"(m) : "l"(1ull), "r"(r));
+  return m - 1ull;
+}
+
 // BWiteration (search/runtime.h:38-42) over a view, on 32-bit interval ends.
 // k in [0, n+1], l in [0, n] always hold for the intervals the search forms.
 // When k and l share a block (the common case once an interval is small)
-// one 32-byte sector serves both ranks.
+// one 32-byte sector serves both ranks.  The '$' row (stored as code 0) is
+// taken out only for symbol 0 in the one block that holds it.
 __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, uint32_t& k, uint32_t& l) {
-  const uint32_t p = v.comp ? sel4(X.comp, b) : b;
-  const DevDir D = dir_of(X, v.d);
+  const uint32_t p = v.comp ? ((X.comp_packed >> (2u * b)) & 3u) : b;
+  const OccBlock* occ = v.d ? X.dir[1].occ : X.dir[0].occ;
   const uint32_t q0 = k >> 6, q1 = l >> 6;
-  const bool a0 = (p == 0) && (q0 == (D.dollar >> 6));  // '$' block correction applies
   uint32_t cnt[4];
   uint4 bits;
-  load_block_m(D.occ + q0, X.load_mode, cnt, bits);
+  load_block_m(occ + q0, X.load_mode, cnt, bits);
   uint64_t m = match_mask(bits, p);
   const uint32_t c0 = sel4(cnt, p);
-  const uint32_t rk = c0 + (uint32_t)__popcll(m & prefix_mask(k & 63)) - ((a0 && k > D.dollar) ? 1u : 0u);
+  uint32_t rk = c0 + (uint32_t)__popcll(m & row_mask(k & 63));
   uint32_t rl;
   if (q1 == q0) {
-    rl = c0 + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a0 && l >= D.dollar) ? 1u : 0u);
+    rl = c0 + (uint32_t)__popcll(m & row_mask((l & 63) + 1));
   } else {
-    load_block_m(D.occ + q1, X.load_mode, cnt, bits);
+    load_block_m(occ + q1, X.load_mode, cnt, bits);
     m = match_mask(bits, p);
-    const bool a1 = (p == 0) && (q1 == (D.dollar >> 6));
-    rl = sel4(cnt, p) + (uint32_t)__popcll(m & prefix_mask((l & 63) + 1)) - ((a1 && l >= D.dollar) ? 1u : 0u);
+    rl = sel4(cnt, p) + (uint32_t)__popcll(m & row_mask((l & 63) + 1));
   }
-  k = sel4(X.C1, p) + rk;
-  l = sel4(X.C, p) + rl;
+  if (p == 0) {
+    const uint32_t dollar = v.d ? X.dir[1].dollar : X.dir[0].dollar;
+    if (k > dollar && q0 == (dollar >> 6)) rk -= 1;
+    if (l >= dollar && q1 == (dollar >> 6)) rl -= 1;
+  }
+  const uint32_t c = sel4(X.C, p);  // C1 = C + 1 (checked when the index is loaded)
+  k = c + 1u + rk;
+  l = c + rl;
 }
 
 // LF of row i on a physical direction: row 0 for the '$' row, else
