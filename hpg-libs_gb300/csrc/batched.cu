@@ -117,15 +117,19 @@ __device__ __forceinline__ uint32_t make_meta(uint32_t j, uint32_t type, uint32_
 template <int D, int MINB, bool CENSUS>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
-  const uint32_t n_reads_ = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
   __shared__ uint32_t stk_k[D][kBlock], stk_l[D][kBlock], stk_j[D][kBlock];
   __shared__ uint32_t c_ek[kBlock], c_el[kBlock], c_meta[kBlock], c_misc[kBlock], c_res[kBlock], c_part[kBlock];
+  __shared__ uint32_t c_read[kBlock];  // read whose chains this lane runs
+  __shared__ uint32_t s_nreads, s_spill_end;
   const int tid = threadIdx.x;
-  const uint32_t n_chains = 4u * n_reads_;
-  const uint32_t spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
+  if (tid == 0) {
+    s_nreads = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
+    s_spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
+  }
   c_meta[tid] = 0;
-  c_misc[tid] = 0;
+  c_misc[tid] = 4u << 4;  // no chain of a read left
   c_res[tid] = 0;
+  __syncthreads();
 
   // hot state
   uint32_t rs = 0;                  // 2 * read + strand
@@ -153,27 +157,21 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
                                              : (p.dir_split == 2 ? 0u : (p.dir_split == 3 ? 1u : 2u));
     c_part[tid] = part0 | (part0 << 3) | (part0 << 5);
   }
-  uint32_t cur_read = 0, chain = 4;
+  // The claim state (read, chain of the read, chain set) lives in shared
+  // memory: a lane touches it once per chain, and the registers it frees let
+  // more blocks stay resident.  A read's offsets are loaded when it is claimed.
   auto next_claim = [&]() -> uint32_t {
     uint32_t st = c_part[tid];
     for (;;) {
       const uint32_t part = st & 3u;
       const uint32_t r = claim_part(p, part);
-      if (r < n_reads_ || part == 2u || (st & 4u) || p.dir_split != 1) {
-        c_part[tid] = (st & ~(3u << 5)) | (part << 5);
+      if (r < s_nreads || part == 2u || (st & 4u) || p.dir_split != 1) {
+        c_part[tid] = (st & ~(3u << 3)) | (part << 3);
         return r;
       }
       st = (st & ~3u) | (part ^ 1u) | 4u;
     }
   };
-  uint32_t nxt_read = drain ? 0xFFFFFFFFu : next_claim();
-  uint64_t nxt_b0 = 0, nxt_b1 = 0;
-  uint32_t nxt_ok = 0;
-  if (nxt_read < n_reads_) {
-    nxt_b0 = p.offs[nxt_read];
-    nxt_b1 = p.offs[nxt_read + 1];
-    nxt_ok = p.ok[nxt_read];
-  }
   (void)chunk;
 
   auto push = [&](uint32_t a, uint32_t b, uint32_t jt) {
@@ -287,7 +285,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       }
       if (drain) {
         const unsigned s = claim(p.spill_head, 1);
-        if (s >= spill_end) break;
+        if (s >= s_spill_end) break;
         const SpillEntry e = p.spill[s];
         if (e.rs == 0xFFFFFFFFu) continue;  // reserved but unused slot
         rs = e.rs;
@@ -300,32 +298,21 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         c_meta[tid] = make_meta(e.jtype & 0xFFFFu, e.jtype >> 16, 0, 0, true);
         continue;
       }
-      if (chain >= ((((c_part[tid] >> 3) & 3u) == 2u) ? 4u : 2u)) {
-        // next read: switch to the prefetched one, prefetch the one after
-        if (nxt_read >= n_reads_) break;
-        cur_read = nxt_read;
-        {
-          const uint32_t st = c_part[tid];
-          c_part[tid] = (st & ~(3u << 3)) | (((st >> 5) & 3u) << 3);
-        }
-        const uint64_t b0 = nxt_b0;
-        const int L = (int)(nxt_b1 - nxt_b0);
-        const uint32_t okr = nxt_ok;
-        nxt_read = next_claim();
-        if (nxt_read < n_reads_) {
-          nxt_b0 = p.offs[nxt_read];
-          nxt_b1 = p.offs[nxt_read + 1];
-          nxt_ok = p.ok[nxt_read];
-        }
-        if (!okr || L < 3 || L > 32767) {
-          chain = 4;  // no chains for this read
-          continue;
-        }
+      uint32_t chain = (misc >> 4) & 7u;
+      if (chain >= ((((c_part[tid] >> 3) & 3u) == 2u) ? 4u : 2u)) {  // next read
+        const uint32_t r = next_claim();
+        if (r >= s_nreads) break;
+        c_read[tid] = r;
+        const uint64_t b0 = p.offs[r];
+        const int L = (int)(p.offs[r + 1] - b0);
+        if (!p.ok[r] || L < 3 || L > 32767) continue;  // no chains for this read (chain stays at its end)
         W = p.codes + b0;
         len = L;
         chain = 0;
       }
-      const uint32_t ci = chain++;
+      c_misc[tid] = (misc & 15u) | ((chain + 1) << 4);
+      const uint32_t ci = chain;
+      const uint32_t cur_read = c_read[tid];
       const uint32_t cur_part = (c_part[tid] >> 3) & 3u;
       // 0: '+' backward, 1: '+' forward, 2: '-' backward, 3: '-' forward
       const uint32_t c = cur_part == 2u ? ci : (cur_part == 0u ? (ci ? 3u : 0u) : (ci ? 2u : 1u));
