@@ -6,7 +6,9 @@
 // including this library's own, to libhpg's definitions); only a process
 // without hpg-libs (tests, ctypes callers) runs these.  Layout and behaviour
 // follow c/src/containers/array_list.{h,c} (array_list_t, growth by the
-// realloc factor, the flag word, an optional lock) and
+// realloc factor, the flag word, an optional lock),
+// c/src/containers/linked_list.{h,c} (linked_list_t: doubly linked items,
+// insert = at the head, insert_last = at the tail) and
 // c/src/bioformats/bam/alignment.c:7-10,253-264 (zeroed allocation, free of
 // the owned strings).
 #include <pthread.h>
@@ -120,6 +122,82 @@ void alignment_free(alignment_t* a) {
   std::free(a->cigar);
   std::free(a->optional_fields);
   std::free(a);
+}
+
+linked_list_t* linked_list_new(int SYNC_MODE) {
+  linked_list_t* l = static_cast<linked_list_t*>(std::calloc(1, sizeof(linked_list_t)));
+  if (!l) return nullptr;
+  l->mode = SYNC_MODE;
+  if (SYNC_MODE == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_init(&l->lock, nullptr);
+  return l;
+}
+
+void linked_list_free(linked_list_t* l, void (*data_callback)(void*)) {
+  if (!l) return;
+  for (linked_list_item_t* it = l->first; it;) {
+    linked_list_item_t* next = it->next;
+    if (data_callback && it->item) data_callback(it->item);
+    std::free(it);
+    it = next;
+  }
+  if (l->mode == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_destroy(&l->lock);
+  std::free(l);
+}
+
+static linked_list_item_t* new_item(void* p) {
+  linked_list_item_t* it = static_cast<linked_list_item_t*>(std::calloc(1, sizeof(linked_list_item_t)));
+  if (it) it->item = p;
+  return it;
+}
+
+int linked_list_insert(void* item_p, linked_list_t* l) {
+  linked_list_item_t* it = new_item(item_p);
+  if (!l || !it) return 0;
+  if (l->mode == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_lock(&l->lock);
+  it->next = l->first;
+  if (l->first) l->first->prev = it;
+  else l->last = it;
+  l->first = it;
+  l->size++;
+  if (l->mode == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_unlock(&l->lock);
+  return 1;
+}
+
+int linked_list_insert_last(void* item_p, linked_list_t* l) {
+  linked_list_item_t* it = new_item(item_p);
+  if (!l || !it) return 0;
+  if (l->mode == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_lock(&l->lock);
+  it->prev = l->last;
+  if (l->last) l->last->next = it;
+  else l->first = it;
+  l->last = it;
+  l->size++;
+  if (l->mode == COLLECTION_MODE_SYNCHRONIZED) pthread_mutex_unlock(&l->lock);
+  return 1;
+}
+
+size_t linked_list_size(linked_list_t* l) { return l ? l->size : 0; }
+
+void* linked_list_get_first(linked_list_t* l) { return l && l->first ? l->first->item : nullptr; }
+
+void* linked_list_get_last(linked_list_t* l) { return l && l->last ? l->last->item : nullptr; }
+
+linked_list_iterator_t* linked_list_iterator_new(linked_list_t* l) {
+  linked_list_iterator_t* it = static_cast<linked_list_iterator_t*>(std::malloc(sizeof(linked_list_iterator_t)));
+  if (!it) return nullptr;
+  it->linked_list_p = l;
+  it->curr_pos = l ? l->first : nullptr;
+  return it;
+}
+
+void linked_list_iterator_free(linked_list_iterator_t* it) { std::free(it); }
+
+void* linked_list_iterator_curr(linked_list_iterator_t* it) { return it && it->curr_pos ? it->curr_pos->item : nullptr; }
+
+void* linked_list_iterator_next(linked_list_iterator_t* it) {
+  if (!it || !it->curr_pos) return nullptr;
+  it->curr_pos = it->curr_pos->next;
+  return it->curr_pos ? it->curr_pos->item : nullptr;
 }
 
 }  // extern "C"

@@ -4,6 +4,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "hpg_bwt_records.h"
@@ -94,9 +95,18 @@ int engine_exact_api(Engine* e, const char* seqs, const uint64_t* offs, size_t n
 // For the listed reads: per chain {good steps, k, l, 0} of the four vector searches.
 int engine_anchor_scan(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* reads, size_t m,
                        uint32_t* out, std::string* err);
+// One lock for the reference-style entry points (alignment lists, seeds,
+// CALs): the engine's stream and workspace serve one call at a time.
+std::mutex& map_api_mutex();
+
 struct MapRow {
   uint32_t row, phys, len_calc;  // SA row, physical index direction (0 backward, 1 forward), located length
 };
+// Seeds: per seed {read, first, last (included), 0}; out per seed {k, l} of the
+// '+' search and {k, l} of the '-' search (k = 1, l = 0 for seeds outside
+// their read or reads outside the alphabet).
+int engine_seed_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* seeds, size_t m,
+                       uint32_t* out, std::string* err);
 int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, std::string* err);
 // Batched form: hits only, no located rows.
 void engine_set_skip_locate(Engine* e, int on);

@@ -23,7 +23,7 @@ using namespace hpgbwt;
 
 namespace {
 
-std::mutex g_mu;  // the engine's stream and workspace serve one call at a time
+std::mutex& g_mu = map_api_mutex();
 
 [[noreturn]] void fatal(const std::string& what) {
   // the reference's fatal path (bwt_commons.h:48-70): report and exit

@@ -73,6 +73,40 @@ __global__ void anchor_scan_kernel(DevIndex X, const uint8_t* __restrict__ codes
   out[t] = o;
 }
 
+// bwt_map_exact_seed (bwt.c:1232-1252): the seed W[first .. last] of a read,
+// '+' BWExactSearchBackward over backward from `last`, '-' BWExactSearchForward
+// over backward_rev (the backward index with complemented symbols) from
+// `first`, both from the full interval; the interval where the search stopped.
+__global__ void seed_search_kernel(DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs,
+                                   const uint8_t* __restrict__ ok, const uint4* __restrict__ seeds, uint32_t m,
+                                   uint4* __restrict__ out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const uint4 sd = seeds[t];
+  const uint64_t b = offs[sd.x];
+  const uint64_t len = offs[sd.x + 1] - b;
+  uint4 o = make_uint4(1, 0, 1, 0);  // nothing to locate
+  if (ok[sd.x] && sd.y <= sd.z && sd.z < len) {
+    const uint8_t* W = codes + b;
+    uint32_t k = 0, l = X.top;
+    for (int64_t i = sd.z; i >= (int64_t)sd.y; --i) {
+      bw_step(X, View{0, 0}, W[i], k, l);
+      if (k > l) break;
+    }
+    o.x = k;
+    o.y = l;
+    k = 0;
+    l = X.top;
+    for (uint32_t i = sd.y; i <= sd.z; ++i) {
+      bw_step(X, View{0, 1}, W[i], k, l);
+      if (k > l) break;
+    }
+    o.z = k;
+    o.w = l;
+  }
+  out[t] = o;
+}
+
 // Reads to the engine's device buffers, encoded (codes + validity flags).
 int upload_reads(Engine* e, const char* seqs, const uint64_t* offs, size_t n, std::string* err) {
   cudaStream_t s = e->stream;
@@ -147,6 +181,36 @@ int engine_anchor_scan(Engine* e, const char* seqs, const uint64_t* offs, size_t
   return 0;
 }
 
+int engine_seed_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* seeds, size_t m,
+                       uint32_t* out, std::string* err) {
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  if (!m) return 0;
+  if (m >= (1ull << 31)) {
+    *err = "too many seeds in one call";
+    return -1;
+  }
+  for (size_t i = 0; i < m; ++i)
+    if (seeds[4 * i] >= n) {
+      *err = "seed of a read outside the batch";
+      return -1;
+    }
+  if (upload_reads(e, seqs, offs, n, err) != 0) return -1;
+  if (!ensure(e, e->slots, 2 * m * sizeof(uint4) + 16)) {
+    *err = "out of device memory (seeds)";
+    return -1;
+  }
+  cudaStream_t s = e->stream;
+  uint4* d_seeds = ptr<uint4>(e->slots);
+  uint4* d_out = d_seeds + m;
+  HPG_CUDA(cudaMemcpyAsync(d_seeds, seeds, m * sizeof(uint4), cudaMemcpyHostToDevice, s), "seeds");
+  count_launches(1);
+  seed_search_kernel<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs),
+                                                                  ptr<uint8_t>(e->ok), d_seeds, (uint32_t)m, d_out);
+  HPG_CUDA(cudaMemcpyAsync(out, d_out, m * sizeof(uint4), cudaMemcpyDeviceToHost, s), "seed intervals");
+  HPG_CUDA(cudaStreamSynchronize(s), "seed search");
+  return 0;
+}
+
 int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, std::string* err) {
   HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
   if (!m) return 0;
@@ -180,6 +244,11 @@ int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, 
 }
 
 void engine_set_skip_locate(Engine* e, int on) { e->skip_locate = on != 0; }
+
+std::mutex& map_api_mutex() {
+  static std::mutex mu;
+  return mu;
+}
 uint32_t engine_sa_top(Engine* e) { return e->X.top; }
 
 }  // namespace hpgbwt

@@ -138,6 +138,167 @@ typedef struct bwt_anchor {
 } bwt_anchor_t;
 #endif
 
+/* ---- hpg-libs linked list (c/src/containers/linked_list.h:35-60) ---- */
+#ifndef LINKED_LIST_H
+#define LINKED_LIST_H
+typedef struct linked_list_item {
+  void *item;
+  struct linked_list_item *prev;
+  struct linked_list_item *next;
+} linked_list_item_t;
+typedef struct linked_list {
+  size_t size;
+  int mode;
+  int flag;
+  int (*compare_fn)(const void *, const void *);
+  pthread_mutex_t lock;
+  pthread_cond_t condition;
+  linked_list_item_t *first;
+  linked_list_item_t *last;
+} linked_list_t;
+linked_list_t *linked_list_new(int SYNC_MODE);
+void linked_list_free(linked_list_t *linked_list_p, void (*data_callback)(void *));
+int linked_list_insert(void *item_p, linked_list_t *linked_list_p);
+int linked_list_insert_last(void *item_p, linked_list_t *linked_list_p);
+size_t linked_list_size(linked_list_t *linked_list_p);
+void *linked_list_get_first(linked_list_t *linked_list_p);
+void *linked_list_get_last(linked_list_t *linked_list_p);
+typedef struct linked_list_iterator {
+  linked_list_t *linked_list_p;
+  linked_list_item_t *curr_pos;
+} linked_list_iterator_t;
+linked_list_iterator_t *linked_list_iterator_new(linked_list_t *linked_list_p);
+void linked_list_iterator_free(linked_list_iterator_t *iterator_p);
+void *linked_list_iterator_curr(linked_list_iterator_t *iterator_p);
+void *linked_list_iterator_next(linked_list_iterator_t *iterator_p);
+#endif
+
+/* ---- seeds and candidate alignment locations (bwt.h:56-66,93-111,123-142,185-198) ---- */
+#ifndef HPG_BWT_CAL_TYPES_DEFINED
+#define HPG_BWT_CAL_TYPES_DEFINED
+typedef struct cal_optarg {
+  size_t min_cal_size;
+  size_t max_cal_distance;
+  size_t num_seeds;
+  size_t min_num_seeds_in_cal;
+  size_t seed_size;
+  size_t min_seed_size;
+  size_t num_errors;
+  size_t max_intron_size;
+  size_t min_intron_size;
+} cal_optarg_t;
+
+typedef struct seed_region {
+  int read_start;
+  int read_end;
+  size_t genome_start;
+  size_t genome_end;
+  int id;
+  int fusion_left;
+  int fusion_right;
+  int strand;
+  int chromosome_id;
+  int num_mismatches;
+  int pos_err;
+  int type_err;
+  array_list_t *errors_list;
+  void *info;
+} seed_region_t;
+
+typedef struct cal {
+  size_t chromosome_id;
+  short int strand;
+  size_t start;
+  size_t end;
+  size_t num_seeds;
+  int read_area;
+  int l_flank;
+  int r_flank;
+  int fill_gaps;
+  int num_targets;
+  int type_seeds;
+  int num_mismatches;
+  linked_list_t *sr_list;
+  linked_list_t *sr_duplicate_list;
+  array_list_t *candidates_seeds_start;
+  array_list_t *candidates_seeds_end;
+  void *info;
+} cal_t;
+
+typedef struct region {
+  size_t chromosome_id;
+  short int strand;
+  size_t start;
+  size_t end;
+  size_t seq_start;
+  size_t seq_end;
+  size_t seq_len;
+  int id;
+  int pos_err;
+  int type_err;
+} region_t;
+#endif
+
+/* bwt.c:128-156, 174-212, 239-249, 282-313, 385-409 */
+cal_optarg_t *cal_optarg_new(const size_t min_cal_size, const size_t max_cal_distance, const size_t num_seeds,
+                             const size_t min_num_seeds_in_cal, const size_t seed_size, const size_t min_seed_size,
+                             const size_t num_errors, const size_t max_intron_size, const size_t min_intron_size);
+void cal_optarg_free(cal_optarg_t *optarg);
+cal_t *cal_new(const size_t chromosome_id, const short int strand, const size_t start, const size_t end,
+               const size_t num_seeds, linked_list_t *sr_list, linked_list_t *sr_duplicate_list);
+void cal_free(cal_t *cal);
+seed_region_t *seed_region_new(int read_start, int read_end, size_t genome_start, size_t genome_end, int id,
+                               int pos_err, int type_err);
+void seed_region_free(seed_region_t *seed_region);
+region_t *region_bwt_new(const size_t chromosome_id, const short int strand, const size_t start, const size_t end,
+                         const size_t seq_start, const size_t seq_end, const size_t seq_len, const int id);
+void region_bwt_free(region_t *region);
+
+/* ---- seeds (bwt.c:1200-1294, 3577-3630) ----
+ * bwt_map_exact_seed: the codes seq[seq_start .. seq_end] (both ends
+ * included) searched exactly on the '+' strand (backward over the backward
+ * index) and the '-' strand (the complemented seed forward over the same
+ * index, i.e. its reverse complement); the '+' rows, then the '-' rows, are
+ * located on the backward suffix array unless the rows counted so far exceed
+ * filter_seed_mappings (a strand over the filter adds nothing, and the count
+ * carries to the next strand).  Every row inside one chromosome becomes a
+ * region_t appended to mapping_list: chromosome 1-based, strand 0 '+' / 1 '-',
+ * genome start 1-based and end = start + (seq_end - seq_start), read span on
+ * the strand searched, seq_len, the seed id.  pos_err and type_err are 0 (the
+ * reference leaves them unset).  Seeds that reach past the read (the reference
+ * reads beyond its buffer there) map nothing.  Returns the regions added.
+ * bwt_map_exact_seeds_seq: the reference's seed plan over an ASCII read (seed
+ * size 16 when <= 10; a 16-base seed at seed_size/2, consecutive seeds, the
+ * last seed_size bases when the length is not a multiple, a 16-base seed
+ * ending seed_size/2 before the end), all seeds in one GPU pass; returns the
+ * list's size.  padding_*, min_seed_size and step_id are ignored, as in the
+ * reference. */
+size_t bwt_map_exact_seed(uint8_t *seq, size_t seq_len, size_t seq_start, size_t seq_end, bwt_optarg_t *bwt_optarg,
+                          bwt_index_t *index, array_list_t *mapping_list, int id);
+size_t bwt_map_exact_seeds_seq(int padding_left, int padding_right, char *seq, size_t seed_size,
+                               size_t min_seed_size, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                               array_list_t *mapping_list, unsigned char step_id);
+
+/* ---- candidate alignment locations (bwt.c:3631-3642, 3832-4031, 4378-4646, 4652-4824) ----
+ * bwt_generate_cals: the seed plan of bwt_map_exact_seeds_seq; each seed's
+ * regions, last first, merged into per-(strand, chromosome) lists of short
+ * CALs within max_cal_distance = the read length (my_cp_list_append_linked_list,
+ * seeds of one id after the first kept in a duplicate list); then, per
+ * chromosome 0..nchromosomes and strand, every short CAL of at least
+ * min_cal_size bases becomes a cal_t appended to cal_list, its seeds merged
+ * by genome position (append_seed_region_linked_list), with the seeds of the
+ * smaller neighbouring CALs within max_intron_size that lie before its first
+ * seed (candidates_seeds_start, id 0) or after its last (candidates_seeds_end,
+ * id 1).  Returns the list's size.
+ * bwt_generate_cals_batch (no reference counterpart): the same for
+ * seqs[0..num_reads) into cal_lists[i], with the seeds of every read in one
+ * GPU pass and the CALs built on the host threads. */
+size_t bwt_generate_cals(char *seq, size_t seed_size, bwt_optarg_t *bwt_optarg, cal_optarg_t *cal_optarg,
+                         bwt_index_t *index, array_list_t *cal_list, unsigned int nchromosomes);
+size_t bwt_generate_cals_batch(char **seqs, size_t num_reads, size_t seed_size, bwt_optarg_t *bwt_optarg,
+                               cal_optarg_t *cal_optarg, bwt_index_t *index, array_list_t **cal_lists,
+                               unsigned int nchromosomes);
+
 /* bwt.h:181-182 */
 bwt_anchor_t *bwt_anchor_new(int strand, int chromosome, size_t start, size_t end, int type);
 void bwt_anchor_free(bwt_anchor_t *bwt_anchor);

@@ -83,6 +83,10 @@ class RefOracle:
                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                          ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
                                          ctypes.POINTER(ctypes.c_size_t)]
+        self.lib.ref_seeds_cals.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
+                                            ctypes.c_size_t, ctypes.c_uint, ctypes.POINTER(ctypes.c_void_p),
+                                            ctypes.POINTER(ctypes.c_size_t)]
         self.lib.ref_blob_free.argtypes = [ctypes.c_void_p]
         self.h = self.lib.ref_index_load(index_dir.encode()) if index_dir else None
 
@@ -108,6 +112,22 @@ class RefOracle:
         self.lib.ref_map_api(self.h, api, fq.seq.ctypes.data, fq.qual.ctypes.data, fq.offs.ctypes.data,
                              fq.ids.ctypes.data, fq.id_offs.ctypes.data, fq.n, filter_read_mappings, flag,
                              ctypes.byref(p), ctypes.byref(n))
+        try:
+            return bytes((ctypes.c_uint8 * n.value).from_address(p.value)) if n.value else b""
+        finally:
+            self.lib.ref_blob_free(p)
+
+    def seeds_cals(self, mode: int, reads: list[bytes], seed_size: int, filter_seed: int, min_cal_size: int,
+                   max_intron: int, nchrom: int) -> bytes:
+        """The reference's bwt_map_exact_seeds_seq (mode 0) or bwt_generate_cals (mode 1) per
+        read, as text (see ref_seeds_cals)."""
+        sys.path.insert(0, str(ROOT / "tests"))
+        from seed_lists import pack
+        buf, offs = pack(reads)
+        p = ctypes.c_void_p()
+        n = ctypes.c_size_t()
+        self.lib.ref_seeds_cals(self.h, mode, buf.ctypes.data, offs.ctypes.data, len(reads), seed_size, filter_seed,
+                                min_cal_size, max_intron, nchrom, ctypes.byref(p), ctypes.byref(n))
         try:
             return bytes((ctypes.c_uint8 * n.value).from_address(p.value)) if n.value else b""
         finally:

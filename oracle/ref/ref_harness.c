@@ -21,6 +21,7 @@
  *                        serialised as described at ref_map_api.
  */
 #include <fcntl.h>
+#include <stdarg.h>
 #include <unistd.h>
 
 #include "bwt.h"
@@ -391,6 +392,75 @@ int ref_map_api(void *vidx, int api, const char *seqs, const char *quals, const 
   }
   quiet_end(q);
   bwt_optarg_free(opt);
+  *out = b.p;
+  *out_len = b.n;
+  return 0;
+}
+
+/* Text lines of the seed and CAL records, the format tests/seed_lists.py
+ * writes for the product's records. */
+static void put_text(blob_t *b, const char *fmt, ...) {
+  char line[256];
+  va_list ap;
+  va_start(ap, fmt);
+  int n = vsnprintf(line, sizeof line, fmt, ap);
+  va_end(ap);
+  if (n > 0) put(b, line, (size_t)n < sizeof line ? (size_t)n : sizeof line - 1);
+}
+
+static void put_seed(blob_t *b, char tag, seed_region_t *s) {
+  put_text(b, "%c %d %d %zu %zu %d\n", tag, s->read_start, s->read_end, s->genome_start, s->genome_end, s->id);
+}
+
+/* ref_seeds_cals: per read (seqs NUL-terminated at offs[i], as ref_map_api),
+ *   mode 0: bwt_map_exact_seeds_seq (bwt.c:3577) into a fresh list:
+ *           "R <returned> <size>" then "G chrom strand start end seq_start seq_end seq_len id" per region;
+ *   mode 1: bwt_generate_cals (bwt.c:3832) into a fresh list:
+ *           "R <returned> <size>" then per CAL "C chrom strand start end num_seeds read_area" followed
+ *           by its seeds: "S ..." (sr_list), "D ..." (sr_duplicate_list), "A ..." / "B ..."
+ *           (candidates_seeds_start / _end), each "read_start read_end genome_start genome_end id".
+ * Fields the reference leaves unset (region pos_err/type_err, the duplicates'
+ * pos_err/type_err, cal flanks) are not written. */
+int ref_seeds_cals(void *vidx, int mode, const char *seqs, const uint64_t *offs, size_t n, size_t seed_size,
+                   int filter_seed, size_t min_cal_size, size_t max_intron, unsigned nchrom, uint8_t **out,
+                   size_t *out_len) {
+  bwt_index_t *index = (bwt_index_t *)vidx;
+  bwt_optarg_t *opt = bwt_optarg_new(1, 1, 200, filter_seed);
+  cal_optarg_t *copt = cal_optarg_new(min_cal_size, 0, 0, 0, seed_size, 0, 0, max_intron, 0);
+  blob_t b = {0};
+  for (size_t i = 0; i < n; i++) {
+    char *seq = (char *)seqs + offs[i];
+    array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_ASYNCHRONIZED);
+    if (mode == 0) {
+      size_t ret = bwt_map_exact_seeds_seq(0, 0, seq, seed_size, 0, opt, index, list, 0);
+      put_text(&b, "R %zu %zu\n", ret, array_list_size(list));
+      for (size_t k = 0; k < array_list_size(list); k++) {
+        region_t *r = (region_t *)array_list_get(k, list);
+        put_text(&b, "G %zu %d %zu %zu %zu %zu %zu %d\n", r->chromosome_id, (int)r->strand, r->start, r->end,
+                 r->seq_start, r->seq_end, r->seq_len, r->id);
+      }
+      array_list_free(list, (void *)region_bwt_free);
+    } else {
+      size_t ret = bwt_generate_cals(seq, seed_size, opt, copt, index, list, nchrom);
+      put_text(&b, "R %zu %zu\n", ret, array_list_size(list));
+      for (size_t k = 0; k < array_list_size(list); k++) {
+        cal_t *c = (cal_t *)array_list_get(k, list);
+        put_text(&b, "C %zu %d %zu %zu %zu %d\n", c->chromosome_id, (int)c->strand, c->start, c->end,
+                 c->num_seeds, c->read_area);
+        for (linked_list_item_t *it = c->sr_list ? c->sr_list->first : NULL; it; it = it->next)
+          put_seed(&b, 'S', (seed_region_t *)it->item);
+        for (linked_list_item_t *it = c->sr_duplicate_list ? c->sr_duplicate_list->first : NULL; it; it = it->next)
+          put_seed(&b, 'D', (seed_region_t *)it->item);
+        for (size_t a = 0; a < array_list_size(c->candidates_seeds_start); a++)
+          put_seed(&b, 'A', (seed_region_t *)array_list_get(a, c->candidates_seeds_start));
+        for (size_t a = 0; a < array_list_size(c->candidates_seeds_end); a++)
+          put_seed(&b, 'B', (seed_region_t *)array_list_get(a, c->candidates_seeds_end));
+      }
+      array_list_free(list, (void *)cal_free);
+    }
+  }
+  bwt_optarg_free(opt);
+  cal_optarg_free(copt);
   *out = b.p;
   *out_len = b.n;
   return 0;

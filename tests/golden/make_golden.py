@@ -41,6 +41,27 @@ API_RUNS = [(api_lists.API_EXACT_READ, 200, 0), (api_lists.API_EXACT_READ, 2, 0)
             (api_lists.API_INEXACT_READ, 0, 1)]
 API_READS = 400  # first reads of each case taken through the entry points
 
+# Seeds and CALs recorded per case (ref_seeds_cals): (mode 0 bwt_map_exact_seeds_seq /
+# 1 bwt_generate_cals, seed_size, filter_seed_mappings, min_cal_size, max_intron_size).
+SEED_RUNS = [(0, 16, 300, 0, 0), (0, 20, 4, 0, 0), (1, 16, 300, 20, 500_000), (1, 20, 40, 30, 1_000),
+             (1, 8, 300, 60, 200)]
+SEED_READS = 300
+
+
+def seed_read_set(seq: np.ndarray, offs: np.ndarray) -> list[bytes]:
+    """Reads the seed entry points are recorded on: upper-case A/C/G/T only and
+    at least 40 bases, so that every seed of the reference's plan lies inside
+    the read (the plan reaches past shorter reads, which the reference then
+    reads beyond their end)."""
+    out = []
+    for i in range(len(offs) - 1):
+        s = seq[offs[i]:offs[i + 1]].tobytes()
+        if len(s) >= 40 and not s.strip(b"ACGT"):
+            out.append(s)
+        if len(out) == SEED_READS:
+            break
+    return out
+
 
 def api_read_set(seq: np.ndarray, offs: np.ndarray) -> list[bytes]:
     """Reads the entry points are recorded on: upper-case A/C/G/T only (other
@@ -54,6 +75,24 @@ def api_read_set(seq: np.ndarray, offs: np.ndarray) -> list[bytes]:
             out.append(s)
         if len(out) == API_READS:
             break
+    return out
+
+
+def spliced_reads(g: np.ndarray, n: int, seed: int) -> list[bytes]:
+    """Reads joined from two pieces of the genome 30-3000 bases apart (either
+    strand), whose seeds fall into two CALs, one often below min_cal_size: they
+    exercise the CAL merges and the candidate seed lists."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        L = int(rng.integers(60, 160))
+        L1 = int(rng.integers(16, L - 16))
+        gap = int(rng.integers(30, 3000))
+        a = int(rng.integers(0, len(g) - L - gap - 1))
+        s = np.concatenate([g[a:a + L1], g[a + L1 + gap:a + gap + L]])
+        if rng.random() < 0.5:
+            s = 3 - s[::-1]
+        out.append(A[s].tobytes())
     return out
 
 CASES = [
@@ -124,6 +163,12 @@ def main() -> int:
             arrays["api_offs"] = np.cumsum([0] + [len(x) for x in fq.seqs]).astype(np.uint64)
             for api, filt, flag in API_RUNS:
                 arrays[f"api{api}_f{filt}_g{flag}"] = np.frombuffer(ro.map_api(api, fq, filt, flag), dtype=np.uint8)
+            sreads = seed_read_set(seq, offs) + spliced_reads(g, 100, seed)
+            arrays["seed_seq"] = np.frombuffer(b"".join(sreads), dtype=np.uint8)
+            arrays["seed_offs"] = np.cumsum([0] + [len(x) for x in sreads]).astype(np.uint64)
+            for mode, ss, filt, minc, intron in SEED_RUNS:
+                arrays[f"seed{mode}_s{ss}_f{filt}_c{minc}_i{intron}"] = np.frombuffer(
+                    ro.seeds_cals(mode, sreads, ss, filt, minc, intron, len(cl)), dtype=np.uint8)
             ro.close()
         np.savez_compressed(HERE / f"{name}.npz", **arrays)
         manifest[name] = {"kind": kind, "length": n, "seed": seed, "chrom_lengths": cl, "sa_ratio": 16,

@@ -54,6 +54,22 @@ class GoldenCase:
         import api_lists
         return api_lists.parse_blob(api, self.arrays[f"api{api}_f{filt}_g{flag}"].tobytes(), n_reads)
 
+    def seed_runs(self):
+        """(mode, seed_size, filter_seed_mappings, min_cal_size, max_intron_size) of the recorded seed/CAL runs."""
+        out = []
+        for k in self.arrays:
+            if k.startswith("seed") and k[4:5].isdigit():
+                m, s, f, c, i = k[4:].split("_")
+                out.append((int(m), int(s[1:]), int(f[1:]), int(c[1:]), int(i[1:])))
+        return sorted(out)
+
+    def seed_reads(self) -> list[bytes]:
+        s, o = self.arrays["seed_seq"], self.arrays["seed_offs"]
+        return [s[o[i]:o[i + 1]].tobytes() for i in range(len(o) - 1)]
+
+    def seed_expected(self, mode: int, seed_size: int, filt: int, min_cal: int, intron: int) -> bytes:
+        return self.arrays[f"seed{mode}_s{seed_size}_f{filt}_c{min_cal}_i{intron}"].tobytes()
+
     def build(self, tmp: Path) -> str:
         fa = tmp / "genome.fa"
         synth.write_fasta(str(fa), self.genome, self.chrom_lengths)

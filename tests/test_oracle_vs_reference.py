@@ -47,3 +47,19 @@ def test_builder_equals_reference_builder_at_other_ratios(tmp_path, ratio):
         q = tmp_path / "mine" / p.name
         assert hashlib.sha256(p.read_bytes()).digest() == hashlib.sha256(q.read_bytes()).digest(), p.name
 
+
+
+def test_seed_fixtures_are_the_reference(tmp_path):
+    """The recorded seed and CAL runs are what the compiled reference writes now."""
+    from golden_cases import GoldenCase
+    gc = GoldenCase("repeats_3chr")
+    index = str(tmp_path / "index")
+    fa = tmp_path / "genome.fa"
+    synth.write_fasta(str(fa), gc.genome, gc.chrom_lengths)
+    RefOracle().build_index(str(fa), index, 16)
+    ro = RefOracle(index)
+    reads = gc.seed_reads()
+    for run in gc.seed_runs():
+        mode, ss, filt, minc, intron = run
+        assert ro.seeds_cals(mode, reads, ss, filt, minc, intron, len(gc.chrom_lengths)) == gc.seed_expected(*run)
+    ro.close()
