@@ -383,6 +383,23 @@ def serving(gi, reads, genome, log, read_label: str = "100bp", locate_limit: int
     return res
 
 
+def cal_generation(gi, reads, log, n: int) -> dict:
+    """bwt_generate_cals_batch (seeds on the GPU, CALs on the host threads) over the
+    first n reads of the batch: seed size 16, filter_seed_mappings 300,
+    min_cal_size 20, max_intron_size 500000; the best of three calls."""
+    rs = [bytes(reads.seq[int(reads.offsets[i]):int(reads.offsets[i + 1])]) for i in range(min(n, len(reads)))]
+    best, counts = None, []
+    for _ in range(3):
+        counts = gi.generate_cals(rs, 1)
+        best = gi.last_cal_seconds if best is None else min(best, gi.last_cal_seconds)
+    out = {"reads": len(rs), "seconds": round(best, 4), "reads_per_s": round(len(rs) / best, 1),
+           "cals_per_read": round(sum(counts) / max(1, len(rs)), 3), "host_threads": os.cpu_count(),
+           "params": {"seed_size": 16, "filter_seed_mappings": 300, "min_cal_size": 20, "max_intron_size": 500000}}
+    log(f"[bench] CAL generation: {out['reads_per_s'] / 1e6:.2f} M reads/s over {len(rs)} reads, "
+        f"{out['cals_per_read']} CALs per read")
+    return out
+
+
 def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     import torch
     from hpgbwt import lib
@@ -489,6 +506,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     rl = wl["read_len"]
     serve = serving(gi, reads, genome, log, f"{rl[0]}_{rl[1]}bp" if isinstance(rl, tuple) else f"{rl}bp",
                     SERVE_LOCATE_LIMIT if wl["genome"] == "large" else 0) if not args.no_serving else None
+    cals = cal_generation(gi, reads, log, args.cal_reads) if args.cal_reads > 0 else None
     e2e_s = dist.max(sum(e2e_t))
     e2e_value = total_reads * args.steps / e2e_s
     h2d = total + 8 * (n + 1)
@@ -544,6 +562,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                       for k, v in res.items()},
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "serving": serve,
+            "cal_generation": cals,
             "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table(),
                            direction_split=gi.direction_split()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
@@ -596,6 +615,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
+    ap.add_argument("--cal-reads", type=int, default=200_000,
+                    help="reads of the batch taken through bwt_generate_cals_batch (0: skip)")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
                                                  "block_load_mode[,start_table[,direction_split]] (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()

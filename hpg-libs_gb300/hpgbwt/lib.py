@@ -8,6 +8,7 @@ device fails.
 from __future__ import annotations
 
 import ctypes
+import time
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -108,6 +109,22 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_direction_split.argtypes = [vp]
     lib.bwt_gpu_set_locate_limit.argtypes = [vp, u64]
+    lib.bwt_optarg_new.restype = vp
+    lib.bwt_optarg_new.argtypes = [sz, sz, ctypes.c_int, ctypes.c_int]
+    lib.bwt_optarg_free.argtypes = [vp]
+    lib.cal_optarg_new.restype = vp
+    lib.cal_optarg_new.argtypes = [sz] * 9
+    lib.cal_optarg_free.argtypes = [vp]
+    lib.array_list_new.restype = vp
+    lib.array_list_new.argtypes = [sz, ctypes.c_float, ctypes.c_int]
+    lib.array_list_size.restype = sz
+    lib.array_list_size.argtypes = [vp]
+    lib.array_list_get.restype = vp
+    lib.array_list_get.argtypes = [sz, vp]
+    lib.array_list_free.argtypes = [vp, vp]
+    lib.cal_free.argtypes = [vp]
+    lib.bwt_generate_cals_batch.restype = sz
+    lib.bwt_generate_cals_batch.argtypes = [vp, sz, sz, vp, vp, vp, vp, ctypes.c_uint]
     lib.bwt_gpu_locate_limit.argtypes = [vp]
     lib.bwt_gpu_locate_limit.restype = u64
     lib.bwt_gpu_start_table.argtypes = [vp]
@@ -262,6 +279,30 @@ class GpuIndex:
 
     def direction_split(self) -> int:
         return int(self.lib.bwt_gpu_direction_split(self.handle))
+
+    def generate_cals(self, reads: list[bytes], nchromosomes: int, seed_size: int = 16,
+                      filter_seed_mappings: int = 300, min_cal_size: int = 20,
+                      max_intron_size: int = 500_000) -> list[int]:
+        """bwt_generate_cals_batch over the reads (ASCII): the number of CALs of each
+        read (the cal_t records are built and freed)."""
+        n = len(reads)
+        bufs = [ctypes.create_string_buffer(r, len(r) + 1) for r in reads]
+        arr = (ctypes.c_void_p * max(1, n))(*[ctypes.addressof(b) for b in bufs])
+        lists = (ctypes.c_void_p * max(1, n))(*[self.lib.array_list_new(16, 1.25, 2) for _ in range(n)])
+        opt = self.lib.bwt_optarg_new(1, 1, 200, filter_seed_mappings)
+        copt = self.lib.cal_optarg_new(min_cal_size, 0, 0, 0, seed_size, 0, 0, max_intron_size, 0)
+        try:
+            t0 = time.perf_counter()
+            self.lib.bwt_generate_cals_batch(arr, n, seed_size, opt, copt, self.handle, lists, nchromosomes)
+            self.last_cal_seconds = time.perf_counter() - t0
+            counts = [int(self.lib.array_list_size(lists[i])) for i in range(n)]
+        finally:
+            free = ctypes.cast(self.lib.cal_free, ctypes.c_void_p)
+            for i in range(n):
+                self.lib.array_list_free(lists[i], free)
+            self.lib.bwt_optarg_free(opt)
+            self.lib.cal_optarg_free(copt)
+        return counts
 
     def set_locate_limit(self, max_rows: int) -> None:
         """Lists (read, strand) covering more than max_rows rows are not located (rs_truncated bit 1); 0 = none."""
