@@ -483,7 +483,10 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     ms_max = head["ms"]
     launches = head["launches"]
     clk_summary = head["clocks"]
-    sectors = head["sectors"]
+    # algorithmic sectors: the census of the plain form, which walks every step
+    # of the reference's searches (a start table in the batched form stands one
+    # lookup for its first steps, so its own census counts less work)
+    sectors = res["plain"]["sectors"]
     stage_sum = [x * args.steps for x in head["stages"]]
     n_hits, n_locs = head["n_hits"], head["n_locs"]
 

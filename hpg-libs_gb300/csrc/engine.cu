@@ -527,10 +527,12 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
     }
   }
   e->X.load_mode = best_mode;
-  // then the direction split of the fused form (rows marked by -50 - mode)
+  // then the direction split of the fused form (rows marked by -50 - mode);
+  // one launch per direction is kept unless another mode is more than 2 %
+  // faster: at equal speed it reads several times less DRAM (one direction's
+  // blocks stay in L2), which leaves bandwidth to transfers and other work
   if (e->tuning.split == 0) {
-    const int was = e->tuning.dir_split;
-    int best_split = was;
+    float t_on[3] = {0, 0, 0};
     for (int on = 0; on < 3; ++on) {
       e->tuning.dir_split = on;
       float t = 0;
@@ -549,11 +551,13 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
         row[4] = (int)(t * 1000.0f);
       }
       ++rows;
-      if (t < best_ms) {
-        best_ms = t;
-        best_split = on;
-      }
+      t_on[on] = t;
     }
+    int best_split = 0;
+    for (int on = 1; on < 3; ++on)
+      if (t_on[on] < t_on[best_split]) best_split = on;
+    if (t_on[2] <= 1.02f * t_on[best_split]) best_split = 2;
+    best_ms = t_on[best_split];
     e->tuning.dir_split = best_split;
   }
   // then the start-table length (rows marked by a first column of -100 - L)
