@@ -465,6 +465,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             gi.set_start_table(vals[4])
         if len(vals) > 5:
             gi.set_direction_split(vals[5])
+        if len(vals) > 6:
+            gi.set_idle_batch(vals[6])
     elif not args.no_autotune:
         t0 = time.time()
         table = gi.autotune(d_seq.data_ptr(), d_off.data_ptr(), n, total, max_len, MAX_RESULTS)
@@ -567,7 +569,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "serving": serve,
             "cal_generation": cals,
             "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table(),
-                           direction_split=gi.direction_split()),
+                           direction_split=gi.direction_split(), idle_batch=gi.idle_batch()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }
@@ -621,7 +623,7 @@ def main():
     ap.add_argument("--cal-reads", type=int, default=200_000,
                     help="reads of the batch taken through bwt_generate_cals_batch (0: skip)")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
-                                                 "block_load_mode[,start_table[,direction_split]] (stack 0 = split, -1 = lockstep)")
+                                                 "block_load_mode[,start_table[,direction_split[,idle_batch]]] (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]

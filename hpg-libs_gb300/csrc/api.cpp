@@ -309,6 +309,16 @@ int bwt_gpu_direction_split(bwt_index_t* index) {
   return e ? engine_dir_split(e) : -1;
 }
 
+void bwt_gpu_set_idle_batch(bwt_index_t* index, int lanes) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_idle_batch(e, lanes);
+}
+
+int bwt_gpu_idle_batch(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_idle_batch(e) : -1;
+}
+
 void bwt_gpu_set_locate_limit(bwt_index_t* index, uint64_t max_rows) {
   Engine* e = engine_of(index);
   if (e) engine_set_locate_limit(e, max_rows);

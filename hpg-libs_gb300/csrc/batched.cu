@@ -212,6 +212,16 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
 
   for (;;) {
     // ---- transitions: next sub-operation, next change point, next chain ----
+    // A lane out of work waits (riding along masked) until p.batch_idle lanes
+    // of its converged group are out of work too, or all of them are, so the
+    // transition code runs for many lanes at once instead of one at a time.
+    bool go = mode == kNone;
+    if (p.batch_idle > 1) {
+      const unsigned grp = __activemask();
+      const unsigned idle = __ballot_sync(grp, mode == kNone);
+      go = go && ((uint32_t)__popc(idle) >= p.batch_idle || idle == grp);
+    }
+    if (go) {
     while (mode == kNone) {
       uint32_t m = c_meta[tid];
       if (meta_in(m)) {
@@ -341,7 +351,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         mode = kChain;
       }
     }
-    if (mode == kNone) break;
+    if (mode == kNone) break;  // no work left for this lane
+    }
+    if (mode == kNone) continue;  // waiting for more lanes to move on with
 
     // ---- the one gather of this iteration --------------------------------
     {

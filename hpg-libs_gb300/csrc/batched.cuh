@@ -53,6 +53,8 @@ struct BatchedParams {
                              // the others those on the forward index (each half then takes the rest);
                              // 2 / 3 = this launch runs only the backward / forward-index chains
   uint32_t num_sms;
+  uint32_t batch_idle;       // fused form: lanes out of work wait until this many lanes of the
+                             // converged group are (or all of them are), then move on together
   unsigned int* spill_head;  // next spill entry to drain
   unsigned int* spill_tail;  // spill entries written
   SpillEntry* spill;
@@ -76,6 +78,7 @@ struct BatchedTuning {
                           // 2: lockstep kernel (4 chains of a read per lane) + drain
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
   int dir_split = 0;      // fused form: 0 mixed, 1 direction by SM half, 2 one launch per direction
+  int batch_idle = 8;     // fused form: idle lanes that move to their next work item together (1: each at once)
 };
 
 // One locate work item per SA row: the row, the owning hit (or request), the

@@ -308,6 +308,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.chain_ctr2 = ctr + 9;
     p.dir_split = e->tuning.split == 0 ? (uint32_t)e->tuning.dir_split : 0u;
     p.num_sms = (uint32_t)e->num_sms;
+    p.batch_idle = (uint32_t)(e->tuning.batch_idle < 1 ? 1 : e->tuning.batch_idle);
     p.spill_head = ctr + 1;
     p.spill_tail = ctr + 2;
     p.spill = ptr<SpillEntry>(e->b_spill);
@@ -439,6 +440,8 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
 }
 
 void engine_set_dir_split(Engine* e, int mode) { e->tuning.dir_split = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+void engine_set_idle_batch(Engine* e, int lanes) { e->tuning.batch_idle = lanes < 1 ? 1 : (lanes > 32 ? 32 : lanes); }
+int engine_idle_batch(Engine* e) { return e->tuning.batch_idle; }
 int engine_dir_split(Engine* e) { return e->tuning.dir_split; }
 void engine_set_locate_limit(Engine* e, uint64_t max_rows) { e->locate_limit = max_rows; }
 uint64_t engine_locate_limit(Engine* e) { return e->locate_limit; }
@@ -586,6 +589,34 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
     }
   }
   if (engine_set_kmer(e, best_kmer, err) != 0) return -1;
+  // then the idle-lane batch of the fused form (rows marked by -200 - batch)
+  if (e->tuning.split == 0) {
+    int best_batch = e->tuning.batch_idle;
+    for (int b : {1, 4, 8, 16}) {
+      e->tuning.batch_idle = b;
+      float t = 0;
+      for (int rep = 0; rep < 2; ++rep) {
+        if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases,
+                                 max_len, max_results, &r, err) != 0)
+          return -1;
+        t = e->stage_ms[kStageSearch];
+      }
+      if (table && rows < max_rows) {
+        int* row = table + 5 * rows;
+        row[0] = -200 - b;
+        row[1] = batched_max_blocks_per_sm(e->tuning);
+        row[2] = e->tuning.stack;
+        row[3] = e->tuning.chunk;
+        row[4] = (int)(t * 1000.0f);
+      }
+      ++rows;
+      if (t < best_ms) {
+        best_ms = t;
+        best_batch = b;
+      }
+    }
+    e->tuning.batch_idle = best_batch;
+  }
   if (rows_out) *rows_out = rows;
   return 0;
 }

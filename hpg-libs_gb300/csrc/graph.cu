@@ -68,6 +68,7 @@ bool same_settings(const GraphPlan* g, const Engine* e) {
   const BatchedTuning& b = e->tuning;
   return a.block == b.block && a.blocks_per_sm == b.blocks_per_sm && a.stack == b.stack && a.chunk == b.chunk &&
          a.min_blocks == b.min_blocks && a.split == b.split && a.dir_split == b.dir_split &&
+         a.batch_idle == b.batch_idle &&
          g->load_mode == e->X.load_mode &&
          g->census == e->census_on && g->skip_locate == e->skip_locate && g->kmer_len == e->X.kmer_len &&
          g->kmer0 == (const void*)e->X.kmer[0];
@@ -125,6 +126,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   p.chain_ctr2 = ctr + 9;
   p.dir_split = g->tuning.split == 0 ? (uint32_t)g->tuning.dir_split : 0u;
   p.num_sms = (uint32_t)e->num_sms;
+  p.batch_idle = (uint32_t)(g->tuning.batch_idle < 1 ? 1 : g->tuning.batch_idle);
   p.spill_head = ctr + 1;
   p.spill_tail = ctr + 2;
   p.spill = g->spill;

@@ -108,6 +108,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_direction_split.argtypes = [vp]
+    lib.bwt_gpu_set_idle_batch.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_idle_batch.argtypes = [vp]
     lib.bwt_gpu_set_locate_limit.argtypes = [vp, u64]
     lib.bwt_optarg_new.restype = vp
     lib.bwt_optarg_new.argtypes = [sz, sz, ctypes.c_int, ctypes.c_int]
@@ -279,6 +281,13 @@ class GpuIndex:
 
     def direction_split(self) -> int:
         return int(self.lib.bwt_gpu_direction_split(self.handle))
+
+    def set_idle_batch(self, lanes: int) -> None:
+        """Fused batched search: idle lanes of a warp take their next work item together, `lanes` at a time."""
+        self.lib.bwt_gpu_set_idle_batch(self.handle, int(lanes))
+
+    def idle_batch(self) -> int:
+        return int(self.lib.bwt_gpu_idle_batch(self.handle))
 
     def generate_cals(self, reads: list[bytes], nchromosomes: int, seed_size: int = 16,
                       filter_seed_mappings: int = 300, min_cal_size: int = 20,
