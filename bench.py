@@ -244,10 +244,17 @@ def cpu_baseline(index_dir: str, reads, seconds: float = 12.0) -> dict:
     ora = PortOracle(index_dir)
     threads = os.cpu_count() or 1
     n_total = len(reads)
-    probe = reads.subset(np.arange(min(2000, n_total)))
-    t = time.perf_counter()
-    ora.search(probe, mode=1, max_results=MAX_RESULTS, threads=threads)
-    rate = len(probe) / max(time.perf_counter() - t, 1e-6)
+    # rate from a probe grown until it runs long enough for the thread start-up not to count
+    m, rate = 2000, 0.0
+    while True:
+        probe = reads.subset(np.arange(min(m, n_total)))
+        t = time.perf_counter()
+        ora.search(probe, mode=1, max_results=MAX_RESULTS, threads=threads)
+        dt = max(time.perf_counter() - t, 1e-6)
+        rate = len(probe) / dt
+        if dt >= 0.5 or len(probe) >= n_total:
+            break
+        m *= 4
     n = int(min(n_total, max(len(probe), rate * seconds)))
     sample = reads.subset(np.arange(n))
     t = time.perf_counter()
