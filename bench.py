@@ -381,9 +381,16 @@ def serving(gi, reads, genome, log, read_label: str = "100bp", locate_limit: int
     for name, sq, of, pn, draw in cases:
         serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)  # captures the plans it needs
         sat = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)
-        loaded = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, 0.7, 2.0, rng,
-                           sat=sat["achieved_reads_per_s"])
-        res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "at_70pct_load": loaded}
+        sweep = {}
+        for load in (0.1, 0.3, 0.5, 0.7, 0.9):  # offered load as a fraction of the saturated rate
+            sweep[f"{int(load * 100)}pct"] = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, load, 2.0, rng,
+                                                       sat=sat["achieved_reads_per_s"])
+        loaded = sweep["70pct"]
+        res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "at_70pct_load": loaded,
+                     "load_sweep": {k: {"p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"],
+                                        "achieved_reads_per_s": v["achieved_reads_per_s"]} for k, v in sweep.items()}}
+        log(f"[bench] serving {name} sweep: " + ", ".join(f"{k} p50 {v['p50_ms']} p99 {v['p99_ms']}"
+                                                         for k, v in sweep.items()))
         log(f"[bench] serving {name}: saturated {sat['achieved_reads_per_s'] / 1e6:.1f} M reads/s; at 70% "
             f"p50 {loaded['p50_ms']} ms p99 {loaded['p99_ms']} ms, {loaded['mean_batch_requests']} req/batch")
     gi.set_locate_limit(0)

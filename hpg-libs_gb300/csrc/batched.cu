@@ -478,6 +478,15 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
   bool active = false;
   uint32_t next = 0, left = 0, sectors = 0;
   for (;;) {
+    // lanes out of chains wait (masked) until p.batch_idle lanes of the
+    // converged group are, or all of them are, and claim the next ones together
+    bool go = !active;
+    if (p.batch_idle > 1) {
+      const unsigned grp = __activemask();
+      const unsigned idle = __ballot_sync(grp, !active);
+      go = go && ((uint32_t)__popc(idle) >= p.batch_idle || idle == grp);
+    }
+    if (!go && !active) continue;
     while (!active) {
       if (left == 0) {
         next = claim(p.chain_ctr, (unsigned)chunk);

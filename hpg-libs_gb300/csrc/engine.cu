@@ -589,8 +589,9 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
     }
   }
   if (engine_set_kmer(e, best_kmer, err) != 0) return -1;
-  // then the idle-lane batch of the fused form (rows marked by -200 - batch)
-  if (e->tuning.split == 0) {
+  // then the idle-lane batch (rows marked by -200 - batch): the fused kernel,
+  // the chain-only kernel of the split form and every form's drain launch use it
+  {
     int best_batch = e->tuning.batch_idle;
     for (int b : {1, 4, 8, 16}) {
       e->tuning.batch_idle = b;

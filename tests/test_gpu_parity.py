@@ -102,7 +102,7 @@ def test_autotuner_keeps_results(case_factory):
     with lib.GpuIndex(c.index) as g:
         table = g.autotune(d_seq.data_ptr(), d_off.data_ptr(), len(reads), int(reads.offsets[-1]),
                            int(np.diff(reads.offsets).max()), 64)
-        assert len(table) in (68, 71, 75) and all(r["search_us"] > 0 for r in table)
+        assert len(table) in (72, 75) and all(r["search_us"] > 0 for r in table)
         chosen = g.get_tuning()
         best_us = min(r["search_us"] for r in table[:60])
         mine = [r["search_us"] for r in table[:60]
