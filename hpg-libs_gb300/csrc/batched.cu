@@ -966,6 +966,13 @@ __global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uin
 }
 
 constexpr unsigned kRowsPerClaim = 4;
+// Lanes whose walk reached a sampled row (or that hold no row) wait, masked,
+// until this many lanes of their converged group have (or all have), and then
+// finish their rows and start the next ones together: a finish makes dependent
+// loads (the SA sample, the karyotype, the next row item), and a warp that
+// waited for one or two finishing lanes almost every step ran at a quarter of
+// the gather rate.
+constexpr unsigned kLocateBatch = 8;
 
 __global__ void __launch_bounds__(kBlock)
     locate_persistent_kernel(DevIndex X, const RowItem* __restrict__ items, uint64_t n_locs,
@@ -981,7 +988,36 @@ __global__ void __launch_bounds__(kBlock)
   bool active = false;
   uint32_t sectors = 0;
   for (;;) {
-    if (!active) {
+    const bool done = !active || sampled_row(X, i);
+    const unsigned grp = __activemask();
+    const unsigned ready = __ballot_sync(grp, done);
+    if (done) {
+      if ((uint32_t)__popc(ready) < kLocateBatch && ready != grp) continue;  // wait for more lanes
+      if (active) {  // the walk reached a sampled row: the key and the chromosome
+        const uint32_t phys = it.phys_len >> 31;
+        const DevDir D = dir_of(X, phys);
+        const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
+        ++sectors;
+        const uint32_t sa = (s + j) % X.walk_mod;
+        const uint64_t len_calc = it.phys_len & 0x7FFFFFFFu;
+        const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
+        const uint32_t id = kar_search(X, key);
+        hpg_loc_t o;
+        o.key = key;
+        o.hit = it.hit;
+        o.pad = 0;
+        if (key + len_calc <= X.kar_offset[id]) {
+          o.valid = 1;
+          o.chrom = id - 1;
+          o.position = X.kar_start[id - 1] + (key - X.kar_offset[id - 1]);
+        } else {
+          o.valid = 0;
+          o.chrom = 0;
+          o.position = 0;
+        }
+        out[it.out] = o;
+        active = false;
+      }
       if (left == 0) {
         r = claim(row_ctr, kRowsPerClaim);
         left = kRowsPerClaim;
@@ -994,39 +1030,16 @@ __global__ void __launch_bounds__(kBlock)
       i = it.row;
       j = 0;
       active = true;
-    }
-    const uint32_t phys = it.phys_len >> 31;
-    if (!sampled_row(X, i)) {
-      i = lf_step(X, dir_of(X, phys), i);
-      ++sectors;
-      if (++j > X.walk_mod) {
-        atomicOr(X.err, kErrWalk);
-        i = 0;
-      }
       continue;
     }
-    const DevDir D = dir_of(X, phys);
-    const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
+    // one LF step of the walk
+    const uint32_t phys = it.phys_len >> 31;
+    i = lf_step(X, dir_of(X, phys), i);
     ++sectors;
-    const uint32_t sa = (s + j) % X.walk_mod;
-    const uint64_t len_calc = it.phys_len & 0x7FFFFFFFu;
-    const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
-    const uint32_t id = kar_search(X, key);
-    hpg_loc_t o;
-    o.key = key;
-    o.hit = it.hit;
-    o.pad = 0;
-    if (key + len_calc <= X.kar_offset[id]) {
-      o.valid = 1;
-      o.chrom = id - 1;
-      o.position = X.kar_start[id - 1] + (key - X.kar_offset[id - 1]);
-    } else {
-      o.valid = 0;
-      o.chrom = 0;
-      o.position = 0;
+    if (++j > X.walk_mod) {
+      atomicOr(X.err, kErrWalk);
+      i = 0;
     }
-    out[it.out] = o;
-    active = false;
   }
   if (census) atomicAdd(census, (unsigned long long)sectors);
 }
