@@ -115,43 +115,74 @@ std::vector<std::vector<std::vector<Region>>> map_seeds(Engine* e, const std::ve
     uint32_t w;  // index into `where`
     int type;    // 1 '+', 0 '-'
   };
-  std::vector<MapRow> rows;
-  std::vector<RowOf> row_of;
-  for (size_t w = 0; w < where.size(); ++w) {
-    const Seed& sd = jobs[where[w].first].seeds[where[w].second];
-    const uint32_t len = (uint32_t)(sd.last - sd.first);
+  // the strands each seed locates (bit 1 '+', bit 0 '-') and its row count,
+  // then the rows of every seed at its prefix-sum offset (seeds in parallel)
+  const size_t W = where.size();
+  std::vector<uint8_t> keep(W);
+  std::vector<uint64_t> first_row(W + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (size_t w = 0; w < W; ++w) {
     int actual = 0;
+    uint8_t kept = 0;
+    uint64_t n_rows = 0;
     for (int type = 1; type >= 0; --type) {
       const uint32_t k = kl[4 * w + (type ? 0 : 2)], l = kl[4 * w + (type ? 1 : 3)];
       actual += (int)((int64_t)l - (int64_t)k + 1);
-      if (actual > filter_seed_mappings) continue;
-      for (uint64_t j = k; j <= l; ++j) {
-        rows.push_back(MapRow{(uint32_t)j, 0u, len});
-        row_of.push_back(RowOf{(uint32_t)w, type});
+      if (actual > filter_seed_mappings || k > l) continue;
+      kept |= (uint8_t)(1u << type);
+      n_rows += (uint64_t)l - k + 1;
+    }
+    keep[w] = kept;
+    first_row[w + 1] = n_rows;
+  }
+  for (size_t w = 0; w < W; ++w) first_row[w + 1] += first_row[w];
+  const size_t n_rows = first_row[W];
+  std::vector<MapRow> rows(n_rows + 1);
+  std::vector<RowOf> row_of(n_rows + 1);
+#pragma omp parallel for schedule(static)
+  for (size_t w = 0; w < W; ++w) {
+    const Seed& sd = jobs[where[w].first].seeds[where[w].second];
+    const uint32_t len = (uint32_t)(sd.last - sd.first);
+    uint64_t at = first_row[w];
+    for (int type = 1; type >= 0; --type) {
+      if (!(keep[w] & (1u << type))) continue;
+      const uint32_t k = kl[4 * w + (type ? 0 : 2)], l = kl[4 * w + (type ? 1 : 3)];
+      for (uint64_t j = k; j <= l; ++j, ++at) {
+        rows[at] = MapRow{(uint32_t)j, 0u, len};
+        row_of[at] = RowOf{(uint32_t)w, type};
       }
     }
   }
-  std::vector<hpg_loc_t> loc(rows.size() + 1);
-  if (!rows.empty() && engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  std::vector<hpg_loc_t> loc(n_rows + 1);
+  if (n_rows && engine_locate_rows(e, rows.data(), n_rows, loc.data(), &err) != 0) fatal(err);
+  // regions per job (jobs in parallel; a job's seeds, and so its rows, are contiguous)
+  std::vector<size_t> job_first(jobs.size() + 1, W);
+  for (size_t w = W; w-- > 0;) job_first[where[w].first] = w;
+  for (size_t j = jobs.size(); j-- > 0;)
+    if (job_first[j] > job_first[j + 1]) job_first[j] = job_first[j + 1];
   std::vector<std::vector<std::vector<Region>>> out(jobs.size());
-  for (size_t j = 0; j < jobs.size(); ++j) out[j].resize(jobs[j].seeds.size());
-  for (size_t r = 0; r < rows.size(); ++r) {
-    const hpg_loc_t& q = loc[r];
-    if (!q.valid) continue;
-    const size_t job = where[row_of[r].w].first, s = where[row_of[r].w].second;
-    const Seed& sd = jobs[job].seeds[s];
-    const size_t len = sd.last - sd.first, n = jobs[job].len;
-    const int type = row_of[r].type;
-    Region g;
-    g.chrom = (size_t)q.chrom + 1;
-    g.strand = !type;
-    g.start = (size_t)q.position + 1;
-    g.end = g.start + len;
-    g.seq_start = type ? sd.first : n - sd.last - 1;
-    g.seq_end = type ? sd.last : n - sd.first - 1;
-    g.seq_len = n;
-    g.id = sd.id;
-    out[job][s].push_back(g);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (size_t job = 0; job < jobs.size(); ++job) {
+    out[job].resize(jobs[job].seeds.size());
+    const size_t n = jobs[job].len;
+    for (uint64_t r = first_row[job_first[job]]; r < first_row[job_first[job + 1]]; ++r) {
+      const hpg_loc_t& q = loc[r];
+      if (!q.valid) continue;
+      const size_t s = where[row_of[r].w].second;
+      const Seed& sd = jobs[job].seeds[s];
+      const size_t len = sd.last - sd.first;
+      const int type = row_of[r].type;
+      Region g;
+      g.chrom = (size_t)q.chrom + 1;
+      g.strand = !type;
+      g.start = (size_t)q.position + 1;
+      g.end = g.start + len;
+      g.seq_start = type ? sd.first : n - sd.last - 1;
+      g.seq_end = type ? sd.last : n - sd.first - 1;
+      g.seq_len = n;
+      g.id = sd.id;
+      out[job][s].push_back(g);
+    }
   }
   return out;
 }
@@ -173,17 +204,19 @@ struct SeedReg {
 struct ShortCal {
   size_t start, end, num_seeds;
   std::list<SeedReg> sr, dup;  // front = the linked list's first item
-  std::vector<uint8_t> seen;   // seeds_ids_array (unsigned char counters)
+  std::vector<uint8_t> seen;   // seeds_ids_array (unsigned char counters), one per seed id of the read
 };
 using CalList = std::list<ShortCal>;
 
-ShortCal new_short_cal(const Region& g) {  // short_cal_new (bwt.c:319-342)
+// short_cal_new (bwt.c:319-342); the reference's table has 1000 entries, of
+// which a read uses its seed ids only (`ids`).
+ShortCal new_short_cal(const Region& g, size_t ids) {
   if (g.id >= kMaxSeeds) fatal("seed id past the CAL seed table (1000 seeds per read)");
   ShortCal c;
   c.start = g.start;
   c.end = g.end;
   c.num_seeds = 1;
-  c.seen.assign(kMaxSeeds, 0);
+  c.seen.assign(ids, 0);
   c.seen[g.id] = 1;
   c.sr.push_front(SeedReg{(int)g.seq_start, (int)g.seq_end, g.start, g.end, g.id});
   return c;
@@ -214,9 +247,9 @@ void select_seed(ShortCal& c, const SeedReg& s) {
 // my_cp_list_append_linked_list (bwt.c:4652-4824): one region into the
 // CAL list of its strand and chromosome, kept ordered by start; CALs within
 // `dist` of each other merge.
-void add_region(CalList& L, const Region& g, size_t dist) {
+void add_region(CalList& L, const Region& g, size_t dist, size_t ids) {
   if (L.empty()) {
-    L.push_front(new_short_cal(g));
+    L.push_front(new_short_cal(g, ids));
     return;
   }
   const SeedReg s{(int)g.seq_start, (int)g.seq_end, g.start, g.end, g.id};
@@ -225,7 +258,7 @@ void add_region(CalList& L, const Region& g, size_t dist) {
   for (; it != L.end(); ++it) {
     if (g.start < it->start) {
       if (g.end + dist < it->start) {  // a new CAL before this one
-        L.insert(it, new_short_cal(g));
+        L.insert(it, new_short_cal(g, ids));
       } else {  // this CAL now starts at the region
         it->start = g.start;
         it->num_seeds++;
@@ -251,7 +284,7 @@ void add_region(CalList& L, const Region& g, size_t dist) {
     }
   }
   if (it == L.end()) {
-    L.push_back(new_short_cal(g));
+    L.push_back(new_short_cal(g, ids));
     return;
   }
   if (!grown) return;
@@ -339,10 +372,11 @@ void build_cals(const std::vector<std::vector<Region>>& regions, size_t read_len
   if (seed_size <= 10) seed_size = 16;
   const size_t nchrom = (size_t)nchromosomes + 1;
   std::vector<CalList> lists(2 * nchrom);  // [strand * nchrom + chromosome]
+  const size_t ids = regions.size();  // seed ids of this read: 0 .. ids - 1
   for (const auto& seed_regions : regions)  // insert_seeds_and_merge: each seed's regions, last first
     for (auto g = seed_regions.rbegin(); g != seed_regions.rend(); ++g) {
       if (g->chrom >= nchrom) fatal("bwt_generate_cals: a seed mapped past nchromosomes");
-      add_region(lists[(size_t)g->strand * nchrom + g->chrom], *g, read_length);
+      add_region(lists[(size_t)g->strand * nchrom + g->chrom], *g, read_length, ids);
     }
   const size_t min_cal_size = cal_optarg->min_cal_size;
   const int max_intron_size = (int)cal_optarg->max_intron_size;
