@@ -414,6 +414,22 @@ def cal_generation(gi, reads, log, n: int) -> dict:
     return out
 
 
+def alignment_lists(gi, reads, log, n: int) -> dict:
+    """bwt_map_inexact_batch, the reference's alignment-list entry point (BWSearch1 and
+    the located rows on the GPU, alignment records on the host), over the first n
+    reads of the batch with filter_read_mappings 200; the best of three calls."""
+    rs = [bytes(reads.seq[int(reads.offsets[i]):int(reads.offsets[i + 1])]) for i in range(min(n, len(reads)))]
+    best, count = None, 0
+    for _ in range(3):
+        count = gi.map_inexact_batch(rs, 200)
+        best = gi.last_map_seconds if best is None else min(best, gi.last_map_seconds)
+    out = {"reads": len(rs), "seconds": round(best, 4), "reads_per_s": round(len(rs) / best, 1),
+           "alignments_per_read": round(count / max(1, len(rs)), 3), "filter_read_mappings": 200}
+    log(f"[bench] bwt_map_inexact_batch: {out['reads_per_s'] / 1e6:.2f} M reads/s over {len(rs)} reads, "
+        f"{out['alignments_per_read']} alignments per read")
+    return out
+
+
 def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     import torch
     from hpgbwt import lib
@@ -526,6 +542,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     serve = serving(gi, reads, genome, log, f"{rl[0]}_{rl[1]}bp" if isinstance(rl, tuple) else f"{rl}bp",
                     SERVE_LOCATE_LIMIT if wl["genome"] == "large" else 0) if not args.no_serving else None
     cals = cal_generation(gi, reads, log, args.cal_reads) if args.cal_reads > 0 else None
+    alns = alignment_lists(gi, reads, log, args.cal_reads) if args.cal_reads > 0 else None
     e2e_s = dist.max(sum(e2e_t))
     e2e_value = total_reads * args.steps / e2e_s
     h2d = total + 8 * (n + 1)
@@ -582,6 +599,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "batched_over_plain": round(res["batched"]["value"] / res["plain"]["value"], 3),
             "serving": serve,
             "cal_generation": cals,
+            "alignment_lists": alns,
             "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table(),
                            direction_split=gi.direction_split(), idle_batch=gi.idle_batch()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
@@ -635,7 +653,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
     ap.add_argument("--cal-reads", type=int, default=200_000,
-                    help="reads of the batch taken through bwt_generate_cals_batch (0: skip)")
+                    help="reads of the batch taken through bwt_generate_cals_batch and bwt_map_inexact_batch "
+                         "(0: skip)")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
                                                  "block_load_mode[,start_table[,direction_split[,idle_batch]]] (stack 0 = split, -1 = lockstep)")
     args = ap.parse_args()

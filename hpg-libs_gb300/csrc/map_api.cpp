@@ -8,6 +8,7 @@
 // here with the reference's field values, order and quirks.  Anchors
 // (bwt.c:1822-1869) take one more scan and locate pass for the reads that end
 // without alignments in a list flagged 1.
+#include <algorithm>
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
@@ -383,6 +384,17 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
   if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
   // 3. alignment records, read by read in order
   std::vector<InexactOutcome> out(n);
+  // reads in parallel when each read's records go to a list of its own (a
+  // caller's list named for two reads would take unlocked inserts from two threads)
+  bool own_lists = true;
+  {
+    std::vector<const void*> seen;
+    for (size_t i = 0; i < n; ++i)
+      if (lists[i]->list) seen.push_back(lists[i]->list);
+    std::sort(seen.begin(), seen.end());
+    own_lists = std::adjacent_find(seen.begin(), seen.end()) == seen.end();
+  }
+#pragma omp parallel for schedule(dynamic, 256) if (own_lists && n > 256)
   for (size_t i = 0; i < n; ++i) out[i] = assemble_inexact(rds[i], plan[i], rs.hits, loc.data(), *lists[i]);
   bwt_gpu_result_free(&rs);
   // 4. anchors for reads left without alignments in a list flagged 1 (bwt.c:2243-2273)

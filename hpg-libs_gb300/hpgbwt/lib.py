@@ -125,6 +125,9 @@ def load() -> ctypes.CDLL:
     lib.array_list_get.argtypes = [sz, vp]
     lib.array_list_free.argtypes = [vp, vp]
     lib.cal_free.argtypes = [vp]
+    lib.bwt_map_inexact_batch.restype = sz
+    lib.bwt_map_inexact_batch.argtypes = [vp, vp, vp, vp, vp]
+    lib.alignment_free.argtypes = [vp]
     lib.bwt_generate_cals_batch.restype = sz
     lib.bwt_generate_cals_batch.argtypes = [vp, sz, sz, vp, vp, vp, vp, ctypes.c_uint]
     lib.bwt_gpu_locate_limit.argtypes = [vp]
@@ -312,6 +315,44 @@ class GpuIndex:
             self.lib.bwt_optarg_free(opt)
             self.lib.cal_optarg_free(copt)
         return counts
+
+    def map_inexact_batch(self, reads: list[bytes], filter_read_mappings: int = 200) -> int:
+        """bwt_map_inexact_batch (the reference's alignment-list entry point) over the
+        reads: the number of alignment records (built and freed); the C call's wall
+        time is left in last_map_seconds."""
+
+        class FastqBatch(ctypes.Structure):  # c/src/bioformats/fastq/fastq_batch.h:24-34
+            _fields_ = [("num_reads", ctypes.c_ulong), ("data_indices_size", ctypes.c_ulong),
+                        ("data_size", ctypes.c_ulong), ("source_id", ctypes.c_int),
+                        ("header_indices", ctypes.c_void_p), ("header", ctypes.c_void_p),
+                        ("data_indices", ctypes.c_void_p), ("seq", ctypes.c_void_p), ("quality", ctypes.c_void_p)]
+        n = len(reads)
+        seq = b"".join(r + b"\0" for r in reads)
+        qual = b"".join(b"I" * len(r) + b"\0" for r in reads)
+        ids = b"".join(b"@r%d\0" % i for i in range(n))
+        didx = np.zeros(n + 1, np.int32)
+        didx[1:] = np.cumsum([len(r) + 1 for r in reads])
+        hidx = np.zeros(n + 1, np.int32)
+        hidx[1:] = np.cumsum([len(b"@r%d" % i) + 1 for i in range(n)])
+        sbuf, qbuf, ibuf = (ctypes.create_string_buffer(x, len(x)) for x in (seq, qual, ids))
+        b = FastqBatch(num_reads=n, header_indices=hidx.ctypes.data, header=ctypes.addressof(ibuf),
+                       data_indices=didx.ctypes.data, seq=ctypes.addressof(sbuf), quality=ctypes.addressof(qbuf))
+        uh, ud = np.zeros(n + 1, np.int32), np.zeros(n + 1, np.int32)
+        ub = [ctypes.create_string_buffer(len(ids) + 1), ctypes.create_string_buffer(len(seq) + 1),
+              ctypes.create_string_buffer(len(seq) + 1)]
+        u = FastqBatch(header_indices=uh.ctypes.data, header=ctypes.addressof(ub[0]), data_indices=ud.ctypes.data,
+                       seq=ctypes.addressof(ub[1]), quality=ctypes.addressof(ub[2]))
+        opt = self.lib.bwt_optarg_new(1, 1, filter_read_mappings, filter_read_mappings)
+        lst = self.lib.array_list_new(max(16, n), 1.25, 2)
+        try:
+            t0 = time.perf_counter()
+            self.lib.bwt_map_inexact_batch(ctypes.byref(b), opt, self.handle, ctypes.byref(u), lst)
+            self.last_map_seconds = time.perf_counter() - t0
+            count = int(self.lib.array_list_size(lst))
+        finally:
+            self.lib.array_list_free(lst, ctypes.cast(self.lib.alignment_free, ctypes.c_void_p))
+            self.lib.bwt_optarg_free(opt)
+        return count
 
     def set_locate_limit(self, max_rows: int) -> None:
         """Lists (read, strand) covering more than max_rows rows are not located (rs_truncated bit 1); 0 = none."""
