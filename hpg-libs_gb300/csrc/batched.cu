@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   int pos = 0, dir = 0;             // read position of the pending step; -1 backward, +1 forward
   uint32_t nb = 0;                  // base of the pending step
   uint32_t mode = kNone;
+  uint32_t win = 0;                 // chain: first J where the helper branches | how many J (<< 16)
   uint32_t sectors = 0;
   // read-level work: the current read's next chain, and the next read claimed
   // and its offsets fetched ahead of time (their loads complete while the
@@ -333,6 +334,11 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       pl = X.top;
       dir = (c & 1u) ? 1 : -1;
       pos = (c & 1u) ? 0 : len - 1;
+      {  // branching positions of this vector search: J in [2, n/2] backward, [n/2 - 1, n - 1] forward
+        const int n = len - 1;
+        const int lo = dir > 0 ? n / 2 - 1 : 2, hi = dir > 0 ? n - 1 : n / 2;
+        win = (uint32_t)lo | ((uint32_t)(hi >= lo ? hi - lo + 1 : 0) << 16);
+      }
       const uint32_t L = X.kmer_len;
       if (L && len >= 2 * (int)L + 2) {
         // The first L steps of a chain from the full interval never reach a
@@ -369,7 +375,6 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
         bw_step(X, View{vsel ^ strand, strand}, nb, k, l);
       }
     }
-    const int stop = dir > 0 ? len - 1 : 0;
     if (mode == kKmer) {
       if (k > l) {  // failed within the first L steps: no change point, no hit
         mode = kNone;
@@ -386,12 +391,11 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       // (k,l) = vector entry at pos, (pk,pl) = entry at J = pos - dir.  The helper
       // branches at J in [2, n/2] (backward, block at 1) and [n/2 - 1, n - 2]
       // (forward, block at n - 1).
-      const int J = pos - dir, n = len - 1;
-      const int jlo = dir > 0 ? n / 2 - 1 : 2, jhi = dir > 0 ? n - 1 : n / 2;
+      const int J = pos - dir;
       const bool differ = (l - k) != (pl - pk);  // sizes are >= -1 here, so 32-bit differences suffice
-      if (differ && J >= jlo && J <= jhi)
-        push(pk, pl, (uint32_t)J | ((dir > 0 ? (J == n - 1 ? kBlkN : kCpFwd) : kCpBwd) << 16));
-      if (k <= l && pos != stop) {
+      if (differ && (uint32_t)(J - (int)(win & 0xFFFFu)) < (win >> 16))
+        push(pk, pl, (uint32_t)J | ((dir > 0 ? (J == len - 2 ? kBlkN : kCpFwd) : kCpBwd) << 16));
+      if (k <= l && (uint32_t)(pos + dir) < (uint32_t)len) {  // a next base to match
         pk = k;
         pl = l;
         pos += dir;
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       }
       mode = kNone;
     } else if (mode == kCont) {
-      if (k <= l && pos != stop) {
+      if (k <= l && (uint32_t)(pos + dir) < (uint32_t)len) {
         pos += dir;
         nb = W[pos];
         continue;
