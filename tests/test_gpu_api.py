@@ -98,6 +98,45 @@ def test_array_list_form(loaded, name):
     L.array_list_free(reads, None)
 
 
+@pytest.mark.parametrize("name", names())
+def test_array_list_form_shared_list(loaded, name):
+    """bwt_map_inexact_array_list with one list named for every read maps them as
+    bwt_map_inexact_read called read after read on that list (the records of a read
+    can depend on what the list already holds: bwt.c:2234-2237 re-marks its first
+    alignment), so the records are built in read order on one thread."""
+    L, cases = loaded
+    gc, index = cases[name]
+    fq = gc.api_fastq()
+    keep = []
+    reads = L.array_list_new(fq.n + 1, 1.25, 2)
+    shared = L.array_list_new(64, 1.25, 2)
+    one_by_one = L.array_list_new(64, 1.25, 2)
+    lists = (ctypes.c_void_p * fq.n)(*([shared] * fq.n))
+    opt = L.bwt_optarg_new(1, 1, 3, 3)  # a small filter: some strands pass it and set the flag
+    with lib.GpuIndex(index) as g:
+        for i in range(fq.n):
+            r = al.FastqRead()
+            o = int(fq.offs[i])
+            r.id = fq.ids.ctypes.data + int(fq.id_offs[i])
+            r.sequence = fq.seq.ctypes.data + o
+            r.quality = fq.qual.ctypes.data + o
+            rc = ctypes.create_string_buffer(al._revcomp(fq.seqs[i]), len(fq.seqs[i]) + 1)
+            r.revcomp = ctypes.addressof(rc)
+            r.length = len(fq.seqs[i])
+            keep += [r, rc]
+            L.array_list_insert(ctypes.addressof(r), reads)
+            L.bwt_map_inexact_read(ctypes.byref(r), opt, g.handle, one_by_one)
+        n_un = ctypes.c_size_t()
+        un = (ctypes.c_size_t * fq.n)()
+        L.bwt_map_inexact_array_list(reads, opt, g.handle, lists, ctypes.byref(n_un), un)
+    L.bwt_optarg_free(opt)
+    got = al.walk_list(L, shared, 0, False)
+    want = al.walk_list(L, one_by_one, 0, False)
+    assert len(got["items"]) > fq.n // 4
+    assert got == want
+    L.array_list_free(reads, None)
+
+
 def test_edge_reads_do_not_break(loaded):
     """Reads the reference cannot take (empty, 1-3 bases, N, lower case) map without faults."""
     L, cases = loaded
