@@ -274,7 +274,7 @@ def _pct(v: list[float], q: float) -> float:
 
 
 def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: float | None, seconds: float,
-              rng: np.random.Generator, sat: float | None = None, burst: int = 48) -> dict:
+              rng: np.random.Generator, sat: float | None = None, burst: int = 192) -> dict:
     """One serving measurement through bwt_gpu_server_*: with load None a burst
     of requests submitted at once (saturated throughput); else Poisson arrivals
     offering `load` x `sat` reads/s for `seconds`.  Requests are slices of a
