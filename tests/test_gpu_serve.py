@@ -119,3 +119,27 @@ def test_server_rejects_and_releases(case_factory):
             srv.release(t)
             with pytest.raises(RuntimeError, match="unknown or released"):
                 srv.release(t)
+
+
+def test_serving_locate_limit(tmp_path_factory):
+    """The serving form applies the index's locate limit like the batched call: lists over
+    the limit keep their hits, get no rows and truncation bit 1, as the oracle's limit."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from low_complexity import low_complexity_case
+    index, reads = low_complexity_case(tmp_path_factory.mktemp("serve_limit"))
+    # requests of the low-complexity reads in three slices
+    n = len(reads.offsets) - 1
+    cuts = [0, 7, 60, n]
+    reqs = [reads.subset(np.arange(a, b)) for a, b in zip(cuts, cuts[1:])]
+    ora = PortOracle(index)
+    with lib.GpuIndex(index) as g:
+        g.set_locate_limit(5000)
+        with lib.Server(g, max_batch_reads=4096, max_results=100) as srv:
+            tickets = [srv.submit(r.seq, r.offsets) for r in reqs]
+            got = [srv.wait(t)[0] for t in tickets]
+    for r, res in zip(reqs, got):
+        want = ora.search(r, mode=lib.MODE_SEARCH1, max_results=100, threads=8, locate_limit=5000)
+        _same(res, want)
+    assert any((res.rs_truncated & 2).any() for res in got)
