@@ -70,6 +70,25 @@ std::vector<Seed> seed_plan(size_t len, size_t seed_size) {
   return out;
 }
 
+// The seed plan of bwt_map_exact_seeds_by_region (bwt.c:4033-4080): seeds of
+// seed_size tiling [start_position, end_position) of the read, ids from 1, and
+// the last seed_size bases of the window when its length is not a multiple.
+std::vector<Seed> seed_plan_window(size_t read_len, int start_position, int end_position, int seed_size) {
+  if (seed_size <= 10) seed_size = 16;
+  const int len = end_position - start_position;
+  std::vector<Seed> out;
+  int id = 1;
+  auto add = [&](long first, long last) {
+    const bool ok = first >= 0 && first <= last && (size_t)last < read_len;
+    out.push_back(Seed{ok ? (size_t)first : 0, ok ? (size_t)last : 0, id++, ok});
+  };
+  const int num = len / seed_size;
+  long off = start_position;
+  for (int i = 0; i < num; ++i, off += seed_size) add(off, off + seed_size - 1);
+  if (len % seed_size > 0) add((long)end_position - seed_size, (long)end_position - 1);
+  return out;
+}
+
 // A located seed (region_bwt_new's fields, bwt.c:1280).
 struct Region {
   size_t chrom;  // 1-based
@@ -537,6 +556,20 @@ size_t bwt_map_exact_seeds_seq(int padding_left, int padding_right, char* seq, s
   Engine* e = engine_for(index);
   const size_t len = std::strlen(seq);
   SeedJob job{seq, len, seed_plan(len, seed_size)};
+  const auto regions = map_seeds(e, {job}, bwt_optarg->filter_seed_mappings);
+  for (const auto& per_seed : regions[0])
+    for (const Region& g : per_seed) array_list_insert(to_region(g), mapping_list);
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_exact_seeds_by_region(int start_position, int end_position, char* seq, int seed_size,
+                                     int min_seed_size, bwt_optarg_t* bwt_optarg, bwt_index_t* index,
+                                     array_list_t* mapping_list) {
+  (void)min_seed_size;
+  std::lock_guard<std::mutex> lk(map_api_mutex());
+  Engine* e = engine_for(index);
+  const size_t len = std::strlen(seq);
+  SeedJob job{seq, len, seed_plan_window(len, start_position, end_position, seed_size)};
   const auto regions = map_seeds(e, {job}, bwt_optarg->filter_seed_mappings);
   for (const auto& per_seed : regions[0])
     for (const Region& g : per_seed) array_list_insert(to_region(g), mapping_list);

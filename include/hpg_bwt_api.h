@@ -278,6 +278,14 @@ size_t bwt_map_exact_seed(uint8_t *seq, size_t seq_len, size_t seq_start, size_t
 size_t bwt_map_exact_seeds_seq(int padding_left, int padding_right, char *seq, size_t seed_size,
                                size_t min_seed_size, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
                                array_list_t *mapping_list, unsigned char step_id);
+/* bwt_map_exact_seeds_by_region (bwt.c:4033-4080): the seeds of seed_size
+ * (16 when <= 10) tiling the read window [start_position, end_position), ids
+ * from 1, plus the window's last seed_size bases when its length is not a
+ * multiple, each mapped as bwt_map_exact_seed does; returns the list's size.
+ * min_seed_size is ignored, as in the reference. */
+size_t bwt_map_exact_seeds_by_region(int start_position, int end_position, char *seq, int seed_size,
+                                     int min_seed_size, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                                     array_list_t *mapping_list);
 
 /* ---- candidate alignment locations (bwt.c:3631-3642, 3832-4031, 4378-4646, 4652-4824) ----
  * bwt_generate_cals: the seed plan of bwt_map_exact_seeds_seq; each seed's

@@ -20,6 +20,7 @@
  *                        3 bwt_map_inexact_read per read (bwt.c:1879), fresh list with `flag`
  *                        serialised as described at ref_map_api.
  */
+#include <ctype.h>
 #include <fcntl.h>
 #include <stdarg.h>
 #include <unistd.h>
@@ -122,6 +123,22 @@ static void fill_hit(hpg_hit_t *h, uint32_t read, int type, const result *r) {
   h->l = r->l;
 }
 
+/* Whether every character of a read is a letter of the index alphabet (either
+ * case).  bwt_init_replace_table (bwt_commons.c:60-92) fills only those 2 x nA
+ * entries of its malloc'ed table, so any other character gives an arbitrary
+ * code, which can index past the C and O tables: such reads are not given to
+ * the reference (the product maps them to no hits). */
+static int in_alphabet(const bwt_index_t *index, const char *s, size_t len) {
+  const char *nt = index->bwt_config.nucleotides;
+  for (size_t i = 0; i < len; i++) {
+    const int c = toupper((unsigned char)s[i]);
+    int ok = 0;
+    for (int a = 0; a < index->bwt_config.nA && !ok; a++) ok = (c == nt[a]);
+    if (!ok) return 0;
+  }
+  return 1;
+}
+
 int ref_search(void *vidx, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
                uint32_t max_results, hpg_result_set_t *out) {
   bwt_index_t *index = (bwt_index_t *)vidx;
@@ -140,6 +157,7 @@ int ref_search(void *vidx, int mode, const char *seqs, const uint64_t *offsets, 
     size_t len = (size_t)(offsets[rd + 1] - offsets[rd]);
     const char *seq = seqs + offsets[rd];
     if (len < 3) continue; /* the helper reads outside its vectors below 3 bases */
+    if (!in_alphabet(index, seq, len)) continue;
     uint8_t *code = (uint8_t *)malloc(len);
     encode_bases(code, (char *)seq, len, index->bwt_config.table);
     int16_t start = 0, end = (int16_t)(len - 1);
@@ -415,6 +433,9 @@ static void put_seed(blob_t *b, char tag, seed_region_t *s) {
 /* ref_seeds_cals: per read (seqs NUL-terminated at offs[i], as ref_map_api),
  *   mode 0: bwt_map_exact_seeds_seq (bwt.c:3577) into a fresh list:
  *           "R <returned> <size>" then "G chrom strand start end seq_start seq_end seq_len id" per region;
+ *   mode 2: bwt_map_exact_seeds_by_region (bwt.c:4033) over the read window
+ *           [min_cal_size, len - max_intron) (the two fields carry the window's offsets),
+ *           written as mode 0;
  *   mode 1: bwt_generate_cals (bwt.c:3832) into a fresh list:
  *           "R <returned> <size>" then per CAL "C chrom strand start end num_seeds read_area" followed
  *           by its seeds: "S ..." (sr_list), "D ..." (sr_duplicate_list), "A ..." / "B ..."
@@ -431,8 +452,11 @@ int ref_seeds_cals(void *vidx, int mode, const char *seqs, const uint64_t *offs,
   for (size_t i = 0; i < n; i++) {
     char *seq = (char *)seqs + offs[i];
     array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_ASYNCHRONIZED);
-    if (mode == 0) {
-      size_t ret = bwt_map_exact_seeds_seq(0, 0, seq, seed_size, 0, opt, index, list, 0);
+    if (mode == 0 || mode == 2) {
+      const size_t len = strlen(seq);
+      size_t ret = mode == 0 ? bwt_map_exact_seeds_seq(0, 0, seq, seed_size, 0, opt, index, list, 0)
+                             : bwt_map_exact_seeds_by_region((int)min_cal_size, (int)(len - max_intron), seq,
+                                                             (int)seed_size, 0, opt, index, list);
       put_text(&b, "R %zu %zu\n", ret, array_list_size(list));
       for (size_t k = 0; k < array_list_size(list); k++) {
         region_t *r = (region_t *)array_list_get(k, list);

@@ -42,9 +42,10 @@ API_RUNS = [(api_lists.API_EXACT_READ, 200, 0), (api_lists.API_EXACT_READ, 2, 0)
 API_READS = 400  # first reads of each case taken through the entry points
 
 # Seeds and CALs recorded per case (ref_seeds_cals): (mode 0 bwt_map_exact_seeds_seq /
-# 1 bwt_generate_cals, seed_size, filter_seed_mappings, min_cal_size, max_intron_size).
+# 1 bwt_generate_cals / 2 bwt_map_exact_seeds_by_region, seed_size, filter_seed_mappings,
+# min_cal_size, max_intron_size); mode 2 reads the last two as the window [a, len - b).
 SEED_RUNS = [(0, 16, 300, 0, 0), (0, 20, 4, 0, 0), (1, 16, 300, 20, 500_000), (1, 20, 40, 30, 1_000),
-             (1, 8, 300, 60, 200)]
+             (1, 8, 300, 60, 200), (2, 16, 300, 5, 3), (2, 20, 40, 0, 7), (2, 8, 300, 11, 0)]
 SEED_READS = 300
 
 

@@ -7,7 +7,7 @@ import ctypes
 
 import numpy as np
 
-MODE_SEEDS, MODE_CALS = 0, 1
+MODE_SEEDS, MODE_CALS, MODE_WINDOW = 0, 1, 2  # MODE_WINDOW: bwt_map_exact_seeds_by_region
 
 
 class Region(ctypes.Structure):  # bwt.h:185-198
@@ -61,6 +61,9 @@ def bind(lib) -> None:
     lib.cal_free.argtypes = [vp]
     lib.bwt_map_exact_seeds_seq.restype = sz
     lib.bwt_map_exact_seeds_seq.argtypes = [ctypes.c_int, ctypes.c_int, vp, sz, sz, vp, vp, vp, ctypes.c_ubyte]
+    lib.bwt_map_exact_seeds_by_region.restype = sz
+    lib.bwt_map_exact_seeds_by_region.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, vp,
+                                                  vp]
     lib.bwt_generate_cals.restype = sz
     lib.bwt_generate_cals.argtypes = [vp, sz, vp, vp, vp, vp, ctypes.c_uint]
     lib.bwt_generate_cals_batch.restype = sz
@@ -99,7 +102,7 @@ def _write(lib, mode: int, ret: int, lst: int, out: list[str]) -> None:
     out.append(f"R {ret} {n}\n")
     for k in range(n):
         p = lib.array_list_get(k, lst)
-        if mode == MODE_SEEDS:
+        if mode in (MODE_SEEDS, MODE_WINDOW):
             r = Region.from_address(p)
             out.append(f"G {r.chromosome_id} {r.strand} {r.start} {r.end} {r.seq_start} {r.seq_end} {r.seq_len} "
                        f"{r.id}\n")
@@ -136,6 +139,10 @@ def product_seeds_cals(lib, index_handle: int, mode: int, reads: list[bytes], se
                 if mode == MODE_SEEDS:
                     ret = lib.bwt_map_exact_seeds_seq(0, 0, ctypes.addressof(b), seed_size, 0, opt, index_handle,
                                                       lst, 0)
+                elif mode == MODE_WINDOW:  # window [min_cal_size, len - max_intron), as ref_seeds_cals mode 2
+                    L = len(b.value)
+                    ret = lib.bwt_map_exact_seeds_by_region(min_cal_size, L - max_intron, ctypes.addressof(b),
+                                                            seed_size, 0, opt, index_handle, lst)
                 else:
                     ret = lib.bwt_generate_cals(ctypes.addressof(b), seed_size, opt, copt, index_handle, lst, nchrom)
                 _write(lib, mode, ret, lst, out)

@@ -174,7 +174,7 @@ def test_recorded_seed_runs_parse():
         reads = gc.seed_reads()
         assert len(reads) > 100 and all(len(r) >= 40 for r in reads)
         runs = gc.seed_runs()
-        assert {m for m, *_ in runs} == {0, 1}
+        assert {m for m, *_ in runs} == {0, 1, 2}
         for run in runs:
             text = gc.seed_expected(*run).decode()
             assert sum(1 for line in text.splitlines() if line.startswith("R ")) == len(reads)

@@ -1,5 +1,5 @@
-"""Seeds and CALs on the GPU (bwt_map_exact_seeds_seq, bwt_map_exact_seed,
-bwt_generate_cals, bwt_generate_cals_batch) against the reference's own records
+"""Seeds and CALs on the GPU (bwt_map_exact_seeds_seq, bwt_map_exact_seeds_by_region,
+bwt_map_exact_seed, bwt_generate_cals, bwt_generate_cals_batch) against the reference's own records
 in the golden fixtures: every region, CAL, seed list, duplicate list and
 candidate list, in order."""
 from __future__ import annotations
