@@ -514,6 +514,22 @@ __global__ void __launch_bounds__(kBlock, MINB) chain_kernel(DevIndex X, Batched
       pl = X.top;
       dir = fwd ? 1 : -1;
       pos = fwd ? 0 : L - 1;
+      const uint32_t KL = X.kmer_len;
+      if (KL && L >= 2 * (int)KL + 2) {
+        // start table: one lookup for the first KL steps, which reach no
+        // branching position (as in the fused kernel)
+        uint32_t code = 0;
+        for (uint32_t i = 0; i < KL; ++i) {
+          const uint32_t b = W[fwd ? (int)i : L - 1 - (int)i];
+          code = (code << 2) | (strand ? sel4(X.comp, b) : b);
+        }
+        const uint2 t = __ldg(((((uint32_t)fwd) ^ strand) ? X.kmer[1] : X.kmer[0]) + code);
+        if (p.census) sectors += 1u;
+        if (t.x > t.y) continue;  // failed within the first KL steps: no change point, no hit
+        k = pk = t.x;
+        l = pl = t.y;
+        pos = fwd ? (int)KL : L - 1 - (int)KL;
+      }
       nb = W[pos];
       active = true;
     }

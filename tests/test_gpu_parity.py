@@ -148,7 +148,7 @@ def test_start_table_lengths_agree(case_factory, symbols):
     with lib.GpuIndex(c.index) as g:
         g.set_start_table(symbols)
         assert g.start_table() == symbols
-        for stack in (2, 4):
+        for stack in (0, 2, 4):  # split form (chain-only kernel) and fused
             g.set_tuning(0, stack, 1, 1)
             _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
         g.set_graph(False)
