@@ -223,9 +223,10 @@ int bwt_gpu_start_table(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
  * every candidate setting (60), keeps the fastest, then picks the fastest
  * block-load form for it (4 more runs), then the direction split (3 more, fused
- * form only), then the start-table length among 0, 8, 10, 11 (4 more).
- * Optional table gets rows of {min_blocks (or -1 - load mode, -50 - split,
- * -100 - table length), blocks_per_sm, stack, chains_per_claim, search us}. */
+ * form only), then the start-table length among 0, 8, 10, 11 (4 more), then
+ * the idle-lane batch among 1, 4, 8, 16 (4 more).  Optional table gets rows of
+ * {min_blocks (or -1 - load mode, -50 - split, -100 - table length, -200 -
+ * idle batch), blocks_per_sm, stack, chains_per_claim, search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
                      int *rows);
