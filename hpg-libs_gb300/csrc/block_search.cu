@@ -1,0 +1,467 @@
+// block_search.cu -- the k-error block search of bwt_map_inexact_read_2
+// (c/src/aligners/bwt/bwt.c:2313-2470): BWSearchCPU (search/search.c:1171-1405)
+// on both strands, one GPU thread per (read, strand), with that function's
+// fragment size max(len / 2, 30) -- one or two fragments, so one error.
+//
+// The reference keeps its partial results in lists: an exact-partial pass
+// appends a branch point for every step where the interval size changes while
+// the error bound D still allows an error (BWExactPartialResults*,
+// search.c:471-646), then a branch pass extends each branch point by a
+// deletion and, per base, an insertion and a mismatch (BWBranchFinalResults*,
+// search.c:116-469).  A thread here replays the walk instead of storing it:
+//   * a first walk over the rest of the read counts the restarts D is made of
+//     (calculateD*, search.c:1045-1169: D at a step is the number of restarts
+//     still ahead, as a byte) and the branch points, so that a list that would
+//     overflow is known before anything is emitted (the reference then drops
+//     the block's branches);
+//   * within the exact-partial range D is the total (the walk has not failed
+//     yet) or the total minus one (the step where it fails), so the total is
+//     all the second walk needs to emit the branches in the reference's order.
+// Results go to a fixed number of slots per work item; the few items with more
+// results run again into an exact range once the counts are scanned.
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "engine_internal.hpp"
+
+namespace hpgbwt {
+
+namespace {
+
+constexpr uint32_t kBlockSlots = 4;  // result slots per (read, strand) in the first pass
+constexpr int kBlockTpb = 128;
+
+struct ItemOut {
+  hpg_hit_t* slot;  // the item's first result slot
+  uint32_t room;    // slots available; results past them are counted only
+  uint32_t cap;     // capacity of the reference's lists (max_results)
+  uint32_t n;       // results kept (<= cap)
+  uint32_t read;
+  uint32_t strand;
+  bool refused;     // a list refused a result (full)
+};
+
+// add_result (search/results.h:93-103) on rl_final.
+__device__ __forceinline__ bool emit(ItemOut& o, uint32_t dir, uint32_t nm, uint32_t kind, uint32_t base, int pos,
+                                     uint32_t k, uint32_t l) {
+  if (o.n >= o.cap) {
+    o.refused = true;
+    return false;
+  }
+  if (o.n < o.room) {
+    hpg_hit_t h;
+    h.read = o.read;
+    h.strand = (uint8_t)o.strand;
+    h.dir = (uint8_t)dir;
+    h.nm = (uint8_t)nm;
+    h.err_kind = (uint8_t)(nm ? kind : 0);
+    h.err_base = (uint8_t)(nm ? base : 0);
+    h.pad0 = 0;
+    h.err_pos = (int16_t)(nm ? pos : 0);
+    h.pad1 = 0;
+    h.k = k;
+    h.l = l;
+    o.slot[o.n] = h;
+  }
+  ++o.n;
+  return true;
+}
+
+// BWExactFinalResultForward (search/search.h:114-155): the block rule, then
+// the walk over W[pos..end]; k, l are updated only when it survives.
+__device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const uint8_t* W, int pos, int end, int bs,
+                                              int last_block, uint32_t& k, uint32_t& l) {
+  const int cb = pos / bs;
+  if (!(cb > last_block || pos == end + 1)) {
+    if (cb < last_block) return false;
+    if (pos % bs == 0) return false;
+  }
+  uint32_t a = k, b = l;
+  for (int i = pos; i <= end; ++i) {
+    bw_step(X, v, W[i], a, b);
+    if (a > b) return false;
+  }
+  k = a;
+  l = b;
+  return true;
+}
+
+// BWExactFinalResultBackward (search/search.h:67-112), over W[pos..start]
+// downwards.  C division truncates toward zero (pos may be -1).
+__device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const uint8_t* W, int pos, int start, int bs,
+                                               int last_block, uint32_t& k, uint32_t& l) {
+  const int cb = pos / bs;
+  if (!(cb < last_block || pos == start - 1)) {
+    if (cb > last_block) return false;
+    if ((pos + 1) % bs == 0) return false;
+  }
+  uint32_t a = k, b = l;
+  for (int i = pos; i >= start; --i) {
+    bw_step(X, v, W[i], a, b);
+    if (a > b) return false;
+  }
+  k = a;
+  l = b;
+  return true;
+}
+
+// The branches of one branch point (interval k..l before the step at `pos`)
+// in BWBranchFinalResultsForward's order for a result without an earlier
+// error (search.c:430-462): deletion, then per base an insertion and a
+// mismatch.  The mismatch starts from the interval the insertion's extension
+// left in the reference's result when that extension survived (the reference
+// resets only `pos` there).  False when rl_final refused a result.
+__device__ bool branch_forward(const DevIndex& X, View v, const uint8_t* W, int pos, int end, int bs, uint32_t k,
+                               uint32_t l, ItemOut& o) {
+  constexpr uint32_t kDir = 1;
+  uint32_t a = k, b = l;
+  if (final_forward(X, v, W, pos + 1, end, bs, 0, a, b) &&
+      !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
+    return false;
+  const uint32_t wp = W[pos];
+  for (uint32_t c = 0; c < 4; ++c) {
+    uint32_t ka = k, la = l;
+    bw_step(X, v, c, ka, la);
+    if (ka > la || c == wp) continue;
+    uint32_t rk = ka, rl = la;
+    a = ka;
+    b = la;
+    if (final_forward(X, v, W, pos, end, bs, 0, a, b)) {
+      if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
+      rk = a;
+      rl = b;
+    }
+    if (final_forward(X, v, W, pos + 1, end, bs, 0, rk, rl) && !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
+      return false;
+  }
+  return true;
+}
+
+// BWBranchFinalResultsBackward (search.c:252-284), the same on the backward side.
+__device__ bool branch_backward(const DevIndex& X, View v, const uint8_t* W, int pos, int bs, uint32_t k, uint32_t l,
+                                ItemOut& o) {
+  constexpr uint32_t kDir = 0;
+  constexpr int start = 0;
+  uint32_t a = k, b = l;
+  if (final_backward(X, v, W, pos - 1, start, bs, 0, a, b) &&
+      !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
+    return false;
+  const uint32_t wp = W[pos];
+  for (uint32_t c = 0; c < 4; ++c) {
+    uint32_t ka = k, la = l;
+    bw_step(X, v, c, ka, la);
+    if (ka > la || c == wp) continue;
+    uint32_t rk = ka, rl = la;
+    a = ka;
+    b = la;
+    if (final_backward(X, v, W, pos, start, bs, 0, a, b)) {
+      if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
+      rk = a;
+      rl = b;
+    }
+    if (final_backward(X, v, W, pos - 1, start, bs, 0, rk, rl) &&
+        !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
+      return false;
+  }
+  return true;
+}
+
+// First walk of a block from the interval k..l at `from` towards `to` (step
+// +1 or -1): the restart walk of calculateD* and, as its prefix up to the
+// first empty interval, the exact-partial walk.  Returns the number of branch
+// points that walk appends; `survive` whether it covers the whole range with
+// a non-empty interval (then k, l hold that interval).
+__device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int from, int to, int dstep, uint32_t& k,
+                               uint32_t& l, bool& survive, uint32_t& zt) {
+  uint32_t a = k, b = l;
+  uint32_t z = 0, changes = 0;
+  bool alive = true, failed_step = false;
+  for (int i = from; i != to + dstep; i += dstep) {
+    const int64_t before = (int64_t)b - (int64_t)a;
+    bw_step(X, v, W[i], a, b);
+    if (alive) {
+      if (a > b) {
+        alive = false;
+        failed_step = true;  // the step that empties the interval changes its size
+      } else if ((int64_t)b - (int64_t)a != before) {
+        ++changes;
+      }
+      if (alive) {
+        k = a;
+        l = b;
+      }
+    }
+    if (a > b) {
+      a = 0;
+      b = X.top;
+      ++z;
+    }
+  }
+  survive = alive;
+  zt = z & 255u;
+  // D before the failing step is the total; at it, the total minus one (bytes)
+  const bool bound_before = zt <= 1u;
+  const bool bound_at = ((zt - 1u) & 255u) <= 1u;
+  return (bound_before ? changes : 0u) + (failed_step && bound_at ? 1u : 0u);
+}
+
+__device__ __forceinline__ void put_anchor(hpg_block_anchor_t* anchors, uint32_t& na, uint32_t dir, int start, int end,
+                                           int pos, uint32_t k, uint32_t l) {
+  if (anchors) {
+    hpg_block_anchor_t x;
+    x.k = k;
+    x.l = l;
+    x.start = (int16_t)start;
+    x.end = (int16_t)end;
+    x.pos = (int16_t)pos;
+    x.dir = (uint8_t)dir;
+    x.pad = 0;
+    anchors[na] = x;
+  }
+  ++na;
+}
+
+// One (read, strand): BWSearchCPU with two fragments or fewer.
+__device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, ItemOut& o,
+                           hpg_block_anchor_t* anchors, uint32_t& na) {
+  // type 1 ('+', strand 0): backward = backward, forward = forward;
+  // type 0 ('-', strand 1): backward = forward_rev, forward = backward_rev (bwt.c:2440-2472)
+  const View bw = strand ? View{1, 1} : View{0, 0};
+  const View fw = strand ? View{0, 1} : View{1, 0};
+  int frag = len / 2;
+  if (frag < 30) frag = 30;
+  const int fragments = len / frag;
+  if (fragments <= 1) {  // search.c:1191-1224: one exact search of the whole read
+    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
+    int i;
+    if (strand) {  // type 0: forward search from the first base
+      for (i = 0; i <= len - 1; ++i) {
+        bw_step(X, fw, W[i], k, l);
+        if (k > l) break;
+        gk = k;
+        gl = l;
+      }
+      put_anchor(anchors, na, 1, 0, i - 1, i, gk, gl);
+      if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
+    } else {
+      for (i = len - 1; i >= 0; --i) {
+        bw_step(X, bw, W[i], k, l);
+        if (k > l) break;
+        gk = k;
+        gl = l;
+      }
+      put_anchor(anchors, na, 0, i + 1, len - 1, i, gk, gl);
+      if (k <= l) emit(o, 0, 0, 0, 0, 0, k, l);
+    }
+    return;
+  }
+  const int end = len - 1;
+
+  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
+  {
+    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
+    int i;
+    for (i = 0; i <= frag - 1; ++i) {
+      bw_step(X, fw, W[i], k, l);
+      if (k > l) break;
+      gk = k;
+      gl = l;
+    }
+    put_anchor(anchors, na, 1, 0, i - 1, i, gk, gl);
+    if (k <= l) {
+      if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
+        o.refused = true;
+        return;
+      }
+      // exact-partial range: pos = frag is past block 0, so the whole rest of
+      // the read, and a walk that survives it is a result (complete search)
+      uint32_t fk = k, fl = l, zt = 0;
+      bool survive = false;
+      const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt);
+      if (points > o.cap) {
+        o.refused = true;  // rl_next overflows: the block's branches are dropped
+      } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
+        const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
+        uint32_t a = k, b = l;
+        for (int p = frag; p <= end; ++p) {
+          const uint32_t pk = a, pl = b;
+          const int64_t before = (int64_t)b - (int64_t)a;
+          bw_step(X, fw, W[p], a, b);
+          const bool failed = a > b;
+          const bool changed = failed || (int64_t)b - (int64_t)a != before;
+          if (changed && (failed ? ok_at : ok_before) && !branch_forward(X, fw, W, p, end, frag, pk, pl, o)) break;
+          if (failed) break;
+        }
+      }
+    }
+  }
+
+  // last block: backward over W[frag .. len-1] (search.c:1360-1402)
+  {
+    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
+    int i;
+    for (i = end; i >= frag; --i) {
+      bw_step(X, bw, W[i], k, l);
+      if (k > l) break;
+      gk = k;
+      gl = l;
+    }
+    put_anchor(anchors, na, 0, i + 1, end, i, gk, gl);
+    if (k <= l) {
+      if (o.cap == 0) {
+        o.refused = true;
+        return;
+      }
+      // exact-partial range: pos = frag - 1 is the first element of block 0
+      // from above, so the rule walks the whole of it without completing
+      uint32_t fk = k, fl = l, zt = 0;
+      bool survive = false;
+      const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt);
+      if (points > o.cap) {
+        o.refused = true;
+      } else {
+        const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
+        uint32_t a = k, b = l;
+        for (int p = frag - 1; p >= 0; --p) {
+          const uint32_t pk = a, pl = b;
+          const int64_t before = (int64_t)b - (int64_t)a;
+          bw_step(X, bw, W[p], a, b);
+          const bool failed = a > b;
+          const bool changed = failed || (int64_t)b - (int64_t)a != before;
+          if (changed && (failed ? ok_at : ok_before) && !branch_backward(X, bw, W, p, frag, pk, pl, o)) break;
+          if (failed) break;
+        }
+      }
+    }
+  }
+}
+
+// Work item g runs item t = items ? items[g] : g (t = 2 * read + strand).
+// Results go to out + (slot_off ? slot_off[t] : t * room).
+__global__ void __launch_bounds__(kBlockTpb) block_search_kernel(
+    DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
+    uint32_t n_items, const uint32_t* __restrict__ items, const uint64_t* __restrict__ slot_off, uint32_t room,
+    uint32_t max_results, hpg_hit_t* __restrict__ out, uint32_t* __restrict__ count, uint8_t* __restrict__ refused,
+    hpg_block_anchor_t* __restrict__ anchors, uint8_t* __restrict__ n_anchors) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_items) return;
+  const uint32_t t = items ? items[g] : g;
+  const uint32_t read = t >> 1;
+  ItemOut o;
+  o.slot = out + (slot_off ? slot_off[t] : (uint64_t)t * room);
+  o.room = room;
+  o.cap = max_results;
+  o.n = 0;
+  o.read = read;
+  o.strand = t & 1u;
+  o.refused = false;
+  uint32_t na = 0;
+  const uint64_t b0 = offs[read];
+  const int len = (int)(offs[read + 1] - b0);
+  if (ok[read] && len >= 3 && len <= 32767)
+    block_item(X, codes + b0, len, o.strand, o, anchors ? anchors + 2ull * t : nullptr, na);
+  if (count) count[t] = o.n;
+  if (refused) refused[t] = o.refused ? 1 : 0;
+  if (n_anchors) n_anchors[t] = (uint8_t)na;
+}
+
+// The first pass's slots of each item, packed at its scanned offset.
+__global__ void block_pack_kernel(const hpg_hit_t* __restrict__ slots, const uint32_t* __restrict__ count,
+                                  const uint64_t* __restrict__ off, uint32_t n_items, hpg_hit_t* __restrict__ out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const uint32_t c = count[t] < kBlockSlots ? count[t] : kBlockSlots;
+  for (uint32_t j = 0; j < c; ++j) out[off[t] + j] = slots[(uint64_t)t * kBlockSlots + j];
+}
+
+unsigned grid_of(size_t n) { return (unsigned)((n + kBlockTpb - 1) / kBlockTpb); }
+
+}  // namespace
+
+int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t max_results,
+                        BlockSearchOut* out, std::string* err) {
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  out->hits.clear();
+  out->count.assign(2 * n, 0);
+  out->refused.assign(2 * n, 0);
+  out->anchors.assign(4 * n, hpg_block_anchor_t{});
+  out->n_anchors.assign(2 * n, 0);
+  out->kernel_ms = 0;
+  if (!n) return 0;
+  if (n >= (1ull << 30)) {
+    *err = "too many reads in one block search";
+    return -1;
+  }
+  if (upload_reads(e, seqs, offs, n, err) != 0) return -1;
+  const size_t T = 2 * n;
+  if (!ensure(e, e->slots, T * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->rs_count, T * 4 + 16) ||
+      !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
+      !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
+      !ensure(e, e->ovf, T + 16)) {
+    *err = oom_message("block search", T * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 14));
+    return -1;
+  }
+  cudaStream_t s = e->stream;
+  uint32_t* d_count = ptr<uint32_t>(e->rs_count);
+  uint64_t* d_off = ptr<uint64_t>(e->hit_off);
+  cudaEventRecord(e->cev[0], s);
+  count_launches(1);
+  block_search_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(
+      e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)T, nullptr, nullptr,
+      kBlockSlots, max_results, ptr<hpg_hit_t>(e->slots), d_count, ptr<uint8_t>(e->rs_trunc),
+      ptr<hpg_block_anchor_t>(e->vecs), ptr<uint8_t>(e->ovf));
+  cudaEventRecord(e->cev[1], s);
+  launch_scan(d_count, T, d_off, ptr<uint64_t>(e->scan_part), s);
+  HPG_CUDA(cudaMemcpyAsync(out->count.data(), d_count, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
+  uint64_t total = 0;
+  HPG_CUDA(cudaMemcpyAsync(&total, d_off + T, 8, cudaMemcpyDeviceToHost, s), "block total");
+  HPG_CUDA(cudaStreamSynchronize(s), "block search");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
+  out->kernel_ms = ms;
+  if (!ensure(e, e->hits, (total + 1) * sizeof(hpg_hit_t))) {
+    *err = oom_message("block search results", (total + 1) * sizeof(hpg_hit_t));
+    return -1;
+  }
+  hpg_hit_t* d_hits = ptr<hpg_hit_t>(e->hits);
+  count_launches(1);
+  block_pack_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->slots), d_count, d_off, (uint32_t)T, d_hits);
+  // items with more results than slots: the same search again, into their exact ranges
+  std::vector<uint32_t> again;
+  for (size_t t = 0; t < T; ++t)
+    if (out->count[t] > kBlockSlots) again.push_back((uint32_t)t);
+  if (!again.empty()) {
+    if (!ensure(e, e->rows, again.size() * 4 + 16)) {
+      *err = oom_message("block search retry list", again.size() * 4);
+      return -1;
+    }
+    HPG_CUDA(cudaMemcpyAsync(e->rows.p, again.data(), again.size() * 4, cudaMemcpyHostToDevice, s), "retry list");
+    cudaEventRecord(e->cev[0], s);
+    count_launches(1);
+    block_search_kernel<<<grid_of(again.size()), kBlockTpb, 0, s>>>(
+        e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)again.size(),
+        ptr<uint32_t>(e->rows), d_off, 0xFFFFFFFFu, max_results, d_hits, nullptr, nullptr, nullptr, nullptr);
+    cudaEventRecord(e->cev[1], s);
+  }
+  out->hits.resize(total);
+  if (total)
+    HPG_CUDA(cudaMemcpyAsync(out->hits.data(), d_hits, total * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
+             "block results");
+  HPG_CUDA(cudaMemcpyAsync(out->refused.data(), e->rs_trunc.p, T, cudaMemcpyDeviceToHost, s), "block flags");
+  HPG_CUDA(cudaMemcpyAsync(out->anchors.data(), e->vecs.p, 2 * T * sizeof(hpg_block_anchor_t),
+                           cudaMemcpyDeviceToHost, s),
+           "block anchors");
+  HPG_CUDA(cudaMemcpyAsync(out->n_anchors.data(), e->ovf.p, T, cudaMemcpyDeviceToHost, s), "block anchor counts");
+  HPG_CUDA(cudaStreamSynchronize(s), "block search results");
+  if (!again.empty()) {
+    cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
+    out->kernel_ms += ms;
+  }
+  e->block_ms = out->kernel_ms;
+  return 0;
+}
+
+float engine_block_ms(Engine* e) { return e->block_ms; }
+
+}  // namespace hpgbwt

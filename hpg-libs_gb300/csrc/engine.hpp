@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "hpg_bwt_records.h"
 #include "index_format.hpp"
@@ -110,6 +111,23 @@ struct MapRow {
 int engine_seed_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* seeds, size_t m,
                        uint32_t* out, std::string* err);
 int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, std::string* err);
+
+// The k-error block search of bwt_map_inexact_read_2 (block_search.cu): per
+// (read, strand) t = 2 * read + strand, count[t] results (hits of item t are
+// contiguous, items in order), refused[t] = 1 when a list of the search was
+// full, anchors[2 * t + a] for a < n_anchors[t].  Reads outside the alphabet
+// or outside 3..32767 bases get nothing.
+struct BlockSearchOut {
+  std::vector<hpg_hit_t> hits;
+  std::vector<uint32_t> count;
+  std::vector<uint8_t> refused;
+  std::vector<hpg_block_anchor_t> anchors;
+  std::vector<uint8_t> n_anchors;
+  float kernel_ms = 0;  // device time of the search kernel(s)
+};
+int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t max_results,
+                        BlockSearchOut* out, std::string* err);
+float engine_block_ms(Engine* e);  // kernel_ms of the last block search
 // Batched form: hits only, no located rows.
 void engine_set_skip_locate(Engine* e, int on);
 uint32_t engine_sa_top(Engine* e);  // last SA row (n)

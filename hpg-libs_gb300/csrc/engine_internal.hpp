@@ -121,6 +121,7 @@ struct Engine {
   bool use_graph = true;
   bool skip_locate = false;  // batched form: hits only, no located rows
   uint64_t locate_limit = 0;  // rows per (read, strand) list beyond which the list is not located; 0 = none
+  float block_ms = 0;         // device time of the last block search
 };
 
 // Grow-only device buffer; `keep` preserves the old contents.
@@ -163,6 +164,10 @@ inline T* ptr(DevBuf& b) {
   return static_cast<T*>(b.p);
 }
 
+
+// Reads to the engine's device buffers, encoded (codes + validity flags);
+// offsets may start anywhere (map_device.cu).
+int upload_reads(Engine* e, const char* seqs, const uint64_t* offs, size_t n, std::string* err);
 
 // Graph form of the batched pipeline (graph.cu).
 int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_t n, uint64_t total,

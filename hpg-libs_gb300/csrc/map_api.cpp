@@ -443,6 +443,269 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
   return out;
 }
 
+// ------------------------------------------------ inexact, block search --
+
+// The cigar of one block-search result and its operation count
+// (bwt.c:2513-2610); false for an error kind the reference skips.
+bool block_cigar(int error, int pos, size_t len, int type, int dir, char* cigar, size_t cap, int* nops) {
+  const unsigned long n = (unsigned long)len;
+  const size_t last = len - 1;
+  if (error == 0) {
+    std::snprintf(cigar, cap, "%lu=", n);
+    *nops = 1;
+  } else if (error == HPG_BWT_MISMATCH) {
+    if (pos == 0) {
+      std::snprintf(cigar, cap, type ? "1S%luM" : "%luM1S", n - 1);
+      *nops = 2;
+    } else if ((size_t)pos == last) {
+      std::snprintf(cigar, cap, type ? "%luM1S" : "1S%luM", n - 1);
+      *nops = 2;
+    } else {
+      std::snprintf(cigar, cap, "%luM", n);
+      *nops = 1;
+    }
+  } else if (error == HPG_BWT_INSERTION) {
+    if (pos == 0) {
+      std::snprintf(cigar, cap, type ? "1M1D%luM" : "%luM1D1M", n - 1);
+    } else if ((size_t)pos == last) {
+      std::snprintf(cigar, cap, type ? "%luM1D1M" : "1M1D%luM", n - 1);
+    } else if (type) {
+      if (dir) std::snprintf(cigar, cap, "%iM1D%luM", pos, n - (unsigned long)pos);
+      else std::snprintf(cigar, cap, "%iM1D%luM", pos + 1, n - (unsigned long)pos - 1);
+    } else {
+      if (dir) std::snprintf(cigar, cap, "%luM1D%dM", n - (unsigned long)pos, pos);
+      else std::snprintf(cigar, cap, "%luM1D%dM", n - (unsigned long)pos - 1, pos + 1);
+    }
+    *nops = 3;
+  } else if (error == HPG_BWT_DELETION) {
+    if (pos == 0) {
+      std::snprintf(cigar, cap, type ? "1I%luM" : "%luM1I", n - 1);
+      *nops = 2;
+    } else if ((size_t)pos == last) {
+      std::snprintf(cigar, cap, type ? "%luM1I" : "1I%luM", n - 1);
+      *nops = 2;
+    } else {
+      if (type) std::snprintf(cigar, cap, "%dM1I%luM", pos, n - (unsigned long)pos - 1);
+      else std::snprintf(cigar, cap, "%luM1I%dM", n - (unsigned long)pos - 1, pos);
+      *nops = 3;
+    }
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// Per read after the block search: the results each type maps until the
+// row filter is passed, and where their located rows start.
+struct BlockPlan {
+  int exceeded_type = -1;  // type whose results passed the filter (the loop stops there)
+  size_t hit0[2] = {0, 0};  // first result of each type in the result array
+  size_t nres[2] = {0, 0};  // results of each type that are mapped
+  size_t row0[2] = {0, 0};  // first located row of each type
+  size_t anchor_t = 0;      // item index of type 1 (type 0 is anchor_t + 1)
+};
+
+// Alignments of one read into its list (bwt.c:2313-2780, the anchors after).
+InexactOutcome assemble_block(const InexactRead& rd, const BlockPlan& P, const BlockSearchOut& B, const hpg_loc_t* loc,
+                              OutList& L) {
+  InexactOutcome res;
+  const size_t len = rd.len;
+  if (len < 5) {  // bwt.c:2321-2337
+    L.insert(new_alignment(nullptr, dup_bytes(rd.seq, len), fmt("%lu", 0), 0, (unsigned)-1, -1,
+                           fmt("%luX", (unsigned long)len), 1, 0, 0, 0));
+    res.added = 1;
+    return res;
+  }
+  std::string rc_store;
+  const char* strand_seq = rd.seq;
+  size_t num = 0;
+  for (int type = 1; type >= 0; --type) {
+    const size_t t = P.anchor_t + (type ? 0 : 1);
+    if (type == 0 && B.count[t]) {  // bwt.c:2477-2479
+      if (rd.revcomp) {
+        strand_seq = rd.revcomp;
+      } else {
+        rc_store.assign(rd.seq, len);
+        seq_reverse_complementary(&rc_store[0], (unsigned)len);
+        strand_seq = rc_store.data();
+      }
+    }
+    std::vector<alignment_t*> tmp;
+    size_t at = P.row0[type];
+    for (size_t h = 0; h < P.nres[type]; ++h) {
+      const hpg_hit_t& x = B.hits[P.hit0[type] + h];
+      const int error = x.nm ? x.err_kind : 0;
+      char cigar[96];
+      int nops = 0;
+      if (!block_cigar(error, x.err_pos, len, type, x.dir, cigar, sizeof cigar, &nops)) continue;
+      for (int64_t j = x.k; j <= x.l; ++j, ++at) {
+        const hpg_loc_t& q = loc[at];
+        if (!q.valid) continue;
+        tmp.push_back(new_alignment(nullptr, dup_bytes(strand_seq, len), fmt("%lu", 0), !type, q.chrom,
+                                    (int)(q.position + 1), dup_str(cigar), nops, 254, 1, num > 0));
+      }
+    }
+    if (P.exceeded_type == type) {  // bwt.c:2628-2633, 2655-2659 (its alignments were never made)
+      L.set_flag(2);
+      break;
+    }
+    // alignments closer than 10 bp on one chromosome (bwt.c:2661-2710)
+    const int nm = (int)tmp.size();
+    std::vector<uint8_t> del(nm, 0);
+    for (int a1 = nm - 1; a1 >= 1; --a1) {
+      if (del[a1]) continue;
+      for (int a2 = a1 - 1; a2 >= 0; --a2) {
+        const size_t dist = (size_t)std::abs(tmp[a1]->position - tmp[a2]->position);
+        if (tmp[a1]->chromosome == tmp[a2]->chromosome && dist < 10 && !del[a2]) {
+          if (tmp[a1]->num_cigar_operations < tmp[a2]->num_cigar_operations) del[a2] = 1;
+          else del[a1] = 1;
+        }
+      }
+    }
+    bool primary_delete = false;
+    for (int m = nm - 1; m >= 0; --m) {
+      alignment_t* a = tmp[m];
+      if (del[m]) {
+        if (!a->secondary_alignment) primary_delete = true;
+        alignment_free(a);
+      } else {
+        L.insert(a);
+        a->secondary_alignment = num > 0;
+        ++num;
+      }
+    }
+    if (primary_delete) static_cast<alignment_t*>(L.get(0))->secondary_alignment = 0;
+  }
+  res.added = num;
+  if (L.size() == 0) {
+    res.anchors = L.flag() == 1;
+  } else {  // bwt.c:2756-2772
+    const size_t idlen = std::strlen(rd.id);
+    for (size_t i = 0; i < L.size(); ++i) {
+      alignment_t* a = static_cast<alignment_t*>(L.get(i));
+      std::free(a->query_name);
+      a->query_name = first_blank(rd.id, idlen);
+      quality_copy(a, rd.quality);
+      optional_fields(a, num, (int)len);
+    }
+    L.set_flag(0);
+  }
+  return res;
+}
+
+// bwt_map_inexact_read_2 (bwt.c:2313-2797) for every read; one block search
+// and one locate pass for all of them, anchors in a third pass.
+std::vector<InexactOutcome> map_block(Engine* e, const std::vector<InexactRead>& rds, const bwt_optarg_t* opt,
+                                      std::vector<OutList*>& lists) {
+  const size_t n = rds.size();
+  std::string err;
+  const int fr = opt->filter_read_mappings;
+  // the reference's result lists hold filter_read_mappings results (bwt.c:2396-2400);
+  // a negative filter is a failed allocation there
+  if (fr < 0) fatal("bwt_map_inexact_read_2: filter_read_mappings is negative (result lists cannot be allocated)");
+  const size_t filter = (size_t)fr;
+  // 1. the block search for reads of 5+ bases
+  Reads R;
+  std::vector<uint32_t> gidx(n, UINT32_MAX);
+  for (size_t i = 0; i < n; ++i)
+    if (rds[i].len >= 5) {
+      gidx[i] = (uint32_t)R.n();
+      R.add(rds[i].seq, rds[i].len);
+    }
+  BlockSearchOut B;
+  if (engine_block_search(e, R.seq.data(), R.offs.data(), R.n(), (uint32_t)fr, &B, &err) != 0) fatal(err);
+  std::vector<uint64_t> item0(2 * R.n() + 1, 0);
+  for (size_t t = 0; t < 2 * R.n(); ++t) item0[t + 1] = item0[t] + B.count[t];
+  // 2. rows to locate: results in order until the rows passed the filter (bwt.c:2618-2634)
+  std::vector<BlockPlan> plan(n);
+  std::vector<MapRow> rows;
+  for (size_t i = 0; i < n; ++i) {
+    if (gidx[i] == UINT32_MAX) continue;
+    BlockPlan& P = plan[i];
+    const size_t g = gidx[i];
+    P.anchor_t = 2 * g;
+    size_t tot = 0;
+    for (int type = 1; type >= 0; --type) {
+      const size_t t = 2 * g + (type ? 0 : 1);
+      P.hit0[type] = item0[t];
+      P.row0[type] = rows.size();
+      for (uint64_t h = item0[t]; h < item0[t + 1]; ++h) {
+        const hpg_hit_t& x = B.hits[h];
+        tot += (size_t)(x.l - x.k);
+        if (tot > filter) {  // that type's alignments are dropped: nothing of it to locate
+          P.exceeded_type = type;
+          P.nres[type] = 0;
+          rows.resize(P.row0[type]);
+          break;
+        }
+        ++P.nres[type];
+        const int error = x.nm ? x.err_kind : 0;
+        uint32_t len_calc = (uint32_t)rds[i].len;
+        if (error == HPG_BWT_DELETION) --len_calc;
+        else if (error == HPG_BWT_INSERTION) ++len_calc;
+        const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)(type ? 0 : 1);  // direction = type ? dir : !dir
+        for (int64_t j = x.k; j <= x.l; ++j) rows.push_back(MapRow{(uint32_t)j, phys, len_calc});
+      }
+      if (P.exceeded_type >= 0) break;
+    }
+  }
+  std::vector<hpg_loc_t> loc(rows.size() + 1);
+  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  // 3. alignment records, reads in parallel when each has a list of its own
+  std::vector<InexactOutcome> out(n);
+  bool own_lists = true;
+  {
+    std::vector<const void*> seen;
+    for (size_t i = 0; i < n; ++i)
+      if (lists[i]->list) seen.push_back(lists[i]->list);
+    std::sort(seen.begin(), seen.end());
+    own_lists = std::adjacent_find(seen.begin(), seen.end()) == seen.end();
+  }
+#pragma omp parallel for schedule(dynamic, 256) if (own_lists && n > 256)
+  for (size_t i = 0; i < n; ++i) out[i] = assemble_block(rds[i], plan[i], B, loc.data(), *lists[i]);
+  // 4. anchors of reads left without alignments in a list flagged 1 (bwt.c:2737-2754):
+  //    the anchors BWSearchCPU left, '+' then '-', each located by
+  //    __bwt_generate_anchor_list (bwt.c:1822-1869) when it spans at most 50 rows
+  struct Want {
+    size_t read;
+    int type, kind;
+    uint32_t nt;
+  };
+  std::vector<Want> wants;
+  rows.clear();
+  for (size_t i = 0; i < n; ++i) {
+    if (!out[i].anchors || gidx[i] == UINT32_MAX) continue;
+    const size_t len = rds[i].len;
+    for (int type = 1; type >= 0; --type) {
+      const size_t t = plan[i].anchor_t + (type ? 0 : 1);
+      for (uint32_t a = 0; a < B.n_anchors[t]; ++a) {
+        const hpg_block_anchor_t& x = B.anchors[2 * t + a];
+        int kind;
+        if ((size_t)(int64_t)x.end == len - 1) kind = type ? BACKWARD_ANCHOR : FORWARD_ANCHOR;
+        else if (x.start == 0) kind = type ? FORWARD_ANCHOR : BACKWARD_ANCHOR;
+        else continue;
+        const uint32_t nt = (uint32_t)(x.end - x.start + 1);
+        const size_t k = (size_t)x.k, l = (size_t)x.l;
+        if (!(l - k < 50)) continue;
+        for (size_t j = k; j <= l; ++j) {
+          rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt});
+          wants.push_back(Want{i, type, kind, nt});
+        }
+      }
+    }
+  }
+  if (wants.empty()) return out;
+  loc.assign(rows.size() + 1, hpg_loc_t{});
+  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
+  for (size_t w = 0; w < wants.size(); ++w) {
+    if (!loc[w].valid) continue;
+    const Want& W = wants[w];
+    lists[W.read]->insert(bwt_anchor_new(!W.type, (int)loc[w].chrom, loc[w].position + 1,
+                                         loc[w].position + W.nt, W.kind));
+  }
+  return out;
+}
+
 InexactRead read_of(const fastq_read_t* r) {
   return InexactRead{r->id, r->sequence, std::strlen(r->sequence), r->revcomp, r->quality};
 }
@@ -644,6 +907,46 @@ size_t bwt_map_inexact_array_list(array_list_t* reads, bwt_optarg_t* opt, bwt_in
     before[i] = array_list_size(lists[i]);
   }
   auto res = map_inexact(e, rds, opt, out);
+  size_t total = 0;
+  *num_unmapped = 0;
+  for (size_t i = 0; i < n; ++i) {
+    bool mapped = false;
+    for (size_t j = before[i]; j < array_list_size(lists[i]) && j < before[i] + res[i].added; ++j)
+      mapped = mapped || static_cast<alignment_t*>(array_list_get(j, lists[i]))->is_seq_mapped;
+    total += res[i].added;
+    if (!mapped) unmapped_indices[(*num_unmapped)++] = i;
+  }
+  return total;
+}
+
+size_t bwt_map_inexact_read_2(fastq_read_t* read, bwt_optarg_t* opt, bwt_index_t* index, array_list_t* mapping_list) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  std::vector<InexactRead> rds{read_of(read)};
+  OutList L;
+  L.list = mapping_list;
+  std::vector<OutList*> lists{&L};
+  map_block(e, rds, opt, lists);
+  if (rds[0].len < 5) return 1;  // bwt.c:2337
+  return array_list_size(mapping_list);
+}
+
+size_t bwt_map_inexact_array_list_2(array_list_t* reads, bwt_optarg_t* opt, bwt_index_t* index, array_list_t** lists,
+                                    size_t* num_unmapped, size_t* unmapped_indices) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Engine* e = engine_for(index);
+  const size_t n = array_list_size(reads);
+  std::vector<InexactRead> rds(n);
+  std::vector<OutList> L(n);
+  std::vector<OutList*> out(n);
+  std::vector<size_t> before(n);
+  for (size_t i = 0; i < n; ++i) {
+    rds[i] = read_of(static_cast<fastq_read_t*>(array_list_get(i, reads)));
+    L[i].list = lists[i];
+    out[i] = &L[i];
+    before[i] = array_list_size(lists[i]);
+  }
+  auto res = map_block(e, rds, opt, out);
   size_t total = 0;
   *num_unmapped = 0;
   for (size_t i = 0; i < n; ++i) {

@@ -107,7 +107,8 @@ __global__ void seed_search_kernel(DevIndex X, const uint8_t* __restrict__ codes
   out[t] = o;
 }
 
-// Reads to the engine's device buffers, encoded (codes + validity flags).
+}  // namespace
+
 int upload_reads(Engine* e, const char* seqs, const uint64_t* offs, size_t n, std::string* err) {
   cudaStream_t s = e->stream;
   const uint64_t total = n ? offs[n] - offs[0] : 0;
@@ -125,6 +126,8 @@ int upload_reads(Engine* e, const char* seqs, const uint64_t* offs, size_t n, st
   HPG_CUDA(cudaStreamSynchronize(s), "encode");  // `rel` is pageable and local
   return 0;
 }
+
+namespace {
 
 int check_walk(Engine* e, std::string* err) {
   uint32_t derr = 0;

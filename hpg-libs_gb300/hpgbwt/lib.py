@@ -18,6 +18,7 @@ LIB_PATH = Path(__file__).resolve().parent.parent / "libhpgbwt.so"
 
 MODE_EXACT = 0
 MODE_SEARCH1 = 1
+MODE_BLOCK = 2
 FORM_PLAIN = 0
 FORM_BATCHED = 1
 
@@ -26,7 +27,9 @@ HIT_DTYPE = np.dtype([("read", "<u4"), ("strand", "u1"), ("dir", "u1"), ("nm", "
                       ("l", "<i8")])
 LOC_DTYPE = np.dtype([("key", "<u8"), ("position", "<u8"), ("hit", "<u4"), ("chrom", "<u4"), ("valid", "<u4"),
                       ("pad", "<u4")])
-assert HIT_DTYPE.itemsize == 32 and LOC_DTYPE.itemsize == 32
+ANCHOR_DTYPE = np.dtype([("k", "<i8"), ("l", "<i8"), ("start", "<i2"), ("end", "<i2"), ("pos", "<i2"),
+                         ("dir", "u1"), ("pad", "u1")])
+assert HIT_DTYPE.itemsize == 32 and LOC_DTYPE.itemsize == 32 and ANCHOR_DTYPE.itemsize == 24
 
 
 class ResultSetC(ctypes.Structure):
@@ -47,6 +50,29 @@ class Result:
         return (np.array_equal(self.hits, other.hits) and np.array_equal(self.locs, other.locs)
                 and np.array_equal(self.rs_count, other.rs_count)
                 and np.array_equal(self.rs_truncated, other.rs_truncated))
+
+
+@dataclass
+class BlockResult:
+    """k-error block search output: the result set plus the anchors, anchors[2 * (2 * read + strand) + a]
+    valid for a < n_anchors[2 * read + strand]."""
+    result: Result
+    anchors: np.ndarray
+    n_anchors: np.ndarray
+
+    def used_anchors(self) -> np.ndarray:
+        """The valid anchors in (read, strand, order) order, unused slots dropped."""
+        keep = np.arange(2)[None, :] < self.n_anchors[:, None]
+        return self.anchors.reshape(-1, 2)[keep]
+
+    def equal(self, other: "BlockResult", truncation: bool = True) -> bool:
+        a, b = self.result, other.result
+        same = (np.array_equal(a.hits, b.hits) and np.array_equal(a.locs, b.locs)
+                and np.array_equal(a.rs_count, b.rs_count))
+        if truncation:
+            same = same and np.array_equal(a.rs_truncated, b.rs_truncated)
+        return (same and np.array_equal(self.n_anchors, other.n_anchors)
+                and np.array_equal(self.used_anchors(), other.used_anchors()))
 
 
 def _arr(ptr: int | None, n: int, dt: np.dtype) -> np.ndarray:
@@ -127,6 +153,12 @@ def load() -> ctypes.CDLL:
     lib.cal_free.argtypes = [vp]
     lib.bwt_map_inexact_batch.restype = sz
     lib.bwt_map_inexact_batch.argtypes = [vp, vp, vp, vp, vp]
+    lib.bwt_map_inexact_array_list_2.restype = sz
+    lib.bwt_map_inexact_array_list_2.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.array_list_insert.argtypes = [vp, vp]
+    lib.bwt_gpu_block_search.argtypes = [vp, vp, vp, sz, u32, ctypes.POINTER(ResultSetC), vp, vp]
+    lib.bwt_gpu_block_search_ms.restype = ctypes.c_float
+    lib.bwt_gpu_block_search_ms.argtypes = [vp]
     lib.alignment_free.argtypes = [vp]
     lib.bwt_generate_cals_batch.restype = sz
     lib.bwt_generate_cals_batch.argtypes = [vp, sz, sz, vp, vp, vp, vp, ctypes.c_uint]
@@ -215,6 +247,25 @@ class GpuIndex:
             return result_from_c(rs, n)
         finally:
             self.lib.bwt_gpu_result_free(ctypes.byref(rs))
+
+    def block_search(self, reads, max_results: int = 1 << 16) -> BlockResult:
+        """k-error block search (bwt_gpu_block_search) of a synth.ReadSet-like object, with anchors."""
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        anchors = np.zeros(4 * n + 1, dtype=ANCHOR_DTYPE)
+        n_anchors = np.zeros(2 * n + 1, dtype=np.uint8)
+        rs = ResultSetC()
+        self._check(self.lib.bwt_gpu_block_search(self.handle, seq.ctypes.data, offs.ctypes.data, n, max_results,
+                                                  ctypes.byref(rs), anchors.ctypes.data, n_anchors.ctypes.data))
+        try:
+            return BlockResult(result_from_c(rs, n), anchors[:4 * n], n_anchors[:2 * n])
+        finally:
+            self.lib.bwt_gpu_result_free(ctypes.byref(rs))
+
+    def block_search_ms(self) -> float:
+        """Device time of the last block search's kernel(s)."""
+        return float(self.lib.bwt_gpu_block_search_ms(self.handle))
 
     def search_device(self, d_seqs: int, d_offs: int, n_reads: int, total_bases: int, max_len: int,
                       mode: int = MODE_SEARCH1, form: int = FORM_PLAIN, max_results: int = 1 << 16) -> ResultSetC:
@@ -353,6 +404,49 @@ class GpuIndex:
             self.lib.array_list_free(lst, ctypes.cast(self.lib.alignment_free, ctypes.c_void_p))
             self.lib.bwt_optarg_free(opt)
         return count
+
+    def map_block_array_list(self, reads: list[bytes], filter_read_mappings: int = 200) -> int:
+        """bwt_map_inexact_array_list_2 (every read as bwt_map_inexact_read_2 maps it) over the
+        reads: the number of alignment records (built and freed); the C call's wall time
+        is left in last_map_seconds."""
+
+        class FastqRead(ctypes.Structure):  # c/src/bioformats/fastq/fastq_read.h:20-32
+            _fields_ = [("id", ctypes.c_void_p), ("sequence", ctypes.c_void_p), ("revcomp", ctypes.c_void_p),
+                        ("quality", ctypes.c_void_p), ("rev_quality", ctypes.c_void_p),
+                        ("adapter", ctypes.c_void_p), ("adapter_revcomp", ctypes.c_void_p),
+                        ("adapter_quality", ctypes.c_void_p), ("length", ctypes.c_int),
+                        ("adapter_length", ctypes.c_int), ("adapter_strand", ctypes.c_int)]
+        n = len(reads)
+        seq = ctypes.create_string_buffer(b"".join(r + b"\0" for r in reads))
+        qual = ctypes.create_string_buffer(b"".join(b"I" * len(r) + b"\0" for r in reads))
+        ids = ctypes.create_string_buffer(b"".join(b"r%d\0" % i for i in range(n)))
+        so, io = 0, 0
+        recs = (FastqRead * max(1, n))()
+        for i, r in enumerate(reads):
+            recs[i].id = ctypes.addressof(ids) + io
+            recs[i].sequence = ctypes.addressof(seq) + so
+            recs[i].quality = ctypes.addressof(qual) + so
+            recs[i].length = len(r)
+            so += len(r) + 1
+            io += len(b"r%d" % i) + 1
+        rl = self.lib.array_list_new(max(16, n), 1.25, 2)
+        for i in range(n):
+            self.lib.array_list_insert(ctypes.addressof(recs[i]), rl)
+        lists = (ctypes.c_void_p * max(1, n))(*[self.lib.array_list_new(4, 1.25, 2) for _ in range(n)])
+        unmapped = (ctypes.c_size_t * max(1, n))()
+        n_un = ctypes.c_size_t()
+        opt = self.lib.bwt_optarg_new(1, 1, filter_read_mappings, filter_read_mappings)
+        try:
+            t0 = time.perf_counter()
+            total = self.lib.bwt_map_inexact_array_list_2(rl, opt, self.handle, lists, ctypes.byref(n_un), unmapped)
+            self.last_map_seconds = time.perf_counter() - t0
+        finally:
+            free = ctypes.cast(self.lib.alignment_free, ctypes.c_void_p)
+            for i in range(n):
+                self.lib.array_list_free(lists[i], free)
+            self.lib.array_list_free(rl, None)
+            self.lib.bwt_optarg_free(opt)
+        return int(total)
 
     def set_locate_limit(self, max_rows: int) -> None:
         """Lists (read, strand) covering more than max_rows rows are not located (rs_truncated bit 1); 0 = none."""

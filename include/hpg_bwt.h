@@ -137,6 +137,24 @@ int hpg_bwt_build_index_on(const char *ref_file, const char *output_dir, unsigne
 int bwt_gpu_search_batch(bwt_index_t *index, int mode, int form, const char *seqs, const uint64_t *offsets,
                          size_t n_reads, uint32_t max_results, hpg_result_set_t *out);
 void bwt_gpu_result_free(hpg_result_set_t *out);
+/* k-error block search of bwt_map_inexact_read_2 (bwt.c:2401-2470): the
+ * search layer's BWSearchCPU (search/search.h:200, search/search.c:1171-1405)
+ * per strand, '+' over (backward, forward) and '-' over (forward_rev,
+ * backward_rev), with the fragment size max(len / 2, 30) -- one or two
+ * fragments, one error -- and result lists of capacity max_results.
+ * out: hits in rl_final order per (read, strand) and every row of every hit
+ * located as bwt.c:2640-2650 (0-based positions; the locate limit applies);
+ * rs_truncated bit 0 = a list of the search refused a result (full).
+ * anchors (4 n_reads entries) and n_anchors (2 n_reads), either may be NULL:
+ * the rl_anchor results of the search, anchors[2 * (2 * read + strand) + a]
+ * for a < n_anchors[2 * read + strand].  Reads as bwt_gpu_search_batch (3 to
+ * 32767 bases in the alphabet, others get nothing).  Release out with
+ * bwt_gpu_result_free.  Returns 0, or -1 (see bwt_gpu_last_error). */
+int bwt_gpu_block_search(bwt_index_t *index, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                         uint32_t max_results, hpg_result_set_t *out, hpg_block_anchor_t *anchors,
+                         uint8_t *n_anchors);
+/* Device time of the last bwt_gpu_block_search's search kernel(s), ms. */
+float bwt_gpu_block_search_ms(bwt_index_t *index);
 
 /* Device-resident form for callers that keep reads in GPU memory: d_seqs and
  * d_offsets are device pointers (offsets relative to d_seqs; total_bases =

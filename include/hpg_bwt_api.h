@@ -355,6 +355,28 @@ size_t bwt_map_inexact_batch(fastq_batch_t *batch, bwt_optarg_t *bwt_optarg, bwt
 size_t bwt_map_inexact_array_list(array_list_t *reads, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
                                   array_list_t **lists, size_t *num_unmapped, size_t *unmapped_indices);
 
+/* ---- inexact mapping by the k-error block search (bwt.h:559, bwt.c:2313-2797) ----
+ * BWSearchCPU on both strands with fragments of max(len / 2, 30) bases (one
+ * error), result lists of capacity filter_read_mappings; every result becomes
+ * alignments: cigar "<len>=" for exact results, soft clips or M/I/D for
+ * one-error ones (bwt.c:2513-2610), 1-based positions, map quality 254 (NM
+ * 254 after the optional fields), the query name's first word.  Rows are
+ * counted over both strands as l - k per result; past filter_read_mappings
+ * the strand's alignments are dropped, the '-' strand is not searched after
+ * the '+' one passed, and the list flag becomes 2 (0 again when alignments
+ * remain).  Alignments closer than 10 bp on one chromosome are merged.  When
+ * the list ends empty with flag 1, the block anchors that touch a read end are
+ * located as bwt_anchor_t items (at most 50 rows each).  Reads shorter than 5
+ * bases get one unmapped record.  A negative filter_read_mappings exits, as
+ * the reference's list allocation does. */
+size_t bwt_map_inexact_read_2(fastq_read_t *read, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                              array_list_t *mapping_list);
+/* No counterpart in the reference: reads[i] (fastq_read_t *) mapped as
+ * bwt_map_inexact_read_2 maps it into lists[i], all reads in one GPU pass;
+ * unmapped_indices lists the reads that got no alignment. */
+size_t bwt_map_inexact_array_list_2(array_list_t *reads, bwt_optarg_t *bwt_optarg, bwt_index_t *index,
+                                    array_list_t **lists, size_t *num_unmapped, size_t *unmapped_indices);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,10 @@ extern "C" {
                                   '-' over forward_rev (search/search.h:9-36). */
 #define HPG_BWT_MODE_SEARCH1 1 /* 4 vector searches + BWSearch1VectorHelper per strand,
                                   as bwt.c:1940-2002. */
+#define HPG_BWT_MODE_BLOCK   2 /* k-error block search BWSearchCPU per strand with the
+                                  fragment size of bwt_map_inexact_read_2 (bwt.c:2413-2470;
+                                  search/search.c:1171-1405): max(len / 2, 30), so one
+                                  error; hits in rl_final order. bwt_gpu_block_search. */
 
 /* Error kinds (c/src/aligners/bwt/bwt_commons.h:15-18). DELETION means one
  * extra base in the read, INSERTION one base missing from it. */
@@ -64,6 +68,21 @@ typedef struct {
   uint32_t valid;    /* key + len_calc <= offset[idx] (bwt.c:2164) */
   uint32_t pad;
 } hpg_loc_t;         /* 32 bytes */
+
+/* Anchor of the k-error block search: the `result` one block's exact search
+ * leaves in rl_anchor (BWExactSearchBackward/Forward with r_anchor,
+ * search/search.h:9-65, called from BWSearchCPU, search/search.c:1171-1405):
+ * the last non-empty interval before the first failing base and the read span
+ * it matched.  At most two per (read, strand), in the order BWSearchCPU adds
+ * them (the first block's forward search, then the last block's backward one). */
+typedef struct {
+  int64_t k, l;      /* 0, 0 when the block's first base already failed */
+  int16_t start;     /* matched span start..end; end = start - 1 when empty */
+  int16_t end;
+  int16_t pos;       /* where the search stopped */
+  uint8_t dir;       /* 0 backward search, 1 forward search */
+  uint8_t pad;
+} hpg_block_anchor_t; /* 24 bytes */
 
 typedef struct {
   size_t n_reads;

@@ -20,6 +20,8 @@
  *   BWSearch1VectorHelper .................. search/search.c:1491-1709
  *   add_result (truncation) ................ search/results.h:93-103
  *   per-read driver ........................ bwt.c:1940-2002
+ *   k-error block search BWSearchCPU ....... search/search.c:1-646,1045-1405; search/search.h:9-155
+ *     as bwt_map_inexact_read_2 drives it .. bwt.c:2401-2470 (one or two fragments)
  *   locate + karyotype ..................... bwt.c:2025-2036, 2158-2166; search/io.h:43-64
  *   index files ............................ search/csafm.c:121-250, search/io.c:26-81,336-362
  */
@@ -505,6 +507,456 @@ static void locate(const fmo_index_t *ix, sink_t *s, uint32_t hid, int64_t k, in
   }
 }
 
+/* ------------------------------------------------ k-error block search -- */
+/*
+ * BWSearchCPU (search/search.c:1171-1405) as bwt_map_inexact_read_2 drives it
+ * (bwt.c:2413-2470): fragment size max(len / 2, 30), hence one or two
+ * fragments and at most one error.  Three or more fragments need
+ * change_direction (search/search.h:157-198), which reads the inverse suffix
+ * array (R/Ri files) that the reference's index generator does not write; no
+ * reference entry point reaches them, and this restatement refuses them.
+ *
+ * Results live in lists with the reference's capacity rule (add_result,
+ * search/results.h:93-103): a full list refuses the result and the function
+ * that tried returns at once ("true").  A list entry is updated in place, as
+ * the reference updates the `result` it iterates over.
+ */
+
+typedef struct {
+  uint8_t dir, nm, kind, base;
+  int16_t err_pos, start, pos, end;
+  int64_t k, l;
+} bres_t; /* the fields of `result` this search touches (one error at most) */
+
+typedef struct {
+  bres_t *v;
+  uint32_t n, cap;
+  int refused; /* a result was refused (reported in rs_truncated bit 0) */
+} blist_t;
+
+static int blist_add(blist_t *L, const bres_t *r) {
+  if (L->n >= L->cap) {
+    L->refused = 1;
+    return 1;
+  }
+  L->v[L->n++] = *r;
+  return 0;
+}
+
+/* BWExactSearchForward/Backward with an anchor (search/search.h:9-65). */
+static void block_exact_forward(const uint8_t *W, const fmo_view_t *v, bres_t *r, bres_t *a) {
+  int64_t k = 0, l = 0, k2 = r->k, l2 = r->l;
+  int16_t i;
+  for (i = r->pos; i <= r->end; i++) {
+    step(v, W[i], &k2, &l2);
+    if (k2 > l2) break;
+    k = k2;
+    l = l2;
+  }
+  memset(a, 0, sizeof *a);
+  a->dir = 1;
+  a->start = r->pos;
+  a->end = (int16_t)(i - 1);
+  a->k = k;
+  a->l = l;
+  a->pos = i;
+  r->k = k2;
+  r->l = l2;
+  r->pos = i;
+}
+
+static void block_exact_backward(const uint8_t *W, const fmo_view_t *v, bres_t *r, bres_t *a) {
+  int64_t k = 0, l = 0, k2 = r->k, l2 = r->l;
+  int16_t i;
+  for (i = r->pos; i >= r->start; i--) {
+    step(v, W[i], &k2, &l2);
+    if (k2 > l2) break;
+    k = k2;
+    l = l2;
+  }
+  memset(a, 0, sizeof *a);
+  a->dir = 0;
+  a->start = (int16_t)(i + 1);
+  a->end = r->pos;
+  a->k = k;
+  a->l = l;
+  a->pos = i;
+  r->k = k2;
+  r->l = l2;
+  r->pos = i;
+}
+
+/* calculateDBackward / calculateDForward (search/search.c:1045-1169): per
+ * position, how many restarts of a greedy exact walk the rest of the read
+ * needs -- the lower bound on errors left.  Byte arithmetic as the reference's
+ * (uint8_t counter, int8_t total). */
+static void block_d_backward(uint8_t *D, const uint8_t *W, int16_t nW, const fmo_view_t *bw, const fmo_view_t *fw,
+                             const bres_t *r, int64_t top) {
+  uint8_t z = 0;
+  int8_t last;
+  int64_t k = r->k, l = r->l;
+  for (int16_t i = r->pos; i >= 0; i--) {
+    step(bw, W[i], &k, &l);
+    if (k > l) {
+      k = 0;
+      l = top;
+      z++;
+    }
+    D[i] = z;
+  }
+  if (r->end == nW - 1) {
+    last = (int8_t)D[0];
+  } else {
+    k = 0;
+    l = top;
+    for (int16_t i = (int16_t)(r->end + 1); i < nW; i++) {
+      step(fw, W[i], &k, &l);
+      if (k > l) {
+        k = 0;
+        l = top;
+        z++;
+      }
+      D[i] = z;
+    }
+    last = (int8_t)D[nW - 1];
+    for (int16_t i = (int16_t)(r->end + 1); i < nW; i++) D[i] = (uint8_t)(last - D[i]);
+  }
+  for (int16_t i = r->pos; i >= 0; i--) D[i] = (uint8_t)(last - D[i]);
+}
+
+static void block_d_forward(uint8_t *D, const uint8_t *W, int16_t nW, const fmo_view_t *bw, const fmo_view_t *fw,
+                            const bres_t *r, int64_t top) {
+  uint8_t z = 0;
+  int8_t last;
+  int64_t k = r->k, l = r->l;
+  for (int16_t i = r->pos; i < nW; i++) {
+    step(fw, W[i], &k, &l);
+    if (k > l) {
+      k = 0;
+      l = top;
+      z++;
+    }
+    D[i] = z;
+  }
+  if (r->start == 0) {
+    last = (int8_t)D[nW - 1];
+  } else {
+    k = 0;
+    l = top;
+    for (int16_t i = (int16_t)(r->start - 1); i >= 0; i--) {
+      step(bw, W[i], &k, &l);
+      if (k > l) {
+        k = 0;
+        l = top;
+        z++;
+      }
+      D[i] = z;
+    }
+    last = (int8_t)D[0];
+    for (int16_t i = (int16_t)(r->start - 1); i >= 0; i--) D[i] = (uint8_t)(last - D[i]);
+  }
+  for (int16_t i = r->pos; i < nW; i++) D[i] = (uint8_t)(last - D[i]);
+}
+
+/* BWExactPartialResultsBackward/Forward (search/search.c:471-646): walk each
+ * result to the end of the block rule's range; every step whose interval
+ * size changes while the error bound D allows one more error is a branch
+ * point (rl_next); a walk that covers the rest of the read survives
+ * (rl_next_i). */
+static int block_partial_backward(const uint8_t *W, const uint8_t *D, uint8_t max_errors, const fmo_view_t *v,
+                                  blist_t *prev, blist_t *next, blist_t *next_i, int16_t bs, int16_t last_block) {
+  for (uint32_t ii = 0; ii < prev->n; ii++) {
+    bres_t *r = &prev->v[ii];
+    const int16_t start = r->start, pos = r->pos;
+    int64_t k = 0, l = 0, k_next = r->k, l_next = r->l;
+    int64_t results, results_next = l_next - k_next;
+    const int16_t cb = (int16_t)(pos / bs);
+    const uint8_t bound = (uint8_t)(max_errors - r->nm);
+    int16_t lbp;
+    int complete;
+    if (cb < last_block || pos == start - 1) {
+      lbp = start;
+      complete = 1;
+    } else if (cb > last_block) {
+      lbp = (int16_t)(((pos + 1) % bs) ? (cb - 1) * bs : cb * bs);
+      complete = 0;
+    } else if ((pos + 1) % bs) {
+      lbp = start;
+      complete = 1;
+    } else {
+      lbp = (int16_t)(cb * bs);
+      complete = 0;
+    }
+    for (int16_t i = pos; i >= lbp; i--) {
+      k = k_next;
+      l = l_next;
+      if (k > l) break;
+      step(v, W[i], &k_next, &l_next);
+      results = results_next;
+      results_next = l_next - k_next;
+      if (results == results_next || bound < D[i]) continue;
+      r->k = k;
+      r->l = l;
+      r->pos = i;
+      if (blist_add(next, r)) return 1;
+    }
+    if (complete && k_next <= l_next) {
+      r->k = k_next;
+      r->l = l_next;
+      r->pos = (int16_t)(start - 1);
+      if (blist_add(next_i, r)) return 1;
+    }
+  }
+  prev->n = 0;
+  return 0;
+}
+
+static int block_partial_forward(const uint8_t *W, const uint8_t *D, uint8_t max_errors, const fmo_view_t *v,
+                                 blist_t *prev, blist_t *next, blist_t *next_i, int16_t bs, int16_t last_block) {
+  for (uint32_t ii = 0; ii < prev->n; ii++) {
+    bres_t *r = &prev->v[ii];
+    const int16_t pos = r->pos, end = r->end;
+    int64_t k = 0, l = 0, k_next = r->k, l_next = r->l;
+    int64_t results, results_next = l_next - k_next;
+    const int16_t cb = (int16_t)(pos / bs);
+    const uint8_t bound = (uint8_t)(max_errors - r->nm);
+    int16_t lbp;
+    int complete;
+    if (cb > last_block || pos == end + 1) {
+      lbp = end;
+      complete = 1;
+    } else if (cb < last_block) {
+      lbp = (int16_t)((pos % bs) ? (cb + 2) * bs - 1 : (cb + 1) * bs - 1);
+      complete = 0;
+    } else if (pos % bs) {
+      lbp = end;
+      complete = 1;
+    } else {
+      lbp = (int16_t)((cb + 1) * bs - 1);
+      complete = 0;
+    }
+    for (int16_t i = pos; i <= lbp; i++) {
+      k = k_next;
+      l = l_next;
+      if (k > l) break;
+      step(v, W[i], &k_next, &l_next);
+      results = results_next;
+      results_next = l_next - k_next;
+      if (results == results_next || bound < D[i]) continue;
+      r->k = k;
+      r->l = l;
+      r->pos = i;
+      if (blist_add(next, r)) return 1;
+    }
+    if (complete && k_next <= l_next) {
+      r->k = k_next;
+      r->l = l_next;
+      r->pos = (int16_t)(end + 1);
+      if (blist_add(next_i, r)) return 1;
+    }
+  }
+  prev->n = 0;
+  return 0;
+}
+
+/* BWExactFinalResultBackward/Forward (search/search.h:67-155): extend one
+ * result over the rest of its range unless the block rule skips it. */
+static int block_final_backward(const uint8_t *W, const fmo_view_t *v, bres_t *r, blist_t *fin, int16_t bs,
+                                int16_t last_block) {
+  const int16_t start = r->start, pos = r->pos;
+  const int16_t cb = (int16_t)(pos / bs);
+  if (!(cb < last_block || pos == start - 1)) {
+    if (cb > last_block) return 0;
+    if (!((pos + 1) % bs)) return 0;
+  }
+  int64_t k = r->k, l = r->l;
+  for (int16_t i = pos; i >= start; i--) {
+    step(v, W[i], &k, &l);
+    if (k > l) break;
+  }
+  if (k <= l) {
+    r->k = k;
+    r->l = l;
+    r->pos = (int16_t)(start - 1);
+    return blist_add(fin, r);
+  }
+  return 0;
+}
+
+static int block_final_forward(const uint8_t *W, const fmo_view_t *v, bres_t *r, blist_t *fin, int16_t bs,
+                               int16_t last_block) {
+  const int16_t pos = r->pos, end = r->end;
+  const int16_t cb = (int16_t)(pos / bs);
+  if (!(cb > last_block || pos == end + 1)) {
+    if (cb < last_block) return 0;
+    if (!(pos % bs)) return 0;
+  }
+  int64_t k = r->k, l = r->l;
+  for (int16_t i = pos; i <= end; i++) {
+    step(v, W[i], &k, &l);
+    if (k > l) break;
+  }
+  if (k <= l) {
+    r->k = k;
+    r->l = l;
+    r->pos = (int16_t)(end + 1);
+    return blist_add(fin, r);
+  }
+  return 0;
+}
+
+/* BWBranchFinalResultsBackward/Forward (search/search.c:116-469), for
+ * results without an earlier error (the only ones one error allows): a
+ * deletion, then per base an insertion and a mismatch.  The mismatch starts
+ * from the interval the insertion's extension left in the result when that
+ * extension survived, as the reference's does (it resets only `pos`). */
+static int block_branch_backward(const uint8_t *W, const fmo_view_t *v, blist_t *prev, blist_t *fin, int16_t bs,
+                                 int16_t last_block) {
+  for (uint32_t ii = 0; ii < prev->n; ii++) {
+    bres_t *r = &prev->v[ii];
+    if (r->dir != 0) continue;
+    const int16_t pos = r->pos;
+    if (pos < r->start) {
+      if (block_final_backward(W, v, r, fin, bs, last_block)) return 1;
+      continue;
+    }
+    if (r->nm) return -1; /* two errors: not reachable with two fragments */
+    const int64_t k = r->k, l = r->l;
+    r->nm = 1;
+    r->kind = HPG_BWT_DELETION;
+    r->base = 0xFF;
+    r->err_pos = pos;
+    r->pos = (int16_t)(pos - 1);
+    if (block_final_backward(W, v, r, fin, bs, last_block)) return 1;
+    for (uint8_t b = 0; b < 4; b++) {
+      int64_t ka = k, la = l;
+      step(v, b, &ka, &la);
+      if (ka > la) continue;
+      if (b != W[pos]) {
+        r->k = ka;
+        r->l = la;
+        r->pos = pos;
+        r->kind = HPG_BWT_INSERTION;
+        r->base = b;
+        if (block_final_backward(W, v, r, fin, bs, last_block)) return 1;
+        r->pos = (int16_t)(pos - 1);
+        r->kind = HPG_BWT_MISMATCH;
+        if (block_final_backward(W, v, r, fin, bs, last_block)) return 1;
+      }
+    }
+  }
+  prev->n = 0;
+  return 0;
+}
+
+static int block_branch_forward(const uint8_t *W, const fmo_view_t *v, blist_t *prev, blist_t *fin, int16_t bs,
+                                int16_t last_block) {
+  for (uint32_t ii = 0; ii < prev->n; ii++) {
+    bres_t *r = &prev->v[ii];
+    if (r->dir != 1) continue;
+    const int16_t pos = r->pos;
+    if (pos > r->end) {
+      if (blist_add(fin, r)) return 1;
+      continue;
+    }
+    if (r->nm) return -1;
+    const int64_t k = r->k, l = r->l;
+    r->nm = 1;
+    r->kind = HPG_BWT_DELETION;
+    r->base = 0xFF;
+    r->err_pos = pos;
+    r->pos = (int16_t)(pos + 1);
+    if (block_final_forward(W, v, r, fin, bs, last_block)) return 1;
+    for (uint8_t b = 0; b < 4; b++) {
+      int64_t ka = k, la = l;
+      step(v, b, &ka, &la);
+      if (ka > la) continue;
+      if (b != W[pos]) {
+        r->k = ka;
+        r->l = la;
+        r->pos = pos;
+        r->kind = HPG_BWT_INSERTION;
+        r->base = b;
+        if (block_final_forward(W, v, r, fin, bs, last_block)) return 1;
+        r->pos = (int16_t)(pos + 1);
+        r->kind = HPG_BWT_MISMATCH;
+        if (block_final_forward(W, v, r, fin, bs, last_block)) return 1;
+      }
+    }
+  }
+  prev->n = 0;
+  return 0;
+}
+
+/* BWSearchCPU for one or two fragments.  L: prev, next, final, anchors. */
+static void block_search(const uint8_t *W, int16_t nW, const fmo_view_t *bw, const fmo_view_t *fw, blist_t *L,
+                         int16_t fragsize, int type, uint8_t *D, int64_t top) {
+  blist_t *prev = &L[0], *next = &L[1], *fin = &L[2], *anch = &L[3];
+  const int16_t fragments = (int16_t)((uint64_t)nW / (uint64_t)fragsize);
+  int16_t half = (int16_t)(fragments / 2);
+  if (fragments % 2) half++;
+  anch->n = 0;
+  bres_t r, a;
+  memset(&r, 0, sizeof r);
+  if (fragments <= 1) {
+    r.k = 0;
+    r.l = top;
+    r.start = 0;
+    r.end = (int16_t)(nW - 1);
+    if (type == 0) {
+      r.dir = 1;
+      r.pos = 0;
+      block_exact_forward(W, fw, &r, &a);
+    } else {
+      r.dir = 0;
+      r.pos = (int16_t)(nW - 1);
+      block_exact_backward(W, bw, &r, &a);
+    }
+    if (blist_add(anch, &a)) return;
+    if (r.k <= r.l) blist_add(fin, &r);
+    return;
+  }
+  if (fragments > 2) return; /* needs the inverse suffix array (header note) */
+
+  /* block 0, forward over the first fragment, then the rest of the read */
+  prev->n = next->n = 0;
+  r.dir = 1;
+  r.k = 0;
+  r.l = top;
+  r.pos = 0;
+  r.start = 0;
+  r.end = (int16_t)(fragsize - 1);
+  block_exact_forward(W, fw, &r, &a);
+  if (blist_add(anch, &a)) return;
+  r.end = (int16_t)(nW - 1);
+  if (r.k <= r.l) {
+    block_d_forward(D, W, nW, bw, fw, &r, top);
+    if (blist_add(prev, &r)) return;
+    /* err_count = fragments - 1 = 1: one partial pass, then the final branches */
+    if (!block_partial_forward(W, D, (uint8_t)(fragments - 1), fw, prev, next, fin, fragsize, (int16_t)(half - 1)))
+      block_branch_forward(W, fw, next, fin, fragsize, (int16_t)(half - 1));
+  }
+
+  /* last block, backward over the last fragment, then the rest of the read */
+  prev->n = next->n = 0;
+  memset(&r, 0, sizeof r);
+  r.dir = 0;
+  r.k = 0;
+  r.l = top;
+  r.pos = (int16_t)(nW - 1);
+  r.start = (int16_t)(fragsize * (fragments - 1));
+  r.end = (int16_t)(nW - 1);
+  block_exact_backward(W, bw, &r, &a);
+  if (blist_add(anch, &a)) return;
+  r.start = 0;
+  if (r.k <= r.l) {
+    block_d_backward(D, W, nW, bw, fw, &r, top);
+    if (blist_add(prev, &r)) return;
+    if (!block_partial_backward(W, D, (uint8_t)(fragments - 1), bw, prev, next, fin, fragsize, 0))
+      block_branch_backward(W, bw, next, fin, fragsize, 0);
+  }
+}
+
 /* ------------------------------------------------------------ per read -- */
 
 /* Rows of a list's kept hits, and whether a locate limit leaves them unlocated
@@ -519,8 +971,8 @@ static int over_limit(const hpg_hit_t *h, uint32_t n, uint64_t limit) {
 }
 
 static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *seq, size_t len, uint32_t max_results,
-                     uint64_t limit, sink_t *s, hpg_hit_t *lbuf, uint8_t *code, int64_t *vecs, uint32_t *rs_count,
-                     uint8_t *rs_trunc) {
+                     uint64_t limit, sink_t *s, hpg_hit_t *lbuf, uint8_t *code, int64_t *vecs, bres_t *bbuf,
+                     uint32_t *rs_count, uint8_t *rs_trunc, hpg_block_anchor_t *anchors, uint8_t *n_anchors) {
   if (len < 3 || len > 32767) return;
   for (size_t i = 0; i < len; i++) {
     code[i] = ix->code_of[(unsigned char)seq[i]];
@@ -548,6 +1000,71 @@ static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *s
           continue;
         }
         locate(ix, s, hid, c.k, c.l, type ? 0 : 1, len);
+      }
+    }
+    return;
+  }
+
+  if (mode == HPG_BWT_MODE_BLOCK) {
+    /* bwt_map_inexact_read_2 (bwt.c:2401-2470): fragment size len / 2, at
+     * least 30; lists of capacity filter_read_mappings, anchors of 2 */
+    int16_t frag = (int16_t)(len / 2);
+    if (frag < 30) frag = 30;
+    for (int type = 1; type >= 0; type--) {
+      const size_t t2 = 2 * (size_t)rd + !type;
+      blist_t L[4] = {{bbuf, 0, max_results, 0},
+                      {bbuf + (size_t)max_results + 1, 0, max_results, 0},
+                      {bbuf + 2 * ((size_t)max_results + 1), 0, max_results, 0},
+                      {bbuf + 3 * ((size_t)max_results + 1), 0, 2, 0}};
+      if (type)
+        block_search(code, (int16_t)len, &ix->bw, &ix->fw, L, frag, type, (uint8_t *)vecs, top);
+      else
+        block_search(code, (int16_t)len, &ix->fw_rev, &ix->bw_rev, L, frag, type, (uint8_t *)vecs, top);
+      const blist_t *fin = &L[2], *anch = &L[3];
+      for (uint32_t t = 0; t < fin->n; t++) {
+        const bres_t *b = &fin->v[t];
+        hpg_hit_t *h = &lbuf[t];
+        memset(h, 0, sizeof *h);
+        h->read = rd;
+        h->strand = (uint8_t)!type;
+        h->dir = b->dir;
+        h->nm = b->nm;
+        if (b->nm) {
+          h->err_kind = b->kind;
+          h->err_base = b->base;
+          h->err_pos = b->err_pos;
+        }
+        h->k = b->k;
+        h->l = b->l;
+      }
+      const int skip = over_limit(lbuf, fin->n, limit);
+      const int refused = L[0].refused | L[1].refused | L[2].refused | L[3].refused;
+      rs_trunc[t2] = (uint8_t)(refused | (skip ? 2 : 0));
+      rs_count[t2] = fin->n;
+      if (n_anchors) {
+        n_anchors[t2] = (uint8_t)anch->n;
+        for (uint32_t a = 0; a < anch->n; a++) {
+          hpg_block_anchor_t *o = &anchors[2 * t2 + a];
+          memset(o, 0, sizeof *o);
+          o->k = anch->v[a].k;
+          o->l = anch->v[a].l;
+          o->start = anch->v[a].start;
+          o->end = anch->v[a].end;
+          o->pos = anch->v[a].pos;
+          o->dir = anch->v[a].dir;
+        }
+      }
+      for (uint32_t t = 0; t < fin->n; t++) {
+        const hpg_hit_t *h = &lbuf[t];
+        uint32_t hid = (uint32_t)s->n_hits;
+        sink_hit(s, h);
+        if (skip) continue;
+        uint8_t err = h->nm ? h->err_kind : 0;
+        int direction = type ? h->dir : !h->dir;
+        uint64_t len_calc = len;
+        if (err == HPG_BWT_DELETION) len_calc--;
+        else if (err == HPG_BWT_INSERTION) len_calc++;
+        locate(ix, s, hid, h->k, h->l, direction, len_calc);
       }
     }
     return;
@@ -583,8 +1100,9 @@ static void one_read(const fmo_index_t *ix, int mode, uint32_t rd, const char *s
 
 /* Batch driver: reads are split into chunks processed by `threads` OpenMP
  * threads (dynamic schedule, as bwt.c:1134), then merged in read order. */
-int fmo_search_limit(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
-                     uint32_t max_results, uint64_t locate_limit, int threads, hpg_result_set_t *out) {
+static int search_impl(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                       uint32_t max_results, uint64_t locate_limit, int threads, hpg_result_set_t *out,
+                       hpg_block_anchor_t *anchors, uint8_t *n_anchors) {
   memset(out, 0, sizeof *out);
   out->n_reads = n_reads;
   out->rs_count = (uint32_t *)calloc(2 * n_reads + 1, sizeof(uint32_t));
@@ -603,14 +1121,17 @@ int fmo_search_limit(const fmo_index_t *ix, int mode, const char *seqs, const ui
     hpg_hit_t *lbuf = (hpg_hit_t *)malloc(((size_t)max_results + 1) * sizeof(hpg_hit_t));
     uint8_t *code = (uint8_t *)malloc(maxlen + 1);
     int64_t *vecs = (int64_t *)malloc(8 * (maxlen + 1) * sizeof(int64_t));
+    bres_t *bbuf = mode == HPG_BWT_MODE_BLOCK ? (bres_t *)malloc((3 * ((size_t)max_results + 1) + 2) * sizeof(bres_t))
+                                              : NULL;
 #pragma omp for schedule(dynamic, 1)
     for (size_t ch = 0; ch < nchunks; ch++) {
       size_t r0 = ch * 256, r1 = r0 + 256 < n_reads ? r0 + 256 : n_reads;
       for (size_t r = r0; r < r1; r++)
         one_read(ix, mode, (uint32_t)r, seqs + offsets[r], (size_t)(offsets[r + 1] - offsets[r]), max_results,
-                 locate_limit, &sinks[ch],
-                 lbuf, code, vecs, out->rs_count, out->rs_truncated);
+                 locate_limit, &sinks[ch], lbuf, code, vecs, bbuf, out->rs_count, out->rs_truncated, anchors,
+                 n_anchors);
     }
+    free(bbuf);
     free(lbuf);
     free(code);
     free(vecs);
@@ -639,6 +1160,22 @@ int fmo_search_limit(const fmo_index_t *ix, int mode, const char *seqs, const ui
   out->n_hits = nh;
   out->n_locs = nl;
   return 0;
+}
+
+int fmo_search_limit(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                     uint32_t max_results, uint64_t locate_limit, int threads, hpg_result_set_t *out) {
+  return search_impl(ix, mode, seqs, offsets, n_reads, max_results, locate_limit, threads, out, NULL, NULL);
+}
+
+/* The k-error block search with its anchors: anchors[2 * (2 * read + strand)
+ * + a] for a < n_anchors[2 * read + strand] (arrays of 4 n and 2 n entries,
+ * n_anchors zeroed here). */
+int fmo_block_search(const fmo_index_t *ix, const char *seqs, const uint64_t *offsets, size_t n_reads,
+                     uint32_t max_results, uint64_t locate_limit, int threads, hpg_result_set_t *out,
+                     hpg_block_anchor_t *anchors, uint8_t *n_anchors) {
+  if (n_anchors) memset(n_anchors, 0, 2 * n_reads);
+  return search_impl(ix, HPG_BWT_MODE_BLOCK, seqs, offsets, n_reads, max_results, locate_limit, threads, out,
+                     anchors, n_anchors);
 }
 
 int fmo_search(const fmo_index_t *ix, int mode, const char *seqs, const uint64_t *offsets, size_t n_reads,

@@ -18,7 +18,7 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent.parent
 sys.path.insert(0, str(ROOT / "hpg-libs_gb300"))
-from hpgbwt.lib import ResultSetC, Result, result_from_c  # noqa: E402
+from hpgbwt.lib import ANCHOR_DTYPE, BlockResult, ResultSetC, Result, result_from_c  # noqa: E402
 
 PORT_LIB = ROOT / "oracle" / "liboracle.so"
 REF_LIB = ROOT / "oracle" / "_ref" / "libhpgref.so"
@@ -37,6 +37,9 @@ class PortOracle:
         self.lib.fmo_search_limit.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                               ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
                                               ctypes.POINTER(ResultSetC)]
+        self.lib.fmo_block_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int,
+                                              ctypes.POINTER(ResultSetC), ctypes.c_void_p, ctypes.c_void_p]
         self.lib.fmo_result_free.argtypes = [ctypes.POINTER(ResultSetC)]
         self.lib.fmo_max_threads.restype = ctypes.c_int
         self.h = self.lib.fmo_index_load(index_dir.encode())
@@ -56,6 +59,22 @@ class PortOracle:
                                   threads, ctypes.byref(rs))
         try:
             return result_from_c(rs, n)
+        finally:
+            self.lib.fmo_result_free(ctypes.byref(rs))
+
+    def block_search(self, reads, max_results: int = 1 << 16, threads: int = 1,
+                     locate_limit: int = 0) -> BlockResult:
+        """k-error block search (BWSearchCPU as bwt_map_inexact_read_2 drives it), with anchors."""
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        anchors = np.zeros(4 * n + 1, dtype=ANCHOR_DTYPE)
+        n_anchors = np.zeros(2 * n + 1, dtype=np.uint8)
+        rs = ResultSetC()
+        self.lib.fmo_block_search(self.h, seq.ctypes.data, offs.ctypes.data, n, max_results, locate_limit, threads,
+                                  ctypes.byref(rs), anchors.ctypes.data, n_anchors.ctypes.data)
+        try:
+            return BlockResult(result_from_c(rs, n), anchors[:4 * n], n_anchors[:2 * n])
         finally:
             self.lib.fmo_result_free(ctypes.byref(rs))
 
@@ -88,6 +107,9 @@ class RefOracle:
                                             ctypes.c_size_t, ctypes.c_uint, ctypes.POINTER(ctypes.c_void_p),
                                             ctypes.POINTER(ctypes.c_size_t)]
         self.lib.ref_blob_free.argtypes = [ctypes.c_void_p]
+        self.lib.ref_block_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                              ctypes.c_uint32, ctypes.POINTER(ResultSetC), ctypes.c_void_p,
+                                              ctypes.c_void_p]
         self.h = self.lib.ref_index_load(index_dir.encode()) if index_dir else None
 
     def build_index(self, fasta: str, outdir: str, ratio: int = 16) -> None:
@@ -102,6 +124,21 @@ class RefOracle:
         self.lib.ref_search(self.h, mode, seq.ctypes.data, offs.ctypes.data, n, max_results, ctypes.byref(rs))
         try:
             return result_from_c(rs, n)
+        finally:
+            self.lib.ref_result_free(ctypes.byref(rs))
+
+    def block_search(self, reads, max_results: int = 1 << 16) -> BlockResult:
+        """The reference's BWSearchCPU per strand as bwt_map_inexact_read_2 calls it (rs_truncated all 0)."""
+        seq = np.ascontiguousarray(reads.seq, dtype=np.uint8)
+        offs = np.ascontiguousarray(reads.offsets, dtype=np.uint64)
+        n = len(offs) - 1
+        anchors = np.zeros(4 * n + 1, dtype=ANCHOR_DTYPE)
+        n_anchors = np.zeros(2 * n + 1, dtype=np.uint8)
+        rs = ResultSetC()
+        self.lib.ref_block_search(self.h, seq.ctypes.data, offs.ctypes.data, n, max_results, ctypes.byref(rs),
+                                  anchors.ctypes.data, n_anchors.ctypes.data)
+        try:
+            return BlockResult(result_from_c(rs, n), anchors[:4 * n], n_anchors[:2 * n])
         finally:
             self.lib.ref_result_free(ctypes.byref(rs))
 

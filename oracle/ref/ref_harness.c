@@ -13,11 +13,14 @@
  *                        mode SEARCH1: the four vector searches of bwt.c:1940-1950,
  *                                      BWSearch1VectorHelper per type (bwt.c:1989-2002)
  *                        then, for every hit, the locate loop of bwt.c:2158-2166.
+ *   ref_block_search  -> BWSearchCPU per type as bwt_map_inexact_read_2 calls it
+ *                        (bwt.c:2401-2470), its results located, and its anchors.
  *   ref_map_api       -> the alignment-list entry points themselves:
  *                        0 bwt_map_exact_read per read (bwt.c:994), fresh list each
  *                        1 bwt_map_exact_seqs over all reads, one thread (bwt.c:1040)
  *                        2 bwt_map_exact_batch over all reads (bwt.c:1097)
  *                        3 bwt_map_inexact_read per read (bwt.c:1879), fresh list with `flag`
+ *                        5 bwt_map_inexact_read_2 per read (bwt.c:2313), fresh list with `flag`
  *                        serialised as described at ref_map_api.
  */
 #include <ctype.h>
@@ -231,6 +234,85 @@ int ref_search(void *vidx, int mode, const char *seqs, const uint64_t *offsets, 
   return 0;
 }
 
+/* The k-error block search as bwt_map_inexact_read_2 runs it (bwt.c:2401-2470):
+ * BWSearchCPU per type with result lists of capacity max_results and anchor
+ * lists of 2, then the locate loop of bwt.c:2640-2650 for every result of
+ * rl_final (positions without that function's +1).  Anchors as
+ * fmo_block_search: anchors[2 * (2 * read + strand) + a], a < n_anchors[..].
+ * rs_truncated stays 0 (BWSearchCPU does not report refused results). */
+int ref_block_search(void *vidx, const char *seqs, const uint64_t *offsets, size_t n_reads, uint32_t max_results,
+                     hpg_result_set_t *out, hpg_block_anchor_t *anchors, uint8_t *n_anchors) {
+  bwt_index_t *index = (bwt_index_t *)vidx;
+  sink_t s;
+  memset(&s, 0, sizeof(s));
+  memset(out, 0, sizeof(*out));
+  out->n_reads = n_reads;
+  out->rs_count = (uint32_t *)calloc(2 * n_reads + 1, sizeof(uint32_t));
+  out->rs_truncated = (uint8_t *)calloc(2 * n_reads + 1, 1);
+  memset(n_anchors, 0, 2 * n_reads);
+  results_list rl_prev, rl_next, rl_prev_i, rl_next_i, rl_final, rl_anch;
+  results_list *lists[] = {&rl_prev, &rl_next, &rl_prev_i, &rl_next_i, &rl_final};
+  for (int i = 0; i < 5; i++) {
+    new_results_list(lists[i], max_results ? max_results : 1);
+    lists[i]->max_results = max_results;
+  }
+  new_results_list(&rl_anch, 2);
+  for (size_t rd = 0; rd < n_reads; rd++) {
+    size_t len = (size_t)(offsets[rd + 1] - offsets[rd]);
+    const char *seq = seqs + offsets[rd];
+    if (len < 3 || len > 32767) continue;
+    if (!in_alphabet(index, seq, len)) continue;
+    uint8_t *code = (uint8_t *)malloc(len);
+    encode_bases(code, (char *)seq, len, index->bwt_config.table);
+    int frag = (int)(len / 2); /* bwt.c:2408-2412: len / (num_errors + 1), at least 30 */
+    if (frag < 30) frag = 30;
+    for (int type = 1; type >= 0; type--) {
+      for (int i = 0; i < 5; i++) lists[i]->num_results = 0;
+      rl_final.read_index = 0;
+      if (type == 1)
+        BWSearchCPU(code, len, index->backward, index->forward, &rl_prev, &rl_next, &rl_prev_i, &rl_next_i,
+                    &rl_final, &rl_anch, (int16_t)frag, 1, index->bwt_config.nA);
+      else
+        BWSearchCPU(code, len, index->forward_rev, index->backward_rev, &rl_prev, &rl_next, &rl_prev_i,
+                    &rl_next_i, &rl_final, &rl_anch, (int16_t)frag, 0, index->bwt_config.nA);
+      const size_t t2 = 2 * rd + !type;
+      out->rs_count[t2] = (uint32_t)rl_final.num_results;
+      for (size_t ii = 0; ii < rl_final.num_results; ii++) {
+        result *r = &rl_final.list[ii];
+        hpg_hit_t h;
+        fill_hit(&h, (uint32_t)rd, type, r);
+        uint32_t hid = (uint32_t)s.n_hits;
+        push_hit(&s, &h);
+        char error = r->num_mismatches ? r->err_kind[0] : 0;
+        size_t direction = type ? r->dir : !r->dir;
+        size_t len_calc = len;
+        if (error == DELETION) len_calc--;
+        else if (error == INSERTION) len_calc++;
+        locate_hit(index, &s, hid, r->k, r->l, direction, len_calc);
+      }
+      n_anchors[t2] = (uint8_t)rl_anch.num_results;
+      for (size_t a = 0; a < rl_anch.num_results; a++) {
+        hpg_block_anchor_t *o = &anchors[2 * t2 + a];
+        memset(o, 0, sizeof(*o));
+        o->k = rl_anch.list[a].k;
+        o->l = rl_anch.list[a].l;
+        o->start = rl_anch.list[a].start;
+        o->end = rl_anch.list[a].end;
+        o->pos = rl_anch.list[a].pos;
+        o->dir = rl_anch.list[a].dir;
+      }
+    }
+    free(code);
+  }
+  for (int i = 0; i < 5; i++) free(lists[i]->list);
+  free(rl_anch.list);
+  out->n_hits = s.n_hits;
+  out->hits = s.hits;
+  out->n_locs = s.n_locs;
+  out->locs = s.locs;
+  return 0;
+}
+
 void ref_result_free(hpg_result_set_t *out) {
   free(out->hits);
   free(out->locs);
@@ -334,10 +416,10 @@ static void free_list(array_list_t *list, int anchors) {
 int ref_map_api(void *vidx, int api, const char *seqs, const char *quals, const uint64_t *offs, const char *ids,
                 const uint64_t *id_offs, size_t n, int filter, int flag, uint8_t **out, size_t *out_len) {
   bwt_index_t *index = (bwt_index_t *)vidx;
-  bwt_optarg_t *opt = bwt_optarg_new(api == 3 ? 1 : 0, 1, filter, filter);
+  bwt_optarg_t *opt = bwt_optarg_new(api == 3 || api == 5 ? 1 : 0, 1, filter, filter);
   blob_t b = {0};
   int q = quiet_begin(); /* bwt_map_exact_seq prints a line per read */
-  if (api == 0 || api == 3) {
+  if (api == 0 || api == 3 || api == 5) {
     for (size_t i = 0; i < n; i++) {
       fastq_read_t r;
       memset(&r, 0, sizeof(r));
@@ -350,9 +432,11 @@ int ref_map_api(void *vidx, int api, const char *seqs, const char *quals, const 
       r.revcomp = rc;
       r.length = (int)len;
       array_list_t *list = array_list_new(16, 1.25f, COLLECTION_MODE_ASYNCHRONIZED);
-      array_list_set_flag(api == 3 ? flag : 0, list);
-      size_t ret = api == 0 ? bwt_map_exact_read(&r, opt, index, list) : bwt_map_inexact_read(&r, opt, index, list);
-      int anchors = api == 3 && len >= 5 && array_list_get_flag(list) == 1;
+      array_list_set_flag(api == 3 || api == 5 ? flag : 0, list);
+      size_t ret = api == 0   ? bwt_map_exact_read(&r, opt, index, list)
+                   : api == 3 ? bwt_map_inexact_read(&r, opt, index, list)
+                              : bwt_map_inexact_read_2(&r, opt, index, list);
+      int anchors = (api == 3 || api == 5) && len >= 5 && array_list_get_flag(list) == 1;
       put_list(&b, list, ret, anchors, len);
       free_list(list, anchors);
       free(rc);

@@ -11,6 +11,8 @@ import struct
 import numpy as np
 
 API_EXACT_READ, API_EXACT_SEQS, API_EXACT_BATCH, API_INEXACT_READ, API_INEXACT_BATCH = 0, 1, 2, 3, 4
+API_INEXACT_READ2 = 5  # bwt_map_inexact_read_2 per read
+PER_READ_APIS = (API_EXACT_READ, API_INEXACT_READ, API_INEXACT_READ2)
 
 
 class FastqSet:
@@ -71,7 +73,7 @@ def _parse_list(r: _Rd):
 
 def parse_blob(api: int, blob: bytes, n_reads: int):
     r = _Rd(blob)
-    if api in (API_EXACT_READ, API_INEXACT_READ):
+    if api in PER_READ_APIS:
         return [_parse_list(r) for _ in range(n_reads)]
     out = {"list": _parse_list(r)}
     if api == API_EXACT_SEQS:
@@ -135,7 +137,7 @@ def bind(lib) -> None:
     lib.array_list_free.argtypes = [vp, vp]
     lib.alignment_free.argtypes = [vp]
     lib.bwt_anchor_free.argtypes = [vp]
-    for f in ("bwt_map_exact_read", "bwt_map_inexact_read"):
+    for f in ("bwt_map_exact_read", "bwt_map_inexact_read", "bwt_map_inexact_read_2"):
         getattr(lib, f).restype = sz
         getattr(lib, f).argtypes = [vp, vp, vp, vp]
     lib.bwt_map_exact_seqs.restype = sz
@@ -143,8 +145,9 @@ def bind(lib) -> None:
     for f in ("bwt_map_exact_batch", "bwt_map_inexact_batch"):
         getattr(lib, f).restype = sz
         getattr(lib, f).argtypes = [vp, vp, vp, vp, vp]
-    lib.bwt_map_inexact_array_list.restype = sz
-    lib.bwt_map_inexact_array_list.argtypes = [vp, vp, vp, vp, vp, vp]
+    for f in ("bwt_map_inexact_array_list", "bwt_map_inexact_array_list_2"):
+        getattr(lib, f).restype = sz
+        getattr(lib, f).argtypes = [vp, vp, vp, vp, vp, vp]
 
 
 def _cstr(p, maxlen=None):
@@ -182,9 +185,10 @@ def walk_list(lib, lst: int, ret: int, anchors: bool, qmax=None, free: bool = Tr
 
 def product_map(lib, index_handle: int, api: int, fq: FastqSet, filter_read_mappings: int, flag: int = 0):
     """The product's entry point on the same reads, shaped like parse_blob's output."""
-    opt = lib.bwt_optarg_new(1 if api == API_INEXACT_READ else 0, 1, filter_read_mappings, filter_read_mappings)
+    inexact = api in (API_INEXACT_READ, API_INEXACT_READ2)
+    opt = lib.bwt_optarg_new(1 if inexact else 0, 1, filter_read_mappings, filter_read_mappings)
     try:
-        if api in (API_EXACT_READ, API_INEXACT_READ):
+        if api in PER_READ_APIS:
             out = []
             for i in range(fq.n):
                 o = int(fq.offs[i])
@@ -197,10 +201,11 @@ def product_map(lib, index_handle: int, api: int, fq: FastqSet, filter_read_mapp
                 r.revcomp = ctypes.addressof(rc)
                 r.length = L
                 lst = lib.array_list_new(16, 1.25, 2)
-                lib.array_list_set_flag(flag if api == API_INEXACT_READ else 0, lst)
-                f = lib.bwt_map_exact_read if api == API_EXACT_READ else lib.bwt_map_inexact_read
+                lib.array_list_set_flag(flag if inexact else 0, lst)
+                f = {API_EXACT_READ: lib.bwt_map_exact_read, API_INEXACT_READ: lib.bwt_map_inexact_read,
+                     API_INEXACT_READ2: lib.bwt_map_inexact_read_2}[api]
                 ret = f(ctypes.byref(r), opt, index_handle, lst)
-                anchors = api == API_INEXACT_READ and L >= 5 and lib.array_list_get_flag(lst) == 1
+                anchors = inexact and L >= 5 and lib.array_list_get_flag(lst) == 1
                 out.append(walk_list(lib, lst, ret, anchors, qmax=L))
             return out
         if api == API_EXACT_SEQS:

@@ -11,7 +11,9 @@ SHA-256 of every index file written by the reference builder
 (bwt_generate_index_files, bwt.c:744-819, at SA ratio 16), the reads, and the
 reference's search outputs (oracle/ref/ref_harness.c: BWExactSearchBackward
 on both strands, and the four vector searches + BWSearch1VectorHelper per
-strand with the bwt.c:2158-2166 locate) for several result-list capacities.
+strand with the bwt.c:2158-2166 locate; the k-error block search BWSearchCPU
+with its anchors) for several result-list capacities, and the alignment lists
+of the entry points.
 """
 from __future__ import annotations
 
@@ -38,7 +40,10 @@ API_RUNS = [(api_lists.API_EXACT_READ, 200, 0), (api_lists.API_EXACT_READ, 2, 0)
             (api_lists.API_EXACT_SEQS, 200, 0), (api_lists.API_EXACT_BATCH, 200, 0),
             (api_lists.API_INEXACT_READ, 200, 0), (api_lists.API_INEXACT_READ, 3, 0),
             (api_lists.API_INEXACT_READ, 200, 1), (api_lists.API_INEXACT_READ, 3, 1),
-            (api_lists.API_INEXACT_READ, 0, 1)]
+            (api_lists.API_INEXACT_READ, 0, 1),
+            (api_lists.API_INEXACT_READ2, 200, 0), (api_lists.API_INEXACT_READ2, 3, 0),
+            (api_lists.API_INEXACT_READ2, 200, 1), (api_lists.API_INEXACT_READ2, 3, 1),
+            (api_lists.API_INEXACT_READ2, 0, 1)]
 API_READS = 400  # first reads of each case taken through the entry points
 
 # Seeds and CALs recorded per case (ref_seeds_cals): (mode 0 bwt_map_exact_seeds_seq /
@@ -158,6 +163,13 @@ def main() -> int:
                     arrays[f"{tag}_locs"] = r.locs
                     arrays[f"{tag}_count"] = r.rs_count
                     arrays[f"{tag}_trunc"] = r.rs_truncated
+            for mr in maxes:  # the k-error block search (BWSearchCPU as bwt_map_inexact_read_2 runs it)
+                b = ro.block_search(rs, max_results=mr)
+                arrays[f"blk_r{mr}_bhits"] = b.result.hits
+                arrays[f"blk_r{mr}_blocs"] = b.result.locs
+                arrays[f"blk_r{mr}_bcount"] = b.result.rs_count
+                arrays[f"blk_r{mr}_banch"] = b.anchors
+                arrays[f"blk_r{mr}_bnanch"] = b.n_anchors
             edge = synth.from_strings(edge_reads(g, cl))
             fq = api_lists.FastqSet(api_read_set(seq, offs)[:API_READS - 20] + api_read_set(edge.seq, edge.offsets))
             arrays["api_seq"] = np.frombuffer(b"".join(fq.seqs), dtype=np.uint8)

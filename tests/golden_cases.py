@@ -36,6 +36,20 @@ class GoldenCase:
         return lib.Result(a[f"{tag}_hits"].view(lib.HIT_DTYPE) if a[f"{tag}_hits"].dtype != lib.HIT_DTYPE
                           else a[f"{tag}_hits"], a[f"{tag}_locs"], a[f"{tag}_count"], a[f"{tag}_trunc"])
 
+    def block_capacities(self) -> list[int]:
+        """Result-list capacities of the recorded k-error block searches."""
+        return sorted(int(k[5:-6]) for k in self.arrays if k.startswith("blk_r") and k.endswith("_bhits"))
+
+    def block_expected(self, mr: int) -> lib.BlockResult:
+        """The reference's block search (rs_truncated is not recorded: all 0)."""
+        a = self.arrays
+        hits = a[f"blk_r{mr}_bhits"]
+        res = lib.Result(hits.view(lib.HIT_DTYPE) if hits.dtype != lib.HIT_DTYPE else hits, a[f"blk_r{mr}_blocs"],
+                         a[f"blk_r{mr}_bcount"], np.zeros_like(a[f"blk_r{mr}_bcount"], dtype=np.uint8))
+        anch = a[f"blk_r{mr}_banch"]
+        return lib.BlockResult(res, anch.view(lib.ANCHOR_DTYPE) if anch.dtype != lib.ANCHOR_DTYPE else anch,
+                               a[f"blk_r{mr}_bnanch"])
+
     def api_runs(self):
         """(api, filter_read_mappings, flag) of the recorded alignment-list runs."""
         out = []

@@ -72,7 +72,7 @@ def test_recorded_lists_parse():
         for api, filt, flag in gc.api_runs():
             blob = gc.arrays[f"api{api}_f{filt}_g{flag}"].tobytes()
             r = al._Rd(blob)
-            if api in (al.API_EXACT_READ, al.API_INEXACT_READ):
+            if api in al.PER_READ_APIS:
                 lists = [al._parse_list(r) for _ in range(fq.n)]
                 assert r.o == len(blob)
                 assert all(x["ret"] == len(x["items"]) for x in lists)  # fresh lists: return = list size
@@ -84,6 +84,12 @@ def test_recorded_lists_parse():
         anchors = sum(it[0] == "anchor" for x in gc.api_expected(al.API_INEXACT_READ, 200, 1, fq.n)
                       for it in x["items"])
         assert anchors > 0 and (2 in flags or name == "iid_1chr")
+        # and those of bwt_map_inexact_read_2 (block search): filter flag, anchors, every cigar shape
+        flags2 = {x["flag"] for x in gc.api_expected(al.API_INEXACT_READ2, 3, 1, fq.n)}
+        items2 = [it for x in gc.api_expected(al.API_INEXACT_READ2, 200, 1, fq.n) for it in x["items"]]
+        cigars = {it[14].rstrip(b"0123456789") for it in items2 if it[0] == "aln"}
+        assert flags2 == {0, 1, 2} and any(it[0] == "anchor" for it in items2)
+        assert {b"=", b"M", b"X"} <= {c[-1:] for c in cigars}
 
 
 def test_result_arrays_past_2gib():

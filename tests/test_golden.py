@@ -42,6 +42,39 @@ def test_oracle_matches_reference_outputs(built_case):
     ora.close()
 
 
+def test_oracle_block_search_matches_reference_outputs(built_case):
+    """The k-error block search (BWSearchCPU as bwt_map_inexact_read_2 runs it): results,
+    located rows and anchors equal the reference's at every recorded list capacity."""
+    c, index = built_case
+    ora = PortOracle(index)
+    caps = c.block_capacities()
+    assert caps
+    for mr in caps:
+        got = ora.block_search(c.reads, max_results=mr, threads=2)
+        assert got.equal(c.block_expected(mr), truncation=False), mr
+        assert not (got.result.rs_truncated & 2).any()
+    ora.close()
+
+
+def test_block_fixtures_exercise_edges():
+    """Exact and one-error results of every kind on both halves, multi-row intervals,
+    lists cut by their capacity (fewer results than without a cap), empty anchors."""
+    kinds, dirs, multi, cut = set(), set(), False, False
+    for name in names():
+        c = GoldenCase(name)
+        caps = c.block_capacities()
+        full = c.block_expected(max(caps))
+        h = full.result.hits
+        kinds |= set(int(x) for x in h["err_kind"][h["nm"] == 1])
+        dirs |= set(int(x) for x in h["dir"])
+        multi |= bool(((h["l"] - h["k"]) > 0).any())
+        for mr in caps:
+            if mr < max(caps):
+                cut |= len(c.block_expected(mr).result.hits) < len(h)
+        assert (h["nm"] == 0).any()
+    assert kinds == {1, 2, 3} and dirs == {0, 1} and multi and cut
+
+
 def test_golden_cases_exercise_edges():
     seen_trunc = seen_invalid = seen_quirk = seen_multi = False
     for name in names():

@@ -33,6 +33,9 @@ def test_port_equals_reference(tmp_path, kind, n, chroms, seed, length, edits, m
         a = ref.search(reads, mode=mode, max_results=maxr)
         b = port.search(reads, mode=mode, max_results=maxr, threads=4)
         assert a.equal(b), (mode, len(a.hits), len(b.hits))
+    a = ref.block_search(reads, max_results=maxr)
+    b = port.block_search(reads, max_results=maxr, threads=4)
+    assert a.equal(b, truncation=False), (len(a.result.hits), len(b.result.hits))
     ref.close()
     port.close()
 
