@@ -260,10 +260,17 @@ def cpu_baseline(index_dir: str, reads, seconds: float = 12.0) -> dict:
     t = time.perf_counter()
     ora.search(sample, mode=1, max_results=MAX_RESULTS, threads=threads)
     dt = time.perf_counter() - t
+    # the k-error block search of bwt_map_inexact_read_2 on a smaller sample (~3 s)
+    nb = int(min(n_total, max(2000, rate * 3.0)))
+    t = time.perf_counter()
+    ora.block_search(reads.subset(np.arange(nb)), max_results=MAX_RESULTS, threads=threads)
+    dtb = time.perf_counter() - t
     ora.close()
     return {"value": n / dt, "unit": "reads/s", "cores": threads, "kind": "port",
             "sample": f"first {n} reads of the rank-0 read batch, same index, OpenMP over {threads} host threads "
-                      f"({dt:.1f}s)"}
+                      f"({dt:.1f}s)",
+            "block_search": {"value": round(nb / dtb, 1), "unit": "reads/s",
+                             "sample": f"first {nb} reads, {threads} host threads ({dtb:.1f}s)"}}
 
 
 def _pct(v: list[float], q: float) -> float:
@@ -430,6 +437,52 @@ def alignment_lists(gi, reads, log, n: int) -> dict:
     return out
 
 
+def block_search_leg(gi, reads, log, n_lists: int) -> dict:
+    """The k-error block search of bwt_map_inexact_read_2 (bwt_gpu_block_search: host reads
+    in, results, located rows and anchors out) over the whole batch, 1024-result lists; the
+    best of three calls, with the search kernels' device time.  Then
+    bwt_map_inexact_array_list_2 (alignment records built on the host) over the first
+    n_lists reads, filter_read_mappings 200."""
+    from hpgbwt import lib
+    n = len(reads)
+    seq = np.ascontiguousarray(reads.seq)
+    offs = np.ascontiguousarray(reads.offsets)
+    anchors = np.zeros(4 * n + 1, dtype=lib.ANCHOR_DTYPE)
+    n_anch = np.zeros(2 * n + 1, dtype=np.uint8)
+    best, kms, hits, locs = None, None, 0, 0
+    for _ in range(3):
+        rs = lib.ResultSetC()
+        t = time.perf_counter()
+        rc = gi.lib.bwt_gpu_block_search(gi.handle, seq.ctypes.data, offs.ctypes.data, n, MAX_RESULTS,
+                                         lib.ctypes.byref(rs), anchors.ctypes.data, n_anch.ctypes.data)
+        dt = time.perf_counter() - t
+        if rc != 0:
+            raise RuntimeError(gi.lib.bwt_gpu_last_error().decode())
+        hits, locs = int(rs.n_hits), int(rs.n_locs)
+        gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rs))
+        best = dt if best is None else min(best, dt)
+        k = gi.block_search_ms()
+        kms = k if kms is None else min(kms, k)
+    out = {"reads": n, "seconds": round(best, 4), "reads_per_s": round(n / best, 1),
+           "kernel_ms": round(kms, 3), "kernel_reads_per_s": round(n / (kms * 1e-3), 1),
+           "hits_per_read": round(hits / max(1, n), 3), "located_rows_per_read": round(locs / max(1, n), 3),
+           "max_results": MAX_RESULTS}
+    log(f"[bench] block search: kernel {out['kernel_reads_per_s'] / 1e6:.1f} M reads/s ({kms:.2f} ms), "
+        f"call {out['reads_per_s'] / 1e6:.2f} M reads/s, {out['hits_per_read']} hits per read")
+    if n_lists > 0:
+        rs_ = [bytes(reads.seq[int(reads.offsets[i]):int(reads.offsets[i + 1])]) for i in range(min(n_lists, n))]
+        bl, count = None, 0
+        for _ in range(3):
+            count = gi.map_block_array_list(rs_, 200)
+            bl = gi.last_map_seconds if bl is None else min(bl, gi.last_map_seconds)
+        out["array_list_2"] = {"reads": len(rs_), "seconds": round(bl, 4), "reads_per_s": round(len(rs_) / bl, 1),
+                               "alignments_per_read": round(count / max(1, len(rs_)), 3),
+                               "filter_read_mappings": 200}
+        log(f"[bench] bwt_map_inexact_array_list_2: {len(rs_) / bl / 1e6:.2f} M reads/s over {len(rs_)} reads, "
+            f"{count / max(1, len(rs_)):.3f} alignments per read")
+    return out
+
+
 def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     import torch
     from hpgbwt import lib
@@ -543,6 +596,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                     SERVE_LOCATE_LIMIT if wl["genome"] == "large" else 0) if not args.no_serving else None
     cals = cal_generation(gi, reads, log, args.cal_reads) if args.cal_reads > 0 else None
     alns = alignment_lists(gi, reads, log, args.cal_reads) if args.cal_reads > 0 else None
+    block = block_search_leg(gi, reads, log, args.cal_reads) if not args.no_block else None
     e2e_s = dist.max(sum(e2e_t))
     e2e_value = total_reads * args.steps / e2e_s
     h2d = total + 8 * (n + 1)
@@ -600,6 +654,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
             "serving": serve,
             "cal_generation": cals,
             "alignment_lists": alns,
+            "block_search": block,
             "tuning": dict(gi.get_tuning(), block_load_mode=gi.load_mode(), start_table=gi.start_table(),
                            direction_split=gi.direction_split(), idle_batch=gi.idle_batch()),
             "autotune": ({"settings": len(table), "best_search_ms": min(r["search_us"] for r in table) / 1e3,
@@ -652,6 +707,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
+    ap.add_argument("--no-block", action="store_true", help="skip the k-error block search leg")
     ap.add_argument("--cal-reads", type=int, default=200_000,
                     help="reads of the batch taken through bwt_generate_cals_batch and bwt_map_inexact_batch "
                          "(0: skip)")

@@ -1019,8 +1019,12 @@ __global__ void __launch_bounds__(kBlock)
         const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
         ++sectors;
         const uint32_t sa = (s + j) % X.walk_mod;
-        const uint64_t len_calc = it.phys_len & 0x7FFFFFFFu;
-        const uint64_t key = phys ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
+        const uint64_t len_calc = it.phys_len & kRowLenMask;
+        uint64_t key = sa;
+        if (phys && (it.phys_len & kRowKey32))  // an int length: the SA_TYPE (32-bit) difference wraps
+          key = (uint32_t)((X.top + 1u) - sa - (uint32_t)len_calc - 1u);
+        else if (phys)
+          key = (uint64_t)((X.top + 1u) - sa) - len_calc - 1u;
         const uint32_t id = kar_search(X, key);
         hpg_loc_t o;
         o.key = key;

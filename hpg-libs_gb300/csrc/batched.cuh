@@ -85,8 +85,14 @@ struct BatchedTuning {
 // output index, and the physical direction with len_calc (bwt.c:2025-2036), so
 // that a lane starting a walk needs a single 16-byte load.
 struct RowItem {
-  uint32_t row, hit, out, phys_len;  // phys_len: direction << 31 | len_calc
+  uint32_t row, hit, out, phys_len;  // phys_len: direction << 31 | kRowKey32 flag | len_calc
 };
+// The forward-direction key size_SA - SA - len_calc - 1 taken in 32 bits: the
+// reference's anchor lists (bwt.c:1853-1855) subtract an int length from
+// SA_TYPE (uint32_t) values, so a row whose suffix is shorter than the length
+// wraps to a large 32-bit key (an invalid location), not a 64-bit one.
+constexpr uint32_t kRowKey32 = 1u << 30;
+constexpr uint32_t kRowLenMask = kRowKey32 - 1u;
 
 // Located rows of one batched call: row items carry 32-bit output indices and
 // rows are claimed through a 32-bit counter that may run a few claims past the

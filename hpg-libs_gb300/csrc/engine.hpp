@@ -104,6 +104,7 @@ std::mutex& map_api_mutex();
 
 struct MapRow {
   uint32_t row, phys, len_calc;  // SA row, physical index direction (0 backward, 1 forward), located length
+  uint32_t key32 = 0;  // 1: the forward key in 32-bit arithmetic, as the anchor lists (bwt.c:1853-1855)
 };
 // Seeds: per seed {read, first, last (included), 0}; out per seed {k, l} of the
 // '+' search and {k, l} of the '-' search (k = 1, l = 0 for seeds outside

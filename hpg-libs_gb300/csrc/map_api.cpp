@@ -426,7 +426,7 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
       const int kind = (c == 0 || c == 2) ? BACKWARD_ANCHOR : FORWARD_ANCHOR;
       if (nt == 0 || !(l - k < 50)) continue;  // at most 50 rows (bwt.c:1851)
       for (size_t j = k; j <= l; ++j) {
-        rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt});
+        rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt, 1});
         wants.push_back(Want{i, c < 2 ? 1 : 0, kind, nt});
       }
     }
@@ -688,7 +688,7 @@ std::vector<InexactOutcome> map_block(Engine* e, const std::vector<InexactRead>&
         const size_t k = (size_t)x.k, l = (size_t)x.l;
         if (!(l - k < 50)) continue;
         for (size_t j = k; j <= l; ++j) {
-          rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt});
+          rows.push_back(MapRow{(uint32_t)j, (uint32_t)kind, nt, 1});
           wants.push_back(Want{i, type, kind, nt});
         }
       }

@@ -230,7 +230,7 @@ int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, 
     items[i].row = rows[i].row;
     items[i].hit = (uint32_t)i;
     items[i].out = (uint32_t)i;
-    items[i].phys_len = (rows[i].phys << 31) | (rows[i].len_calc & 0x7FFFFFFFu);
+    items[i].phys_len = (rows[i].phys << 31) | (rows[i].key32 ? kRowKey32 : 0u) | (rows[i].len_calc & kRowLenMask);
   }
   if (!ensure(e, e->b_rowhit, m * sizeof(RowItem) + 16) || !ensure(e, e->locs, m * sizeof(hpg_loc_t) + 16) ||
       !ensure(e, e->b_ctr, 64)) {

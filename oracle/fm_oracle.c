@@ -511,10 +511,11 @@ static void locate(const fmo_index_t *ix, sink_t *s, uint32_t hid, int64_t k, in
 /*
  * BWSearchCPU (search/search.c:1171-1405) as bwt_map_inexact_read_2 drives it
  * (bwt.c:2413-2470): fragment size max(len / 2, 30), hence one or two
- * fragments and at most one error.  Three or more fragments need
- * change_direction (search/search.h:157-198), which reads the inverse suffix
- * array (R/Ri files) that the reference's index generator does not write; no
- * reference entry point reaches them, and this restatement refuses them.
+ * fragments and at most one error.  Three or more fragments (a caller of
+ * BWSearchCPU with a smaller fragment size) add the partial branch passes
+ * and change_direction (search/search.h:157-198), which reads the inverse
+ * suffix array (R/Ri, loaded by bwt_index_new with inverse_sa); no entry
+ * point of bwt.c reaches them, and this restatement refuses them.
  *
  * Results live in lists with the reference's capacity rule (add_result,
  * search/results.h:93-103): a full list refuses the result and the function

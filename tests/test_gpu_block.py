@@ -73,7 +73,10 @@ def test_block_search_repetitive_reads_and_locate_limit(tmp_path):
             want = ora.block_search(reads, max_results=mr, threads=8)
             got = g.block_search(reads, max_results=mr)
             assert got.equal(want), mr
-            assert (got.result.rs_count > 4).any()
+            if mr >= 100:
+                assert (got.result.rs_count > 4).any()  # more results than first-pass slots
+        # at 7, a homopolymer read's ~75 branch points per block overflow the list:
+        # the reference drops the block's branches
         assert (want.result.rs_truncated & 1).any()
         g.set_locate_limit(5000)
         lim = g.block_search(reads, max_results=100)
