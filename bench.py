@@ -463,8 +463,19 @@ def block_search_leg(gi, reads, log, n_lists: int) -> dict:
         best = dt if best is None else min(best, dt)
         k = gi.block_search_ms()
         kms = k if kms is None else min(kms, k)
+    # one more call with the sector census on (not timed): occupancy-block sectors the kernel reads
+    gi.set_census(True)
+    rs = lib.ResultSetC()
+    if gi.lib.bwt_gpu_block_search(gi.handle, seq.ctypes.data, offs.ctypes.data, n, MAX_RESULTS,
+                                   lib.ctypes.byref(rs), None, None) != 0:
+        raise RuntimeError(gi.lib.bwt_gpu_last_error().decode())
+    gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rs))
+    sectors = gi.census()
+    gi.set_census(False)
     out = {"reads": n, "seconds": round(best, 4), "reads_per_s": round(n / best, 1),
            "kernel_ms": round(kms, 3), "kernel_reads_per_s": round(n / (kms * 1e-3), 1),
+           "sectors_per_read": round(sectors / max(1, n), 2),
+           "gather_gsectors_per_s": round(sectors / (kms * 1e-3) / 1e9, 1),
            "hits_per_read": round(hits / max(1, n), 3), "located_rows_per_read": round(locs / max(1, n), 3),
            "max_results": MAX_RESULTS}
     log(f"[bench] block search: kernel {out['kernel_reads_per_s'] / 1e6:.1f} M reads/s ({kms:.2f} ms), "

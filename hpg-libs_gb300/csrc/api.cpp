@@ -178,66 +178,11 @@ int bwt_gpu_block_search(bwt_index_t* index, const char* seqs, const uint64_t* o
                          uint8_t* n_anchors) {
   Engine* e = engine_of(index);
   if (!e || !out || (n_reads && (!seqs || !offsets))) return fail("bwt_gpu_block_search: null argument");
-  std::memset(out, 0, sizeof(*out));
   std::string err;
-  BlockSearchOut b;
-  if (engine_block_search(e, seqs, offsets, n_reads, max_results, &b, &err) != 0) return fail(err);
-  // every row of every hit; (read, strand) lists over the locate limit stay unlocated
-  const size_t T = 2 * n_reads;
-  const uint64_t limit = engine_locate_limit(e);
-  std::vector<MapRow> rows;
-  std::vector<uint32_t> owner;
-  std::vector<uint8_t> trunc(T + 1, 0);
-  size_t h = 0;
-  for (size_t t = 0; t < T; ++t) {
-    const size_t c = b.count[t];
-    trunc[t] = b.refused[t];
-    uint64_t n_rows = 0;
-    for (size_t j = h; j < h + c; ++j) n_rows += (uint64_t)(b.hits[j].l - b.hits[j].k + 1);
-    if (limit && n_rows > limit) {
-      trunc[t] |= 2;
-      h += c;
-      continue;
-    }
-    const size_t rd = t >> 1;
-    const uint32_t len = (uint32_t)(offsets[rd + 1] - offsets[rd]);
-    for (size_t j = h; j < h + c; ++j) {
-      const hpg_hit_t& x = b.hits[j];
-      const int error = x.nm ? x.err_kind : 0;
-      uint32_t len_calc = len;
-      if (error == HPG_BWT_DELETION) --len_calc;
-      else if (error == HPG_BWT_INSERTION) ++len_calc;
-      const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir
-      for (int64_t r = x.k; r <= x.l; ++r) {
-        rows.push_back(MapRow{(uint32_t)r, phys, len_calc});
-        owner.push_back((uint32_t)j);
-      }
-    }
-    h += c;
-  }
-  out->n_reads = n_reads;
-  out->n_hits = b.hits.size();
-  out->n_locs = rows.size();
-  out->hits = (hpg_hit_t*)host_pool_alloc((b.hits.size() + 1) * sizeof(hpg_hit_t));
-  out->locs = (hpg_loc_t*)host_pool_alloc((rows.size() + 1) * sizeof(hpg_loc_t));
-  out->rs_count = (uint32_t*)host_pool_alloc((T + 1) * 4);
-  out->rs_truncated = (uint8_t*)host_pool_alloc(T + 1);
-  if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
-    bwt_gpu_result_free(out);
-    return fail("bwt_gpu_block_search: out of host memory");
-  }
-  if (!b.hits.empty()) std::memcpy(out->hits, b.hits.data(), b.hits.size() * sizeof(hpg_hit_t));
-  if (T) {
-    std::memcpy(out->rs_count, b.count.data(), T * 4);
-    std::memcpy(out->rs_truncated, trunc.data(), T);
-  }
-  if (!rows.empty() && engine_locate_rows(e, rows.data(), rows.size(), out->locs, &err) != 0) {
+  if (engine_block_search_result(e, seqs, offsets, n_reads, max_results, out, anchors, n_anchors, &err) != 0) {
     bwt_gpu_result_free(out);
     return fail(err);
   }
-  for (size_t i = 0; i < rows.size(); ++i) out->locs[i].hit = owner[i];
-  if (anchors && T) std::memcpy(anchors, b.anchors.data(), 2 * T * sizeof(hpg_block_anchor_t));
-  if (n_anchors && T) std::memcpy(n_anchors, b.n_anchors.data(), T);
   return 0;
 }
 

@@ -21,9 +21,12 @@
 // results run again into an exact range once the counts are scanned.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "engine_internal.hpp"
+#include "host_pool.hpp"
 
 namespace hpgbwt {
 
@@ -40,7 +43,15 @@ struct ItemOut {
   uint32_t read;
   uint32_t strand;
   bool refused;     // a list refused a result (full)
+  uint32_t sectors; // occurrence-block sectors the item read (census)
 };
+
+// BWiteration over a view, counting the 32-byte sectors it reads (one when k
+// and l share an occurrence block, else two).
+__device__ __forceinline__ void step(const DevIndex& X, View v, uint32_t c, uint32_t& k, uint32_t& l, uint32_t& sec) {
+  sec += (k >> 6) == (l >> 6) ? 1u : 2u;
+  bw_step(X, v, c, k, l);
+}
 
 // add_result (search/results.h:93-103) on rl_final.
 __device__ __forceinline__ bool emit(ItemOut& o, uint32_t dir, uint32_t nm, uint32_t kind, uint32_t base, int pos,
@@ -71,7 +82,7 @@ __device__ __forceinline__ bool emit(ItemOut& o, uint32_t dir, uint32_t nm, uint
 // BWExactFinalResultForward (search/search.h:114-155): the block rule, then
 // the walk over W[pos..end]; k, l are updated only when it survives.
 __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const uint8_t* W, int pos, int end, int bs,
-                                              int last_block, uint32_t& k, uint32_t& l) {
+                                              int last_block, uint32_t& k, uint32_t& l, uint32_t& sec) {
   const int cb = pos / bs;
   if (!(cb > last_block || pos == end + 1)) {
     if (cb < last_block) return false;
@@ -79,7 +90,7 @@ __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const u
   }
   uint32_t a = k, b = l;
   for (int i = pos; i <= end; ++i) {
-    bw_step(X, v, W[i], a, b);
+    step(X, v, W[i], a, b, sec);
     if (a > b) return false;
   }
   k = a;
@@ -90,7 +101,7 @@ __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const u
 // BWExactFinalResultBackward (search/search.h:67-112), over W[pos..start]
 // downwards.  C division truncates toward zero (pos may be -1).
 __device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const uint8_t* W, int pos, int start, int bs,
-                                               int last_block, uint32_t& k, uint32_t& l) {
+                                               int last_block, uint32_t& k, uint32_t& l, uint32_t& sec) {
   const int cb = pos / bs;
   if (!(cb < last_block || pos == start - 1)) {
     if (cb > last_block) return false;
@@ -98,7 +109,7 @@ __device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const 
   }
   uint32_t a = k, b = l;
   for (int i = pos; i >= start; --i) {
-    bw_step(X, v, W[i], a, b);
+    step(X, v, W[i], a, b, sec);
     if (a > b) return false;
   }
   k = a;
@@ -116,23 +127,23 @@ __device__ bool branch_forward(const DevIndex& X, View v, const uint8_t* W, int 
                                uint32_t l, ItemOut& o) {
   constexpr uint32_t kDir = 1;
   uint32_t a = k, b = l;
-  if (final_forward(X, v, W, pos + 1, end, bs, 0, a, b) &&
+  if (final_forward(X, v, W, pos + 1, end, bs, 0, a, b, o.sectors) &&
       !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
     return false;
   const uint32_t wp = W[pos];
   for (uint32_t c = 0; c < 4; ++c) {
     uint32_t ka = k, la = l;
-    bw_step(X, v, c, ka, la);
+    step(X, v, c, ka, la, o.sectors);
     if (ka > la || c == wp) continue;
     uint32_t rk = ka, rl = la;
     a = ka;
     b = la;
-    if (final_forward(X, v, W, pos, end, bs, 0, a, b)) {
+    if (final_forward(X, v, W, pos, end, bs, 0, a, b, o.sectors)) {
       if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
       rk = a;
       rl = b;
     }
-    if (final_forward(X, v, W, pos + 1, end, bs, 0, rk, rl) && !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
+    if (final_forward(X, v, W, pos + 1, end, bs, 0, rk, rl, o.sectors) && !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
       return false;
   }
   return true;
@@ -144,23 +155,23 @@ __device__ bool branch_backward(const DevIndex& X, View v, const uint8_t* W, int
   constexpr uint32_t kDir = 0;
   constexpr int start = 0;
   uint32_t a = k, b = l;
-  if (final_backward(X, v, W, pos - 1, start, bs, 0, a, b) &&
+  if (final_backward(X, v, W, pos - 1, start, bs, 0, a, b, o.sectors) &&
       !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
     return false;
   const uint32_t wp = W[pos];
   for (uint32_t c = 0; c < 4; ++c) {
     uint32_t ka = k, la = l;
-    bw_step(X, v, c, ka, la);
+    step(X, v, c, ka, la, o.sectors);
     if (ka > la || c == wp) continue;
     uint32_t rk = ka, rl = la;
     a = ka;
     b = la;
-    if (final_backward(X, v, W, pos, start, bs, 0, a, b)) {
+    if (final_backward(X, v, W, pos, start, bs, 0, a, b, o.sectors)) {
       if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
       rk = a;
       rl = b;
     }
-    if (final_backward(X, v, W, pos - 1, start, bs, 0, rk, rl) &&
+    if (final_backward(X, v, W, pos - 1, start, bs, 0, rk, rl, o.sectors) &&
         !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
       return false;
   }
@@ -173,13 +184,13 @@ __device__ bool branch_backward(const DevIndex& X, View v, const uint8_t* W, int
 // points that walk appends; `survive` whether it covers the whole range with
 // a non-empty interval (then k, l hold that interval).
 __device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int from, int to, int dstep, uint32_t& k,
-                               uint32_t& l, bool& survive, uint32_t& zt) {
+                               uint32_t& l, bool& survive, uint32_t& zt, uint32_t& sec) {
   uint32_t a = k, b = l;
   uint32_t z = 0, changes = 0;
   bool alive = true, failed_step = false;
   for (int i = from; i != to + dstep; i += dstep) {
     const int64_t before = (int64_t)b - (int64_t)a;
-    bw_step(X, v, W[i], a, b);
+    step(X, v, W[i], a, b, sec);
     if (alive) {
       if (a > b) {
         alive = false;
@@ -237,7 +248,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
     int i;
     if (strand) {  // type 0: forward search from the first base
       for (i = 0; i <= len - 1; ++i) {
-        bw_step(X, fw, W[i], k, l);
+        step(X, fw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
@@ -246,7 +257,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
       if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
     } else {
       for (i = len - 1; i >= 0; --i) {
-        bw_step(X, bw, W[i], k, l);
+        step(X, bw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
@@ -263,7 +274,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
     uint32_t k = 0, l = X.top, gk = 0, gl = 0;
     int i;
     for (i = 0; i <= frag - 1; ++i) {
-      bw_step(X, fw, W[i], k, l);
+      step(X, fw, W[i], k, l, o.sectors);
       if (k > l) break;
       gk = k;
       gl = l;
@@ -278,7 +289,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
       // the read, and a walk that survives it is a result (complete search)
       uint32_t fk = k, fl = l, zt = 0;
       bool survive = false;
-      const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt);
+      const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
       if (points > o.cap) {
         o.refused = true;  // rl_next overflows: the block's branches are dropped
       } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
@@ -287,7 +298,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
         for (int p = frag; p <= end; ++p) {
           const uint32_t pk = a, pl = b;
           const int64_t before = (int64_t)b - (int64_t)a;
-          bw_step(X, fw, W[p], a, b);
+          step(X, fw, W[p], a, b, o.sectors);
           const bool failed = a > b;
           const bool changed = failed || (int64_t)b - (int64_t)a != before;
           if (changed && (failed ? ok_at : ok_before) && !branch_forward(X, fw, W, p, end, frag, pk, pl, o)) break;
@@ -302,7 +313,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
     uint32_t k = 0, l = X.top, gk = 0, gl = 0;
     int i;
     for (i = end; i >= frag; --i) {
-      bw_step(X, bw, W[i], k, l);
+      step(X, bw, W[i], k, l, o.sectors);
       if (k > l) break;
       gk = k;
       gl = l;
@@ -317,7 +328,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
       // from above, so the rule walks the whole of it without completing
       uint32_t fk = k, fl = l, zt = 0;
       bool survive = false;
-      const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt);
+      const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt, o.sectors);
       if (points > o.cap) {
         o.refused = true;
       } else {
@@ -326,7 +337,7 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
         for (int p = frag - 1; p >= 0; --p) {
           const uint32_t pk = a, pl = b;
           const int64_t before = (int64_t)b - (int64_t)a;
-          bw_step(X, bw, W[p], a, b);
+          step(X, bw, W[p], a, b, o.sectors);
           const bool failed = a > b;
           const bool changed = failed || (int64_t)b - (int64_t)a != before;
           if (changed && (failed ? ok_at : ok_before) && !branch_backward(X, bw, W, p, frag, pk, pl, o)) break;
@@ -343,7 +354,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_search_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
     uint32_t n_items, const uint32_t* __restrict__ items, const uint64_t* __restrict__ slot_off, uint32_t room,
     uint32_t max_results, hpg_hit_t* __restrict__ out, uint32_t* __restrict__ count, uint8_t* __restrict__ refused,
-    hpg_block_anchor_t* __restrict__ anchors, uint8_t* __restrict__ n_anchors) {
+    hpg_block_anchor_t* __restrict__ anchors, uint8_t* __restrict__ n_anchors, unsigned long long* census) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_items) return;
   const uint32_t t = items ? items[g] : g;
@@ -356,6 +367,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_search_kernel(
   o.read = read;
   o.strand = t & 1u;
   o.refused = false;
+  o.sectors = 0;
   uint32_t na = 0;
   const uint64_t b0 = offs[read];
   const int len = (int)(offs[read + 1] - b0);
@@ -364,6 +376,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_search_kernel(
   if (count) count[t] = o.n;
   if (refused) refused[t] = o.refused ? 1 : 0;
   if (n_anchors) n_anchors[t] = (uint8_t)na;
+  if (census) atomicAdd(census, (unsigned long long)o.sectors);
 }
 
 // The first pass's slots of each item, packed at its scanned offset.
@@ -375,7 +388,126 @@ __global__ void block_pack_kernel(const hpg_hit_t* __restrict__ slots, const uin
   for (uint32_t j = 0; j < c; ++j) out[off[t] + j] = slots[(uint64_t)t * kBlockSlots + j];
 }
 
+// Rows of each hit for the locate pass: l - k + 1, or 0 for every hit of a
+// (read, strand) list whose rows pass the locate limit (that list's flag bit 1).
+__global__ void block_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint32_t* __restrict__ count,
+                                  const uint64_t* __restrict__ off, uint32_t n_items, uint64_t limit,
+                                  uint32_t* __restrict__ hit_rows, uint8_t* __restrict__ flags) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_items) return;
+  const uint64_t h0 = off[t], h1 = h0 + count[t];
+  uint64_t rows = 0;
+  for (uint64_t h = h0; h < h1; ++h) rows += (uint64_t)(hits[h].l - hits[h].k + 1);
+  const bool over = limit && rows > limit;
+  for (uint64_t h = h0; h < h1; ++h) hit_rows[h] = over ? 0u : (uint32_t)(hits[h].l - hits[h].k + 1);
+  if (over) flags[t] |= 2;
+}
+
+// One locate item per row: row r belongs to the hit whose row range holds it
+// (binary search over the scanned row counts; empty ranges are never chosen).
+// len_calc as bwt.c:2497-2510: the read length, one less for a DELETION, one
+// more for an INSERTION; the direction is dir, flipped on the '-' strand.
+__global__ void block_items_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ row_off,
+                                   uint32_t n_hits, uint64_t n_rows, const uint64_t* __restrict__ offs,
+                                   RowItem* __restrict__ items) {
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < n_rows;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = n_hits;  // last h with row_off[h] <= r
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (row_off[mid] <= r) lo = mid;
+      else hi = mid;
+    }
+    const hpg_hit_t x = hits[lo];
+    uint32_t len = (uint32_t)(offs[x.read + 1] - offs[x.read]);
+    const uint32_t err = x.nm ? x.err_kind : 0u;
+    if (err == HPG_BWT_DELETION) --len;
+    else if (err == HPG_BWT_INSERTION) ++len;
+    RowItem it;
+    it.row = (uint32_t)(x.k + (int64_t)(r - row_off[lo]));
+    it.hit = lo;
+    it.out = (uint32_t)r;
+    it.phys_len = ((uint32_t)(x.dir ^ x.strand) << 31) | (len & kRowLenMask);
+    items[r] = it;
+  }
+}
+
 unsigned grid_of(size_t n) { return (unsigned)((n + kBlockTpb - 1) / kBlockTpb); }
+
+// The search of every (read, strand) of the uploaded batch; on return the
+// device holds the packed hits (e->hits), per-item counts (e->rs_count) and
+// hit offsets (e->hit_off), refused flags (e->rs_trunc), anchors (e->vecs)
+// and anchor counts (e->ovf); counts also on the host.
+int block_search_device(Engine* e, size_t n, uint32_t max_results, std::vector<uint32_t>& count, uint64_t* total_out,
+                        std::string* err) {
+  const size_t T = 2 * n;
+  if (!ensure(e, e->slots, T * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->rs_count, T * 4 + 16) ||
+      !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
+      !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
+      !ensure(e, e->ovf, T + 16) || !ensure(e, e->census, 16)) {
+    *err = oom_message("block search", T * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 14));
+    return -1;
+  }
+  cudaStream_t s = e->stream;
+  uint32_t* d_count = ptr<uint32_t>(e->rs_count);
+  uint64_t* d_off = ptr<uint64_t>(e->hit_off);
+  unsigned long long* census = e->census_on ? ptr<unsigned long long>(e->census) : nullptr;
+  if (census) cudaMemsetAsync(census, 0, 8, s);
+  cudaEventRecord(e->cev[0], s);
+  count_launches(1);
+  block_search_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(
+      e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)T, nullptr, nullptr,
+      kBlockSlots, max_results, ptr<hpg_hit_t>(e->slots), d_count, ptr<uint8_t>(e->rs_trunc),
+      ptr<hpg_block_anchor_t>(e->vecs), ptr<uint8_t>(e->ovf), census);
+  cudaEventRecord(e->cev[1], s);
+  launch_scan(d_count, T, d_off, ptr<uint64_t>(e->scan_part), s);
+  count.resize(T);
+  HPG_CUDA(cudaMemcpyAsync(count.data(), d_count, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
+  uint64_t total = 0;
+  HPG_CUDA(cudaMemcpyAsync(&total, d_off + T, 8, cudaMemcpyDeviceToHost, s), "block total");
+  if (census) HPG_CUDA(cudaMemcpyAsync(&e->census_val, census, 8, cudaMemcpyDeviceToHost, s), "block census");
+  HPG_CUDA(cudaStreamSynchronize(s), "block search");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
+  e->block_ms = ms;
+  if (!ensure(e, e->hits, (total + 1) * sizeof(hpg_hit_t))) {
+    *err = oom_message("block search results", (total + 1) * sizeof(hpg_hit_t));
+    return -1;
+  }
+  hpg_hit_t* d_hits = ptr<hpg_hit_t>(e->hits);
+  count_launches(1);
+  block_pack_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->slots), d_count, d_off, (uint32_t)T, d_hits);
+  // items with more results than slots: the same search again, into their exact ranges
+  std::vector<uint32_t> again;
+  for (size_t t = 0; t < T; ++t)
+    if (count[t] > kBlockSlots) again.push_back((uint32_t)t);
+  if (!again.empty()) {
+    if (!ensure(e, e->rows, again.size() * 4 + 16)) {
+      *err = oom_message("block search retry list", again.size() * 4);
+      return -1;
+    }
+    HPG_CUDA(cudaMemcpyAsync(e->rows.p, again.data(), again.size() * 4, cudaMemcpyHostToDevice, s), "retry list");
+    cudaEventRecord(e->cev[0], s);
+    count_launches(1);
+    block_search_kernel<<<grid_of(again.size()), kBlockTpb, 0, s>>>(
+        e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)again.size(),
+        ptr<uint32_t>(e->rows), d_off, 0xFFFFFFFFu, max_results, d_hits, nullptr, nullptr, nullptr, nullptr, nullptr);
+    cudaEventRecord(e->cev[1], s);
+    HPG_CUDA(cudaStreamSynchronize(s), "block search retry");  // `again` is pageable and local
+    cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
+    e->block_ms += ms;
+  }
+  *total_out = total;
+  return 0;
+}
+
+int check_block_args(size_t n, std::string* err) {
+  if (n >= (1ull << 30)) {
+    *err = "too many reads in one block search";
+    return -1;
+  }
+  return 0;
+}
 
 }  // namespace
 
@@ -389,64 +521,14 @@ int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_
   out->n_anchors.assign(2 * n, 0);
   out->kernel_ms = 0;
   if (!n) return 0;
-  if (n >= (1ull << 30)) {
-    *err = "too many reads in one block search";
-    return -1;
-  }
-  if (upload_reads(e, seqs, offs, n, err) != 0) return -1;
-  const size_t T = 2 * n;
-  if (!ensure(e, e->slots, T * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->rs_count, T * 4 + 16) ||
-      !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
-      !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
-      !ensure(e, e->ovf, T + 16)) {
-    *err = oom_message("block search", T * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 14));
-    return -1;
-  }
-  cudaStream_t s = e->stream;
-  uint32_t* d_count = ptr<uint32_t>(e->rs_count);
-  uint64_t* d_off = ptr<uint64_t>(e->hit_off);
-  cudaEventRecord(e->cev[0], s);
-  count_launches(1);
-  block_search_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(
-      e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)T, nullptr, nullptr,
-      kBlockSlots, max_results, ptr<hpg_hit_t>(e->slots), d_count, ptr<uint8_t>(e->rs_trunc),
-      ptr<hpg_block_anchor_t>(e->vecs), ptr<uint8_t>(e->ovf));
-  cudaEventRecord(e->cev[1], s);
-  launch_scan(d_count, T, d_off, ptr<uint64_t>(e->scan_part), s);
-  HPG_CUDA(cudaMemcpyAsync(out->count.data(), d_count, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
+  if (check_block_args(n, err) != 0 || upload_reads(e, seqs, offs, n, err) != 0) return -1;
   uint64_t total = 0;
-  HPG_CUDA(cudaMemcpyAsync(&total, d_off + T, 8, cudaMemcpyDeviceToHost, s), "block total");
-  HPG_CUDA(cudaStreamSynchronize(s), "block search");
-  float ms = 0;
-  cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
-  out->kernel_ms = ms;
-  if (!ensure(e, e->hits, (total + 1) * sizeof(hpg_hit_t))) {
-    *err = oom_message("block search results", (total + 1) * sizeof(hpg_hit_t));
-    return -1;
-  }
-  hpg_hit_t* d_hits = ptr<hpg_hit_t>(e->hits);
-  count_launches(1);
-  block_pack_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->slots), d_count, d_off, (uint32_t)T, d_hits);
-  // items with more results than slots: the same search again, into their exact ranges
-  std::vector<uint32_t> again;
-  for (size_t t = 0; t < T; ++t)
-    if (out->count[t] > kBlockSlots) again.push_back((uint32_t)t);
-  if (!again.empty()) {
-    if (!ensure(e, e->rows, again.size() * 4 + 16)) {
-      *err = oom_message("block search retry list", again.size() * 4);
-      return -1;
-    }
-    HPG_CUDA(cudaMemcpyAsync(e->rows.p, again.data(), again.size() * 4, cudaMemcpyHostToDevice, s), "retry list");
-    cudaEventRecord(e->cev[0], s);
-    count_launches(1);
-    block_search_kernel<<<grid_of(again.size()), kBlockTpb, 0, s>>>(
-        e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)again.size(),
-        ptr<uint32_t>(e->rows), d_off, 0xFFFFFFFFu, max_results, d_hits, nullptr, nullptr, nullptr, nullptr);
-    cudaEventRecord(e->cev[1], s);
-  }
+  if (block_search_device(e, n, max_results, out->count, &total, err) != 0) return -1;
+  const size_t T = 2 * n;
+  cudaStream_t s = e->stream;
   out->hits.resize(total);
   if (total)
-    HPG_CUDA(cudaMemcpyAsync(out->hits.data(), d_hits, total * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
+    HPG_CUDA(cudaMemcpyAsync(out->hits.data(), e->hits.p, total * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
              "block results");
   HPG_CUDA(cudaMemcpyAsync(out->refused.data(), e->rs_trunc.p, T, cudaMemcpyDeviceToHost, s), "block flags");
   HPG_CUDA(cudaMemcpyAsync(out->anchors.data(), e->vecs.p, 2 * T * sizeof(hpg_block_anchor_t),
@@ -454,11 +536,94 @@ int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_
            "block anchors");
   HPG_CUDA(cudaMemcpyAsync(out->n_anchors.data(), e->ovf.p, T, cudaMemcpyDeviceToHost, s), "block anchor counts");
   HPG_CUDA(cudaStreamSynchronize(s), "block search results");
-  if (!again.empty()) {
-    cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
-    out->kernel_ms += ms;
+  out->kernel_ms = e->block_ms;
+  return 0;
+}
+
+int engine_block_search_result(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t max_results,
+                               hpg_result_set_t* out, hpg_block_anchor_t* anchors, uint8_t* n_anchors,
+                               std::string* err) {
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  std::memset(out, 0, sizeof(*out));
+  out->n_reads = n;
+  const size_t T = 2 * n;
+  std::vector<uint32_t> count;
+  uint64_t total = 0;
+  if (n) {
+    if (check_block_args(n, err) != 0 || upload_reads(e, seqs, offs, n, err) != 0) return -1;
+    if (block_search_device(e, n, max_results, count, &total, err) != 0) return -1;
   }
-  e->block_ms = out->kernel_ms;
+  cudaStream_t s = e->stream;
+  // rows of every hit (lists over the locate limit: none), their items, the locate pass
+  uint64_t n_rows = 0;
+  if (total) {
+    if (total >= 0xFFFFFFFFull) {
+      *err = "too many block search results in one call";
+      return -1;
+    }
+    if (!ensure(e, e->ovf_count, total * 4 + 16) || !ensure(e, e->loc_off, (total + 1) * 8) ||
+        !ensure(e, e->scan_part, std::max(scan_parts(total), scan_parts(T)) * 8)) {
+      *err = oom_message("block search rows", total * 12);
+      return -1;
+    }
+    count_launches(1);
+    block_rows_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->hits), ptr<uint32_t>(e->rs_count),
+                                                       ptr<uint64_t>(e->hit_off), (uint32_t)T, e->locate_limit,
+                                                       ptr<uint32_t>(e->ovf_count), ptr<uint8_t>(e->rs_trunc));
+    launch_scan(ptr<uint32_t>(e->ovf_count), total, ptr<uint64_t>(e->loc_off), ptr<uint64_t>(e->scan_part), s);
+    HPG_CUDA(cudaMemcpyAsync(&n_rows, ptr<uint64_t>(e->loc_off) + total, 8, cudaMemcpyDeviceToHost, s), "row total");
+    HPG_CUDA(cudaStreamSynchronize(s), "block rows");
+    if (n_rows > kMaxLocateRows) {
+      *err = "block search: " + std::to_string(n_rows) + " rows to locate in one call (set a locate limit)";
+      return -1;
+    }
+    if (n_rows) {
+      if (!ensure(e, e->b_rowhit, n_rows * sizeof(RowItem) + 16) ||
+          !ensure(e, e->locs, n_rows * sizeof(hpg_loc_t) + 16) || !ensure(e, e->b_ctr, 64)) {
+        *err = oom_message("block search locate", n_rows * (sizeof(RowItem) + sizeof(hpg_loc_t)));
+        return -1;
+      }
+      const uint64_t blocks = std::min<uint64_t>((n_rows + kBlockTpb - 1) / kBlockTpb, (uint64_t)e->num_sms * 16);
+      count_launches(1);
+      block_items_kernel<<<(unsigned)blocks, kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->hits), ptr<uint64_t>(e->loc_off),
+                                                               (uint32_t)total, n_rows, ptr<uint64_t>(e->offs),
+                                                               static_cast<RowItem*>(e->b_rowhit.p));
+      launch_locate_items(e->X, static_cast<const RowItem*>(e->b_rowhit.p), n_rows, ptr<hpg_loc_t>(e->locs),
+                          ptr<unsigned int>(e->b_ctr) + 5, e->num_sms, s);
+    }
+  }
+  out->hits = (hpg_hit_t*)host_pool_alloc((total + 1) * sizeof(hpg_hit_t));
+  out->locs = (hpg_loc_t*)host_pool_alloc((n_rows + 1) * sizeof(hpg_loc_t));
+  out->rs_count = (uint32_t*)host_pool_alloc((T + 1) * 4);
+  out->rs_truncated = (uint8_t*)host_pool_alloc(T + 1);
+  if (!out->hits || !out->locs || !out->rs_count || !out->rs_truncated) {
+    *err = "out of host memory (block search results)";
+    return -1;
+  }
+  out->n_hits = total;
+  out->n_locs = n_rows;
+  if (T) {
+    std::memcpy(out->rs_count, count.data(), T * 4);
+    HPG_CUDA(cudaMemcpyAsync(out->rs_truncated, e->rs_trunc.p, T, cudaMemcpyDeviceToHost, s), "block flags");
+    if (anchors)
+      HPG_CUDA(cudaMemcpyAsync(anchors, e->vecs.p, 2 * T * sizeof(hpg_block_anchor_t), cudaMemcpyDeviceToHost, s),
+               "block anchors");
+    if (n_anchors) HPG_CUDA(cudaMemcpyAsync(n_anchors, e->ovf.p, T, cudaMemcpyDeviceToHost, s), "anchor counts");
+  }
+  if (total)
+    HPG_CUDA(cudaMemcpyAsync(out->hits, e->hits.p, total * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
+             "block results");
+  if (n_rows)
+    HPG_CUDA(cudaMemcpyAsync(out->locs, e->locs.p, n_rows * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, s),
+             "located rows");
+  HPG_CUDA(cudaStreamSynchronize(s), "block search results");
+  uint32_t derr = 0;
+  HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+  if (derr) {
+    cudaMemset(e->d_err, 0, 4);
+    *err = "corrupt index: suffix-array walk did not reach a sampled row";
+    return -1;
+  }
   return 0;
 }
 

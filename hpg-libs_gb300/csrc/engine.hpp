@@ -128,7 +128,13 @@ struct BlockSearchOut {
 };
 int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t max_results,
                         BlockSearchOut* out, std::string* err);
-float engine_block_ms(Engine* e);  // kernel_ms of the last block search
+// The same search with every row of every hit located on the device (the
+// locate limit applies), as a result set in pooled host arrays; anchors and
+// n_anchors (4 n and 2 n entries) may be null.
+int engine_block_search_result(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint32_t max_results,
+                               hpg_result_set_t* out, hpg_block_anchor_t* anchors, uint8_t* n_anchors,
+                               std::string* err);
+float engine_block_ms(Engine* e);  // device time of the last block search's kernels
 // Batched form: hits only, no located rows.
 void engine_set_skip_locate(Engine* e, int on);
 uint32_t engine_sa_top(Engine* e);  // last SA row (n)
