@@ -217,9 +217,9 @@ __device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int 
   return (bound_before ? changes : 0u) + (failed_step && bound_at ? 1u : 0u);
 }
 
-__device__ __forceinline__ void put_anchor(hpg_block_anchor_t* anchors, uint32_t& na, uint32_t dir, int start, int end,
-                                           int pos, uint32_t k, uint32_t l) {
-  if (anchors) {
+__device__ __forceinline__ void put_anchor(hpg_block_anchor_t* anchor, uint32_t& aflag, uint32_t dir, int start,
+                                           int end, int pos, uint32_t k, uint32_t l) {
+  if (anchor) {
     hpg_block_anchor_t x;
     x.k = k;
     x.l = l;
@@ -228,49 +228,71 @@ __device__ __forceinline__ void put_anchor(hpg_block_anchor_t* anchors, uint32_t
     x.pos = (int16_t)pos;
     x.dir = (uint8_t)dir;
     x.pad = 0;
-    anchors[na] = x;
+    *anchor = x;
   }
-  ++na;
+  aflag |= 1u;
 }
 
-// One (read, strand): BWSearchCPU with two fragments or fewer.
-__device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, ItemOut& o,
-                           hpg_block_anchor_t* anchors, uint32_t& na) {
+// Fragments of a read: bwt.c:2408-2412 takes len / (num_errors + 1), at least
+// 30, and BWSearchCPU divides the length by it (search.c:1175).
+__device__ __forceinline__ int fragments_of(int len, int& frag) {
+  frag = len / 2;
+  if (frag < 30) frag = 30;
+  return len / frag;
+}
+
+// The block of a (read, strand) that runs on physical index direction `phys`:
+// 0 block 0 (or the one exact search of a single-fragment read), 1 the last
+// block, -1 none.  Block 0 searches forward over `forward` ('+': the forward
+// index; '-': backward_rev, the backward index), the last block backward over
+// `backward` ('+': the backward index; '-': forward_rev, the forward index); a
+// single-fragment read's exact search is on the backward index for both
+// strands ('+' backward over backward, '-' forward over backward_rev).
+__device__ __forceinline__ int part_on(uint32_t strand, int fragments, uint32_t phys) {
+  if (fragments <= 1) return phys == 0 ? 0 : -1;
+  return (strand ^ phys) ? 0 : 1;
+}
+
+// One block of a (read, strand) (BWSearchCPU, search.c:1171-1405, with two
+// fragments or fewer), its results emitted as if the list were empty; the
+// merge cuts the last block's results to the room block 0 left.  aflag bit 0:
+// the block's anchor was set; bit 1: the block-0 fragment matched (with lists
+// of capacity 0 BWSearchCPU then returns before the last block).
+__device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
+                           hpg_block_anchor_t* anchor, uint32_t& aflag) {
   // type 1 ('+', strand 0): backward = backward, forward = forward;
   // type 0 ('-', strand 1): backward = forward_rev, forward = backward_rev (bwt.c:2440-2472)
   const View bw = strand ? View{1, 1} : View{0, 0};
   const View fw = strand ? View{0, 1} : View{1, 0};
-  int frag = len / 2;
-  if (frag < 30) frag = 30;
-  const int fragments = len / frag;
+  int frag = 30;
+  const int fragments = fragments_of(len, frag);
+  const int end = len - 1;
   if (fragments <= 1) {  // search.c:1191-1224: one exact search of the whole read
     uint32_t k = 0, l = X.top, gk = 0, gl = 0;
     int i;
     if (strand) {  // type 0: forward search from the first base
-      for (i = 0; i <= len - 1; ++i) {
+      for (i = 0; i <= end; ++i) {
         step(X, fw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
       }
-      put_anchor(anchors, na, 1, 0, i - 1, i, gk, gl);
+      put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
       if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
     } else {
-      for (i = len - 1; i >= 0; --i) {
+      for (i = end; i >= 0; --i) {
         step(X, bw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
       }
-      put_anchor(anchors, na, 0, i + 1, len - 1, i, gk, gl);
+      put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
       if (k <= l) emit(o, 0, 0, 0, 0, 0, k, l);
     }
     return;
   }
-  const int end = len - 1;
 
-  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
-  {
+  if (part == 0) {  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
     uint32_t k = 0, l = X.top, gk = 0, gl = 0;
     int i;
     for (i = 0; i <= frag - 1; ++i) {
@@ -279,113 +301,177 @@ __device__ void block_item(const DevIndex& X, const uint8_t* W, int len, uint32_
       gk = k;
       gl = l;
     }
-    put_anchor(anchors, na, 1, 0, i - 1, i, gk, gl);
-    if (k <= l) {
-      if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
-        o.refused = true;
-        return;
-      }
-      // exact-partial range: pos = frag is past block 0, so the whole rest of
-      // the read, and a walk that survives it is a result (complete search)
-      uint32_t fk = k, fl = l, zt = 0;
-      bool survive = false;
-      const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
-      if (points > o.cap) {
-        o.refused = true;  // rl_next overflows: the block's branches are dropped
-      } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
-        const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
-        uint32_t a = k, b = l;
-        for (int p = frag; p <= end; ++p) {
-          const uint32_t pk = a, pl = b;
-          const int64_t before = (int64_t)b - (int64_t)a;
-          step(X, fw, W[p], a, b, o.sectors);
-          const bool failed = a > b;
-          const bool changed = failed || (int64_t)b - (int64_t)a != before;
-          if (changed && (failed ? ok_at : ok_before) && !branch_forward(X, fw, W, p, end, frag, pk, pl, o)) break;
-          if (failed) break;
-        }
+    put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
+    if (k > l) return;
+    aflag |= 2u;
+    if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
+      o.refused = true;
+      return;
+    }
+    // exact-partial range: pos = frag is past block 0, so the whole rest of
+    // the read, and a walk that survives it is a result (complete search)
+    uint32_t fk = k, fl = l, zt = 0;
+    bool survive = false;
+    const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
+    if (points > o.cap) {
+      o.refused = true;  // rl_next overflows: the block's branches are dropped
+    } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
+      const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
+      uint32_t a = k, b = l;
+      for (int p = frag; p <= end; ++p) {
+        const uint32_t pk = a, pl = b;
+        const int64_t before = (int64_t)b - (int64_t)a;
+        step(X, fw, W[p], a, b, o.sectors);
+        const bool failed = a > b;
+        const bool changed = failed || (int64_t)b - (int64_t)a != before;
+        if (changed && (failed ? ok_at : ok_before) && !branch_forward(X, fw, W, p, end, frag, pk, pl, o)) break;
+        if (failed) break;
       }
     }
+    return;
   }
 
   // last block: backward over W[frag .. len-1] (search.c:1360-1402)
-  {
-    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
-    int i;
-    for (i = end; i >= frag; --i) {
-      step(X, bw, W[i], k, l, o.sectors);
-      if (k > l) break;
-      gk = k;
-      gl = l;
-    }
-    put_anchor(anchors, na, 0, i + 1, end, i, gk, gl);
-    if (k <= l) {
-      if (o.cap == 0) {
-        o.refused = true;
-        return;
-      }
-      // exact-partial range: pos = frag - 1 is the first element of block 0
-      // from above, so the rule walks the whole of it without completing
-      uint32_t fk = k, fl = l, zt = 0;
-      bool survive = false;
-      const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt, o.sectors);
-      if (points > o.cap) {
-        o.refused = true;
-      } else {
-        const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
-        uint32_t a = k, b = l;
-        for (int p = frag - 1; p >= 0; --p) {
-          const uint32_t pk = a, pl = b;
-          const int64_t before = (int64_t)b - (int64_t)a;
-          step(X, bw, W[p], a, b, o.sectors);
-          const bool failed = a > b;
-          const bool changed = failed || (int64_t)b - (int64_t)a != before;
-          if (changed && (failed ? ok_at : ok_before) && !branch_backward(X, bw, W, p, frag, pk, pl, o)) break;
-          if (failed) break;
-        }
-      }
-    }
+  uint32_t k = 0, l = X.top, gk = 0, gl = 0;
+  int i;
+  for (i = end; i >= frag; --i) {
+    step(X, bw, W[i], k, l, o.sectors);
+    if (k > l) break;
+    gk = k;
+    gl = l;
+  }
+  put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
+  if (k > l) return;
+  if (o.cap == 0) {
+    o.refused = true;
+    return;
+  }
+  // exact-partial range: pos = frag - 1 is the first element of block 0
+  // from above, so the rule walks the whole of it without completing
+  uint32_t fk = k, fl = l, zt = 0;
+  bool survive = false;
+  const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt, o.sectors);
+  if (points > o.cap) {
+    o.refused = true;
+    return;
+  }
+  const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
+  uint32_t a = k, b = l;
+  for (int p = frag - 1; p >= 0; --p) {
+    const uint32_t pk = a, pl = b;
+    const int64_t before = (int64_t)b - (int64_t)a;
+    step(X, bw, W[p], a, b, o.sectors);
+    const bool failed = a > b;
+    const bool changed = failed || (int64_t)b - (int64_t)a != before;
+    if (changed && (failed ? ok_at : ok_before) && !branch_backward(X, bw, W, p, frag, pk, pl, o)) break;
+    if (failed) break;
   }
 }
 
-// Work item g runs item t = items ? items[g] : g (t = 2 * read + strand).
-// Results go to out + (slot_off ? slot_off[t] : t * room).
-__global__ void __launch_bounds__(kBlockTpb) block_search_kernel(
+// Per-block state of a batch: list t = 2 * read + strand has blocks 2t (block
+// 0 or the one exact search) and 2t + 1 (the last block).
+struct PartState {
+  hpg_hit_t* slots;               // kBlockSlots results per block (first pass)
+  uint32_t* count;                // results per block, each as if alone in the list
+  uint8_t* refused;               // a list of the block refused a result
+  uint8_t* aflag;                 // put_anchor / block-0 match bits
+  hpg_block_anchor_t* anchor;     // the block's anchor
+};
+
+// First pass (items == nullptr): thread g runs the block of list g that is on
+// physical direction `phys`, into its slots (one launch per direction, so that
+// the launch reads one direction's occurrence blocks).  Retry: item items[g] =
+// 2 * list + part runs again into the list's final range, the last block after
+// block 0's results and cut to the room they left.
+__global__ void __launch_bounds__(kBlockTpb) block_part_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
-    uint32_t n_items, const uint32_t* __restrict__ items, const uint64_t* __restrict__ slot_off, uint32_t room,
-    uint32_t max_results, hpg_hit_t* __restrict__ out, uint32_t* __restrict__ count, uint8_t* __restrict__ refused,
-    hpg_block_anchor_t* __restrict__ anchors, uint8_t* __restrict__ n_anchors, unsigned long long* census) {
+    uint32_t n_items, const uint32_t* __restrict__ items, uint32_t phys, uint32_t max_results, PartState ps,
+    const uint64_t* __restrict__ list_off, hpg_hit_t* __restrict__ hits, unsigned long long* census) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_items) return;
-  const uint32_t t = items ? items[g] : g;
-  const uint32_t read = t >> 1;
+  // first pass: the '+' lists in the first half of the threads, the '-' ones in
+  // the second, so that a warp's lanes run the same block code (per direction,
+  // '+' and '-' run different blocks)
+  const uint32_t half = n_items >> 1;
+  const uint32_t list = items ? items[g] >> 1 : (g < half ? 2 * g : 2 * (g - half) + 1);
+  const uint32_t read = list >> 1, strand = list & 1u;
+  const uint64_t b0 = offs[read];
+  const int len = (int)(offs[read + 1] - b0);
+  if (!ok[read] || len < 3 || len > 32767) return;
+  int part;
+  if (items) {
+    part = (int)(items[g] & 1u);
+  } else {
+    int frag = 30;
+    part = part_on(strand, fragments_of(len, frag), phys);
+    if (part < 0) return;
+  }
+  const uint32_t it = 2 * list + (uint32_t)part;
   ItemOut o;
-  o.slot = out + (slot_off ? slot_off[t] : (uint64_t)t * room);
-  o.room = room;
   o.cap = max_results;
   o.n = 0;
   o.read = read;
-  o.strand = t & 1u;
+  o.strand = strand;
   o.refused = false;
   o.sectors = 0;
-  uint32_t na = 0;
-  const uint64_t b0 = offs[read];
-  const int len = (int)(offs[read + 1] - b0);
-  if (ok[read] && len >= 3 && len <= 32767)
-    block_item(X, codes + b0, len, o.strand, o, anchors ? anchors + 2ull * t : nullptr, na);
-  if (count) count[t] = o.n;
-  if (refused) refused[t] = o.refused ? 1 : 0;
-  if (n_anchors) n_anchors[t] = (uint8_t)na;
+  if (items) {
+    const uint32_t n0 = ps.count[2 * list];
+    const uint32_t room1 = max_results - n0;
+    const uint32_t m1 = ps.count[2 * list + 1] < room1 ? ps.count[2 * list + 1] : room1;
+    o.slot = hits + list_off[list] + (part ? n0 : 0u);
+    o.room = part ? m1 : n0;
+  } else {
+    o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+    o.room = kBlockSlots;
+  }
+  uint32_t aflag = 0;
+  block_part(X, codes + b0, len, strand, part, o, items ? nullptr : ps.anchor + it, aflag);
+  if (!items) {
+    ps.count[it] = o.n;
+    ps.refused[it] = o.refused ? 1 : 0;
+    ps.aflag[it] = (uint8_t)aflag;
+  }
   if (census) atomicAdd(census, (unsigned long long)o.sectors);
 }
 
-// The first pass's slots of each item, packed at its scanned offset.
-__global__ void block_pack_kernel(const hpg_hit_t* __restrict__ slots, const uint32_t* __restrict__ count,
-                                  const uint64_t* __restrict__ off, uint32_t n_items, hpg_hit_t* __restrict__ out) {
+// The two blocks of each list as BWSearchCPU leaves them in one list: block
+// 0's results, then the last block's up to the capacity (a full list refuses
+// the rest); both anchors, except the last block's when the lists have no room
+// at all and block 0 matched (BWSearchCPU returned before the last block).
+// Blocks whose results do not fit their slots are appended to `retry`
+// (any order: each writes a fixed range).
+__global__ void block_merge_kernel(PartState ps, uint32_t n_lists, uint32_t max_results, uint32_t* __restrict__ count,
+                                   uint8_t* __restrict__ refused, hpg_block_anchor_t* __restrict__ anchors,
+                                   uint8_t* __restrict__ n_anchors, uint32_t* __restrict__ retry,
+                                   uint32_t* __restrict__ n_retry) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n_items) return;
-  const uint32_t c = count[t] < kBlockSlots ? count[t] : kBlockSlots;
-  for (uint32_t j = 0; j < c; ++j) out[off[t] + j] = slots[(uint64_t)t * kBlockSlots + j];
+  if (t >= n_lists) return;
+  const uint32_t n0 = ps.count[2 * t], n1 = ps.count[2 * t + 1];
+  const uint32_t room1 = max_results - n0;
+  const uint32_t m1 = n1 < room1 ? n1 : room1;
+  count[t] = n0 + m1;
+  if (n0 > kBlockSlots) retry[atomicAdd(n_retry, 1u)] = 2 * t;
+  if (m1 > kBlockSlots) retry[atomicAdd(n_retry, 1u)] = 2 * t + 1;
+  refused[t] = (ps.refused[2 * t] | ps.refused[2 * t + 1] | (n1 > room1 ? 1 : 0)) ? 1 : 0;
+  const uint32_t f0 = ps.aflag[2 * t], f1 = ps.aflag[2 * t + 1];
+  uint32_t na = 0;
+  if (f0 & 1u) anchors[2ull * t + na++] = ps.anchor[2 * t];
+  if ((f1 & 1u) && !(max_results == 0 && (f0 & 2u))) anchors[2ull * t + na++] = ps.anchor[2 * t + 1];
+  n_anchors[t] = (uint8_t)na;
+}
+
+// The first pass's slots of each list, packed at its scanned offset.
+__global__ void block_pack_kernel(PartState ps, const uint64_t* __restrict__ off, uint32_t n_lists,
+                                  uint32_t max_results, hpg_hit_t* __restrict__ out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_lists) return;
+  const uint32_t n0 = ps.count[2 * t], n1 = ps.count[2 * t + 1];
+  const uint32_t room1 = max_results - n0;
+  const uint32_t m1 = n1 < room1 ? n1 : room1;
+  const uint32_t c0 = n0 < kBlockSlots ? n0 : kBlockSlots, c1 = m1 < kBlockSlots ? m1 : kBlockSlots;
+  hpg_hit_t* dst = out + off[t];
+  for (uint32_t j = 0; j < c0; ++j) dst[j] = ps.slots[(2ull * t) * kBlockSlots + j];
+  for (uint32_t j = 0; j < c1; ++j) dst[n0 + j] = ps.slots[(2ull * t + 1) * kBlockSlots + j];
 }
 
 // Rows of each hit for the locate pass: l - k + 1, or 0 for every hit of a
@@ -435,36 +521,56 @@ __global__ void block_items_kernel(const hpg_hit_t* __restrict__ hits, const uin
 unsigned grid_of(size_t n) { return (unsigned)((n + kBlockTpb - 1) / kBlockTpb); }
 
 // The search of every (read, strand) of the uploaded batch; on return the
-// device holds the packed hits (e->hits), per-item counts (e->rs_count) and
+// device holds the packed hits (e->hits), per-list counts (e->rs_count) and
 // hit offsets (e->hit_off), refused flags (e->rs_trunc), anchors (e->vecs)
-// and anchor counts (e->ovf); counts also on the host.
-int block_search_device(Engine* e, size_t n, uint32_t max_results, std::vector<uint32_t>& count, uint64_t* total_out,
-                        std::string* err) {
-  const size_t T = 2 * n;
-  if (!ensure(e, e->slots, T * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->rs_count, T * 4 + 16) ||
-      !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
+// and anchor counts (e->ovf); list counts also on the host.  Per-block state
+// lives in the batched form's buffers (b_arr, b_sorted, b_seg, b_res), unused
+// between calls.
+int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* total_out, std::string* err) {
+  const size_t T = 2 * n, P = 4 * n;
+  if (!ensure(e, e->b_res, P * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->b_arr, P * 4 + 16) ||
+      !ensure(e, e->b_sorted, 2 * P + 16) || !ensure(e, e->b_seg, P * sizeof(hpg_block_anchor_t) + 16) ||
+      !ensure(e, e->rs_count, T * 4 + 16) || !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
       !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
-      !ensure(e, e->ovf, T + 16) || !ensure(e, e->census, 16)) {
-    *err = oom_message("block search", T * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 14));
+      !ensure(e, e->ovf, T + 16) || !ensure(e, e->census, 16) || !ensure(e, e->rows, P * 4 + 16) ||
+      !ensure(e, e->b_ctr, 64)) {
+    *err = oom_message("block search", P * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 16));
     return -1;
   }
   cudaStream_t s = e->stream;
+  PartState ps;
+  ps.slots = ptr<hpg_hit_t>(e->b_res);
+  ps.count = ptr<uint32_t>(e->b_arr);
+  ps.refused = ptr<uint8_t>(e->b_sorted);
+  ps.aflag = ps.refused + P;
+  ps.anchor = ptr<hpg_block_anchor_t>(e->b_seg);
+  uint32_t* n_retry = ptr<uint32_t>(e->b_ctr) + 12;
+  cudaMemsetAsync(ps.count, 0, P * 4, s);
+  cudaMemsetAsync(ps.refused, 0, 2 * P, s);
+  cudaMemsetAsync(n_retry, 0, 4, s);
   uint32_t* d_count = ptr<uint32_t>(e->rs_count);
   uint64_t* d_off = ptr<uint64_t>(e->hit_off);
   unsigned long long* census = e->census_on ? ptr<unsigned long long>(e->census) : nullptr;
   if (census) cudaMemsetAsync(census, 0, 8, s);
+  const uint8_t* codes = ptr<uint8_t>(e->codes);
+  const uint64_t* offs = ptr<uint64_t>(e->offs);
+  const uint8_t* ok = ptr<uint8_t>(e->ok);
   cudaEventRecord(e->cev[0], s);
-  count_launches(1);
-  block_search_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(
-      e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)T, nullptr, nullptr,
-      kBlockSlots, max_results, ptr<hpg_hit_t>(e->slots), d_count, ptr<uint8_t>(e->rs_trunc),
-      ptr<hpg_block_anchor_t>(e->vecs), ptr<uint8_t>(e->ovf), census);
+  for (uint32_t phys = 0; phys < 2; ++phys) {  // one launch per index direction
+    count_launches(1);
+    block_part_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
+                                                       max_results, ps, nullptr, nullptr, census);
+  }
   cudaEventRecord(e->cev[1], s);
+  count_launches(1);
+  block_merge_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ps, (uint32_t)T, max_results, d_count, ptr<uint8_t>(e->rs_trunc),
+                                                      ptr<hpg_block_anchor_t>(e->vecs), ptr<uint8_t>(e->ovf),
+                                                      ptr<uint32_t>(e->rows), n_retry);
   launch_scan(d_count, T, d_off, ptr<uint64_t>(e->scan_part), s);
-  count.resize(T);
-  HPG_CUDA(cudaMemcpyAsync(count.data(), d_count, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
   uint64_t total = 0;
+  uint32_t again = 0;
   HPG_CUDA(cudaMemcpyAsync(&total, d_off + T, 8, cudaMemcpyDeviceToHost, s), "block total");
+  HPG_CUDA(cudaMemcpyAsync(&again, n_retry, 4, cudaMemcpyDeviceToHost, s), "block retries");
   if (census) HPG_CUDA(cudaMemcpyAsync(&e->census_val, census, 8, cudaMemcpyDeviceToHost, s), "block census");
   HPG_CUDA(cudaStreamSynchronize(s), "block search");
   float ms = 0;
@@ -476,24 +582,14 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, std::vector<u
   }
   hpg_hit_t* d_hits = ptr<hpg_hit_t>(e->hits);
   count_launches(1);
-  block_pack_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ptr<hpg_hit_t>(e->slots), d_count, d_off, (uint32_t)T, d_hits);
-  // items with more results than slots: the same search again, into their exact ranges
-  std::vector<uint32_t> again;
-  for (size_t t = 0; t < T; ++t)
-    if (count[t] > kBlockSlots) again.push_back((uint32_t)t);
-  if (!again.empty()) {
-    if (!ensure(e, e->rows, again.size() * 4 + 16)) {
-      *err = oom_message("block search retry list", again.size() * 4);
-      return -1;
-    }
-    HPG_CUDA(cudaMemcpyAsync(e->rows.p, again.data(), again.size() * 4, cudaMemcpyHostToDevice, s), "retry list");
+  block_pack_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(ps, d_off, (uint32_t)T, max_results, d_hits);
+  if (again) {  // blocks with more results than slots: the same search again, into their final ranges
     cudaEventRecord(e->cev[0], s);
     count_launches(1);
-    block_search_kernel<<<grid_of(again.size()), kBlockTpb, 0, s>>>(
-        e->X, ptr<uint8_t>(e->codes), ptr<uint64_t>(e->offs), ptr<uint8_t>(e->ok), (uint32_t)again.size(),
-        ptr<uint32_t>(e->rows), d_off, 0xFFFFFFFFu, max_results, d_hits, nullptr, nullptr, nullptr, nullptr, nullptr);
+    block_part_kernel<<<grid_of(again), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, again, ptr<uint32_t>(e->rows), 0,
+                                                           max_results, ps, d_off, d_hits, nullptr);
     cudaEventRecord(e->cev[1], s);
-    HPG_CUDA(cudaStreamSynchronize(s), "block search retry");  // `again` is pageable and local
+    HPG_CUDA(cudaStreamSynchronize(s), "block search retry");
     cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
     e->block_ms += ms;
   }
@@ -523,9 +619,10 @@ int engine_block_search(Engine* e, const char* seqs, const uint64_t* offs, size_
   if (!n) return 0;
   if (check_block_args(n, err) != 0 || upload_reads(e, seqs, offs, n, err) != 0) return -1;
   uint64_t total = 0;
-  if (block_search_device(e, n, max_results, out->count, &total, err) != 0) return -1;
+  if (block_search_device(e, n, max_results, &total, err) != 0) return -1;
   const size_t T = 2 * n;
   cudaStream_t s = e->stream;
+  HPG_CUDA(cudaMemcpyAsync(out->count.data(), e->rs_count.p, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
   out->hits.resize(total);
   if (total)
     HPG_CUDA(cudaMemcpyAsync(out->hits.data(), e->hits.p, total * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
@@ -547,11 +644,10 @@ int engine_block_search_result(Engine* e, const char* seqs, const uint64_t* offs
   std::memset(out, 0, sizeof(*out));
   out->n_reads = n;
   const size_t T = 2 * n;
-  std::vector<uint32_t> count;
   uint64_t total = 0;
   if (n) {
     if (check_block_args(n, err) != 0 || upload_reads(e, seqs, offs, n, err) != 0) return -1;
-    if (block_search_device(e, n, max_results, count, &total, err) != 0) return -1;
+    if (block_search_device(e, n, max_results, &total, err) != 0) return -1;
   }
   cudaStream_t s = e->stream;
   // rows of every hit (lists over the locate limit: none), their items, the locate pass
@@ -603,7 +699,7 @@ int engine_block_search_result(Engine* e, const char* seqs, const uint64_t* offs
   out->n_hits = total;
   out->n_locs = n_rows;
   if (T) {
-    std::memcpy(out->rs_count, count.data(), T * 4);
+    HPG_CUDA(cudaMemcpyAsync(out->rs_count, e->rs_count.p, T * 4, cudaMemcpyDeviceToHost, s), "block counts");
     HPG_CUDA(cudaMemcpyAsync(out->rs_truncated, e->rs_trunc.p, T, cudaMemcpyDeviceToHost, s), "block flags");
     if (anchors)
       HPG_CUDA(cudaMemcpyAsync(anchors, e->vecs.p, 2 * T * sizeof(hpg_block_anchor_t), cudaMemcpyDeviceToHost, s),
