@@ -46,10 +46,11 @@ struct ItemOut {
   uint32_t sectors; // occurrence-block sectors the item read (census)
 };
 
-// BWiteration over a view, counting the 32-byte sectors it reads (one when k
-// and l share an occurrence block, else two).
+// BWiteration over a view; with C (the census instance) it also counts the
+// 32-byte sectors it reads (one when k and l share an occurrence block, else two).
+template <bool C>
 __device__ __forceinline__ void step(const DevIndex& X, View v, uint32_t c, uint32_t& k, uint32_t& l, uint32_t& sec) {
-  sec += (k >> 6) == (l >> 6) ? 1u : 2u;
+  if (C) sec += (k >> 6) == (l >> 6) ? 1u : 2u;
   bw_step(X, v, c, k, l);
 }
 
@@ -81,6 +82,7 @@ __device__ __forceinline__ bool emit(ItemOut& o, uint32_t dir, uint32_t nm, uint
 
 // BWExactFinalResultForward (search/search.h:114-155): the block rule, then
 // the walk over W[pos..end]; k, l are updated only when it survives.
+template <bool C>
 __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const uint8_t* W, int pos, int end, int bs,
                                               int last_block, uint32_t& k, uint32_t& l, uint32_t& sec) {
   const int cb = pos / bs;
@@ -90,7 +92,7 @@ __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const u
   }
   uint32_t a = k, b = l;
   for (int i = pos; i <= end; ++i) {
-    step(X, v, W[i], a, b, sec);
+    step<C>(X, v, W[i], a, b, sec);
     if (a > b) return false;
   }
   k = a;
@@ -100,6 +102,7 @@ __device__ __forceinline__ bool final_forward(const DevIndex& X, View v, const u
 
 // BWExactFinalResultBackward (search/search.h:67-112), over W[pos..start]
 // downwards.  C division truncates toward zero (pos may be -1).
+template <bool C>
 __device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const uint8_t* W, int pos, int start, int bs,
                                                int last_block, uint32_t& k, uint32_t& l, uint32_t& sec) {
   const int cb = pos / bs;
@@ -109,7 +112,7 @@ __device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const 
   }
   uint32_t a = k, b = l;
   for (int i = pos; i >= start; --i) {
-    step(X, v, W[i], a, b, sec);
+    step<C>(X, v, W[i], a, b, sec);
     if (a > b) return false;
   }
   k = a;
@@ -123,55 +126,57 @@ __device__ __forceinline__ bool final_backward(const DevIndex& X, View v, const 
 // mismatch.  The mismatch starts from the interval the insertion's extension
 // left in the reference's result when that extension survived (the reference
 // resets only `pos` there).  False when rl_final refused a result.
+template <bool C>
 __device__ bool branch_forward(const DevIndex& X, View v, const uint8_t* W, int pos, int end, int bs, uint32_t k,
                                uint32_t l, ItemOut& o) {
   constexpr uint32_t kDir = 1;
   uint32_t a = k, b = l;
-  if (final_forward(X, v, W, pos + 1, end, bs, 0, a, b, o.sectors) &&
+  if (final_forward<C>(X, v, W, pos + 1, end, bs, 0, a, b, o.sectors) &&
       !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
     return false;
   const uint32_t wp = W[pos];
   for (uint32_t c = 0; c < 4; ++c) {
     uint32_t ka = k, la = l;
-    step(X, v, c, ka, la, o.sectors);
+    step<C>(X, v, c, ka, la, o.sectors);
     if (ka > la || c == wp) continue;
     uint32_t rk = ka, rl = la;
     a = ka;
     b = la;
-    if (final_forward(X, v, W, pos, end, bs, 0, a, b, o.sectors)) {
+    if (final_forward<C>(X, v, W, pos, end, bs, 0, a, b, o.sectors)) {
       if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
       rk = a;
       rl = b;
     }
-    if (final_forward(X, v, W, pos + 1, end, bs, 0, rk, rl, o.sectors) && !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
+    if (final_forward<C>(X, v, W, pos + 1, end, bs, 0, rk, rl, o.sectors) && !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
       return false;
   }
   return true;
 }
 
 // BWBranchFinalResultsBackward (search.c:252-284), the same on the backward side.
+template <bool C>
 __device__ bool branch_backward(const DevIndex& X, View v, const uint8_t* W, int pos, int bs, uint32_t k, uint32_t l,
                                 ItemOut& o) {
   constexpr uint32_t kDir = 0;
   constexpr int start = 0;
   uint32_t a = k, b = l;
-  if (final_backward(X, v, W, pos - 1, start, bs, 0, a, b, o.sectors) &&
+  if (final_backward<C>(X, v, W, pos - 1, start, bs, 0, a, b, o.sectors) &&
       !emit(o, kDir, 1, HPG_BWT_DELETION, 0xFF, pos, a, b))
     return false;
   const uint32_t wp = W[pos];
   for (uint32_t c = 0; c < 4; ++c) {
     uint32_t ka = k, la = l;
-    step(X, v, c, ka, la, o.sectors);
+    step<C>(X, v, c, ka, la, o.sectors);
     if (ka > la || c == wp) continue;
     uint32_t rk = ka, rl = la;
     a = ka;
     b = la;
-    if (final_backward(X, v, W, pos, start, bs, 0, a, b, o.sectors)) {
+    if (final_backward<C>(X, v, W, pos, start, bs, 0, a, b, o.sectors)) {
       if (!emit(o, kDir, 1, HPG_BWT_INSERTION, c, pos, a, b)) return false;
       rk = a;
       rl = b;
     }
-    if (final_backward(X, v, W, pos - 1, start, bs, 0, rk, rl, o.sectors) &&
+    if (final_backward<C>(X, v, W, pos - 1, start, bs, 0, rk, rl, o.sectors) &&
         !emit(o, kDir, 1, HPG_BWT_MISMATCH, c, pos, rk, rl))
       return false;
   }
@@ -183,6 +188,7 @@ __device__ bool branch_backward(const DevIndex& X, View v, const uint8_t* W, int
 // first empty interval, the exact-partial walk.  Returns the number of branch
 // points that walk appends; `survive` whether it covers the whole range with
 // a non-empty interval (then k, l hold that interval).
+template <bool C>
 __device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int from, int to, int dstep, uint32_t& k,
                                uint32_t& l, bool& survive, uint32_t& zt, uint32_t& sec) {
   uint32_t a = k, b = l;
@@ -190,7 +196,7 @@ __device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int 
   bool alive = true, failed_step = false;
   for (int i = from; i != to + dstep; i += dstep) {
     const int64_t before = (int64_t)b - (int64_t)a;
-    step(X, v, W[i], a, b, sec);
+    step<C>(X, v, W[i], a, b, sec);
     if (alive) {
       if (a > b) {
         alive = false;
@@ -258,6 +264,7 @@ __device__ __forceinline__ int part_on(uint32_t strand, int fragments, uint32_t 
 // merge cuts the last block's results to the room block 0 left.  aflag bit 0:
 // the block's anchor was set; bit 1: the block-0 fragment matched (with lists
 // of capacity 0 BWSearchCPU then returns before the last block).
+template <bool C>
 __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
                            hpg_block_anchor_t* anchor, uint32_t& aflag) {
   // type 1 ('+', strand 0): backward = backward, forward = forward;
@@ -272,7 +279,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     int i;
     if (strand) {  // type 0: forward search from the first base
       for (i = 0; i <= end; ++i) {
-        step(X, fw, W[i], k, l, o.sectors);
+        step<C>(X, fw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
@@ -281,7 +288,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
       if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
     } else {
       for (i = end; i >= 0; --i) {
-        step(X, bw, W[i], k, l, o.sectors);
+        step<C>(X, bw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
         gl = l;
@@ -296,7 +303,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     uint32_t k = 0, l = X.top, gk = 0, gl = 0;
     int i;
     for (i = 0; i <= frag - 1; ++i) {
-      step(X, fw, W[i], k, l, o.sectors);
+      step<C>(X, fw, W[i], k, l, o.sectors);
       if (k > l) break;
       gk = k;
       gl = l;
@@ -312,7 +319,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     // the read, and a walk that survives it is a result (complete search)
     uint32_t fk = k, fl = l, zt = 0;
     bool survive = false;
-    const uint32_t points = first_walk(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
+    const uint32_t points = first_walk<C>(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
     if (points > o.cap) {
       o.refused = true;  // rl_next overflows: the block's branches are dropped
     } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
@@ -321,10 +328,10 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
       for (int p = frag; p <= end; ++p) {
         const uint32_t pk = a, pl = b;
         const int64_t before = (int64_t)b - (int64_t)a;
-        step(X, fw, W[p], a, b, o.sectors);
+        step<C>(X, fw, W[p], a, b, o.sectors);
         const bool failed = a > b;
         const bool changed = failed || (int64_t)b - (int64_t)a != before;
-        if (changed && (failed ? ok_at : ok_before) && !branch_forward(X, fw, W, p, end, frag, pk, pl, o)) break;
+        if (changed && (failed ? ok_at : ok_before) && !branch_forward<C>(X, fw, W, p, end, frag, pk, pl, o)) break;
         if (failed) break;
       }
     }
@@ -335,7 +342,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
   uint32_t k = 0, l = X.top, gk = 0, gl = 0;
   int i;
   for (i = end; i >= frag; --i) {
-    step(X, bw, W[i], k, l, o.sectors);
+    step<C>(X, bw, W[i], k, l, o.sectors);
     if (k > l) break;
     gk = k;
     gl = l;
@@ -350,7 +357,7 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
   // from above, so the rule walks the whole of it without completing
   uint32_t fk = k, fl = l, zt = 0;
   bool survive = false;
-  const uint32_t points = first_walk(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt, o.sectors);
+  const uint32_t points = first_walk<C>(X, bw, W, frag - 1, 0, -1, fk, fl, survive, zt, o.sectors);
   if (points > o.cap) {
     o.refused = true;
     return;
@@ -360,10 +367,10 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
   for (int p = frag - 1; p >= 0; --p) {
     const uint32_t pk = a, pl = b;
     const int64_t before = (int64_t)b - (int64_t)a;
-    step(X, bw, W[p], a, b, o.sectors);
+    step<C>(X, bw, W[p], a, b, o.sectors);
     const bool failed = a > b;
     const bool changed = failed || (int64_t)b - (int64_t)a != before;
-    if (changed && (failed ? ok_at : ok_before) && !branch_backward(X, bw, W, p, frag, pk, pl, o)) break;
+    if (changed && (failed ? ok_at : ok_before) && !branch_backward<C>(X, bw, W, p, frag, pk, pl, o)) break;
     if (failed) break;
   }
 }
@@ -383,6 +390,7 @@ struct PartState {
 // the launch reads one direction's occurrence blocks).  Retry: item items[g] =
 // 2 * list + part runs again into the list's final range, the last block after
 // block 0's results and cut to the room they left.
+template <bool C>
 __global__ void __launch_bounds__(kBlockTpb) block_part_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
     uint32_t n_items, const uint32_t* __restrict__ items, uint32_t phys, uint32_t max_results, PartState ps,
@@ -425,13 +433,13 @@ __global__ void __launch_bounds__(kBlockTpb) block_part_kernel(
     o.room = kBlockSlots;
   }
   uint32_t aflag = 0;
-  block_part(X, codes + b0, len, strand, part, o, items ? nullptr : ps.anchor + it, aflag);
+  block_part<C>(X, codes + b0, len, strand, part, o, items ? nullptr : ps.anchor + it, aflag);
   if (!items) {
     ps.count[it] = o.n;
     ps.refused[it] = o.refused ? 1 : 0;
     ps.aflag[it] = (uint8_t)aflag;
   }
-  if (census) atomicAdd(census, (unsigned long long)o.sectors);
+  if (C) atomicAdd(census, (unsigned long long)o.sectors);
 }
 
 // The two blocks of each list as BWSearchCPU leaves them in one list: block
@@ -558,8 +566,12 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   cudaEventRecord(e->cev[0], s);
   for (uint32_t phys = 0; phys < 2; ++phys) {  // one launch per index direction
     count_launches(1);
-    block_part_kernel<<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
-                                                       max_results, ps, nullptr, nullptr, census);
+    if (census)
+      block_part_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
+                                                               max_results, ps, nullptr, nullptr, census);
+    else
+      block_part_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
+                                                                max_results, ps, nullptr, nullptr, nullptr);
   }
   cudaEventRecord(e->cev[1], s);
   count_launches(1);
@@ -586,7 +598,7 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   if (again) {  // blocks with more results than slots: the same search again, into their final ranges
     cudaEventRecord(e->cev[0], s);
     count_launches(1);
-    block_part_kernel<<<grid_of(again), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, again, ptr<uint32_t>(e->rows), 0,
+    block_part_kernel<false><<<grid_of(again), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, again, ptr<uint32_t>(e->rows), 0,
                                                            max_results, ps, d_off, d_hits, nullptr);
     cudaEventRecord(e->cev[1], s);
     HPG_CUDA(cudaStreamSynchronize(s), "block search retry");
