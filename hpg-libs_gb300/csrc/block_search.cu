@@ -213,6 +213,9 @@ __device__ uint32_t first_walk(const DevIndex& X, View v, const uint8_t* W, int 
       a = 0;
       b = X.top;
       ++z;
+      // three restarts with too few steps left for the byte count to wrap: D
+      // allows no error anywhere in the range, so there is no branch point
+      if (z >= 3 && z + (uint32_t)(dstep > 0 ? to - i : i - to) < 256) break;
     }
   }
   survive = alive;
@@ -322,16 +325,19 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     const uint32_t points = first_walk<C>(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
     if (points > o.cap) {
       o.refused = true;  // rl_next overflows: the block's branches are dropped
-    } else if (!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) {
+    } else if ((!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) && points) {
+      // the second walk, up to the last branch point
       const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
-      uint32_t a = k, b = l;
+      uint32_t a = k, b = l, left = points;
       for (int p = frag; p <= end; ++p) {
         const uint32_t pk = a, pl = b;
         const int64_t before = (int64_t)b - (int64_t)a;
         step<C>(X, fw, W[p], a, b, o.sectors);
         const bool failed = a > b;
         const bool changed = failed || (int64_t)b - (int64_t)a != before;
-        if (changed && (failed ? ok_at : ok_before) && !branch_forward<C>(X, fw, W, p, end, frag, pk, pl, o)) break;
+        if (changed && (failed ? ok_at : ok_before)) {
+          if (!branch_forward<C>(X, fw, W, p, end, frag, pk, pl, o) || --left == 0) break;
+        }
         if (failed) break;
       }
     }
@@ -362,15 +368,18 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     o.refused = true;
     return;
   }
+  // the second walk, up to the last branch point
   const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
-  uint32_t a = k, b = l;
-  for (int p = frag - 1; p >= 0; --p) {
+  uint32_t a = k, b = l, left = points;
+  for (int p = frag - 1; p >= 0 && left; --p) {
     const uint32_t pk = a, pl = b;
     const int64_t before = (int64_t)b - (int64_t)a;
     step<C>(X, bw, W[p], a, b, o.sectors);
     const bool failed = a > b;
     const bool changed = failed || (int64_t)b - (int64_t)a != before;
-    if (changed && (failed ? ok_at : ok_before) && !branch_backward<C>(X, bw, W, p, frag, pk, pl, o)) break;
+    if (changed && (failed ? ok_at : ok_before)) {
+      if (!branch_backward<C>(X, bw, W, p, frag, pk, pl, o) || --left == 0) break;
+    }
     if (failed) break;
   }
 }
