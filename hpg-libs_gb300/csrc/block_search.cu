@@ -1,14 +1,15 @@
 // block_search.cu -- the k-error block search of bwt_map_inexact_read_2
 // (c/src/aligners/bwt/bwt.c:2313-2470): BWSearchCPU (search/search.c:1171-1405)
-// on both strands, one GPU thread per (read, strand), with that function's
-// fragment size max(len / 2, 30) -- one or two fragments, so one error.
+// on both strands with that function's fragment size max(len / 2, 30) -- one
+// or two fragments, so one error.
 //
 // The reference keeps its partial results in lists: an exact-partial pass
 // appends a branch point for every step where the interval size changes while
 // the error bound D still allows an error (BWExactPartialResults*,
 // search.c:471-646), then a branch pass extends each branch point by a
 // deletion and, per base, an insertion and a mismatch (BWBranchFinalResults*,
-// search.c:116-469).  A thread here replays the walk instead of storing it:
+// search.c:116-469).  A thread here runs one block of a (read, strand) and
+// replays the walk instead of storing it:
 //   * a first walk over the rest of the read counts the restarts D is made of
 //     (calculateD*, search.c:1045-1169: D at a step is the number of restarts
 //     still ahead, as a byte) and the branch points, so that a list that would
@@ -16,9 +17,13 @@
 //     the block's branches);
 //   * within the exact-partial range D is the total (the walk has not failed
 //     yet) or the total minus one (the step where it fails), so the total is
-//     all the second walk needs to emit the branches in the reference's order.
-// Results go to a fixed number of slots per work item; the few items with more
-// results run again into an exact range once the counts are scanned.
+//     all the second walk needs to emit the branches in the reference's order;
+//     it stops at the last branch point.
+// Every block stays on one physical index direction, and one launch per
+// direction keeps that direction's occurrence blocks in L2; a merge then puts
+// each list's two blocks together as the reference's single list.  Results go
+// to a fixed number of slots per block; the few blocks with more results run
+// again into their final range.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,7 +37,7 @@ namespace hpgbwt {
 
 namespace {
 
-constexpr uint32_t kBlockSlots = 4;  // result slots per (read, strand) in the first pass
+constexpr uint32_t kBlockSlots = 4;  // result slots per block in the first pass
 constexpr int kBlockTpb = 128;
 
 struct ItemOut {
