@@ -267,24 +267,31 @@ __device__ __forceinline__ int part_on(uint32_t strand, int fragments, uint32_t 
   return (strand ^ phys) ? 0 : 1;
 }
 
-// One block of a (read, strand) (BWSearchCPU, search.c:1171-1405, with two
-// fragments or fewer), its results emitted as if the list were empty; the
-// merge cuts the last block's results to the room block 0 left.  aflag bit 0:
-// the block's anchor was set; bit 1: the block-0 fragment matched (with lists
+// The views of a strand: type 1 ('+', strand 0) searches backward over
+// `backward` and forward over `forward`; type 0 ('-', strand 1) over
+// forward_rev and backward_rev (bwt.c:2440-2472).
+__device__ __forceinline__ View backward_view(uint32_t strand) { return strand ? View{1, 1} : View{0, 0}; }
+__device__ __forceinline__ View forward_view(uint32_t strand) { return strand ? View{0, 1} : View{1, 0}; }
+
+// Head of one block of a (read, strand) (BWSearchCPU, search.c:1171-1405, with
+// two fragments or fewer): the exact search of the block's fragment and its
+// anchor.  A single-fragment read's one exact search is all its work (its
+// result is emitted here).  True, with the fragment's interval in k, l, when
+// the block goes on (its fragment matched and the lists have room).  aflag
+// bit 0: the anchor was set; bit 1: the block-0 fragment matched (with lists
 // of capacity 0 BWSearchCPU then returns before the last block).
 template <bool C>
-__device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
-                           hpg_block_anchor_t* anchor, uint32_t& aflag) {
-  // type 1 ('+', strand 0): backward = backward, forward = forward;
-  // type 0 ('-', strand 1): backward = forward_rev, forward = backward_rev (bwt.c:2440-2472)
-  const View bw = strand ? View{1, 1} : View{0, 0};
-  const View fw = strand ? View{0, 1} : View{1, 0};
+__device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
+                           hpg_block_anchor_t* anchor, uint32_t& aflag, uint32_t& k, uint32_t& l) {
+  const View bw = backward_view(strand), fw = forward_view(strand);
   int frag = 30;
   const int fragments = fragments_of(len, frag);
   const int end = len - 1;
+  uint32_t gk = 0, gl = 0;
+  int i;
+  k = 0;
+  l = X.top;
   if (fragments <= 1) {  // search.c:1191-1224: one exact search of the whole read
-    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
-    int i;
     if (strand) {  // type 0: forward search from the first base
       for (i = 0; i <= end; ++i) {
         step<C>(X, fw, W[i], k, l, o.sectors);
@@ -304,12 +311,9 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
       put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
       if (k <= l) emit(o, 0, 0, 0, 0, 0, k, l);
     }
-    return;
+    return false;
   }
-
   if (part == 0) {  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
-    uint32_t k = 0, l = X.top, gk = 0, gl = 0;
-    int i;
     for (i = 0; i <= frag - 1; ++i) {
       step<C>(X, fw, W[i], k, l, o.sectors);
       if (k > l) break;
@@ -317,12 +321,37 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
       gl = l;
     }
     put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
-    if (k > l) return;
+    if (k > l) return false;
     aflag |= 2u;
-    if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
-      o.refused = true;
-      return;
+  } else {  // last block: backward over W[frag .. len-1] (search.c:1360-1402)
+    for (i = end; i >= frag; --i) {
+      step<C>(X, bw, W[i], k, l, o.sectors);
+      if (k > l) break;
+      gk = k;
+      gl = l;
     }
+    put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
+    if (k > l) return false;
+  }
+  if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
+    o.refused = true;
+    return false;
+  }
+  return true;
+}
+
+// Tail of a block whose fragment matched with interval k..l: the rest of the
+// read (first walk, the complete result of block 0, the second walk and the
+// branches), emitted as if the list were empty; the merge cuts the last
+// block's results to the room block 0 left.
+template <bool C>
+__device__ void block_tail(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
+                           uint32_t k, uint32_t l) {
+  int frag = 30;
+  fragments_of(len, frag);
+  const int end = len - 1;
+  if (part == 0) {
+    const View fw = forward_view(strand);
     // exact-partial range: pos = frag is past block 0, so the whole rest of
     // the read, and a walk that survives it is a result (complete search)
     uint32_t fk = k, fl = l, zt = 0;
@@ -330,40 +359,26 @@ __device__ void block_part(const DevIndex& X, const uint8_t* W, int len, uint32_
     const uint32_t points = first_walk<C>(X, fw, W, frag, end, 1, fk, fl, survive, zt, o.sectors);
     if (points > o.cap) {
       o.refused = true;  // rl_next overflows: the block's branches are dropped
-    } else if ((!survive || emit(o, 1, 0, 0, 0, 0, fk, fl)) && points) {
-      // the second walk, up to the last branch point
-      const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
-      uint32_t a = k, b = l, left = points;
-      for (int p = frag; p <= end; ++p) {
-        const uint32_t pk = a, pl = b;
-        const int64_t before = (int64_t)b - (int64_t)a;
-        step<C>(X, fw, W[p], a, b, o.sectors);
-        const bool failed = a > b;
-        const bool changed = failed || (int64_t)b - (int64_t)a != before;
-        if (changed && (failed ? ok_at : ok_before)) {
-          if (!branch_forward<C>(X, fw, W, p, end, frag, pk, pl, o) || --left == 0) break;
-        }
-        if (failed) break;
+      return;
+    }
+    if ((survive && !emit(o, 1, 0, 0, 0, 0, fk, fl)) || !points) return;
+    // the second walk, up to the last branch point
+    const bool ok_before = zt <= 1u, ok_at = ((zt - 1u) & 255u) <= 1u;
+    uint32_t a = k, b = l, left = points;
+    for (int p = frag; p <= end; ++p) {
+      const uint32_t pk = a, pl = b;
+      const int64_t before = (int64_t)b - (int64_t)a;
+      step<C>(X, fw, W[p], a, b, o.sectors);
+      const bool failed = a > b;
+      const bool changed = failed || (int64_t)b - (int64_t)a != before;
+      if (changed && (failed ? ok_at : ok_before)) {
+        if (!branch_forward<C>(X, fw, W, p, end, frag, pk, pl, o) || --left == 0) break;
       }
+      if (failed) break;
     }
     return;
   }
-
-  // last block: backward over W[frag .. len-1] (search.c:1360-1402)
-  uint32_t k = 0, l = X.top, gk = 0, gl = 0;
-  int i;
-  for (i = end; i >= frag; --i) {
-    step<C>(X, bw, W[i], k, l, o.sectors);
-    if (k > l) break;
-    gk = k;
-    gl = l;
-  }
-  put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
-  if (k > l) return;
-  if (o.cap == 0) {
-    o.refused = true;
-    return;
-  }
+  const View bw = backward_view(strand);
   // exact-partial range: pos = frag - 1 is the first element of block 0
   // from above, so the rule walks the whole of it without completing
   uint32_t fk = k, fl = l, zt = 0;
@@ -399,61 +414,117 @@ struct PartState {
   hpg_block_anchor_t* anchor;     // the block's anchor
 };
 
-// First pass (items == nullptr): thread g runs the block of list g that is on
-// physical direction `phys`, into its slots (one launch per direction, so that
-// the launch reads one direction's occurrence blocks).  Retry: item items[g] =
-// 2 * list + part runs again into the list's final range, the last block after
-// block 0's results and cut to the room they left.
+// Head pass over physical direction `phys`: thread g runs the head of the
+// block of its list that is on that direction (the '+' lists in the first half
+// of the threads, the '-' ones in the second, so that a warp's lanes run the
+// same block code), and appends the blocks that go on to `queue` as {block,
+// k, l}.  One launch per direction, so that it reads one direction's
+// occurrence blocks.
 template <bool C>
-__global__ void __launch_bounds__(kBlockTpb) block_part_kernel(
+__global__ void __launch_bounds__(kBlockTpb) block_head_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
-    uint32_t n_items, const uint32_t* __restrict__ items, uint32_t phys, uint32_t max_results, PartState ps,
-    const uint64_t* __restrict__ list_off, hpg_hit_t* __restrict__ hits, unsigned long long* census) {
+    uint32_t n_lists, uint32_t phys, uint32_t max_results, PartState ps, uint4* __restrict__ queue,
+    uint32_t* __restrict__ n_queue, unsigned long long* census) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_items) return;
-  // first pass: the '+' lists in the first half of the threads, the '-' ones in
-  // the second, so that a warp's lanes run the same block code (per direction,
-  // '+' and '-' run different blocks)
-  const uint32_t half = n_items >> 1;
-  const uint32_t list = items ? items[g] >> 1 : (g < half ? 2 * g : 2 * (g - half) + 1);
+  if (g >= n_lists) return;
+  const uint32_t half = n_lists >> 1;
+  const uint32_t list = g < half ? 2 * g : 2 * (g - half) + 1;
   const uint32_t read = list >> 1, strand = list & 1u;
   const uint64_t b0 = offs[read];
   const int len = (int)(offs[read + 1] - b0);
-  if (!ok[read] || len < 3 || len > 32767) return;
-  int part;
-  if (items) {
-    part = (int)(items[g] & 1u);
-  } else {
+  bool go = false;
+  uint32_t it = 0, k = 0, l = 0;
+  if (ok[read] && len >= 3 && len <= 32767) {
     int frag = 30;
-    part = part_on(strand, fragments_of(len, frag), phys);
-    if (part < 0) return;
+    const int part = part_on(strand, fragments_of(len, frag), phys);
+    if (part >= 0) {
+      it = 2 * list + (uint32_t)part;
+      ItemOut o;
+      o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+      o.room = kBlockSlots;
+      o.cap = max_results;
+      o.n = 0;
+      o.read = read;
+      o.strand = strand;
+      o.refused = false;
+      o.sectors = 0;
+      uint32_t aflag = 0;
+      go = block_head<C>(X, codes + b0, len, strand, part, o, ps.anchor + it, aflag, k, l);
+      ps.count[it] = o.n;
+      ps.refused[it] = o.refused ? 1 : 0;
+      ps.aflag[it] = (uint8_t)aflag;
+      if (C) atomicAdd(census, (unsigned long long)o.sectors);
+    }
   }
-  const uint32_t it = 2 * list + (uint32_t)part;
+  // warp-aggregated append
+  const unsigned mask = __ballot_sync(__activemask(), go);
+  if (go) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(n_queue, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = make_uint4(it, k, l, 0u);
+  }
+}
+
+// Tail pass over the queued blocks of one direction (the launch covers the
+// largest queue; threads past its length return): every lane starts a block
+// whose fragment matched.
+template <bool C>
+__global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
+    DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint4* __restrict__ queue,
+    const uint32_t* __restrict__ n_queue, uint32_t max_results, PartState ps, unsigned long long* census) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= *n_queue) return;
+  const uint4 q = queue[g];
+  const uint32_t it = q.x, list = it >> 1, part = it & 1u;
+  const uint32_t read = list >> 1, strand = list & 1u;
+  const uint64_t b0 = offs[read];
+  const int len = (int)(offs[read + 1] - b0);
   ItemOut o;
+  o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+  o.room = kBlockSlots;
   o.cap = max_results;
   o.n = 0;
   o.read = read;
   o.strand = strand;
   o.refused = false;
   o.sectors = 0;
-  if (items) {
-    const uint32_t n0 = ps.count[2 * list];
-    const uint32_t room1 = max_results - n0;
-    const uint32_t m1 = ps.count[2 * list + 1] < room1 ? ps.count[2 * list + 1] : room1;
-    o.slot = hits + list_off[list] + (part ? n0 : 0u);
-    o.room = part ? m1 : n0;
-  } else {
-    o.slot = ps.slots + (uint64_t)it * kBlockSlots;
-    o.room = kBlockSlots;
-  }
-  uint32_t aflag = 0;
-  block_part<C>(X, codes + b0, len, strand, part, o, items ? nullptr : ps.anchor + it, aflag);
-  if (!items) {
-    ps.count[it] = o.n;
-    ps.refused[it] = o.refused ? 1 : 0;
-    ps.aflag[it] = (uint8_t)aflag;
-  }
+  block_tail<C>(X, codes + b0, len, strand, (int)part, o, q.y, q.z);
+  ps.count[it] = o.n;
+  ps.refused[it] = o.refused ? 1 : 0;
   if (C) atomicAdd(census, (unsigned long long)o.sectors);
+}
+
+// Retry: block items[g] = 2 * list + part, whose results did not fit its
+// slots, runs again (head and tail) into the list's final range, the last
+// block after block 0's results and cut to the room they left.
+__global__ void __launch_bounds__(kBlockTpb) block_retry_kernel(
+    DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, uint32_t n_items,
+    const uint32_t* __restrict__ items, uint32_t max_results, PartState ps, const uint64_t* __restrict__ list_off,
+    hpg_hit_t* __restrict__ hits) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_items) return;
+  const uint32_t it = items[g], list = it >> 1, part = it & 1u;
+  const uint32_t read = list >> 1, strand = list & 1u;
+  const uint64_t b0 = offs[read];
+  const int len = (int)(offs[read + 1] - b0);
+  const uint32_t n0 = ps.count[2 * list];
+  const uint32_t room1 = max_results - n0;
+  const uint32_t m1 = ps.count[2 * list + 1] < room1 ? ps.count[2 * list + 1] : room1;
+  ItemOut o;
+  o.slot = hits + list_off[list] + (part ? n0 : 0u);
+  o.room = part ? m1 : n0;
+  o.cap = max_results;
+  o.n = 0;
+  o.read = read;
+  o.strand = strand;
+  o.refused = false;
+  o.sectors = 0;
+  uint32_t aflag = 0, k = 0, l = 0;
+  if (block_head<false>(X, codes + b0, len, strand, (int)part, o, nullptr, aflag, k, l))
+    block_tail<false>(X, codes + b0, len, strand, (int)part, o, k, l);
 }
 
 // The two blocks of each list as BWSearchCPU leaves them in one list: block
@@ -555,7 +626,7 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
       !ensure(e, e->rs_count, T * 4 + 16) || !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
       !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
       !ensure(e, e->ovf, T + 16) || !ensure(e, e->census, 16) || !ensure(e, e->rows, P * 4 + 16) ||
-      !ensure(e, e->b_ctr, 64)) {
+      !ensure(e, e->b_ctr, 64) || !ensure(e, e->b_spill, T * sizeof(uint4) + 16)) {
     *err = oom_message("block search", P * (kBlockSlots * sizeof(hpg_hit_t) + 2 * sizeof(hpg_block_anchor_t) + 16));
     return -1;
   }
@@ -577,15 +648,23 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   const uint8_t* codes = ptr<uint8_t>(e->codes);
   const uint64_t* offs = ptr<uint64_t>(e->offs);
   const uint8_t* ok = ptr<uint8_t>(e->ok);
+  uint4* queue = ptr<uint4>(e->b_spill);
+  uint32_t* n_queue = ptr<uint32_t>(e->b_ctr) + 13;
   cudaEventRecord(e->cev[0], s);
-  for (uint32_t phys = 0; phys < 2; ++phys) {  // one launch per index direction
-    count_launches(1);
-    if (census)
-      block_part_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
-                                                               max_results, ps, nullptr, nullptr, census);
-    else
-      block_part_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, nullptr, phys,
-                                                                max_results, ps, nullptr, nullptr, nullptr);
+  for (uint32_t phys = 0; phys < 2; ++phys) {  // one head and one tail launch per index direction
+    cudaMemsetAsync(n_queue, 0, 4, s);
+    count_launches(2);
+    if (census) {
+      block_head_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys, max_results,
+                                                               ps, queue, n_queue, census);
+      block_tail_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
+                                                               census);
+    } else {
+      block_head_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys,
+                                                                max_results, ps, queue, n_queue, nullptr);
+      block_tail_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
+                                                                nullptr);
+    }
   }
   cudaEventRecord(e->cev[1], s);
   count_launches(1);
@@ -612,8 +691,8 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   if (again) {  // blocks with more results than slots: the same search again, into their final ranges
     cudaEventRecord(e->cev[0], s);
     count_launches(1);
-    block_part_kernel<false><<<grid_of(again), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, again, ptr<uint32_t>(e->rows), 0,
-                                                           max_results, ps, d_off, d_hits, nullptr);
+    block_retry_kernel<<<grid_of(again), kBlockTpb, 0, s>>>(e->X, codes, offs, again, ptr<uint32_t>(e->rows),
+                                                            max_results, ps, d_off, d_hits);
     cudaEventRecord(e->cev[1], s);
     HPG_CUDA(cudaStreamSynchronize(s), "block search retry");
     cudaEventElapsedTime(&ms, e->cev[0], e->cev[1]);
