@@ -19,6 +19,12 @@ L2 flushed with a 256 MiB write before every step); ``e2e`` goes through the
 C ABI call ``bwt_gpu_search_batch`` with pinned host reads and host result
 arrays, host<->device copies inside the timed region.
 
+Secondary legs in the same JSON line (not the headline): the serving form
+(p50/p99 latency under Poisson load), CAL generation, the alignment-list
+entry points, and the k-error block search of bwt_map_inexact_read_2
+(``block_search``: its kernels' device time, the bwt_gpu_block_search call with
+host buffers, a sector census, and bwt_map_inexact_array_list_2).
+
 ``--impl reference`` times the reference algorithm on the host cores (the C
 restatement in oracle/, OpenMP over all cores) on a bounded sample of the
 same workload.
