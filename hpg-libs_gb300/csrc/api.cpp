@@ -18,9 +18,6 @@
 using namespace hpgbwt;
 
 namespace hpgbwt {
-int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_ascii, const uint64_t* d_offs,
-                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err,
-                   unsigned long long* steps_out);
 DevIndex engine_dev_index(void* engine);
 const uint8_t* engine_code_table(void* engine);
 int gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double* sectors_per_s,
@@ -263,26 +260,6 @@ int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t s
   std::string err;
   if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err, 0) != 0)
     return fail(err.empty() ? "bwt_gpu_gather_ceiling: null argument" : err);
-  return 0;
-}
-
-int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
-                         double* sectors_per_s) {
-  std::string err;
-  if (!sectors_per_s || gather_ceiling(device, bytes, blocks, steps, sectors_per_s, &err, work) != 0)
-    return fail(err.empty() ? "bwt_gpu_gather_probe: null argument" : err);
-  return 0;
-}
-
-int bwt_gpu_fm_probe(bwt_index_t* index, const uint8_t* d_seqs, const uint64_t* d_offsets, size_t n_reads,
-                     uint32_t reps, float* ms, unsigned long long* steps) {
-  Engine* e = engine_of(index);
-  if (!e || !ms) return fail("bwt_gpu_fm_probe: null argument");
-  std::string err;
-  cudaSetDevice(engine_device(e));
-  if (fm_chain_probe(engine_dev_index(e), engine_code_table(e), d_seqs, d_offsets, (uint32_t)n_reads, reps, ms,
-                     &err, steps) != 0)
-    return fail(err);
   return 0;
 }
 

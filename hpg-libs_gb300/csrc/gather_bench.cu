@@ -51,74 +51,7 @@ __global__ void __launch_bounds__(128) gather_chain_kernel(const uint4* __restri
   if (acc == 0x9E3779B9u) atomicAdd(sink, 1ull);
 }
 
-// Pure FM steps: one thread per read runs the full backward search of the read
-// over the backward index (no vectors, no branching, no output but a
-// checksum).  Reads taken from the forward strand keep every lane busy for
-// the whole read, so this is the best case of the real access pattern.
-__global__ void __launch_bounds__(128) fm_chain_probe_kernel(DevIndex X, const uint8_t* __restrict__ ascii,
-                                                             const uint64_t* __restrict__ offs, uint32_t n_reads,
-                                                             const uint8_t* __restrict__ table, uint32_t reps,
-                                                             uint32_t variant, unsigned long long* sink) {
-  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_reads) return;
-  const uint64_t b = offs[r];
-  const int len = (int)(offs[r + 1] - b);
-  uint32_t acc = 0, steps = 0;
-  for (uint32_t rep = 0; rep < reps; ++rep) {
-    // variant 0: backward search on the backward index; 1: forward search on
-    // the forward index; 2: odd reads do 0, even reads do 1 (both indexes live)
-    const uint32_t v = variant == 2 ? (r & 1u) : variant;
-    uint32_t k = 0, l = X.top;
-    for (int t = 0; t < len; ++t) {
-      const int i = v ? t : len - 1 - t;
-      const uint32_t c = table[ascii[b + i]] & 3u;
-      bw_step(X, View{v, 0}, c, k, l);
-      ++steps;
-      if (k > l) break;
-    }
-    acc += k ^ l;
-  }
-  atomicAdd(sink, (unsigned long long)steps + (acc == 0x9E3779B9u ? 1ull : 0ull));
-}
-
 }  // namespace
-
-// Rank steps per second of fm_chain_probe_kernel over device reads.
-int fm_chain_probe(const DevIndex& X, const uint8_t* table, const uint8_t* d_ascii, const uint64_t* d_offs,
-                   uint32_t n_reads, uint32_t reps, float* ms_out, std::string* err,
-                   unsigned long long* steps_out) {
-  const uint32_t variant = reps >> 16;
-  reps &= 0xFFFFu;
-  unsigned long long* sink = nullptr;
-  if (cudaMalloc(&sink, 8) != cudaSuccess) {
-    cudaGetLastError();
-    *err = "out of device memory";
-    return -1;
-  }
-  cudaStream_t s;
-  cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  cudaEvent_t a, b;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
-  const unsigned grid = (n_reads + 127) / 128;
-  fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, 1, variant, sink);
-  cudaMemsetAsync(sink, 0, 8, s);
-  cudaEventRecord(a, s);
-  fm_chain_probe_kernel<<<grid, 128, 0, s>>>(X, d_ascii, d_offs, n_reads, table, reps, variant, sink);
-  cudaEventRecord(b, s);
-  const cudaError_t ce = cudaStreamSynchronize(s);
-  cudaEventElapsedTime(ms_out, a, b);
-  if (steps_out) cudaMemcpy(steps_out, sink, 8, cudaMemcpyDeviceToHost);
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  cudaStreamDestroy(s);
-  cudaFree(sink);
-  if (ce != cudaSuccess) {
-    *err = std::string("fm probe: ") + cudaGetErrorString(ce);
-    return -1;
-  }
-  return 0;
-}
 
 // Sectors per second of dependent random 32-byte sector reads over a buffer
 // of `bytes`, with `blocks` x 128 threads each following `steps` hops and

@@ -3,14 +3,18 @@
 // bwt_gpu_search1_noalloc runs the plain one-thread-per-(read, strand)
 // BWSearch1 search without any device allocation of its own.  Its per-thread
 // scratch (the read codes and the two interval vectors of the helper) lives in
-// one file-scope __device__ array of fixed size, which every GPU that loads
-// this library holds until the process exits.
+// one file-scope __device__ array of fixed size, which every GPU that has run
+// a call holds until the process exits.
 //
 // Host code cannot use the array's name as a device address (on the host it
 // names a stand-in object), so the address is looked up with
 // cudaGetSymbolAddress once per device, with that device current, on the
-// first call made on that device.  That first call should therefore come
-// before any stream capture on the device.
+// first call made on that device.  Under CUDA's lazy module loading (the
+// default since CUDA 12.2) the array itself comes into being at that same
+// moment, when the runtime loads this file's module: the first call on a
+// device is the one that reserves the 16 MiB, and later calls allocate
+// nothing.  That first call should therefore come before another allocator
+// takes the device's free memory, and before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -52,11 +56,14 @@ __global__ void __launch_bounds__(128)
   const uint32_t T = 2 * n_reads;
   if (t >= T) return;
   const uint32_t read = t >> 1, strand = t & 1;
-  const uint64_t b = offs[read];
-  const int len = (int)(offs[read + 1] - b);
+  const uint64_t b = offs[read], e = offs[read + 1];
+  // Offsets that run backwards, or a read longer than len_cap, get no hits;
+  // the length is narrowed to int only after that check.
+  const bool span_ok = e >= b && e - b <= (uint64_t)len_cap;
+  const int len = span_ok ? (int)(e - b) : 0;
   uint8_t* W = scratch + (size_t)t * len_cap;
   uint2* vecs = reinterpret_cast<uint2*>(scratch + align256((size_t)T * len_cap));
-  bool ok = len >= 3 && (uint32_t)len <= len_cap;
+  bool ok = span_ok && len >= 3;
   for (int i = 0; ok && i < len; ++i) {
     const uint8_t c = table[ascii[b + i]];
     ok = c != 0xFF;
@@ -172,7 +179,9 @@ int bwt_gpu_search1_noalloc(bwt_index_t* index, const char* d_seqs, const uint64
                                                  (uint32_t)n_reads, (uint32_t)len_cap, max_results,
                                                  static_cast<unsigned char*>(scratch), d_hits, d_counts, d_truncated);
     count_launches(1);
-    const cudaError_t ce = cudaGetLastError();
+    // Peek, so that an error left pending by an earlier, unrelated call on
+    // this thread is neither cleared nor reported as this launch's failure.
+    const cudaError_t ce = cudaPeekAtLastError();
     if (ce != cudaSuccess) {
       err = std::string("bwt_gpu_search1_noalloc: launch failed: ") + cudaGetErrorString(ce);
       rc = -1;

@@ -27,7 +27,9 @@ BUILD = PKG / "_build"
 LIB = PKG / "libhpgbwt.so"
 ORACLE_SRC = ROOT / "oracle" / "fm_oracle.c"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
-REF_DIR = Path(os.environ.get("HPG_REFERENCE_DIR", "/root/reference"))
+# The reference checkout the oracle library is compiled from: HPG_REFERENCE_DIR,
+# else a checkout named "reference" beside this repository's directory.
+REF_DIR = Path(os.environ.get("HPG_REFERENCE_DIR") or (ROOT.parent / "reference"))
 REF_LIB = ROOT / "oracle" / "_ref" / "libhpgref.so"
 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"

@@ -51,6 +51,24 @@ class Result:
                 and np.array_equal(self.rs_count, other.rs_count)
                 and np.array_equal(self.rs_truncated, other.rs_truncated))
 
+    def subset(self, reads: np.ndarray) -> "Result":
+        """The records of the given reads (ascending batch indices), renumbered as
+        the result of a batch holding only those reads: read ids become their
+        positions in `reads`, hit ids count the kept hits."""
+        reads = np.asarray(reads, dtype=np.int64)
+        n = len(self.rs_count) // 2
+        new_read = np.full(n, -1, dtype=np.int64)
+        new_read[reads] = np.arange(len(reads))
+        keep_hit = new_read[self.hits["read"].astype(np.int64)] >= 0
+        hits = self.hits[keep_hit].copy()
+        hits["read"] = new_read[hits["read"].astype(np.int64)].astype(np.uint32)
+        new_hit = np.cumsum(keep_hit, dtype=np.int64) - 1
+        keep_loc = keep_hit[self.locs["hit"].astype(np.int64)] if len(self.locs) else np.zeros(0, dtype=bool)
+        locs = self.locs[keep_loc].copy()
+        locs["hit"] = new_hit[locs["hit"].astype(np.int64)].astype(np.uint32)
+        rows = np.stack([2 * reads, 2 * reads + 1], axis=1).ravel()
+        return Result(hits, locs, self.rs_count[rows].copy(), self.rs_truncated[rows].copy())
+
 
 @dataclass
 class BlockResult:
@@ -116,8 +134,6 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_chunk.argtypes = [vp, sz]
     lib.bwt_gpu_set_tuning.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.bwt_gpu_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
-    lib.bwt_gpu_fm_probe.argtypes = [vp, vp, vp, sz, u32, ctypes.POINTER(ctypes.c_float),
-                                     ctypes.POINTER(ctypes.c_ulonglong)]
     lib.bwt_gpu_set_load_mode.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_load_mode.argtypes = [vp]
     lib.bwt_gpu_server_new.restype = vp
@@ -172,7 +188,6 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_index_bytes.restype = sz
     lib.bwt_gpu_index_bytes.argtypes = [vp]
     lib.bwt_gpu_gather_ceiling.argtypes = [ctypes.c_int, sz, u32, u32, ctypes.POINTER(ctypes.c_double)]
-    lib.bwt_gpu_gather_probe.argtypes = [ctypes.c_int, sz, u32, u32, u32, ctypes.POINTER(ctypes.c_double)]
     lib.hpg_bwt_build_index.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
                                         ctypes.c_char_p, ctypes.c_char_p, sz]
     lib.hpg_bwt_build_index_on.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int,
@@ -189,14 +204,6 @@ def gather_ceiling(device: int, nbytes: int, blocks: int, steps: int) -> float:
     lib = load()
     v = ctypes.c_double()
     if lib.bwt_gpu_gather_ceiling(device, nbytes, blocks, steps, ctypes.byref(v)) != 0:
-        raise RuntimeError(lib.bwt_gpu_last_error().decode())
-    return v.value
-
-
-def gather_probe(device: int, nbytes: int, blocks: int, steps: int, work: int) -> float:
-    lib = load()
-    v = ctypes.c_double()
-    if lib.bwt_gpu_gather_probe(device, nbytes, blocks, steps, work, ctypes.byref(v)) != 0:
         raise RuntimeError(lib.bwt_gpu_last_error().decode())
     return v.value
 
@@ -310,14 +317,6 @@ class GpuIndex:
         rows.value = min(rows.value, 128)
         return [{"register_bound_blocks": table[5 * i], "blocks_per_sm": table[5 * i + 1], "stack": table[5 * i + 2],
                  "chains_per_claim": table[5 * i + 3], "search_us": table[5 * i + 4]} for i in range(rows.value)]
-
-    def fm_probe(self, d_seqs: int, d_offs: int, n_reads: int, reps: int = 1) -> tuple[float, int]:
-        """(device ms, rank steps)"""
-        ms = ctypes.c_float()
-        steps = ctypes.c_ulonglong()
-        self._check(self.lib.bwt_gpu_fm_probe(self.handle, d_seqs, d_offs, n_reads, reps, ctypes.byref(ms),
-                                              ctypes.byref(steps)))
-        return ms.value, int(steps.value)
 
     def set_load_mode(self, mode: int) -> None:
         self.lib.bwt_gpu_set_load_mode(self.handle, mode)

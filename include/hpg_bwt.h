@@ -255,17 +255,6 @@ size_t bwt_gpu_index_bytes(bwt_index_t *index);
 /* Measured ceiling of dependent random 32-byte sector reads over a buffer of
  * `bytes` on `device` (blocks x 128 threads, `steps` hops each), in sectors/s. */
 int bwt_gpu_gather_ceiling(int device, size_t bytes, uint32_t blocks, uint32_t steps, double *sectors_per_s);
-/* The same gather with `work` dependent hash rounds between hops (how much
- * per-step arithmetic the memory system hides at a given occupancy). */
-int bwt_gpu_gather_probe(int device, size_t bytes, uint32_t blocks, uint32_t steps, uint32_t work,
-                         double *sectors_per_s);
-/* Best case of the real access pattern: one thread per read runs only the
- * full exact search, (reps & 0xFFFF) times (device reads as for
- * bwt_gpu_search_device); reps >> 16 selects backward search on the backward
- * index (0), forward search on the forward index (1) or half of each (2).
- * Device time in *ms, rank steps taken in *steps (may be NULL). */
-int bwt_gpu_fm_probe(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
-                     uint32_t reps, float *ms, unsigned long long *steps);
 /* Message of the last failed call on this thread. */
 const char *bwt_gpu_last_error(void);
 
@@ -278,14 +267,17 @@ const char *bwt_gpu_last_error(void);
  * allocate device memory: processes whose HBM is owned by another allocator
  * (a serving runtime that has reserved the whole device for its own pool and
  * forbids side allocations), and latency-critical threads, where a
- * cudaMalloc/cudaFree can stall on device-wide synchronisation.  This call
- * allocates nothing: its scratch is one fixed 16 MiB array that every GPU
- * loading the library holds until the process exits
- * (bwt_gpu_noalloc_scratch_bytes()).
+ * cudaMalloc/cudaFree can stall on device-wide synchronisation.  Its scratch
+ * is one fixed 16 MiB array per device (bwt_gpu_noalloc_scratch_bytes()),
+ * held until the process exits.  With CUDA's default lazy module loading the
+ * runtime creates that array on the first call made on a device, so that
+ * first call is the one that takes device memory: make it right after
+ * bwt_index_new, before another allocator reserves the device's free memory
+ * and before any stream capture.  Every later call allocates nothing.
  *
  * All buffers are the caller's device memory: d_seqs/d_offsets as in
- * bwt_gpu_search_device (max_len must cover the longest read; longer reads
- * get no hits); d_hits holds 2 * n_reads * max_results records,
+ * bwt_gpu_search_device (max_len must cover the longest read; longer reads,
+ * and reads whose offsets run backwards, get no hits); d_hits holds 2 * n_reads * max_results records,
  * hit i of (read r, strand s) at [(2*r + s) * max_results + i]; d_counts and
  * d_truncated hold 2 * n_reads entries.  The kernel is launched on `stream`
  * (the index's stream when NULL) and the call returns without waiting.
@@ -297,9 +289,9 @@ const char *bwt_gpu_last_error(void);
  * read, so no call depends on what an earlier call left there, but every call
  * on a device shares it: calls whose kernels overlap on the GPU race and must
  * be serialised by the caller (one stream, or events).  The first call on a
- * device looks up the scratch's device address (cudaGetSymbolAddress with
- * that device current); make that first call before any stream capture.
- * Returns 0 once the kernel is queued. */
+ * device also looks up the scratch's device address (cudaGetSymbolAddress
+ * with that device current).  Returns 0 once the kernel is queued; a runtime
+ * error left pending by earlier work on the calling thread is not consumed. */
 int bwt_gpu_search1_noalloc(bwt_index_t *index, const char *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                             uint32_t max_len, uint32_t max_results, hpg_hit_t *d_hits, uint32_t *d_counts,
                             uint8_t *d_truncated, void *stream);
