@@ -304,6 +304,16 @@ int bwt_gpu_direction_split(bwt_index_t* index) {
   return e ? engine_dir_split(e) : -1;
 }
 
+void bwt_gpu_set_wave_group(bwt_index_t* index, int reads) {
+  Engine* e = engine_of(index);
+  if (e) engine_set_wave_group(e, reads);
+}
+
+int bwt_gpu_wave_group(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_wave_group(e) : -1;
+}
+
 void bwt_gpu_set_idle_batch(bwt_index_t* index, int lanes) {
   Engine* e = engine_of(index);
   if (e) engine_set_idle_batch(e, lanes);

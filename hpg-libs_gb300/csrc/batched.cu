@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "batched.cuh"
+#include "batched_dev.cuh"
 #include "kernels.cuh"
 #include "search_core.cuh"
 
@@ -16,55 +17,7 @@ namespace {
 
 constexpr int kBlock = 128;
 
-// Change-point entry types.
-enum : uint32_t { kCpBwd = 0, kCpFwd = 1, kBlk1 = 2, kBlkN = 3 };
-// Sub-operations of an entry: 0 deletion, then per base b: 1+3b aux step,
-// 2+3b insertion, 3+3b mismatch; 13 = finished.
-constexpr uint32_t kSubEnd = 13;
-
-// Order keys: section << 28 | t << 8 | slot, following the helper's emission
-// order: exact hit, j=1 block, backward j ascending, j=n-1 block, forward j descending.
-__device__ __forceinline__ uint32_t order_key(uint32_t section, uint32_t t, uint32_t slot) {
-  return (section << 28) | (t << 8) | slot;
-}
-
-// Pool slots are reserved per lane in chunks, so an emission normally waits on
-// no atomic: the per-list arrival count is a fire-and-forget reduction and
-// the list position is assigned later by the scatter kernel.
-constexpr unsigned kResChunk = 8;
-
-__device__ __forceinline__ void write_hit(const BatchedParams& p, unsigned slot, uint32_t rs, uint32_t key,
-                                          uint32_t k, uint32_t l, uint32_t meta) {
-  atomicAdd(&p.rs_count[rs], 1u);  // result unused: compiles to a reduction
-  if (slot < p.res_cap) {
-    PendingHit h;
-    h.rs = rs;
-    h.key = key;
-    h.k = k;
-    h.l = l;
-    h.meta = meta;
-    h.idx = 0;
-    p.res[slot] = h;
-  } else {
-    atomicOr(p.status, kStatusResFull);
-  }
-}
-
-__device__ __forceinline__ void emit_hit(const BatchedParams& p, uint32_t rs, uint32_t key, uint32_t k, uint32_t l,
-                                         uint32_t meta) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  unsigned base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(p.res_total, (unsigned)g.size());
-  base = g.shfl(base, 0) + g.thread_rank();
-  write_hit(p, base, rs, key, k, l, meta);
-}
-
-__device__ __forceinline__ unsigned claim(unsigned int* ctr, unsigned n) {
-  cg::coalesced_group g = cg::coalesced_threads();
-  unsigned base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(ctr, (unsigned)g.size() * n);
-  return g.shfl(base, 0) + g.thread_rank() * n;
-}
+using namespace bdev;
 
 // Next read of a chain set (part 0: the chains on the backward index, 1: those
 // on the forward index, 2: all four), aggregated per warp and per set.
@@ -82,38 +35,6 @@ __device__ __forceinline__ uint32_t sm_id() {
   return r;
 }
 
-// Chunked pool slot for the calling lane (cold state c_res = next slot | left << 28).
-__device__ __forceinline__ unsigned res_slot(const BatchedParams& p, uint32_t& c_res) {
-  unsigned left = c_res >> 28;
-  if (left == 0) {
-    c_res = claim(p.res_total, kResChunk);
-    left = kResChunk;
-    if (c_res >= (1u << 28)) {  // beyond what the packed form holds: fall back to single slots
-      c_res = 0;
-      return claim(p.res_total, 1) | 0u;
-    }
-  }
-  const unsigned slot = c_res & 0x0FFFFFFFu;
-  c_res = (slot + 1) | ((left - 1) << 28);
-  return slot;
-}
-
-// Lane modes.
-enum : uint32_t { kNone = 0, kChain = 1, kCont = 2, kSingle = 3, kKmer = 4 };
-
-// Cold lane state lives in shared memory (one word per lane and field), so
-// that the registers hold only what every step touches.
-//   meta: J (16 bits) | entry type << 16 | sub-operation << 18 | block err_pos << 22 | in entry << 24
-//   misc: stack depth (4 bits) | chains left in the claimed chunk << 4
-__device__ __forceinline__ uint32_t meta_j(uint32_t m) { return m & 0xFFFFu; }
-__device__ __forceinline__ uint32_t meta_type(uint32_t m) { return (m >> 16) & 3u; }
-__device__ __forceinline__ uint32_t meta_sub(uint32_t m) { return (m >> 18) & 15u; }
-__device__ __forceinline__ uint32_t meta_bpos(uint32_t m) { return (m >> 22) & 3u; }
-__device__ __forceinline__ bool meta_in(uint32_t m) { return (m >> 24) & 1u; }
-__device__ __forceinline__ uint32_t make_meta(uint32_t j, uint32_t type, uint32_t sub, uint32_t bpos, bool in) {
-  return j | (type << 16) | (sub << 18) | (bpos << 22) | ((in ? 1u : 0u) << 24);
-}
-
 template <int D, int MINB, bool CENSUS>
 __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X, BatchedParams p, int drain,
                                                                       int chunk) {
@@ -123,7 +44,7 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
   __shared__ uint32_t s_nreads, s_spill_end;
   const int tid = threadIdx.x;
   if (tid == 0) {
-    s_nreads = p.n_reads_dev ? *p.n_reads_dev : p.n_reads;
+    s_nreads = p.read_list ? min(*p.read_list_n, p.long_cap) : (p.n_reads_dev ? *p.n_reads_dev : p.n_reads);
     s_spill_end = drain ? min(*(volatile unsigned int*)p.spill_tail, p.spill_cap) : 0u;
   }
   c_meta[tid] = 0;
@@ -311,8 +232,9 @@ __global__ void __launch_bounds__(kBlock, MINB) batched_search_kernel(DevIndex X
       }
       uint32_t chain = (misc >> 4) & 7u;
       if (chain >= ((((c_part[tid] >> 3) & 3u) == 2u) ? 4u : 2u)) {  // next read
-        const uint32_t r = next_claim();
-        if (r >= s_nreads) break;
+        const uint32_t rc = next_claim();
+        if (rc >= s_nreads) break;
+        const uint32_t r = p.read_list ? p.read_list[rc] : rc;
         c_read[tid] = r;
         const uint64_t b0 = p.offs[r];
         const int L = (int)(p.offs[r + 1] - b0);
@@ -1125,6 +1047,7 @@ int occupancy_d(const BatchedTuning& t) {
 }  // namespace
 
 int batched_max_blocks_per_sm(const BatchedTuning& t) {
+  if (t.split == 3) return wave_max_blocks_per_sm(t);
   if (t.split == 2) {
     int per_sm = 0;
     if (t.min_blocks >= 16)
@@ -1164,6 +1087,10 @@ int batched_max_blocks_per_sm(const BatchedTuning& t) {
 
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                            cudaStream_t s) {
+  if (t.split == 3 && !drain) {  // warp-cooperative chains and branches
+    launch_wave_search(X, p, t, num_sms, s);
+    return;
+  }
   if (t.split == 2 && !drain) {  // lockstep chains, one lane per read
     int per_sm = 0;
     if (t.min_blocks >= 16) {
@@ -1305,6 +1232,86 @@ void launch_build_kmer(const DevIndex& X, uint32_t d, uint32_t L, uint2* out, cu
   const uint32_t n = 1u << (2 * L);
   count_launches(1);
   build_kmer_kernel<<<(n + 255) / 256, 256, 0, s>>>(X, d, L, out);
+}
+
+
+void launch_search_stage(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms,
+                         unsigned int* ctr, uint32_t* long_list, uint32_t long_cap, SpillEntry* blocks,
+                         uint32_t block_cap, cudaEvent_t mid, bool external, cudaStream_t s) {
+  auto mark = [&]() {
+    if (!mid) return;
+    if (external)
+      cudaEventRecordWithFlags(mid, s, cudaEventRecordExternal);
+    else
+      cudaEventRecord(mid, s);
+  };
+  if (t.split == 1) {
+    // one index direction at a time: chains on the backward index and their
+    // change points, then chains on the forward index and theirs
+    BatchedTuning t0 = t;
+    BatchedParams p1 = p;
+    p1.chain_ctr = ctr + 8;
+    t0.phase = 0;
+    launch_batched_search(X, p, t0, num_sms, false, s);
+    launch_batched_search(X, p, t0, num_sms, true, s);
+    cudaMemcpyAsync(ctr + 1, ctr + 2, 4, cudaMemcpyDeviceToDevice, s);  // drain resumes at the queue tail
+    mark();
+    t0.phase = 1;
+    launch_batched_search(X, p1, t0, num_sms, false, s);
+    launch_batched_search(X, p1, t0, num_sms, true, s);
+  } else if (t.split == 3) {
+    // warp-cooperative launches (one per index direction, or one for both), the
+    // fused kernel over the reads too long for a warp's group buffer, then the
+    // change points that did not fit the warps' stacks, and the blocks
+    BatchedParams pw = p;
+    pw.wave_group = (uint32_t)(t.group < 1 ? 1 : (t.group > 32 ? 32 : t.group));
+    pw.long_list = long_list;
+    pw.long_n = ctr + 10;
+    pw.long_cap = long_cap;
+    pw.blocks = blocks;
+    pw.block_n = ctr + 13;
+    pw.block_cap = block_cap;
+    if (t.dir_split == 2) {
+      pw.dir_split = 2;
+      launch_wave_search(X, pw, t, num_sms, s);
+      pw.dir_split = 3;
+      launch_wave_search(X, pw, t, num_sms, s);
+    } else {
+      pw.dir_split = 0;
+      launch_wave_search(X, pw, t, num_sms, s);
+    }
+    BatchedParams pl = p;
+    BatchedTuning tl = t;
+    tl.split = 0;
+    tl.dir_split = 0;
+    pl.dir_split = 0;
+    pl.chain_ctr = ctr + 11;
+    pl.read_list = long_list;
+    pl.read_list_n = ctr + 10;
+    pl.long_cap = long_cap;
+    launch_batched_search(X, pl, tl, num_sms, false, s);
+    mark();
+    // queued change points' branches, eight per change point; the blocks among
+    // them join the block list, which the fused kernel's drain then empties
+    launch_wave_branches(X, p, blocks, ctr + 13, block_cap, num_sms, s);
+    BatchedParams pb = p;
+    pb.spill = blocks;
+    pb.spill_head = ctr + 12;
+    pb.spill_tail = ctr + 13;
+    pb.spill_cap = block_cap;
+    launch_batched_search(X, pb, tl, num_sms, true, s);
+  } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
+    launch_batched_search(X, p, t, num_sms, false, s);
+    BatchedParams p1 = p;
+    p1.dir_split = 3;
+    launch_batched_search(X, p1, t, num_sms, false, s);
+    mark();
+    launch_batched_search(X, p, t, num_sms, true, s);
+  } else {
+    launch_batched_search(X, p, t, num_sms, false, s);
+    mark();
+    launch_batched_search(X, p, t, num_sms, true, s);
+  }
 }
 
 }  // namespace hpgbwt

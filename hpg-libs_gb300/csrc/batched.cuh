@@ -66,6 +66,21 @@ struct BatchedParams {
   uint32_t* rs_count;        // [2 * n_reads] arrivals per (read, strand)
   unsigned int* status;      // bit 0: result pool full, bit 1: spill queue full
   unsigned long long* census;
+  // warp-cooperative form (wave.cu): reads claimed per warp group; reads too long for a
+  // group buffer are appended to long_list (long_n of them, long_cap at most) for the
+  // fused kernel; j = 1 / j = n-1 blocks go to `blocks` (block_n, block_cap) for the
+  // fused drain
+  uint32_t wave_group = 32;
+  uint64_t codes_len = 0;  // bytes of `codes` that may be read (its allocation)
+  uint32_t* long_list = nullptr;
+  unsigned int* long_n = nullptr;
+  uint32_t long_cap = 0;
+  SpillEntry* blocks = nullptr;
+  unsigned int* block_n = nullptr;
+  uint32_t block_cap = 0;
+  // fused form: when set, claim i runs read read_list[i], for i < *read_list_n
+  const uint32_t* read_list = nullptr;
+  const unsigned int* read_list_n = nullptr;
 };
 
 struct BatchedTuning {
@@ -75,10 +90,12 @@ struct BatchedTuning {
   int chunk = 1;          // chains claimed per lane per refill (1, 2 or 4)
   int min_blocks = 1;     // register bound: 1 (compiler's choice), 12 or 16 resident blocks per SM
   int split = 0;          // 0: fused (per-lane stacks); 1: chain-only kernel + drain of every change point;
-                          // 2: lockstep kernel (4 chains of a read per lane) + drain
+                          // 2: lockstep kernel (4 chains of a read per lane) + drain;
+                          // 3: warp-cooperative kernels (wave.cu) + the fused kernel over their long reads and blocks
   int phase = 2;          // set by the engine for split launches: 0/1 one index direction, 2 both
   int dir_split = 0;      // fused form: 0 mixed, 1 direction by SM half, 2 one launch per direction
   int batch_idle = 8;     // fused form: idle lanes that move to their next work item together (1: each at once)
+  int group = 32;         // warp-cooperative form (split 3): reads a warp claims at a time (32 / group lanes per read)
 };
 
 // One locate work item per SA row: the row, the owning hit (or request), the
@@ -100,6 +117,12 @@ constexpr uint32_t kRowLenMask = kRowKey32 - 1u;
 constexpr uint64_t kMaxLocateRows = 0xF0000000ull;
 
 constexpr unsigned kStatusResFull = 1u, kStatusSpillFull = 2u, kStatusLocFull = 4u, kStatusBadInput = 8u;
+// warp-cooperative search: a warp found live work counted for a group buffer that nothing
+// held (an internal inconsistency; the batch is failed rather than trusted)
+constexpr unsigned kStatusWaveAcct = 32u;
+// Reads longer than this many bases may not fit a warp group buffer of the
+// warp-cooperative form; a batch holds at most total_bases / kWaveLongMin + 1 such reads.
+constexpr uint64_t kWaveLongMin = 4000;
 
 // Locate sizes of the graph form: with `status` set, the hit and row counts
 // are read from device memory, rows beyond `locs_cap` raise kStatusLocFull,
@@ -115,6 +138,24 @@ struct LocateSizes {
 void launch_batched_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms, bool drain,
                            cudaStream_t s);
 int batched_max_blocks_per_sm(const BatchedTuning& t);
+// The warp-cooperative search (wave.cu), one launch: p.dir_split 2 / 3 runs the
+// backward- / forward-index chains, anything else all four chains of a read.
+void launch_wave_search(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms,
+                        cudaStream_t s);
+int wave_max_blocks_per_sm(const BatchedTuning& t);
+// The helper's branches of the change points queued in p.spill (from
+// p.spill_head on), eight continuations per change point; j = 1 / j = n-1 block
+// entries are copied to `blocks` (count in *block_n) for the fused drain.
+void launch_wave_branches(const DevIndex& X, const BatchedParams& p, SpillEntry* blocks, unsigned int* block_n,
+                          uint32_t block_cap, int num_sms, cudaStream_t s);
+// The whole search stage of a tuning: the search launches, then (after `mid`,
+// recorded when not null) the drain of queued change points.  `ctr` is the
+// counter block (16 words, zeroed); the warp-cooperative form also needs
+// `long_list` (room for its long reads) and `blocks` (room for the j = 1 /
+// j = n-1 blocks among the change points, as many as the queue holds).
+void launch_search_stage(const DevIndex& X, const BatchedParams& p, const BatchedTuning& t, int num_sms,
+                         unsigned int* ctr, uint32_t* long_list, uint32_t long_cap, SpillEntry* blocks,
+                         uint32_t block_cap, cudaEvent_t mid, bool external, cudaStream_t s);
 
 // Finalize: scatter pending hits into (read, strand) segments, sort each by
 // key, truncate; kept counts to `kept`, truncation flags to `trunc`.

@@ -276,8 +276,11 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   (void)d_offs_u8;
   cudaStream_t s = e->stream;
   const size_t T = 2ull * n;
+  // reads too long for a warp group buffer of the warp-cooperative form (at most one per kWaveLongMin bases)
+  const uint32_t long_cap = (uint32_t)std::min<size_t>(e->codes.cap / kWaveLongMin + 2, 0xFFFFFFF0u);
   if (!ensure(e, e->b_ctr, 64) || !ensure(e, e->b_arr, T * 4 + 16) || !ensure(e, e->b_seg, (T + 1) * 8) ||
-      !ensure(e, e->hit_off, (T + 1) * 8) || !ensure(e, e->scan_part, scan_parts(T) * 8)) {
+      !ensure(e, e->hit_off, (T + 1) * 8) || !ensure(e, e->scan_part, scan_parts(T) * 8) ||
+      !ensure(e, e->b_long, (size_t)long_cap * 4)) {
     *err = "out of device memory (batched counters)";
     return -1;
   }
@@ -288,9 +291,11 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
   unsigned int* ctr = ptr<unsigned int>(e->b_ctr);  // [0] chains [1] spill head [2] spill tail [3] results [4] status [5..7] locate [8] phase-1 chains
   uint32_t status = 0, res_total = 0;
   for (int attempt = 0; attempt < 8; ++attempt) {
+    const bool wave = e->tuning.split == 3;
     if (!ensure(e, e->b_res, (size_t)e->b_res_cap * sizeof(PendingHit)) ||
         !ensure(e, e->b_sorted, (size_t)e->b_res_cap * sizeof(PendingHit)) ||
-        !ensure(e, e->b_spill, (size_t)e->b_spill_cap * sizeof(SpillEntry))) {
+        !ensure(e, e->b_spill, (size_t)e->b_spill_cap * sizeof(SpillEntry)) ||
+        (wave && !ensure(e, e->b_blocks, (size_t)e->b_spill_cap * sizeof(SpillEntry)))) {
       *err = "out of device memory (batched pools)";
       return -1;
     }
@@ -299,6 +304,7 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     if (census) cudaMemsetAsync(census, 0, 8, s);
     BatchedParams p;
     p.codes = ptr<uint8_t>(e->codes);
+    p.codes_len = e->codes.cap;
     p.offs = d_offs;
     p.ok = ptr<uint8_t>(e->ok);
     p.n_reads = n;
@@ -320,32 +326,9 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     p.status = ctr + 4;
     p.census = census;
     cudaEventRecord(e->cev[0], s);
-    if (e->tuning.split == 1) {
-      // one index direction at a time: chains on the backward index and their
-      // change points, then chains on the forward index and theirs
-      BatchedTuning t = e->tuning;
-      BatchedParams p1 = p;
-      p1.chain_ctr = ctr + 8;
-      t.phase = 0;
-      launch_batched_search(e->X, p, t, e->num_sms, false, s);
-      launch_batched_search(e->X, p, t, e->num_sms, true, s);
-      cudaMemcpyAsync(ctr + 1, ctr + 2, 4, cudaMemcpyDeviceToDevice, s);  // drain resumes at the queue tail
-      cudaEventRecord(e->dev_mid, s);
-      t.phase = 1;
-      launch_batched_search(e->X, p1, t, e->num_sms, false, s);
-      launch_batched_search(e->X, p1, t, e->num_sms, true, s);
-    } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
-      launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
-      BatchedParams p1 = p;
-      p1.dir_split = 3;
-      launch_batched_search(e->X, p1, e->tuning, e->num_sms, false, s);
-      cudaEventRecord(e->dev_mid, s);
-      launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
-    } else {
-      launch_batched_search(e->X, p, e->tuning, e->num_sms, false, s);
-      cudaEventRecord(e->dev_mid, s);
-      launch_batched_search(e->X, p, e->tuning, e->num_sms, true, s);
-    }
+    launch_search_stage(e->X, p, e->tuning, e->num_sms, ctr, ptr<uint32_t>(e->b_long), long_cap,
+                        wave ? ptr<SpillEntry>(e->b_blocks) : nullptr, wave ? e->b_spill_cap : 0u, e->dev_mid, false,
+                        s);
     cudaEventRecord(e->cev[1], s);
     uint32_t h[5];
     HPG_CUDA(cudaMemcpyAsync(h, ctr, 20, cudaMemcpyDeviceToHost, s), "batched counters");
@@ -353,6 +336,10 @@ int run_batched(Engine* e, const uint8_t* d_offs_u8, const uint64_t* d_offs, uin
     status = h[4];
     res_total = h[3];
     if (!status) break;
+    if (status & kStatusWaveAcct) {
+      *err = "internal error: inconsistent work counts in the warp-cooperative search";
+      return -1;
+    }
     if (status & kStatusResFull) e->b_res_cap = (uint32_t)std::min<size_t>((size_t)res_total * 2 + 4096, 0xFFFFFFF0u);
     if (status & kStatusSpillFull) e->b_spill_cap = (uint32_t)std::min<size_t>((size_t)h[2] * 2 + 4096, 0xFFFFFFF0u);
   }
@@ -440,6 +427,17 @@ void engine_set_tuning(Engine* e, int min_blocks, int blocks_per_sm, int stack, 
 }
 
 void engine_set_dir_split(Engine* e, int mode) { e->tuning.dir_split = mode < 0 ? 0 : (mode > 2 ? 2 : mode); }
+void engine_set_wave_group(Engine* e, int reads) {
+  if (reads <= 0) {
+    if (e->tuning.split == 3) e->tuning.split = 0;
+    return;
+  }
+  e->tuning.split = 3;
+  e->tuning.group = reads > 32 ? 32 : reads;
+  // the warp-cooperative kernel is built for register bounds of 1, 8 and 12 blocks per SM
+  e->tuning.min_blocks = e->tuning.min_blocks >= 12 ? 12 : (e->tuning.min_blocks >= 8 ? 8 : 1);
+}
+int engine_wave_group(Engine* e) { return e->tuning.split == 3 ? e->tuning.group : 0; }
 void engine_set_idle_batch(Engine* e, int lanes) { e->tuning.batch_idle = lanes < 1 ? 1 : (lanes > 32 ? 32 : lanes); }
 int engine_idle_batch(Engine* e) { return e->tuning.batch_idle; }
 int engine_dir_split(Engine* e) { return e->tuning.dir_split; }
@@ -452,8 +450,8 @@ int engine_load_mode(Engine* e) { return (int)e->X.load_mode; }
 void engine_get_tuning(Engine* e, int* out5) {
   out5[0] = e->tuning.block;
   out5[1] = batched_max_blocks_per_sm(e->tuning);
-  out5[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
-  out5[3] = e->tuning.chunk;
+  out5[2] = e->tuning.split == 3 ? -2 : (e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack));
+  out5[3] = e->tuning.split == 3 ? e->tuning.group : e->tuning.chunk;
   out5[4] = e->tuning.min_blocks;
 }
 
@@ -503,6 +501,38 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
           best = e->tuning;
         }
       }
+  // the warp-cooperative form: reads per warp group (lanes per read = 32 / group)
+  // x register bound x one launch per index direction or one for both; rows
+  // carry stack -2 and the group in the chains column
+  for (int grp : {8, 16, 32})
+    for (int mb : {8, 12})
+      for (int ds : {0, 2}) {
+        engine_set_tuning(e, mb, 0, 4, 1);
+        e->tuning.split = 3;
+        e->tuning.min_blocks = mb;
+        e->tuning.group = grp;
+        e->tuning.dir_split = ds;
+        float t = 0;
+        for (int rep = 0; rep < 2; ++rep) {
+          if (engine_search_device(e, HPG_BWT_MODE_SEARCH1, kFormBatched, d_seqs, d_offs, n_reads, total_bases,
+                                   max_len, max_results, &r, err) != 0)
+            return -1;
+          t = e->stage_ms[kStageSearch];
+        }
+        if (table && rows < max_rows) {
+          int* row = table + 5 * rows;
+          row[0] = mb;
+          row[1] = batched_max_blocks_per_sm(e->tuning);
+          row[2] = -2;
+          row[3] = grp;
+          row[4] = (int)(t * 1000.0f);
+        }
+        ++rows;
+        if (t < best_ms) {
+          best_ms = t;
+          best = e->tuning;
+        }
+      }
   e->tuning = best;
   // then the block-load form, with the chosen setting
   uint32_t best_mode = e->X.load_mode;
@@ -519,8 +549,8 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
       int* row = table + 5 * rows;
       row[0] = -1 - mode;  // load-mode rows are marked by a negative first column
       row[1] = batched_max_blocks_per_sm(e->tuning);
-      row[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
-      row[3] = e->tuning.chunk;
+      row[2] = e->tuning.split == 3 ? -2 : (e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack));
+      row[3] = e->tuning.split == 3 ? e->tuning.group : e->tuning.chunk;
       row[4] = (int)(t * 1000.0f);
     }
     ++rows;
@@ -578,8 +608,8 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
       int* row = table + 5 * rows;
       row[0] = -100 - L;
       row[1] = batched_max_blocks_per_sm(e->tuning);
-      row[2] = e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack);
-      row[3] = e->tuning.chunk;
+      row[2] = e->tuning.split == 3 ? -2 : (e->tuning.split == 2 ? -1 : (e->tuning.split ? 0 : e->tuning.stack));
+      row[3] = e->tuning.split == 3 ? e->tuning.group : e->tuning.chunk;
       row[4] = (int)(t * 1000.0f);
     }
     ++rows;

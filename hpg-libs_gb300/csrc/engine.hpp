@@ -70,6 +70,8 @@ void engine_set_load_mode(Engine* e, int mode);
 // launch per direction.
 void engine_set_dir_split(Engine* e, int mode);
 int engine_dir_split(Engine* e);
+void engine_set_wave_group(Engine* e, int reads);
+int engine_wave_group(Engine* e);
 void engine_set_idle_batch(Engine* e, int lanes);
 int engine_idle_batch(Engine* e);
 void engine_set_locate_limit(Engine* e, uint64_t max_rows);

@@ -51,7 +51,8 @@ struct GraphPlan {
   uint8_t* codes = nullptr;
   uint8_t* ok = nullptr;
   unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
-                            // [5..7] locate [8] phase-1 chains
+                            // [5..7] locate [8] phase-1 chains [9] forward-index reads [10] long reads
+                            // [11] long-read claims [12] block head [13] block tail
   uint32_t* arr = nullptr;  // arrivals per (read, strand)
   uint64_t* seg = nullptr;
   uint64_t* hit_off = nullptr;
@@ -68,6 +69,9 @@ struct GraphPlan {
   hpg_loc_t* locs = nullptr;
   unsigned long long* census_d = nullptr;
   uint64_t* summary_d = nullptr;
+  uint32_t* long_list = nullptr;  // reads too long for the warp-cooperative form's group buffers
+  uint32_t long_cap = 0;
+  SpillEntry* blocks = nullptr;   // j = 1 / j = n-1 blocks of the warp-cooperative form (spill_cap entries)
   // pinned host words
   uint64_t* h_summary = nullptr;  // [0] status | results << 32, [1] spill tail, [2] hits, [3] rows, [4] census
   uint32_t* h_hdr = nullptr;
@@ -97,7 +101,7 @@ struct Engine {
   DevBuf seqs, offs, codes, ok, rs_count, rs_trunc, vecs, slots, ovf, ovf_count, hit_off, scan_part, hits, rows,
       loc_off, locs, census;
   // batched form
-  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit;
+  DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit, b_long, b_blocks;
   uint32_t b_res_cap = 0, b_spill_cap = 0;
   BatchedTuning tuning;
   int num_sms = 0;

@@ -68,7 +68,7 @@ bool same_settings(const GraphPlan* g, const Engine* e) {
   const BatchedTuning& b = e->tuning;
   return a.block == b.block && a.blocks_per_sm == b.blocks_per_sm && a.stack == b.stack && a.chunk == b.chunk &&
          a.min_blocks == b.min_blocks && a.split == b.split && a.dir_split == b.dir_split &&
-         a.batch_idle == b.batch_idle &&
+         a.batch_idle == b.batch_idle && a.group == b.group &&
          g->load_mode == e->X.load_mode &&
          g->census == e->census_on && g->skip_locate == e->skip_locate && g->kmer_len == e->X.kmer_len &&
          g->kmer0 == (const void*)e->X.kmer[0];
@@ -91,6 +91,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
       !grab(g, &g->rows, ((size_t)g->res_cap + 1) * 4) || !grab(g, &g->loc_off, ((size_t)g->res_cap + 2) * 8) ||
       !grab(g, &g->items, (g->locs_cap + 1) * locate_row_item_bytes()) ||
       !grab(g, &g->locs, (g->locs_cap + 1) * sizeof(hpg_loc_t)) || !grab(g, &g->census_d, 16) ||
+      !grab(g, &g->long_list, (size_t)g->long_cap * 4) ||
+      (g->tuning.split == 3 && !grab(g, &g->blocks, (size_t)g->spill_cap * sizeof(SpillEntry))) ||
       !grab(g, &g->summary_d, 64)) {
     *err = "out of device memory (graph plan)";
     return -1;
@@ -117,6 +119,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
 
   BatchedParams p;
   p.codes = g->codes;
+  p.codes_len = g->bases_cap + 64;
   p.offs = g->offs;
   p.ok = g->ok;
   p.n_reads = g->n_cap;
@@ -137,30 +140,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   p.rs_count = g->arr;
   p.status = status;
   p.census = census;
-  if (g->tuning.split == 1) {
-    BatchedTuning t = g->tuning;
-    BatchedParams p1 = p;
-    p1.chain_ctr = ctr + 8;
-    t.phase = 0;
-    launch_batched_search(e->X, p, t, e->num_sms, false, s);
-    launch_batched_search(e->X, p, t, e->num_sms, true, s);
-    cudaMemcpyAsync(ctr + 1, ctr + 2, 4, cudaMemcpyDeviceToDevice, s);  // drain resumes at the queue tail
-    record(g->ev[2], s);
-    t.phase = 1;
-    launch_batched_search(e->X, p1, t, e->num_sms, false, s);
-    launch_batched_search(e->X, p1, t, e->num_sms, true, s);
-  } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
-    launch_batched_search(e->X, p, g->tuning, e->num_sms, false, s);
-    BatchedParams p1 = p;
-    p1.dir_split = 3;
-    launch_batched_search(e->X, p1, g->tuning, e->num_sms, false, s);
-    record(g->ev[2], s);
-    launch_batched_search(e->X, p, g->tuning, e->num_sms, true, s);
-  } else {
-    launch_batched_search(e->X, p, g->tuning, e->num_sms, false, s);
-    record(g->ev[2], s);
-    launch_batched_search(e->X, p, g->tuning, e->num_sms, true, s);
-  }
+  launch_search_stage(e->X, p, g->tuning, e->num_sms, ctr, g->long_list, g->long_cap, g->blocks,
+                      g->blocks ? g->spill_cap : 0u, g->ev[2], true, s);
   record(g->ev[3], s);
 
   // ordered finalize over the capacity (lists past the batch are empty)
@@ -264,6 +245,7 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   g = new GraphPlan();
   g->n_cap = (uint32_t)n_cap;
   g->bases_cap = old ? std::max(old->bases_cap, bases_cap) : bases_cap;
+  g->long_cap = (uint32_t)std::min<uint64_t>(g->bases_cap / kWaveLongMin + 2, 0xFFFFFFF0u);
   g->res_cap = res_cap;
   g->spill_cap = spill_cap;
   g->locs_cap = locs_cap;
@@ -312,6 +294,10 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
   const uint32_t status = (uint32_t)h[0];
   if (status & kStatusBadInput) {
     *err = "read offsets must be non-decreasing and reads at most 32767 bases";
+    return -1;
+  }
+  if (status & kStatusWaveAcct) {
+    *err = "internal error: inconsistent work counts in the warp-cooperative search";
     return -1;
   }
   if (status) {

@@ -150,6 +150,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_direction_split.argtypes = [vp]
+    lib.bwt_gpu_set_wave_group.argtypes = [vp, ctypes.c_int]
+    lib.bwt_gpu_wave_group.argtypes = [vp]
     lib.bwt_gpu_set_idle_batch.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_idle_batch.argtypes = [vp]
     lib.bwt_gpu_set_locate_limit.argtypes = [vp, u64]
@@ -334,6 +336,13 @@ class GpuIndex:
 
     def direction_split(self) -> int:
         return int(self.lib.bwt_gpu_direction_split(self.handle))
+
+    def set_wave_group(self, reads: int) -> None:
+        """Warp-cooperative batched search with `reads` reads per warp group (0: back to the fused form)."""
+        self.lib.bwt_gpu_set_wave_group(self.handle, int(reads))
+
+    def wave_group(self) -> int:
+        return int(self.lib.bwt_gpu_wave_group(self.handle))
 
     def set_idle_batch(self, lanes: int) -> None:
         """Fused batched search: idle lanes of a warp take their next work item together, `lanes` at a time."""

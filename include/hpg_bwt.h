@@ -214,6 +214,17 @@ void bwt_gpu_set_pipeline_chunk(bwt_index_t *index, size_t reads);
  * direction's occurrence blocks at a time.  Results are identical. */
 void bwt_gpu_set_direction_split(bwt_index_t *index, int mode);
 int bwt_gpu_direction_split(bwt_index_t *index);
+/* Warp-cooperative form of the batched search (no reference counterpart; the
+ * reference's helper, search/search.c:1491-1709, runs one read per CPU
+ * thread): 1..32 selects it, with that many reads claimed by a warp at a time
+ * (32 / reads lanes per read); their bases are staged in shared memory, and
+ * the warp's lanes share the group's chains and one stack of change points.
+ * The direction split (0 or 2), register bound (1, 8 or 12 blocks per SM),
+ * idle batch, start table and block-load form apply to it as to the fused
+ * form.  0 returns to the fused form.  Results are identical. */
+void bwt_gpu_set_wave_group(bwt_index_t *index, int reads);
+/* Reads per warp group of the warp-cooperative form, 0 when another form is selected. */
+int bwt_gpu_wave_group(bwt_index_t *index);
 /* Idle-lane batch of the batched search (fused form): a lane that finished its
  * work item waits, masked, until this many lanes of its warp have (or all
  * active ones have), and they take their next items together, so the code that

@@ -102,10 +102,12 @@ def test_autotuner_keeps_results(case_factory):
     with lib.GpuIndex(c.index) as g:
         table = g.autotune(d_seq.data_ptr(), d_off.data_ptr(), len(reads), int(reads.offsets[-1]),
                            int(np.diff(reads.offsets).max()), 64)
-        assert len(table) in (72, 75) and all(r["search_us"] > 0 for r in table)
+        # 60 fused/split/lockstep settings, 12 warp-cooperative ones, 4 load forms,
+        # 3 direction splits (fused form only), 4 start tables, 4 idle batches
+        assert len(table) in (84, 87) and all(r["search_us"] > 0 for r in table)
         chosen = g.get_tuning()
-        best_us = min(r["search_us"] for r in table[:60])
-        mine = [r["search_us"] for r in table[:60]
+        best_us = min(r["search_us"] for r in table[:72])
+        mine = [r["search_us"] for r in table[:72]
                 if (r["stack"], r["chains_per_claim"], r["register_bound_blocks"]) ==
                 (chosen["stack"], chosen["chains_per_claim"], chosen["register_bound_blocks"])]
         assert mine and min(mine) <= best_us + 1  # the fastest setting (ties rounded to 1 us) was kept
@@ -229,3 +231,84 @@ def test_locate_limit_matches_oracle(tmp_path_factory, form, graph):
     assert (want.rs_truncated & 2).any() and len(want.locs) > 0
     _assert_same(got, want)
     _assert_same(again, ora.search(reads, mode=lib.MODE_SEARCH1, max_results=100, threads=8))
+
+
+def _mixed_reads(c, n, seed, lo=3, hi=250):
+    """Skipped, short and odd reads around a main batch of mixed lengths and edits."""
+    main = synth.reads(c.genome, n, seed, length=(lo, hi), edits="mix_30_50_20")
+    odd = synth.from_strings([b"", b"AC", b"ACGTN" * 5, b"GATTACA", b""] * 40)
+    seq = np.concatenate([odd.seq, main.seq, odd.seq])
+    offs = np.concatenate([odd.offsets, main.offsets[1:] + odd.offsets[-1],
+                           odd.offsets[1:] + odd.offsets[-1] + main.offsets[-1]]).astype(np.uint64)
+    return synth.ReadSet(seq, offs, np.zeros(1), np.zeros(1), np.zeros(1))
+
+
+@pytest.mark.parametrize("group", [1, 8, 32])
+@pytest.mark.parametrize("split", [0, 2])
+@pytest.mark.parametrize("idle,minb", [(1, 12), (8, 12), (16, 8), (4, 1)])
+def test_wave_form_agrees(case_factory, group, split, idle, minb):
+    """The warp-cooperative form (reads per warp group x direction split x idle
+    batch x register bound) gives the oracle's answer, direct and from the graph."""
+    c = case_factory("repeats", 300_000, 3, 3)
+    reads = _mixed_reads(c, 5000, 61)
+    want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
+    with lib.GpuIndex(c.index) as g:
+        g.set_tuning(0, 4, 1, minb)
+        g.set_wave_group(group)
+        g.set_direction_split(split)
+        g.set_idle_batch(idle)
+        assert g.wave_group() == group and g.get_tuning()["stack"] == -2
+        _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+        g.set_graph(False)
+        _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+
+
+@pytest.mark.parametrize("symbols", [0, 8, 11])
+def test_wave_start_table_and_truncation(case_factory, symbols):
+    c = case_factory("human_like", 200_000, 5, 5)
+    reads = synth.reads(c.genome, 4000, 67, length=(12, 150), edits="mix_30_50_20")
+    ora = PortOracle(c.index)
+    with lib.GpuIndex(c.index) as g:
+        g.set_start_table(symbols)
+        g.set_wave_group(16)
+        for mr in (0, 3, 1 << 16):
+            _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED, max_results=mr),
+                         ora.search(reads, mode=lib.MODE_SEARCH1, max_results=mr, threads=8))
+
+
+def test_wave_long_reads(case_factory):
+    """Reads too long for a warp's 4096-base group buffer go to the fused kernel
+    through the long-read list; the rest of the batch stays warp-cooperative."""
+    c = case_factory("iid", 200_000, 71, 1)
+    A = np.frombuffer(b"ACGT", dtype=np.uint8)
+    g0 = c.genome
+    long = [A[g0[1000:5100]].tobytes(), A[g0[20000:30000]].tobytes(), A[g0[50000:54065]].tobytes(),
+            A[g0[60000:64050]].tobytes(), A[g0[90000:122767]].tobytes()]
+    short = synth.reads(c.genome, 300, 73, length=(36, 250), edits="mix_30_50_20")
+    seqs = []
+    for i in range(len(short)):
+        seqs.append(short.read(i))
+        if i % 60 == 0:
+            seqs.append(long[(i // 60) % len(long)])
+    reads = synth.from_strings(seqs)
+    assert np.diff(reads.offsets).max() == 32767
+    want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
+    with lib.GpuIndex(c.index) as g:
+        for split in (0, 2):
+            g.set_wave_group(32)
+            g.set_direction_split(split)
+            _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+            g.set_graph(False)
+            _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+            g.set_graph(True)
+
+
+@pytest.mark.parametrize("max_results", [100, 1024])
+def test_wave_overflowing_stacks(tmp_path_factory, max_results):
+    """Low-complexity reads find more change points than a warp's stack holds:
+    the rest go through the device queue and the branch launch."""
+    index, reads = low_complexity_case(tmp_path_factory.mktemp(f"lowcx_wave_{max_results}"))
+    want = PortOracle(index).search(reads, mode=lib.MODE_SEARCH1, max_results=max_results, threads=8)
+    with lib.GpuIndex(index) as g:
+        g.set_wave_group(32)
+        _assert_same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED, max_results=max_results), want)
