@@ -182,6 +182,12 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   cudaMemset(en->d_err, 0, 4);
   en->X.err = en->d_err;
   en->X.load_mode = 2;
+  // default batched form: warp-cooperative, 16 reads per warp group, one launch
+  // per index direction, 12 resident blocks per SM (the autotuner may pick another)
+  en->tuning.split = 3;
+  en->tuning.group = 16;
+  en->tuning.dir_split = 2;
+  en->tuning.min_blocks = 12;
   en->X.kmer_len = 0;
   en->X.kmer[0] = en->X.kmer[1] = nullptr;
 

@@ -183,8 +183,12 @@ void bwt_gpu_set_chunk(bwt_index_t *index, size_t reads);
  * memory (2, 4 or 8; more spill to the device queue; 0 = split form: a
  * chain-only kernel queues every change point for the drain launch; -1 =
  * lockstep form: one lane per read advances the read's four vector searches
- * together and queues change points), chains claimed per refill (1..8).  get: {threads per block, blocks per SM, stack depth,
- * chains per claim, register bound}. */
+ * together and queues change points), chains claimed per refill (1..8).  Setting
+ * a tuning selects the fused, split or lockstep form; an index opens in the
+ * warp-cooperative form (bwt_gpu_set_wave_group: 16 reads per warp group, one
+ * launch per index direction, 12 blocks per SM).  get: {threads per block,
+ * blocks per SM, stack depth (-2: warp-cooperative), chains per claim (reads
+ * per warp group in the warp-cooperative form), register bound}. */
 void bwt_gpu_set_tuning(bwt_index_t *index, int min_blocks, int blocks_per_sm, int stack_depth,
                         int chains_per_claim);
 void bwt_gpu_get_tuning(bwt_index_t *index, int *out5);
