@@ -703,6 +703,7 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
         if i == args.warmup + args.steps - 1:
             e2e_result = lib.result_from_c(rsc, n)
         gi.lib.bwt_gpu_result_free(lib.ctypes.byref(rsc))
+    log(f"[bench] e2e calls (ms): {[round(x * 1e3, 2) for x in e2e_t]}")
     rl = wl["read_len"]
     search1 = mode == lib.MODE_SEARCH1
     serve = serving(gi, reads, genome, log, f"{rl[0]}_{rl[1]}bp" if isinstance(rl, tuple) else f"{rl}bp",
