@@ -927,52 +927,68 @@ __global__ void __launch_bounds__(kBlock)
   uint32_t r = 0, left = 0;
   uint32_t i = 0, j = 0;
   RowItem it{0, 0, 0, 0};
+  // Software pipeline: the next row item of the lane's claim is loaded while the
+  // current walk runs, and a finished walk's sampled-SA value is loaded then
+  // written out at the lane's next refill, so a refill waits on no load.
+  RowItem nx{0, 0, 0, 0};
+  RowItem pit{0, 0, 0, 0};  // the finished walk whose output is pending
+  uint32_t ps = 0, pj = 0;  // its sample and steps
+  bool pending = false;
   bool active = false;
   uint32_t sectors = 0;
+  auto finish = [&]() {  // the pending walk's key and chromosome
+    const uint32_t sa = (ps + pj) % X.walk_mod;
+    const uint32_t phys = pit.phys_len >> 31;
+    const uint64_t len_calc = pit.phys_len & kRowLenMask;
+    uint64_t key = sa;
+    if (phys && (pit.phys_len & kRowKey32))  // an int length: the SA_TYPE (32-bit) difference wraps
+      key = (uint32_t)((X.top + 1u) - sa - (uint32_t)len_calc - 1u);
+    else if (phys)
+      key = (uint64_t)((X.top + 1u) - sa) - len_calc - 1u;
+    const uint32_t id = kar_search(X, key);
+    hpg_loc_t o;
+    o.key = key;
+    o.hit = pit.hit;
+    o.pad = 0;
+    if (key + len_calc <= X.kar_offset[id]) {
+      o.valid = 1;
+      o.chrom = id - 1;
+      o.position = X.kar_start[id - 1] + (key - X.kar_offset[id - 1]);
+    } else {
+      o.valid = 0;
+      o.chrom = 0;
+      o.position = 0;
+    }
+    out[pit.out] = o;
+    pending = false;
+  };
   for (;;) {
     const bool done = !active || sampled_row(X, i);
     const unsigned grp = __activemask();
     const unsigned ready = __ballot_sync(grp, done);
     if (done) {
       if ((uint32_t)__popc(ready) < kLocateBatch && ready != grp) continue;  // wait for more lanes
-      if (active) {  // the walk reached a sampled row: the key and the chromosome
-        const uint32_t phys = it.phys_len >> 31;
-        const DevDir D = dir_of(X, phys);
-        const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
+      if (pending) finish();  // the previous walk of this lane: its sample has arrived by now
+      if (active) {  // the walk reached a sampled row: load the sample, write the row next time
+        const DevDir D = dir_of(X, it.phys_len >> 31);
+        ps = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
         ++sectors;
-        const uint32_t sa = (s + j) % X.walk_mod;
-        const uint64_t len_calc = it.phys_len & kRowLenMask;
-        uint64_t key = sa;
-        if (phys && (it.phys_len & kRowKey32))  // an int length: the SA_TYPE (32-bit) difference wraps
-          key = (uint32_t)((X.top + 1u) - sa - (uint32_t)len_calc - 1u);
-        else if (phys)
-          key = (uint64_t)((X.top + 1u) - sa) - len_calc - 1u;
-        const uint32_t id = kar_search(X, key);
-        hpg_loc_t o;
-        o.key = key;
-        o.hit = it.hit;
-        o.pad = 0;
-        if (key + len_calc <= X.kar_offset[id]) {
-          o.valid = 1;
-          o.chrom = id - 1;
-          o.position = X.kar_start[id - 1] + (key - X.kar_offset[id - 1]);
-        } else {
-          o.valid = 0;
-          o.chrom = 0;
-          o.position = 0;
-        }
-        out[it.out] = o;
+        pj = j;
+        pit = it;
+        pending = true;
         active = false;
       }
       if (left == 0) {
         r = claim(row_ctr, kRowsPerClaim);
         left = kRowsPerClaim;
+        if (r < n_locs) nx = items[r];
       } else {
         ++r;
       }
       --left;
       if (r >= n_locs) break;
-      it = items[r];
+      it = nx;
+      if (left > 0 && r + 1 < n_locs) nx = items[r + 1];  // the next row, loaded during this walk
       i = it.row;
       j = 0;
       active = true;
@@ -987,6 +1003,7 @@ __global__ void __launch_bounds__(kBlock)
       i = 0;
     }
   }
+  if (pending) finish();
   if (census) atomicAdd(census, (unsigned long long)sectors);
 }
 
