@@ -601,7 +601,7 @@ int engine_autotune(Engine* e, const uint8_t* d_seqs, const uint64_t* d_offs, si
   }
   // then the start-table length (rows marked by a first column of -100 - L)
   int best_kmer = (int)e->X.kmer_len;
-  for (int L : {0, 8, 10, 11}) {
+  for (int L : {0, 8, 10, 11, 12}) {
     if (engine_set_kmer(e, L, err) != 0) return -1;
     float t = 0;
     for (int rep = 0; rep < 2; ++rep) {

@@ -246,20 +246,23 @@ int bwt_gpu_idle_batch(bwt_index_t *index);
  * cover millions of rows each.  0, the default, locates every row. */
 void bwt_gpu_set_locate_limit(bwt_index_t *index, uint64_t max_rows);
 uint64_t bwt_gpu_locate_limit(bwt_index_t *index);
-/* Start table of the batched search (fused form): a chain of a read of at
- * least 2L+2 bases starts with one lookup of its first L symbols in a table of
- * 4^L intervals per index direction (8 MB each at L = 10) instead of L
- * dependent steps.  0 = no table (the default; the autotuner tries 8, 10, 11),
- * at most 12.  Results are identical. */
+/* Start table of the batched search (fused and warp-cooperative forms): a
+ * chain of a read of at least 2L+2 bases starts with one lookup of its first L
+ * symbols in a table of 4^L intervals per index direction (8 MB each at L = 10)
+ * instead of L dependent steps.  0 = no table (the default; the autotuner tries
+ * 8, 10, 11, 12), at most 12.  Results are identical. */
 int bwt_gpu_set_start_table(bwt_index_t *index, int symbols);
 int bwt_gpu_start_table(bwt_index_t *index);
 /* Autotuner: times the batched search on a device-resident read batch for
- * every candidate setting (60), keeps the fastest, then picks the fastest
+ * every candidate setting (60 fused, split and lockstep settings, then 12
+ * warp-cooperative ones: 8, 16 or 32 reads per warp group x register bound 8
+ * or 12 x direction split 0 or 2), keeps the fastest, then picks the fastest
  * block-load form for it (4 more runs), then the direction split (3 more, fused
- * form only), then the start-table length among 0, 8, 10, 11 (4 more), then
- * the idle-lane batch among 1, 4, 8, 16 (4 more).  Optional table gets rows of
- * {min_blocks (or -1 - load mode, -50 - split, -100 - table length, -200 -
- * idle batch), blocks_per_sm, stack, chains_per_claim, search us}. */
+ * form only), then the start-table length among 0, 8, 10, 11, 12 (5 more),
+ * then the idle-lane batch among 1, 4, 8, 16 (4 more).  Optional table gets
+ * rows of {min_blocks (or -1 - load mode, -50 - split, -100 - table length,
+ * -200 - idle batch), blocks_per_sm, stack (-2: warp-cooperative),
+ * chains_per_claim (reads per warp group), search us}. */
 int bwt_gpu_autotune(bwt_index_t *index, const uint8_t *d_seqs, const uint64_t *d_offsets, size_t n_reads,
                      uint64_t total_bases, uint32_t max_len, uint32_t max_results, int *table, int max_rows,
                      int *rows);
