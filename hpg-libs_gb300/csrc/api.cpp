@@ -304,6 +304,11 @@ int bwt_gpu_direction_split(bwt_index_t* index) {
   return e ? engine_dir_split(e) : -1;
 }
 
+double bwt_gpu_map_device_seconds(bwt_index_t* index) {
+  Engine* e = engine_of(index);
+  return e ? engine_map_device_seconds(e) : 0.0;
+}
+
 void bwt_gpu_set_wave_group(bwt_index_t* index, int reads) {
   Engine* e = engine_of(index);
   if (e) engine_set_wave_group(e, reads);

@@ -940,9 +940,8 @@ int host_result(Engine* e, const DeviceResult& r, size_t n_reads, hpg_result_set
 
 }  // namespace
 
-int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
-                       uint32_t max_results, hpg_result_set_t* out, std::string* err) {
-  std::memset(out, 0, sizeof(*out));
+int engine_search_host_keep(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
+                            uint32_t max_results, DeviceResult* r, std::string* err) {
   HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
   if (n_reads && offs[n_reads] < offs[0]) {
     *err = "read offsets must be non-decreasing";
@@ -967,30 +966,9 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
       for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
       o = rel.data();
     }
-    // Pipelined on request only: on GB300 the copies slow the latency-bound
-    // search by about as long as they take, so overlapping them gains nothing.
-    const size_t pchunk = e->pipe_chunk;
-    if (pchunk && pchunk != SIZE_MAX && n_reads >= 2 * pchunk && !e->census_on) {
-      if (run_graph_pipelined(e, seqs, offs, n_reads, total, max_results, out, err) != 0) {
-        bwt_gpu_result_free(out);
-        return -1;
-      }
-      uint32_t derr = 0;
-      HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
-      if (derr) {
-        cudaMemset(e->d_err, 0, 4);
-        bwt_gpu_result_free(out);
-        *err = "corrupt index: suffix-array walk did not reach a sampled row";
-        return -1;
-      }
-      return 0;
-    }
     static const uint64_t zero = 0;
-    DeviceResult r;
-    if (finish_graph(e, seqs + (n_reads ? offs[0] : 0), n_reads ? o : &zero, (uint32_t)n_reads, total, max_results,
-                     &r, err) != 0)
-      return -1;
-    return host_result(e, r, n_reads, out, err);
+    return finish_graph(e, seqs + (n_reads ? offs[0] : 0), n_reads ? o : &zero, (uint32_t)n_reads, total,
+                        max_results, r, err);
   }
   uint32_t max_len = 0;
   for (size_t i = 0; i < n_reads; ++i) {
@@ -1013,10 +991,41 @@ int engine_search_host(Engine* e, int mode, int form, const char* seqs, const ui
   for (size_t i = 0; i <= n_reads; ++i) rel[i] = offs[i] - offs[0];
   if (total) HPG_CUDA(cudaMemcpyAsync(e->seqs.p, seqs + offs[0], total, cudaMemcpyHostToDevice, s), "upload reads");
   HPG_CUDA(cudaMemcpyAsync(e->offs.p, rel.data(), (n_reads + 1) * 8, cudaMemcpyHostToDevice, s), "upload offsets");
-  DeviceResult r;
-  if (engine_search_device(e, mode, form, ptr<uint8_t>(e->seqs), ptr<uint64_t>(e->offs), n_reads, total, max_len,
-                           max_results, &r, err) != 0)
+  return engine_search_device(e, mode, form, ptr<uint8_t>(e->seqs), ptr<uint64_t>(e->offs), n_reads, total, max_len,
+                              max_results, r, err);
+}
+
+int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
+                       uint32_t max_results, hpg_result_set_t* out, std::string* err) {
+  std::memset(out, 0, sizeof(*out));
+  HPG_CUDA(cudaSetDevice(e->device), "cudaSetDevice");
+  if (n_reads && offs[n_reads] < offs[0]) {
+    *err = "read offsets must be non-decreasing";
     return -1;
+  }
+  // Pipelined on request only: on GB300 the copies slow the latency-bound
+  // search by about as long as they take, so overlapping them gains nothing.
+  const size_t pchunk = e->pipe_chunk;
+  if (form == kFormBatched && mode == HPG_BWT_MODE_SEARCH1 && e->use_graph && pchunk && pchunk != SIZE_MAX &&
+      n_reads >= 2 * pchunk && !e->census_on && n_reads < (1ull << 31) &&
+      (n_reads ? offs[n_reads] - offs[0] : 0) <= (1ull << 40)) {
+    const uint64_t total = n_reads ? offs[n_reads] - offs[0] : 0;
+    if (run_graph_pipelined(e, seqs, offs, n_reads, total, max_results, out, err) != 0) {
+      bwt_gpu_result_free(out);
+      return -1;
+    }
+    uint32_t derr = 0;
+    HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
+    if (derr) {
+      cudaMemset(e->d_err, 0, 4);
+      bwt_gpu_result_free(out);
+      *err = "corrupt index: suffix-array walk did not reach a sampled row";
+      return -1;
+    }
+    return 0;
+  }
+  DeviceResult r;
+  if (engine_search_host_keep(e, mode, form, seqs, offs, n_reads, max_results, &r, err) != 0) return -1;
   return host_result(e, r, n_reads, out, err);
 }
 

@@ -46,6 +46,10 @@ int engine_search_device(Engine* e, int mode, int form, const uint8_t* d_seqs, c
                          uint64_t total_bases, uint32_t max_len, uint32_t max_results, DeviceResult* out,
                          std::string* err);
 
+// Host reads in, results left on the device as engine_search_device leaves them.
+int engine_search_host_keep(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
+                            uint32_t max_results, DeviceResult* out, std::string* err);
+
 // Host reads in, host records out (malloc'ed; free with hpg_result_free).
 int engine_search_host(Engine* e, int mode, int form, const char* seqs, const uint64_t* offs, size_t n_reads,
                        uint32_t max_results, hpg_result_set_t* out, std::string* err);
@@ -114,6 +118,29 @@ struct MapRow {
 int engine_seed_search(Engine* e, const char* seqs, const uint64_t* offs, size_t n, const uint32_t* seeds, size_t m,
                        uint32_t* out, std::string* err);
 int engine_locate_rows(Engine* e, const MapRow* rows, size_t m, hpg_loc_t* out, std::string* err);
+
+// bwt_map_inexact_read's alignments for a batch of reads (5+ bases each),
+// decided on the device: BWSearch1 with lists of capacity filter_read_mappings,
+// the row filter over both strands, the located rows, the 10 bp merge and the
+// list order (bwt.c:1978-2237).  Read i's records are rec[rec_off[i] ..
+// rec_off[i] + n_rec[i]): {chromosome | strand << 31, position}; flags[i] bit 0:
+// flag 2 (a strand passed the filter), bit 1: the list's first alignment loses
+// its secondary mark (bwt.c:2234-2237), bit 2: more rows than a 32-bit count.
+struct MapRec {
+  uint32_t chrom_strand;  // chromosome | strand << 31
+  int32_t position;
+};
+struct InexactRecords {
+  std::vector<uint32_t> n_rec;
+  std::vector<uint8_t> flags;
+  std::vector<uint64_t> rec_off;
+  std::vector<MapRec> rec;
+};
+int engine_inexact_records(Engine* e, const char* seqs, const uint64_t* offs, size_t n, int filter_read_mappings,
+                           InexactRecords* out, std::string* err);
+// Wall time of the last alignment-list call's device pass (search to records), seconds.
+void engine_note_map_device_seconds(Engine* e, double s);
+double engine_map_device_seconds(Engine* e);
 
 // The k-error block search of bwt_map_inexact_read_2 (block_search.cu): per
 // (read, strand) t = 2 * read + strand, count[t] results (hits of item t are

@@ -9,6 +9,7 @@
 // (bwt.c:1822-1869) take one more scan and locate pass for the reads that end
 // without alignments in a list flagged 1.
 #include <algorithm>
+#include <chrono>
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
@@ -47,6 +48,10 @@ char* dup_bytes(const char* s, size_t n) {
 }
 
 char* dup_str(const char* s) { return dup_bytes(s, std::strlen(s)); }
+
+double wall_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 char* fmt(const char* f, unsigned long v) {
   char buf[48];
@@ -232,22 +237,17 @@ void optional_fields(alignment_t* a, size_t n_mappings, int read_length) {
   a->optional_fields_length = 21;
 }
 
-// Per read after the search: what the reference locates, strand by strand.
-struct InexactPlan {
-  int exceeded_type = -1;          // strand (type) whose rows passed the filter, or -1
-  bool has_minus_results = false;  // the '-' helper returned results (bwt.c:2003-2006)
-  size_t row0[2] = {0, 0};         // first located row of each type's exact hits
-  std::vector<uint32_t> hits[2];   // included exact hits (indices into the hit array) per type
-};
-
 struct InexactOutcome {
   size_t added = 0;       // alignments this call put in the list
   bool anchors = false;   // list ended empty with flag 1
 };
 
-// Alignments of one read into its list (bwt.c:1896-2289, without the anchors).
-InexactOutcome assemble_inexact(const InexactRead& rd, const InexactPlan& P, const hpg_hit_t* hits,
-                                const hpg_loc_t* loc, OutList& L) {
+// Alignments of one read into its list (bwt.c:1896-2289, without the
+// anchors), from the records the device decided: which rows, in which order,
+// with which flags (engine_inexact_records).  Only the records' allocation and
+// their strings are made here.
+InexactOutcome assemble_inexact(const InexactRead& rd, uint32_t n_rec, const MapRec* rec, uint8_t flags,
+                                OutList& L) {
   InexactOutcome res;
   const size_t len = rd.len;
   if (len < 5) {  // bwt.c:1900-1917
@@ -257,68 +257,28 @@ InexactOutcome assemble_inexact(const InexactRead& rd, const InexactPlan& P, con
     return res;
   }
   std::string rc_store;
-  const char* strand_seq = rd.seq;
-  size_t num = 0;
-  for (int type = 1; type >= 0; --type) {
-    if (type == 0 && P.has_minus_results) {
-      if (rd.revcomp) {
-        strand_seq = rd.revcomp;
-      } else {
-        rc_store.assign(rd.seq, len);
-        seq_reverse_complementary(&rc_store[0], (unsigned)len);
-        strand_seq = rc_store.data();
-      }
+  const char* minus_seq = rd.revcomp;
+  for (uint32_t r = 0; r < n_rec; ++r) {
+    const int strand = (int)(rec[r].chrom_strand >> 31);
+    if (strand && !minus_seq) {  // the '-' strand's sequence (bwt.c:2003-2006)
+      rc_store.assign(rd.seq, len);
+      seq_reverse_complementary(&rc_store[0], (unsigned)len);
+      minus_seq = rc_store.data();
     }
-    if (P.exceeded_type == type) {  // bwt.c:2180-2184
-      L.set_flag(2);
-      break;
-    }
-    std::vector<alignment_t*> tmp;
-    size_t at = P.row0[type];
-    for (uint32_t h : P.hits[type]) {
-      const hpg_hit_t& x = hits[h];
-      for (int64_t j = x.k; j <= x.l; ++j, ++at) {
-        const hpg_loc_t& q = loc[at];
-        if (!q.valid) continue;
-        tmp.push_back(new_alignment(dup_str(rd.id), dup_bytes(strand_seq, len), fmt("%lu", 0), !type, q.chrom,
-                                    (int)q.position, fmt("%luM", (unsigned long)len), 1, 0, 1, num > 0));
-      }
-    }
-    // alignments closer than 10 bp on one chromosome (bwt.c:2190-2221)
-    const int nm = (int)tmp.size();
-    std::vector<uint8_t> del(nm, 0);
-    for (int a1 = nm - 1; a1 >= 1; --a1) {
-      if (del[a1]) continue;
-      for (int a2 = a1 - 1; a2 >= 0; --a2) {
-        const size_t dist = (size_t)std::abs(tmp[a1]->position - tmp[a2]->position);
-        if (tmp[a1]->chromosome == tmp[a2]->chromosome && dist < 10 && !del[a2]) {
-          if (tmp[a1]->num_cigar_operations < tmp[a2]->num_cigar_operations) del[a2] = 1;
-          else del[a1] = 1;
-        }
-      }
-    }
-    bool primary_delete = false;
-    for (int m = nm - 1; m >= 0; --m) {  // taken from the back, appended (bwt.c:2223-2235)
-      alignment_t* a = tmp[m];
-      if (del[m]) {
-        if (!a->secondary_alignment) primary_delete = true;
-        alignment_free(a);
-      } else {
-        L.insert(a);
-        a->secondary_alignment = num > 0;
-        ++num;
-      }
-    }
-    if (primary_delete) static_cast<alignment_t*>(L.get(0))->secondary_alignment = 0;
+    L.insert(new_alignment(dup_str(rd.id), dup_bytes(strand ? minus_seq : rd.seq, len), nullptr, strand,
+                           rec[r].chrom_strand & 0x7FFFFFFFu, rec[r].position, fmt("%luM", (unsigned long)len), 1, 0,
+                           1, r > 0));
   }
-  res.added = num;
+  if (flags & 1) L.set_flag(2);  // bwt.c:2180-2184
+  if (flags & 2) static_cast<alignment_t*>(L.get(0))->secondary_alignment = 0;  // bwt.c:2234-2237
+  res.added = n_rec;
   if (L.size() == 0) {
     res.anchors = L.flag() == 1;
   } else {
     for (size_t i = 0; i < L.size(); ++i) {
       alignment_t* a = static_cast<alignment_t*>(L.get(i));
       quality_copy(a, rd.quality);
-      optional_fields(a, num, (int)len);
+      optional_fields(a, n_rec, (int)len);
     }
     L.set_flag(0);
   }
@@ -330,59 +290,26 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
                                         std::vector<OutList*>& lists) {
   const size_t n = rds.size();
   std::string err;
-  const int fr = opt->filter_read_mappings;
-  const size_t filter = (size_t)(long)fr;
-  // 1. BWSearch1 hits (result lists of capacity filter_read_mappings) for reads of 5+ bases
-  Reads R;
+  // 1. reads of 5+ bases, concatenated for the device
   std::vector<uint32_t> gidx(n, UINT32_MAX);
+  std::vector<uint64_t> offs(1, 0);
+  offs.reserve(n + 1);
   for (size_t i = 0; i < n; ++i)
     if (rds[i].len >= 5) {
-      gidx[i] = (uint32_t)R.n();
-      R.add(rds[i].seq, rds[i].len);
+      gidx[i] = (uint32_t)(offs.size() - 1);
+      offs.push_back(offs.back() + rds[i].len);
     }
-  hpg_result_set_t rs;
-  std::memset(&rs, 0, sizeof rs);
-  if (R.n()) {
-    engine_set_skip_locate(e, 1);
-    const int rc = engine_search_host(e, HPG_BWT_MODE_SEARCH1, kFormBatched, R.seq.data(), R.offs.data(), R.n(),
-                                      fr > 0 ? (uint32_t)fr : 0u, &rs, &err);
-    engine_set_skip_locate(e, 0);
-    if (rc != 0) fatal(err);
-  }
-  std::vector<uint64_t> hit0(2 * R.n() + 1, 0);
-  for (size_t t = 0; t < 2 * R.n(); ++t) hit0[t + 1] = hit0[t] + rs.rs_count[t];
-  // 2. rows the reference locates: exact hits until a strand passes the filter
-  std::vector<InexactPlan> plan(n);
-  std::vector<MapRow> rows;
-  for (size_t i = 0; i < n; ++i) {
-    if (gidx[i] == UINT32_MAX) continue;
-    InexactPlan& P = plan[i];
-    const size_t g = gidx[i];
-    P.has_minus_results = rs.rs_count[2 * g + 1] > 0;
-    size_t tot = 0;  // rows counted over both strands (bwt.c:1978, 2148-2149)
-    for (int type = 1; type >= 0 && P.exceeded_type < 0; --type) {
-      const size_t t = 2 * g + (type ? 0 : 1);
-      P.row0[type] = rows.size();
-      const size_t mark = rows.size();
-      for (uint64_t h = hit0[t]; h < hit0[t + 1]; ++h) {
-        const hpg_hit_t& x = rs.hits[h];
-        if (x.nm) continue;
-        tot += (size_t)(x.l - x.k);
-        if (tot > filter) {
-          P.exceeded_type = type;
-          P.hits[type].clear();
-          rows.resize(mark);  // that strand's alignments are dropped
-          break;
-        }
-        P.hits[type].push_back((uint32_t)h);
-        const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)(type ? 0 : 1);  // direction = type ? dir : !dir
-        for (int64_t j = x.k; j <= x.l; ++j) rows.push_back(MapRow{(uint32_t)j, phys, (uint32_t)rds[i].len});
-      }
-    }
-  }
-  std::vector<hpg_loc_t> loc(rows.size() + 1);
-  if (engine_locate_rows(e, rows.data(), rows.size(), loc.data(), &err) != 0) fatal(err);
-  // 3. alignment records, read by read in order
+  const size_t m = offs.size() - 1;
+  std::string seq(offs.back(), '\0');
+#pragma omp parallel for schedule(static) if (n > 4096)
+  for (size_t i = 0; i < n; ++i)
+    if (gidx[i] != UINT32_MAX) std::memcpy(&seq[offs[gidx[i]]], rds[i].seq, rds[i].len);
+  // 2. the search, the rows, the merge and the order, on the device
+  InexactRecords R;
+  const double t0 = wall_seconds();
+  if (engine_inexact_records(e, seq.data(), offs.data(), m, opt->filter_read_mappings, &R, &err) != 0) fatal(err);
+  engine_note_map_device_seconds(e, wall_seconds() - t0);
+  // 3. alignment records, read by read
   std::vector<InexactOutcome> out(n);
   // reads in parallel when each read's records go to a list of its own (a
   // caller's list named for two reads would take unlocked inserts from two threads)
@@ -395,8 +322,17 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
     own_lists = std::adjacent_find(seen.begin(), seen.end()) == seen.end();
   }
 #pragma omp parallel for schedule(dynamic, 256) if (own_lists && n > 256)
-  for (size_t i = 0; i < n; ++i) out[i] = assemble_inexact(rds[i], plan[i], rs.hits, loc.data(), *lists[i]);
-  bwt_gpu_result_free(&rs);
+  for (size_t i = 0; i < n; ++i) {
+    const uint32_t g = gidx[i];
+    if (g == UINT32_MAX) {
+      out[i] = assemble_inexact(rds[i], 0, nullptr, 0, *lists[i]);
+      continue;
+    }
+    if (R.flags[g] & 4) fatal("too many rows to locate for one read");
+    out[i] = assemble_inexact(rds[i], R.n_rec[g], R.rec.data() + R.rec_off[g], R.flags[g], *lists[i]);
+  }
+  std::vector<MapRow> rows;
+  std::vector<hpg_loc_t> loc;
   // 4. anchors for reads left without alignments in a list flagged 1 (bwt.c:2243-2273)
   std::vector<uint32_t> need;
   Reads A;
@@ -866,6 +802,9 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
   std::vector<OutList*> lists(n);
   for (size_t i = 0; i < n; ++i) lists[i] = &L[i];
   map_inexact(e, rds, opt, lists);
+  // the records into the caller's list, in read order; the unmapped reads'
+  // slots in the unmapped batch (indices first, then the copies in parallel)
+  std::vector<int64_t> slot(n, -1);
   size_t u = 0;
   unmapped_batch->header_indices[0] = 0;
   unmapped_batch->data_indices[0] = 0;
@@ -878,14 +817,22 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
     if (mapped) continue;
     const size_t hlen = (size_t)(batch->header_indices[i + 1] - batch->header_indices[i]);
     const size_t qlen = (size_t)(batch->data_indices[i + 1] - batch->data_indices[i]);
+    slot[i] = (int64_t)u;
     ++u;
-    std::memcpy(unmapped_batch->header + unmapped_batch->header_indices[u - 1], batch->header + batch->header_indices[i],
-                hlen);
-    std::memcpy(unmapped_batch->seq + unmapped_batch->data_indices[u - 1], batch->seq + batch->data_indices[i], qlen);
-    std::memcpy(unmapped_batch->quality + unmapped_batch->data_indices[u - 1], batch->quality + batch->data_indices[i],
-                qlen);
     unmapped_batch->data_indices[u] = unmapped_batch->data_indices[u - 1] + (int)qlen;
     unmapped_batch->header_indices[u] = unmapped_batch->header_indices[u - 1] + (int)hlen;
+  }
+#pragma omp parallel for schedule(static) if (n > 4096)
+  for (size_t i = 0; i < n; ++i) {
+    if (slot[i] < 0) continue;
+    const size_t v = (size_t)slot[i];
+    const size_t hlen = (size_t)(batch->header_indices[i + 1] - batch->header_indices[i]);
+    const size_t qlen = (size_t)(batch->data_indices[i + 1] - batch->data_indices[i]);
+    std::memcpy(unmapped_batch->header + unmapped_batch->header_indices[v], batch->header + batch->header_indices[i],
+                hlen);
+    std::memcpy(unmapped_batch->seq + unmapped_batch->data_indices[v], batch->seq + batch->data_indices[i], qlen);
+    std::memcpy(unmapped_batch->quality + unmapped_batch->data_indices[v], batch->quality + batch->data_indices[i],
+                qlen);
   }
   unmapped_batch->num_reads = u;
   return array_list_size(mapping_list);

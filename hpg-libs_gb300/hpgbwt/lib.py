@@ -150,6 +150,8 @@ def load() -> ctypes.CDLL:
     lib.bwt_gpu_set_start_table.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_set_direction_split.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_direction_split.argtypes = [vp]
+    lib.bwt_gpu_map_device_seconds.restype = ctypes.c_double
+    lib.bwt_gpu_map_device_seconds.argtypes = [vp]
     lib.bwt_gpu_set_wave_group.argtypes = [vp, ctypes.c_int]
     lib.bwt_gpu_wave_group.argtypes = [vp]
     lib.bwt_gpu_set_idle_batch.argtypes = [vp, ctypes.c_int]
@@ -407,6 +409,42 @@ class GpuIndex:
             t0 = time.perf_counter()
             self.lib.bwt_map_inexact_batch(ctypes.byref(b), opt, self.handle, ctypes.byref(u), lst)
             self.last_map_seconds = time.perf_counter() - t0
+            self.last_map_device_seconds = float(self.lib.bwt_gpu_map_device_seconds(self.handle))
+            count = int(self.lib.array_list_size(lst))
+        finally:
+            self.lib.array_list_free(lst, ctypes.cast(self.lib.alignment_free, ctypes.c_void_p))
+            self.lib.bwt_optarg_free(opt)
+        return count
+
+    def map_inexact_batch_arrays(self, seq: np.ndarray, offsets: np.ndarray, filter_read_mappings: int = 200) -> int:
+        """map_inexact_batch over reads given as concatenated bases and n+1 offsets
+        (fastq_batch buffers built with numpy: large batches)."""
+        n = len(offsets) - 1
+
+        class FastqBatch(ctypes.Structure):  # c/src/bioformats/fastq/fastq_batch.h:24-34
+            _fields_ = [("num_reads", ctypes.c_ulong), ("data_indices_size", ctypes.c_ulong),
+                        ("data_size", ctypes.c_ulong), ("source_id", ctypes.c_int),
+                        ("header_indices", ctypes.c_void_p), ("header", ctypes.c_void_p),
+                        ("data_indices", ctypes.c_void_p), ("seq", ctypes.c_void_p), ("quality", ctypes.c_void_p)]
+        offs = np.asarray(offsets, dtype=np.int64)
+        data = np.insert(np.asarray(seq, dtype=np.uint8), offs[1:], 0)
+        qual = np.where(data == 0, 0, ord("I")).astype(np.uint8)
+        didx = (offs + np.arange(n + 1)).astype(np.int32)
+        ids = np.frombuffer(b"".join(b"@r%09d\0" % i for i in range(n)), dtype=np.uint8)
+        hidx = (np.arange(n + 1) * 12).astype(np.int32)
+        b = FastqBatch(num_reads=n, header_indices=hidx.ctypes.data, header=ids.ctypes.data,
+                       data_indices=didx.ctypes.data, seq=data.ctypes.data, quality=qual.ctypes.data)
+        uh, ud = np.zeros(n + 1, np.int32), np.zeros(n + 1, np.int32)
+        ub = [np.zeros(len(ids) + 1, np.uint8), np.zeros(len(data) + 1, np.uint8), np.zeros(len(data) + 1, np.uint8)]
+        u = FastqBatch(header_indices=uh.ctypes.data, header=ub[0].ctypes.data, data_indices=ud.ctypes.data,
+                       seq=ub[1].ctypes.data, quality=ub[2].ctypes.data)
+        opt = self.lib.bwt_optarg_new(1, 1, filter_read_mappings, filter_read_mappings)
+        lst = self.lib.array_list_new(max(16, n), 1.25, 2)
+        try:
+            t0 = time.perf_counter()
+            self.lib.bwt_map_inexact_batch(ctypes.byref(b), opt, self.handle, ctypes.byref(u), lst)
+            self.last_map_seconds = time.perf_counter() - t0
+            self.last_map_device_seconds = float(self.lib.bwt_gpu_map_device_seconds(self.handle))
             count = int(self.lib.array_list_size(lst))
         finally:
             self.lib.array_list_free(lst, ctypes.cast(self.lib.alignment_free, ctypes.c_void_p))

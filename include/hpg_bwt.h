@@ -229,6 +229,12 @@ int bwt_gpu_direction_split(bwt_index_t *index);
 void bwt_gpu_set_wave_group(bwt_index_t *index, int reads);
 /* Reads per warp group of the warp-cooperative form, 0 when another form is selected. */
 int bwt_gpu_wave_group(bwt_index_t *index);
+/* Wall time, in seconds, of the device pass of the last bwt_map_inexact_batch /
+ * bwt_map_inexact_array_list / bwt_map_inexact_read call on this index: the
+ * search, the row filter, the located rows, the 10 bp merge and the list order
+ * (the rest of the call is the host's allocation of the records).  No
+ * counterpart in the reference. */
+double bwt_gpu_map_device_seconds(bwt_index_t *index);
 /* Idle-lane batch of the batched search (fused form): a lane that finished its
  * work item waits, masked, until this many lanes of its warp have (or all
  * active ones have), and they take their next items together, so the code that
