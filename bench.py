@@ -261,22 +261,27 @@ def measured_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str, kernel: str) -> tuple[float | None, str | None]:
+def profiled_traffic(workload: str, kernel: str, tuning: dict) -> tuple[float | None, str | None]:
     """DRAM bytes (read + write) of one search step of `kernel` on this exact
     workload, from the committed one-pass ncu capture of the full-size step
-    (profiles/<kernel>_<workload>_traffic.txt: a line "dram_bytes_per_step: B
-    <tuning>"), and where it came from; (None, None) where no capture of this
-    workload exists."""
+    (profiles/<kernel>_<workload>_traffic.txt: a line "dram_bytes_per_step: B"
+    and a line "tuning: k=v ..."), and where it came from; (None, reason) where
+    no capture of this workload at this tuning exists."""
     p = ROOT / "profiles" / f"{kernel}_{workload}_traffic.txt"
     if not p.exists():
         return None, None
+    val, want = None, {}
     for line in p.read_text().splitlines():
         if line.startswith("dram_bytes_per_step:"):
             try:
-                return float(line.split(":", 1)[1].split()[0]), f"ncu capture of this workload's full step, {p.name}"
+                val = float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None, None
-    return None, None
+        elif line.startswith("tuning:"):
+            want = dict(kv.split("=") for kv in line.split(":", 1)[1].split())
+    if any(str(tuning.get(k)) != v for k, v in want.items()):
+        return None, f"{p.name} was captured at {want}, not at this run's tuning"
+    return val, f"ncu capture of this workload's full step at this tuning, {p.name}"
 
 
 def compare_results(got, want) -> dict:
@@ -651,7 +656,11 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     if args.tuning:
         vals = [int(x) for x in args.tuning.split(",")]
         st, ch, mb, lm = vals[:4]
-        gi.set_tuning(0, st, ch, mb)
+        if st == -2:  # warp-cooperative form, `ch` reads per warp group
+            gi.set_tuning(0, 4, 1, mb)
+            gi.set_wave_group(ch)
+        else:
+            gi.set_tuning(0, st, ch, mb)
         gi.set_load_mode(lm)
         if len(vals) > 4:
             gi.set_start_table(vals[4])
@@ -729,14 +738,17 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
     peak, peak_kind = measured_peaks()
     algo_bytes = 32.0 * sectors + total + 16.0 * n_hits
     achieved = algo_bytes / (search_ms * 1e-3) / 1e9
-    traffic, traffic_src = profiled_traffic(args.workload, "batched_search_kernel")
+    kernel = "wave_search_kernel" if gi.wave_group() else "batched_search_kernel"
+    traffic, traffic_src = profiled_traffic(args.workload, kernel,
+                                            {"group": gi.wave_group(), "start_table": gi.start_table(),
+                                             "load_mode": gi.load_mode(), "direction_split": gi.direction_split()})
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
                 "basis": "algorithmic bytes (census index sectors of the reference's steps x 32 B + read bytes + "
                          "16 B per hit) over the search stage's CUDA-event time, against the measured HBM copy "
                          "bandwidth; the index is mostly served from L2, so this is not DRAM throughput "
                          "(dram_frac is)",
-                "kernel": "batched_search_kernel", "peak_kind": peak_kind,
+                "kernel": kernel, "peak_kind": peak_kind,
                 "algorithmic_bytes_per_read": round(algo_bytes / n, 1),
                 "traffic_source": traffic_src,
                 "dram_gbs": round(traffic / (search_ms * 1e-3) / 1e9, 1) if traffic else None,
@@ -855,7 +867,8 @@ def main():
                     help="reads of the batch taken through bwt_generate_cals_batch and bwt_map_inexact_batch "
                          "(0: skip)")
     ap.add_argument("--tuning", default="", help="fix the batched tuning: stack,chains_per_claim,register_bound,"
-                                                 "block_load_mode[,start_table[,direction_split[,idle_batch]]] (stack 0 = split, -1 = lockstep)")
+                                                 "block_load_mode[,start_table[,direction_split[,idle_batch]]] (stack 0 = split, -1 = lockstep, "
+                                                 "-2 = warp-cooperative with chains_per_claim reads per warp group)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     wl = WORKLOADS[args.workload]
