@@ -9,7 +9,9 @@
 // (bwt.c:1822-1869) take one more scan and locate pass for the reads that end
 // without alignments in a list flagged 1.
 #include <algorithm>
+#include <charconv>
 #include <chrono>
+#include <memory>
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
@@ -51,6 +53,29 @@ char* dup_str(const char* s) { return dup_bytes(s, std::strlen(s)); }
 
 double wall_seconds() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Time split of a call, printed to stderr when HPG_BWT_TIMING is set in the
+// environment (a diagnostic for tuning the host side; silent otherwise).
+struct Stopwatch {
+  const char* what;
+  bool on;
+  double t;
+  explicit Stopwatch(const char* w) : what(w), on(std::getenv("HPG_BWT_TIMING") != nullptr), t(wall_seconds()) {}
+  void mark(const char* step) {
+    if (!on) return;
+    const double now = wall_seconds();
+    std::fprintf(stderr, "[hpgbwt] %s: %s %.2f ms\n", what, step, (now - t) * 1e3);
+    t = now;
+  }
+};
+
+// "<len>M" (bwt.c:2125-2130) without printf.
+char* cigar_match(size_t len) {
+  char buf[24];
+  const auto r = std::to_chars(buf, buf + sizeof buf - 2, (unsigned long)len);
+  *r.ptr = 'M';
+  return dup_bytes(buf, (size_t)(r.ptr - buf) + 1);
 }
 
 char* fmt(const char* f, unsigned long v) {
@@ -266,7 +291,7 @@ InexactOutcome assemble_inexact(const InexactRead& rd, uint32_t n_rec, const Map
       minus_seq = rc_store.data();
     }
     L.insert(new_alignment(dup_str(rd.id), dup_bytes(strand ? minus_seq : rd.seq, len), nullptr, strand,
-                           rec[r].chrom_strand & 0x7FFFFFFFu, rec[r].position, fmt("%luM", (unsigned long)len), 1, 0,
+                           rec[r].chrom_strand & 0x7FFFFFFFu, rec[r].position, cigar_match(len), 1, 0,
                            1, r > 0));
   }
   if (flags & 1) L.set_flag(2);  // bwt.c:2180-2184
@@ -290,6 +315,7 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
                                         std::vector<OutList*>& lists) {
   const size_t n = rds.size();
   std::string err;
+  Stopwatch sw("map_inexact");
   // 1. reads of 5+ bases, concatenated for the device
   std::vector<uint32_t> gidx(n, UINT32_MAX);
   std::vector<uint64_t> offs(1, 0);
@@ -300,15 +326,17 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
       offs.push_back(offs.back() + rds[i].len);
     }
   const size_t m = offs.size() - 1;
-  std::string seq(offs.back(), '\0');
+  std::unique_ptr<char[]> seq(new char[offs.back() + 1]);
 #pragma omp parallel for schedule(static) if (n > 4096)
   for (size_t i = 0; i < n; ++i)
-    if (gidx[i] != UINT32_MAX) std::memcpy(&seq[offs[gidx[i]]], rds[i].seq, rds[i].len);
+    if (gidx[i] != UINT32_MAX) std::memcpy(seq.get() + offs[gidx[i]], rds[i].seq, rds[i].len);
+  sw.mark("reads concatenated");
   // 2. the search, the rows, the merge and the order, on the device
   InexactRecords R;
   const double t0 = wall_seconds();
-  if (engine_inexact_records(e, seq.data(), offs.data(), m, opt->filter_read_mappings, &R, &err) != 0) fatal(err);
+  if (engine_inexact_records(e, seq.get(), offs.data(), m, opt->filter_read_mappings, &R, &err) != 0) fatal(err);
   engine_note_map_device_seconds(e, wall_seconds() - t0);
+  sw.mark("device pass");
   // 3. alignment records, read by read
   std::vector<InexactOutcome> out(n);
   // reads in parallel when each read's records go to a list of its own (a
@@ -331,6 +359,7 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
     if (R.flags[g] & 4) fatal("too many rows to locate for one read");
     out[i] = assemble_inexact(rds[i], R.n_rec[g], R.rec.data() + R.rec_off[g], R.flags[g], *lists[i]);
   }
+  sw.mark("records allocated");
   std::vector<MapRow> rows;
   std::vector<hpg_loc_t> loc;
   // 4. anchors for reads left without alignments in a list flagged 1 (bwt.c:2243-2273)
@@ -791,17 +820,20 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
   std::lock_guard<std::mutex> lk(g_mu);
   Engine* e = engine_for(index);
   const size_t n = batch->num_reads;
-  std::vector<std::string> rc(n);
+  Stopwatch sw("bwt_map_inexact_batch");
   std::vector<InexactRead> rds(n);
+#pragma omp parallel for schedule(static) if (n > 4096)
   for (size_t i = 0; i < n; ++i) {
     const char* s = batch->seq + batch->data_indices[i];
     rds[i] = InexactRead{batch->header + batch->header_indices[i], s, std::strlen(s), nullptr,
                          batch->quality + batch->data_indices[i]};
   }
+  sw.mark("reads");
   std::vector<OutList> L(n);
   std::vector<OutList*> lists(n);
   for (size_t i = 0; i < n; ++i) lists[i] = &L[i];
   map_inexact(e, rds, opt, lists);
+  sw.mark("map_inexact");
   // the records into the caller's list, in read order; the unmapped reads'
   // slots in the unmapped batch (indices first, then the copies in parallel)
   std::vector<int64_t> slot(n, -1);
@@ -835,6 +867,7 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
                 qlen);
   }
   unmapped_batch->num_reads = u;
+  sw.mark("list and unmapped batch");
   return array_list_size(mapping_list);
 }
 
