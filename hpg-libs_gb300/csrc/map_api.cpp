@@ -212,12 +212,16 @@ struct InexactRead {
 // (batch forms) whose items the caller collects.
 struct OutList {
   array_list_t* list = nullptr;
+  // a fresh list: first `cap` items in slots (a caller's flat array), any more in `fresh`
+  void** slots = nullptr;
+  uint32_t nslots = 0, cap = 0;
   std::vector<void*> fresh;
   int fresh_flag = 0;
-  size_t size() { return list ? array_list_size(list) : fresh.size(); }
-  void* get(size_t i) { return list ? array_list_get(i, list) : fresh[i]; }
+  size_t size() { return list ? array_list_size(list) : nslots + fresh.size(); }
+  void* get(size_t i) { return list ? array_list_get(i, list) : (i < nslots ? slots[i] : fresh[i - nslots]); }
   void insert(void* p) {
     if (list) array_list_insert(p, list);
+    else if (nslots < cap) slots[nslots++] = p;
     else fresh.push_back(p);
   }
   int flag() { return list ? array_list_get_flag(list) : fresh_flag; }
@@ -266,6 +270,10 @@ struct InexactOutcome {
   size_t added = 0;       // alignments this call put in the list
   bool anchors = false;   // list ended empty with flag 1
 };
+
+// The flat slot array of the last map_inexact call's fresh lists (the calls
+// hold the entry points' lock, so one array serves them).
+std::unique_ptr<void*[]> g_flat_slots;
 
 // Alignments of one read into its list (bwt.c:1896-2289, without the
 // anchors), from the records the device decided: which rows, in which order,
@@ -337,7 +345,17 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
   if (engine_inexact_records(e, seq.get(), offs.data(), m, opt->filter_read_mappings, &R, &err) != 0) fatal(err);
   engine_note_map_device_seconds(e, wall_seconds() - t0);
   sw.mark("device pass");
-  // 3. alignment records, read by read
+  // 3. alignment records, read by read (fresh lists get their slots in one
+  // flat array, sized from the records the device decided)
+  std::vector<uint64_t> slot0(n + 1, 0);
+  for (size_t i = 0; i < n; ++i)
+    slot0[i + 1] = slot0[i] + (lists[i]->list ? 0 : (gidx[i] == UINT32_MAX ? 1 : R.n_rec[gidx[i]]));
+  std::unique_ptr<void*[]> flat(new void*[slot0[n] + 1]);
+  for (size_t i = 0; i < n; ++i)
+    if (!lists[i]->list) {
+      lists[i]->slots = flat.get() + slot0[i];
+      lists[i]->cap = (uint32_t)(slot0[i + 1] - slot0[i]);
+    }
   std::vector<InexactOutcome> out(n);
   // reads in parallel when each read's records go to a list of its own (a
   // caller's list named for two reads would take unlocked inserts from two threads)
@@ -360,6 +378,7 @@ std::vector<InexactOutcome> map_inexact(Engine* e, const std::vector<InexactRead
     out[i] = assemble_inexact(rds[i], R.n_rec[g], R.rec.data() + R.rec_off[g], R.flags[g], *lists[i]);
   }
   sw.mark("records allocated");
+  g_flat_slots = std::move(flat);
   std::vector<MapRow> rows;
   std::vector<hpg_loc_t> loc;
   // 4. anchors for reads left without alignments in a list flagged 1 (bwt.c:2243-2273)
@@ -841,11 +860,11 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
   unmapped_batch->header_indices[0] = 0;
   unmapped_batch->data_indices[0] = 0;
   for (size_t i = 0; i < n; ++i) {
-    bool mapped = false;
-    for (void* p : L[i].fresh) {
-      array_list_insert(p, mapping_list);
-      mapped = mapped || static_cast<alignment_t*>(p)->is_seq_mapped;
-    }
+    OutList& li = L[i];
+    for (uint32_t j = 0; j < li.nslots; ++j) array_list_insert(li.slots[j], mapping_list);
+    for (void* p : li.fresh) array_list_insert(p, mapping_list);
+    // reads of 5+ bases get mapped records only; shorter ones one unmapped record
+    const bool mapped = rds[i].len >= 5 && li.nslots + li.fresh.size() > 0;
     if (mapped) continue;
     const size_t hlen = (size_t)(batch->header_indices[i + 1] - batch->header_indices[i]);
     const size_t qlen = (size_t)(batch->data_indices[i + 1] - batch->data_indices[i]);
@@ -867,6 +886,7 @@ size_t bwt_map_inexact_batch(fastq_batch_t* batch, bwt_optarg_t* opt, bwt_index_
                 qlen);
   }
   unmapped_batch->num_reads = u;
+  g_flat_slots.reset();
   sw.mark("list and unmapped batch");
   return array_list_size(mapping_list);
 }
