@@ -8,10 +8,11 @@
 // rates of earlier batches), stages them side by side in the capacity plan's
 // device buffers (one copy per request straight from the client's memory), and
 // replays the captured pipeline once for all of them: the requests' reads share
-// the persistent search and locate kernels.  While a batch runs the worker
-// already forms the next one from whatever arrived meanwhile, so a request
-// waits at most for the batch in flight.  Results are rebased to each
-// request's own read and hit numbering on the device and copied to pinned host
+// the persistent search and locate kernels.  Two batches are in flight, in the
+// two plans of their capacity class: while one replays on the index's stream,
+// the next one's reads go in on a copy stream and the previous one's results,
+// rebased to each request's own read and hit numbering on the device, come out
+// on another, so the replays run back to back.  Results land in pinned host
 // buffers, which clients read in place until they release the request.
 #include <cuda_runtime.h>
 
@@ -148,8 +149,11 @@ struct Server {
   int next_set = 0;
   uint64_t* h_offs[2] = {nullptr, nullptr};
   uint32_t* h_seg[2] = {nullptr, nullptr};
-  uint32_t* d_seg = nullptr;
-  uint64_t* d_bounds = nullptr;
+  uint32_t* d_seg[2] = {nullptr, nullptr};
+  uint64_t* d_bounds[2] = {nullptr, nullptr};
+  uint32_t* h_err = nullptr;  // pinned copy of the index's error word, per slot
+  // per pipeline slot: inputs sent, replay done, results out
+  cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_run[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
 
   // admission estimates, updated from finished batches
   double hits_per_read = 4.0, rows_per_read = 16.0;
@@ -206,21 +210,37 @@ struct Server {
     sg[b->reqs.size()] = r;
   }
 
-  int launch(Batch* b, std::string* err) {
-    cudaStream_t s = e->stream;
-    b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err);
+  // Send a batch's reads, offsets and segment table on the input stream and
+  // queue its replay behind them, in the batch's pipeline slot.
+  int issue(Batch* b, std::string* err) {
+    cudaStream_t cs = e->stream, h2d = e->xs[0];
+    const int k = b->slot;
+    b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err, k);
     if (!b->g) return -1;
+    HPG_CUDA(cudaEventSynchronize(ev_in[k]), "serving staging");  // the slot's previous tables were sent
+    prepare(b);
+    // inputs once the slot's previous replay has read its own, the table once its rebase is done
+    HPG_CUDA(cudaStreamWaitEvent(h2d, ev_run[k], 0), "serving order");
+    HPG_CUDA(cudaStreamWaitEvent(h2d, ev_out[k], 0), "serving order");
     uint64_t at = 0;
     for (const ServeReq* q : b->reqs) {
       if (q->bases)
-        HPG_CUDA(cudaMemcpyAsync(b->g->seqs + at, q->seqs + q->offs[0], q->bases, cudaMemcpyDefault, s),
+        HPG_CUDA(cudaMemcpyAsync(b->g->seqs + at, q->seqs + q->offs[0], q->bases, cudaMemcpyDefault, h2d),
                  "stage reads");
       at += q->bases;
     }
-    HPG_CUDA(cudaMemcpyAsync(b->g->offs, h_offs[b->slot], ((size_t)b->n + 1) * 8, cudaMemcpyHostToDevice, s),
+    HPG_CUDA(cudaMemcpyAsync(b->g->offs, h_offs[k], ((size_t)b->n + 1) * 8, cudaMemcpyHostToDevice, h2d),
              "stage offsets");
+    HPG_CUDA(cudaMemcpyAsync(d_seg[k], h_seg[k], (b->reqs.size() + 1) * 4, cudaMemcpyHostToDevice, h2d),
+             "segments");
+    HPG_CUDA(cudaEventRecord(ev_in[k], h2d), "serving order");
+    // the replay once its inputs are in and the slot's previous results are out
+    HPG_CUDA(cudaStreamWaitEvent(cs, ev_in[k], 0), "serving order");
+    HPG_CUDA(cudaStreamWaitEvent(cs, ev_out[k], 0), "serving order");
     b->t_launch = now_ms();
-    return graph_launch(e, b->g, b->n, max_results, err);
+    if (graph_launch(e, b->g, b->n, max_results, err) != 0) return -1;
+    HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
+    return 0;
   }
 
   ResultBuf* take_set(size_t hits, size_t locs, size_t rs, size_t segs, std::string* err) {
@@ -264,69 +284,78 @@ struct Server {
     cv_done.notify_all();
   }
 
-  // Wait for a launched batch, rebase and copy its results, publish them.
-  int finish(Batch* b, Batch* next, bool have_next, bool* next_launched, std::string* err) {
-    cudaStream_t s = e->stream;
-    DeviceResult r;
-    GraphPlan grow;
-    int rc = graph_collect(e, b->g, b->n, &grow, &r, err);
-    if (rc == 1) {  // a pool overflowed: grow it and run the batch again (staged inputs carried over)
-      ++regrows;
-      if (run_batched_graph(e, b->g->seqs, b->g->offs, b->n, b->bases, max_results, &r, err) != 0) return -1;
-      b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err);
-      if (!b->g) return -1;
-    } else if (rc < 0) {
+  // Wait for a batch's replay, rebase and copy its results out on the output
+  // stream (the other slot's batch keeps the GPU busy meanwhile), publish them.
+  int collect(Batch* b, std::string* err) {
+    cudaStream_t cs = e->stream, h2d = e->xs[0], d2h = e->xs[1];
+    const int k = b->slot;
+    HPG_CUDA(cudaEventSynchronize(ev_run[k]), "batched pipeline");
+    GraphPlan* g = b->g;
+    const uint64_t* h = g->h_summary;
+    const uint32_t status = (uint32_t)h[0];
+    if (status & kStatusBadInput) {
+      *err = "read offsets must be non-decreasing and reads at most 32767 bases";
       return -1;
     }
+    if (status & kStatusWaveAcct) {
+      *err = "internal error: inconsistent work counts in the warp-cooperative search";
+      return -1;
+    }
+    if (status) {  // a pool overflowed: drain the pipeline, grow the pool and run the batch again
+      ++regrows;
+      HPG_CUDA(cudaStreamSynchronize(h2d), "serving drain");
+      HPG_CUDA(cudaStreamSynchronize(d2h), "serving drain");
+      HPG_CUDA(cudaStreamSynchronize(cs), "serving drain");
+      DeviceResult r;
+      if (run_batched_graph(e, g->seqs, g->offs, b->n, b->bases, max_results, &r, err) != 0) return -1;
+      g = b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err, k);
+      if (!g) return -1;
+      h = g->h_summary;
+      HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
+    }
     gpu_ms += now_ms() - b->t_launch;
-    uint32_t derr = 0;
-    HPG_CUDA(cudaMemcpy(&derr, e->d_err, 4, cudaMemcpyDeviceToHost), "error word");
-    if (derr) {
-      cudaMemset(e->d_err, 0, 4);
+    const uint64_t nh = h[2], nl = g->skip_locate ? 0 : h[3];
+    const size_t nseg = b->reqs.size();
+    ResultBuf* rb = take_set(nh, nl, 2ull * b->n, nseg, err);
+    if (!rb) return -1;
+    HPG_CUDA(cudaStreamWaitEvent(d2h, ev_run[k], 0), "serving order");
+    const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(nh, nl), nseg + 1);
+    const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
+    count_launches(1);
+    serve_rebase_kernel<<<grid, 256, 0, d2h>>>(g->hits, nh, g->locs, nl, g->hit_off, g->loc_off, d_seg[k],
+                                               (uint32_t)nseg, d_bounds[k]);
+    if (nh)
+      HPG_CUDA(cudaMemcpyAsync(rb->hits, g->hits, nh * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, d2h), "copy hits");
+    if (nl)
+      HPG_CUDA(cudaMemcpyAsync(rb->locs, g->locs, nl * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, d2h), "copy rows");
+    if (b->n) {
+      HPG_CUDA(cudaMemcpyAsync(rb->cnt, g->kept, 2ull * b->n * 4, cudaMemcpyDeviceToHost, d2h), "copy counts");
+      HPG_CUDA(cudaMemcpyAsync(rb->trunc, g->trunc, 2ull * b->n, cudaMemcpyDeviceToHost, d2h), "copy flags");
+    }
+    HPG_CUDA(cudaMemcpyAsync(rb->bounds, d_bounds[k], (nseg + 1) * 16, cudaMemcpyDeviceToHost, d2h),
+             "copy bounds");
+    HPG_CUDA(cudaMemcpyAsync(h_err + k, e->d_err, 4, cudaMemcpyDeviceToHost, d2h), "error word");
+    HPG_CUDA(cudaEventRecord(rb->done, d2h), "result event");
+    HPG_CUDA(cudaEventRecord(ev_out[k], d2h), "serving order");
+    HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
+    HPG_CUDA(cudaGetLastError(), "rebase kernel");
+    if (h_err[k]) {
+      cudaMemsetAsync(e->d_err, 0, 4, d2h);
       *err = "corrupt index: suffix-array walk did not reach a sampled row";
       return -1;
     }
-    const size_t nseg = b->reqs.size();
-    ResultBuf* rb = take_set(r.n_hits, r.n_locs, 2ull * b->n, nseg, err);
-    if (!rb) return -1;
-    HPG_CUDA(cudaMemcpyAsync(d_seg, h_seg[b->slot], (nseg + 1) * 4, cudaMemcpyHostToDevice, s), "segments");
-    const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(r.n_hits, r.n_locs), nseg + 1);
-    const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
-    count_launches(1);
-    serve_rebase_kernel<<<grid, 256, 0, s>>>(b->g->hits, r.n_hits, b->g->locs, r.n_locs, b->g->hit_off,
-                                             b->g->loc_off, d_seg, (uint32_t)nseg, d_bounds);
-    if (r.n_hits)
-      HPG_CUDA(cudaMemcpyAsync(rb->hits, b->g->hits, r.n_hits * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, s),
-               "copy hits");
-    if (r.n_locs)
-      HPG_CUDA(cudaMemcpyAsync(rb->locs, b->g->locs, r.n_locs * sizeof(hpg_loc_t), cudaMemcpyDeviceToHost, s),
-               "copy rows");
-    if (b->n) {
-      HPG_CUDA(cudaMemcpyAsync(rb->cnt, r.rs_count, 2ull * b->n * 4, cudaMemcpyDeviceToHost, s), "copy counts");
-      HPG_CUDA(cudaMemcpyAsync(rb->trunc, r.rs_truncated, 2ull * b->n, cudaMemcpyDeviceToHost, s), "copy flags");
-    }
-    HPG_CUDA(cudaMemcpyAsync(rb->bounds, d_bounds, (nseg + 1) * 16, cudaMemcpyDeviceToHost, s), "copy bounds");
-    HPG_CUDA(cudaEventRecord(rb->done, s), "result event");
-    // the next batch goes to the GPU behind these copies
-    if (have_next) {
-      std::string e2;
-      if (launch(next, &e2) != 0) fail(next, e2);
-      else *next_launched = true;
-    }
-    HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
-    HPG_CUDA(cudaGetLastError(), "rebase kernel");
     const double t = now_ms();
     std::lock_guard<std::mutex> lk(mu);
-    for (size_t k = 0; k < nseg; ++k) {
-      ServeReq* q = b->reqs[k];
-      q->set = (int)(rb - sets);
-      q->read0 = h_seg[b->slot][k];
-      q->hit0 = rb->bounds[2 * k];
-      q->nh = rb->bounds[2 * k + 2] - q->hit0;
-      q->loc0 = rb->bounds[2 * k + 1];
-      q->nl = rb->bounds[2 * k + 3] - q->loc0;
-      q->state = 2;
-      q->t_done = t;
+    for (size_t q = 0; q < nseg; ++q) {
+      ServeReq* r = b->reqs[q];
+      r->set = (int)(rb - sets);
+      r->read0 = h_seg[k][q];
+      r->hit0 = rb->bounds[2 * q];
+      r->nh = rb->bounds[2 * q + 2] - r->hit0;
+      r->loc0 = rb->bounds[2 * q + 1];
+      r->nl = rb->bounds[2 * q + 3] - r->loc0;
+      r->state = 2;
+      r->t_done = t;
       rb->refs++;
     }
     ++batches;
@@ -335,7 +364,7 @@ struct Server {
     max_batch_reads = std::max<uint64_t>(max_batch_reads, b->n);
     max_batch_reqs = std::max<uint64_t>(max_batch_reqs, nseg);
     if (b->n >= 1024) {  // smoothed, biased up: admission must not undershoot
-      const double hpr = (double)r.n_hits / b->n, rpr = (double)r.n_locs / b->n;
+      const double hpr = (double)nh / b->n, rpr = (double)nl / b->n;
       hits_per_read = std::max(hpr, 0.8 * hits_per_read + 0.2 * hpr);
       rows_per_read = std::max(rpr, 0.8 * rows_per_read + 0.2 * rpr);
     }
@@ -349,50 +378,42 @@ struct Server {
 
   void run() {
     cudaSetDevice(e->device);
-    Batch cur, nxt;
+    Batch batch[2];
+    std::deque<Batch*> inflight;
     int slot = 0;
-    bool have_cur = false;
     for (;;) {
-      if (!have_cur) {
+      // keep two batches in flight while requests wait
+      while (inflight.size() < 2) {
+        Batch* b = &batch[slot];
         {
           std::unique_lock<std::mutex> lk(mu);
-          cv_work.wait(lk, [&] { return stop || !queue.empty(); });
-          if (queue.empty()) return;  // stopping with nothing left
-          cur.slot = slot;
-          slot ^= 1;
-          form(&cur);
+          if (inflight.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+          if (queue.empty()) break;
+          b->slot = slot;
+          form(b);
         }
-        prepare(&cur);
+        if (b->reqs.empty()) break;
         std::string err;
-        if (launch(&cur, &err) != 0) {
-          fail(&cur, err);
+        if (issue(b, &err) != 0) {
+          fail(b, err);
           continue;
         }
-        have_cur = true;
-      }
-      bool have_next = false;
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        if (!queue.empty()) {
-          nxt.slot = slot;
-          form(&nxt);
-          have_next = !nxt.reqs.empty();
-        }
-      }
-      if (have_next) {
+        inflight.push_back(b);
         slot ^= 1;
-        prepare(&nxt);  // host work overlapping the batch in flight
       }
+      if (inflight.empty()) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (stop && queue.empty()) return;  // stopping with nothing left
+        continue;
+      }
+      Batch* b = inflight.front();
+      inflight.pop_front();
       std::string err;
-      bool next_launched = false;
-      if (finish(&cur, &nxt, have_next, &next_launched, &err) != 0) {
-        fail(&cur, err);
-        if (have_next && !next_launched) fail(&nxt, "batch before it failed: " + err);
+      if (collect(b, &err) != 0) {
+        fail(b, err);
         std::lock_guard<std::mutex> lk(mu);
         fatal = err;
       }
-      std::swap(cur, nxt);
-      have_cur = next_launched;
     }
   }
 };
@@ -423,8 +444,16 @@ Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_base
     ok = cudaHostAlloc(reinterpret_cast<void**>(&S->h_offs[k]), (max_batch_reads + 1) * 8, 0) == cudaSuccess &&
          cudaHostAlloc(reinterpret_cast<void**>(&S->h_seg[k]), (S->max_segs + 1) * 4, 0) == cudaSuccess;
   }
-  ok = ok && cudaMalloc(&S->d_seg, (S->max_segs + 1) * 4) == cudaSuccess &&
-       cudaMalloc(&S->d_bounds, (S->max_segs + 1) * 16) == cudaSuccess;
+  for (int k = 0; k < 2 && ok; ++k)
+    ok = cudaMalloc(&S->d_seg[k], (S->max_segs + 1) * 4) == cudaSuccess &&
+         cudaMalloc(&S->d_bounds[k], (S->max_segs + 1) * 16) == cudaSuccess &&
+         cudaEventCreateWithFlags(&S->ev_in[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&S->ev_run[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&S->ev_out[k], cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaHostAlloc(reinterpret_cast<void**>(&S->h_err), 16, 0) == cudaSuccess;
+  if (ok && !e->xs[0])
+    ok = cudaStreamCreateWithFlags(&e->xs[0], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaStreamCreateWithFlags(&e->xs[1], cudaStreamNonBlocking) == cudaSuccess;
   for (int k = 0; k < kSets && ok; ++k) ok = cudaEventCreateWithFlags(&S->sets[k].done, cudaEventDisableTiming) ==
                                             cudaSuccess;
   if (!ok) {
@@ -448,6 +477,8 @@ void server_destroy(Server* S) {
     S->worker.join();
   }
   cudaStreamSynchronize(S->e->stream);
+  for (cudaStream_t x : S->e->xs)
+    if (x) cudaStreamSynchronize(x);
   for (ResultBuf& rb : S->sets) {
     cudaFreeHost(rb.hits);
     cudaFreeHost(rb.locs);
@@ -460,8 +491,14 @@ void server_destroy(Server* S) {
     cudaFreeHost(S->h_offs[k]);
     cudaFreeHost(S->h_seg[k]);
   }
-  cudaFree(S->d_seg);
-  cudaFree(S->d_bounds);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(S->d_seg[k]);
+    cudaFree(S->d_bounds[k]);
+    if (S->ev_in[k]) cudaEventDestroy(S->ev_in[k]);
+    if (S->ev_run[k]) cudaEventDestroy(S->ev_run[k]);
+    if (S->ev_out[k]) cudaEventDestroy(S->ev_out[k]);
+  }
+  if (S->h_err) cudaFreeHost(S->h_err);
   for (auto& kv : S->reqs) delete kv.second;
   delete S;
 }
