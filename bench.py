@@ -374,7 +374,7 @@ def _pct(v: list[float], q: float) -> float:
 
 
 def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: float | None, seconds: float,
-              rng: np.random.Generator, sat: float | None = None, burst: int = 192) -> dict:
+              rng: np.random.Generator, sat: float | None = None, burst: int = 192, max_batch: int = 1 << 20) -> dict:
     """One serving measurement through bwt_gpu_server_*: with load None a burst
     of requests submitted at once (saturated throughput); else Poisson arrivals
     offering `load` x `sat` reads/s for `seconds`.  Requests are slices of a
@@ -384,7 +384,7 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
     import queue
     from hpgbwt import lib
     L = gi.lib
-    srv = lib.Server(gi, max_batch_reads=1 << 20, max_results=MAX_RESULTS)
+    srv = lib.Server(gi, max_batch_reads=max_batch, max_results=MAX_RESULTS)
     st0 = srv.stats()
     pend: queue.Queue = queue.Queue()
     lat: list[float] = []

@@ -18,6 +18,8 @@
 
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -154,6 +156,11 @@ struct Server {
   uint32_t* h_err = nullptr;  // pinned copy of the index's error word, per slot
   // per pipeline slot: inputs sent, replay done, results out
   cudaEvent_t ev_in[2] = {nullptr, nullptr}, ev_run[2] = {nullptr, nullptr}, ev_out[2] = {nullptr, nullptr};
+  // time split, printed when the server is freed if HPG_BWT_TIMING is set: replay device
+  // time (events around each replay), host time blocked on replays and on result copies
+  bool timing = std::getenv("HPG_BWT_TIMING") != nullptr;
+  cudaEvent_t tv0[2] = {nullptr, nullptr}, tv1[2] = {nullptr, nullptr};
+  double t_replay = 0, t_wait_run = 0, t_wait_out = 0, t_issue = 0;
 
   // admission estimates, updated from finished batches
   double hits_per_read = 4.0, rows_per_read = 16.0;
@@ -238,8 +245,11 @@ struct Server {
     HPG_CUDA(cudaStreamWaitEvent(cs, ev_in[k], 0), "serving order");
     HPG_CUDA(cudaStreamWaitEvent(cs, ev_out[k], 0), "serving order");
     b->t_launch = now_ms();
+    if (timing) cudaEventRecord(tv0[k], cs);
     if (graph_launch(e, b->g, b->n, max_results, err) != 0) return -1;
+    if (timing) cudaEventRecord(tv1[k], cs);
     HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
+    if (timing) t_issue += now_ms() - b->t_launch;
     return 0;
   }
 
@@ -289,7 +299,14 @@ struct Server {
   int collect(Batch* b, std::string* err) {
     cudaStream_t cs = e->stream, h2d = e->xs[0], d2h = e->xs[1];
     const int k = b->slot;
+    const double w0 = now_ms();
     HPG_CUDA(cudaEventSynchronize(ev_run[k]), "batched pipeline");
+    if (timing) {
+      t_wait_run += now_ms() - w0;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, tv0[k], tv1[k]);
+      t_replay += ms;
+    }
     GraphPlan* g = b->g;
     const uint64_t* h = g->h_summary;
     const uint32_t status = (uint32_t)h[0];
@@ -337,7 +354,9 @@ struct Server {
     HPG_CUDA(cudaMemcpyAsync(h_err + k, e->d_err, 4, cudaMemcpyDeviceToHost, d2h), "error word");
     HPG_CUDA(cudaEventRecord(rb->done, d2h), "result event");
     HPG_CUDA(cudaEventRecord(ev_out[k], d2h), "serving order");
+    const double w1 = now_ms();
     HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
+    if (timing) t_wait_out += now_ms() - w1;
     HPG_CUDA(cudaGetLastError(), "rebase kernel");
     if (h_err[k]) {
       cudaMemsetAsync(e->d_err, 0, 4, d2h);
@@ -449,7 +468,8 @@ Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_base
          cudaMalloc(&S->d_bounds[k], (S->max_segs + 1) * 16) == cudaSuccess &&
          cudaEventCreateWithFlags(&S->ev_in[k], cudaEventDisableTiming) == cudaSuccess &&
          cudaEventCreateWithFlags(&S->ev_run[k], cudaEventDisableTiming) == cudaSuccess &&
-         cudaEventCreateWithFlags(&S->ev_out[k], cudaEventDisableTiming) == cudaSuccess;
+         cudaEventCreateWithFlags(&S->ev_out[k], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreate(&S->tv0[k]) == cudaSuccess && cudaEventCreate(&S->tv1[k]) == cudaSuccess;
   ok = ok && cudaHostAlloc(reinterpret_cast<void**>(&S->h_err), 16, 0) == cudaSuccess;
   if (ok && !e->xs[0])
     ok = cudaStreamCreateWithFlags(&e->xs[0], cudaStreamNonBlocking) == cudaSuccess &&
@@ -479,6 +499,12 @@ void server_destroy(Server* S) {
   cudaStreamSynchronize(S->e->stream);
   for (cudaStream_t x : S->e->xs)
     if (x) cudaStreamSynchronize(x);
+  if (S->timing && S->batches)
+    std::fprintf(stderr,
+                 "[hpgbwt] server: %llu batches, %.0f reads per batch; per batch: replay %.3f ms on the device, "
+                 "host blocked %.3f ms on replays and %.3f ms on result copies, issue %.3f ms\n",
+                 (unsigned long long)S->batches, (double)S->reads / S->batches, S->t_replay / S->batches,
+                 S->t_wait_run / S->batches, S->t_wait_out / S->batches, S->t_issue / S->batches);
   for (ResultBuf& rb : S->sets) {
     cudaFreeHost(rb.hits);
     cudaFreeHost(rb.locs);
@@ -497,6 +523,8 @@ void server_destroy(Server* S) {
     if (S->ev_in[k]) cudaEventDestroy(S->ev_in[k]);
     if (S->ev_run[k]) cudaEventDestroy(S->ev_run[k]);
     if (S->ev_out[k]) cudaEventDestroy(S->ev_out[k]);
+    if (S->tv0[k]) cudaEventDestroy(S->tv0[k]);
+    if (S->tv1[k]) cudaEventDestroy(S->tv1[k]);
   }
   if (S->h_err) cudaFreeHost(S->h_err);
   for (auto& kv : S->reqs) delete kv.second;
