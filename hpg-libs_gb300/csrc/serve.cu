@@ -108,6 +108,7 @@ struct Batch {
   uint64_t bases = 0;
   int slot = 0;  // staging slot of its offsets and segment table
   GraphPlan* g = nullptr;
+  ResultBuf* rb = nullptr;  // result set its copies go to, once they are queued
   double t_launch = 0;
 };
 
@@ -160,7 +161,8 @@ struct Server {
   // time (events around each replay), host time blocked on replays and on result copies
   bool timing = std::getenv("HPG_BWT_TIMING") != nullptr;
   cudaEvent_t tv0[2] = {nullptr, nullptr}, tv1[2] = {nullptr, nullptr};
-  double t_replay = 0, t_wait_run = 0, t_wait_out = 0, t_issue = 0;
+  double t_replay = 0, t_wait_run = 0, t_wait_out = 0, t_issue = 0, t_plan = 0, t_prep = 0, t_copies = 0,
+         t_take = 0, t_publish = 0, t_form = 0;
 
   // admission estimates, updated from finished batches
   double hits_per_read = 4.0, rows_per_read = 16.0;
@@ -222,13 +224,20 @@ struct Server {
   int issue(Batch* b, std::string* err) {
     cudaStream_t cs = e->stream, h2d = e->xs[0];
     const int k = b->slot;
+    const double p0 = now_ms();
     b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err, k);
     if (!b->g) return -1;
     HPG_CUDA(cudaEventSynchronize(ev_in[k]), "serving staging");  // the slot's previous tables were sent
+    const double p1 = now_ms();
     prepare(b);
-    // inputs once the slot's previous replay has read its own, the table once its rebase is done
+    const double p2 = now_ms();
+    if (timing) {
+      t_plan += p1 - p0;
+      t_prep += p2 - p1;
+    }
+    // inputs once the slot's previous replay has read its own, the segment table once
+    // the slot's previous rebase has read it
     HPG_CUDA(cudaStreamWaitEvent(h2d, ev_run[k], 0), "serving order");
-    HPG_CUDA(cudaStreamWaitEvent(h2d, ev_out[k], 0), "serving order");
     uint64_t at = 0;
     for (const ServeReq* q : b->reqs) {
       if (q->bases)
@@ -238,9 +247,11 @@ struct Server {
     }
     HPG_CUDA(cudaMemcpyAsync(b->g->offs, h_offs[k], ((size_t)b->n + 1) * 8, cudaMemcpyHostToDevice, h2d),
              "stage offsets");
+    HPG_CUDA(cudaStreamWaitEvent(h2d, ev_out[k], 0), "serving order");
     HPG_CUDA(cudaMemcpyAsync(d_seg[k], h_seg[k], (b->reqs.size() + 1) * 4, cudaMemcpyHostToDevice, h2d),
              "segments");
     HPG_CUDA(cudaEventRecord(ev_in[k], h2d), "serving order");
+    if (timing) t_copies += now_ms() - p2;
     // the replay once its inputs are in and the slot's previous results are out
     HPG_CUDA(cudaStreamWaitEvent(cs, ev_in[k], 0), "serving order");
     HPG_CUDA(cudaStreamWaitEvent(cs, ev_out[k], 0), "serving order");
@@ -294,9 +305,11 @@ struct Server {
     cv_done.notify_all();
   }
 
-  // Wait for a batch's replay, rebase and copy its results out on the output
-  // stream (the other slot's batch keeps the GPU busy meanwhile), publish them.
-  int collect(Batch* b, std::string* err) {
+  // Wait for a batch's replay, then queue its rebase and result copies on the
+  // output stream (the other slot's batch keeps the GPU busy meanwhile).  The
+  // slot's inputs are free from here on: the next batch of the slot is sent
+  // before these results are waited for.
+  int collect_start(Batch* b, std::string* err) {
     cudaStream_t cs = e->stream, h2d = e->xs[0], d2h = e->xs[1];
     const int k = b->slot;
     const double w0 = now_ms();
@@ -333,8 +346,10 @@ struct Server {
     gpu_ms += now_ms() - b->t_launch;
     const uint64_t nh = h[2], nl = g->skip_locate ? 0 : h[3];
     const size_t nseg = b->reqs.size();
+    const double k0 = now_ms();
     ResultBuf* rb = take_set(nh, nl, 2ull * b->n, nseg, err);
     if (!rb) return -1;
+    if (timing) t_take += now_ms() - k0;
     HPG_CUDA(cudaStreamWaitEvent(d2h, ev_run[k], 0), "serving order");
     const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(nh, nl), nseg + 1);
     const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
@@ -354,21 +369,32 @@ struct Server {
     HPG_CUDA(cudaMemcpyAsync(h_err + k, e->d_err, 4, cudaMemcpyDeviceToHost, d2h), "error word");
     HPG_CUDA(cudaEventRecord(rb->done, d2h), "result event");
     HPG_CUDA(cudaEventRecord(ev_out[k], d2h), "serving order");
+    b->rb = rb;
+    return 0;
+  }
+
+  // Wait for a batch's result copies and publish them to its requests.
+  int collect_finish(Batch* b, std::string* err) {
+    const int k = b->slot;
+    ResultBuf* rb = b->rb;
+    const size_t nseg = b->reqs.size();
     const double w1 = now_ms();
     HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
     if (timing) t_wait_out += now_ms() - w1;
     HPG_CUDA(cudaGetLastError(), "rebase kernel");
     if (h_err[k]) {
-      cudaMemsetAsync(e->d_err, 0, 4, d2h);
+      cudaMemsetAsync(e->d_err, 0, 4, e->xs[1]);
       *err = "corrupt index: suffix-array walk did not reach a sampled row";
       return -1;
     }
     const double t = now_ms();
     std::lock_guard<std::mutex> lk(mu);
+    uint32_t read0 = 0;  // the slot's staged segment table may already hold the next batch's
     for (size_t q = 0; q < nseg; ++q) {
       ServeReq* r = b->reqs[q];
       r->set = (int)(rb - sets);
-      r->read0 = h_seg[k][q];
+      r->read0 = read0;
+      read0 += r->n;
       r->hit0 = rb->bounds[2 * q];
       r->nh = rb->bounds[2 * q + 2] - r->hit0;
       r->loc0 = rb->bounds[2 * q + 1];
@@ -383,7 +409,8 @@ struct Server {
     max_batch_reads = std::max<uint64_t>(max_batch_reads, b->n);
     max_batch_reqs = std::max<uint64_t>(max_batch_reqs, nseg);
     if (b->n >= 1024) {  // smoothed, biased up: admission must not undershoot
-      const double hpr = (double)nh / b->n, rpr = (double)nl / b->n;
+      const double hpr = (double)(rb->bounds[2 * nseg] - rb->bounds[0]) / b->n,
+                   rpr = (double)(rb->bounds[2 * nseg + 1] - rb->bounds[1]) / b->n;
       hits_per_read = std::max(hpr, 0.8 * hits_per_read + 0.2 * hpr);
       rows_per_read = std::max(rpr, 0.8 * rows_per_read + 0.2 * rpr);
     }
@@ -392,26 +419,32 @@ struct Server {
       if (e->plans && e->plans[i]) plan_bytes += e->plans[i]->bytes;
     b->reqs.clear();
     cv_done.notify_all();
+    if (timing) t_publish += now_ms() - t;
     return 0;
   }
 
   void run() {
     cudaSetDevice(e->device);
-    Batch batch[2];
+    // two batches replaying or queued, plus one whose results are being copied out;
+    // batches finish in the order they were issued, so a batch object comes back
+    // into use three issues later, after it was published
+    Batch batch[3];
     std::deque<Batch*> inflight;
-    int slot = 0;
-    for (;;) {
-      // keep two batches in flight while requests wait
+    int slot = 0, next_obj = 0;
+    auto fill = [&](bool may_wait) {  // keep two batches in flight while requests wait
       while (inflight.size() < 2) {
-        Batch* b = &batch[slot];
+        Batch* b = &batch[next_obj];
         {
           std::unique_lock<std::mutex> lk(mu);
-          if (inflight.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
-          if (queue.empty()) break;
+          if (may_wait && inflight.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+          if (queue.empty()) return;
           b->slot = slot;
+          const double f0 = now_ms();
           form(b);
+          if (timing) t_form += now_ms() - f0;
         }
-        if (b->reqs.empty()) break;
+        if (b->reqs.empty()) return;
+        next_obj = (next_obj + 1) % 3;
         std::string err;
         if (issue(b, &err) != 0) {
           fail(b, err);
@@ -420,6 +453,9 @@ struct Server {
         inflight.push_back(b);
         slot ^= 1;
       }
+    };
+    for (;;) {
+      fill(true);
       if (inflight.empty()) {
         std::lock_guard<std::mutex> lk(mu);
         if (stop && queue.empty()) return;  // stopping with nothing left
@@ -428,7 +464,12 @@ struct Server {
       Batch* b = inflight.front();
       inflight.pop_front();
       std::string err;
-      if (collect(b, &err) != 0) {
+      int rc = collect_start(b, &err);
+      if (rc == 0) {
+        fill(false);  // the freed slot's next inputs travel while its results come out
+        rc = collect_finish(b, &err);
+      }
+      if (rc != 0) {
         fail(b, err);
         std::lock_guard<std::mutex> lk(mu);
         fatal = err;
@@ -476,6 +517,18 @@ Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_base
          cudaStreamCreateWithFlags(&e->xs[1], cudaStreamNonBlocking) == cudaSuccess;
   for (int k = 0; k < kSets && ok; ++k) ok = cudaEventCreateWithFlags(&S->sets[k].done, cudaEventDisableTiming) ==
                                             cudaSuccess;
+  // result sets sized for two hits and two located rows per read of a full batch up
+  // front (they grow past that when a batch needs it), so that pinning host memory
+  // stays out of the first batches' latency
+  for (int k = 0; k < kSets && ok; ++k) {
+    ResultBuf& rb = S->sets[k];
+    size_t c1 = 0, c2 = 0;
+    ok = pinned_grow(&rb.hits, &rb.hits_cap, 2 * max_batch_reads + 1) &&
+         pinned_grow(&rb.locs, &rb.locs_cap, 2 * max_batch_reads + 1) &&
+         pinned_grow(&rb.bounds, &rb.seg_cap, 2 * S->max_segs + 2) &&
+         pinned_grow(&rb.cnt, &c1, 2 * max_batch_reads + 1) && pinned_grow(&rb.trunc, &c2, 2 * max_batch_reads + 1);
+    rb.rs_cap = std::min(c1, c2);
+  }
   if (!ok) {
     cudaGetLastError();
     *err = "out of memory (serving buffers)";
@@ -502,9 +555,12 @@ void server_destroy(Server* S) {
   if (S->timing && S->batches)
     std::fprintf(stderr,
                  "[hpgbwt] server: %llu batches, %.0f reads per batch; per batch: replay %.3f ms on the device, "
-                 "host blocked %.3f ms on replays and %.3f ms on result copies, issue %.3f ms\n",
+                 "host blocked %.3f ms on replays and %.3f ms on result copies; host work: form %.3f, plan %.3f, "
+                 "tables %.3f, copy calls %.3f, launch %.3f, result set %.3f, publish %.3f ms\n",
                  (unsigned long long)S->batches, (double)S->reads / S->batches, S->t_replay / S->batches,
-                 S->t_wait_run / S->batches, S->t_wait_out / S->batches, S->t_issue / S->batches);
+                 S->t_wait_run / S->batches, S->t_wait_out / S->batches, S->t_form / S->batches,
+                 S->t_plan / S->batches, S->t_prep / S->batches, S->t_copies / S->batches, S->t_issue / S->batches,
+                 S->t_take / S->batches, S->t_publish / S->batches);
   for (ResultBuf& rb : S->sets) {
     cudaFreeHost(rb.hits);
     cudaFreeHost(rb.locs);
