@@ -107,6 +107,7 @@ def bench_config(wl: dict, n_reads: int, world: int, total_bases: int) -> dict:
             "sa_ratio": SA_RATIO, "o_ratio": 64,
             "l2": f"flushed (256 MiB write) before every step; reads {total_bases / 1e6:.0f} MB > L2",
             "parallelism": f"replica x{world} (reads sharded)"}
+SERVE_MAX_BATCH = 1 << 21  # reads per served batch at most
 SERVE_LOCATE_LIMIT = 10_000  # serving against the 3.1 Gbp genome: rows per (read, strand) list located at most
 
 
@@ -166,6 +167,16 @@ def read_seed(rank: int) -> int:
 
 def prepare(wl: dict, rank: int, dist):
     """Genome + index (shared by ranks, cached per call) and this rank's reads."""
+    t0 = time.time()
+    index_dir, genome, t_gen = genome_and_index(wl, rank, dist)
+    reads = make_reads(wl, genome, read_seed(rank))
+    log(f"[bench] rank {rank}: genome ({t_gen:.1f}s) + index + reads ready in {time.time() - t0:.1f}s")
+    return index_dir, reads, genome
+
+
+def genome_and_index(wl: dict, rank: int, dist):
+    """The workload's genome and the directory of its index (built by rank 0 once
+    per cache directory; the 3.1 Gbp genome on rank 0's GPU)."""
     from hpgbwt import lib, synth
     key = f"{wl['genome']}_{wl['genome_bp']}_r{SA_RATIO}"
     base = Path(os.environ.get("HPG_BENCH_CACHE", tempfile.gettempdir())) / "hpgbwt_bench" / key
@@ -185,9 +196,7 @@ def prepare(wl: dict, rank: int, dist):
         log(f"[bench] index of {wl['genome_bp'] // 1_000_000} Mbp built in {time.time() - t1:.1f}s "
             f"({'GPU' if large else 'host'} suffix arrays)")
     dist.barrier()
-    reads = make_reads(wl, genome, read_seed(rank))
-    log(f"[bench] rank {rank}: genome ({t_gen:.1f}s) + index + reads ready in {time.time() - t0:.1f}s")
-    return str(base / "index"), reads, genome
+    return str(base / "index"), genome, t_gen
 
 
 def make_reads(wl: dict, genome, seed: int):
@@ -374,17 +383,22 @@ def _pct(v: list[float], q: float) -> float:
 
 
 def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: float | None, seconds: float,
-              rng: np.random.Generator, sat: float | None = None, burst: int = 192, max_batch: int = 1 << 20) -> dict:
+              rng: np.random.Generator, sat: float | None = None, burst: int = 192, max_batch: int = 1 << 20,
+              srv=None) -> dict:
     """One serving measurement through bwt_gpu_server_*: with load None a burst
     of requests submitted at once (saturated throughput); else Poisson arrivals
     offering `load` x `sat` reads/s for `seconds`.  Requests are slices of a
     pinned read pool; latency is submit (scheduled arrival, when the submitter
-    lags) to results readable in host memory."""
+    lags) to results readable in host memory.  A server passed in is kept open
+    (a long-running server, its result buffers already grown); else one is
+    made for this run."""
     import ctypes
     import queue
     from hpgbwt import lib
     L = gi.lib
-    srv = lib.Server(gi, max_batch_reads=max_batch, max_results=MAX_RESULTS)
+    own = srv is None
+    if own:
+        srv = lib.Server(gi, max_batch_reads=max_batch, max_results=MAX_RESULTS)
     st0 = srv.stats()
     pend: queue.Queue = queue.Queue()
     lat: list[float] = []
@@ -442,51 +456,48 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
     pend.put(None)
     th.join()
     st = srv.stats()
-    srv.close()
+    if own:
+        srv.close()
     span = t_done[0] - t0
     nb = st["batches"] - st0["batches"]
     out = {"requests": n_req, "reads": done_reads[0], "achieved_reads_per_s": round(done_reads[0] / span, 1),
            "p50_ms": round(_pct(lat, 50), 3), "p99_ms": round(_pct(lat, 99), 3), "max_ms": round(max(lat), 3),
            "mean_ms": round(float(np.mean(lat)), 3), "batches": int(nb),
-           "mean_batch_reads": round(st["reads"] / max(1, st["batches"]), 1),
-           "mean_batch_requests": round(st["requests"] / max(1, st["batches"]), 2),
-           "max_batch_requests": int(st["max_batch_requests"]), "pool_regrowths": int(st["regrowths"]),
+           "mean_batch_reads": round((st["reads"] - st0["reads"]) / max(1, nb), 1),
+           "mean_batch_requests": round((st["requests"] - st0["requests"]) / max(1, nb), 2),
+           "max_batch_requests": int(st["max_batch_requests"]), "pool_regrowths": int(st["regrowths"] - st0["regrowths"]),
            "plan_hbm_bytes": int(st["plan_bytes"]), "hbm_budget_bytes": int(st["hbm_budget"])}
     if offered is not None:
         out = {"offered_load": load, "offered_reads_per_s": round(offered, 1), **out}
     return out
 
 
-def serving(gi, reads, genome, log, read_label: str = "100bp", locate_limit: int = 0) -> dict:
-    """The serving form at 70 % offered load: 64k-read requests of the batch
-    read model, and requests of log-uniform 1k-256k reads of 50-300 bp.  A
-    nonzero locate_limit leaves lists covering more rows unlocated (against a
-    3.1 Gbp genome with perfect tandem runs, a 50 bp read inside a homopolymer
-    run covers millions of rows)."""
+def serve_cases(gi, cases, log, locate_limit: int, rng: np.random.Generator, max_batch: int) -> dict:
+    """Each case (name, ReadSet pool, request-size draw) on one server, as a
+    long-running service: a warm-up burst (it captures the plans the case needs
+    and grows the result buffers), the saturated rate of a burst of about 48M
+    reads, then Poisson arrivals at 10-90 % of that rate for 2 s each."""
     import torch
-    from hpgbwt import synth
-    rng = np.random.default_rng(7)
-    res = {"locate_limit": locate_limit}
+    from hpgbwt import lib
+    res = {"locate_limit": locate_limit, "max_batch_reads": max_batch}
     gi.set_locate_limit(locate_limit)
-    pin_seq = torch.from_numpy(reads.seq).pin_memory()
-    pin_off = torch.from_numpy(reads.offsets.view(np.int64)).pin_memory()
-    t = time.time()
-    mix = synth.reads_fast_var(genome, 600_000, 11, 50, 300, "subst_capped")
-    mix_seq = torch.from_numpy(mix.seq).pin_memory()
-    mix_off = torch.from_numpy(mix.offsets.view(np.int64)).pin_memory()
-    log(f"[bench] serving read pools ready ({time.time() - t:.1f}s)")
-    cases = [(f"requests_64k_{read_label}", pin_seq, pin_off, len(reads), lambda: 65536),
-             ("requests_1k_256k_50_300bp", mix_seq, mix_off, len(mix),
-              lambda: int(np.exp(rng.uniform(np.log(1024), np.log(262144)))))]
-    for name, sq, of, pn, draw in cases:
-        serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)  # captures the plans it needs
-        sat = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, None, 0, rng)
+    for name, pool, draw in cases:
+        sq = torch.from_numpy(pool.seq).pin_memory()
+        of = torch.from_numpy(pool.offsets.view(np.int64)).pin_memory()
+        mean_n = float(np.mean([draw() for _ in range(4096)]))
+        burst = max(192, int(48e6 / mean_n))
+        args = (gi, sq.data_ptr(), of.data_ptr(), len(pool), draw)
+        srv = lib.Server(gi, max_batch_reads=max_batch, max_results=MAX_RESULTS)
+        serve_run(*args, None, 0, rng, burst=burst, srv=srv)
+        sat = serve_run(*args, None, 0, rng, burst=burst, srv=srv)
         sweep = {}
         for load in (0.1, 0.3, 0.5, 0.7, 0.9):  # offered load as a fraction of the saturated rate
-            sweep[f"{int(load * 100)}pct"] = serve_run(gi, sq.data_ptr(), of.data_ptr(), pn, draw, load, 2.0, rng,
-                                                       sat=sat["achieved_reads_per_s"])
+            sweep[f"{int(load * 100)}pct"] = serve_run(*args, load, 2.0, rng, sat=sat["achieved_reads_per_s"],
+                                                       srv=srv)
+        srv.close()
         loaded = sweep["70pct"]
-        res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "at_70pct_load": loaded,
+        res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "saturated_burst_requests": burst,
+                     "saturated_mean_batch_reads": sat["mean_batch_reads"], "at_70pct_load": loaded,
                      "load_sweep": {k: {"p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"],
                                         "achieved_reads_per_s": v["achieved_reads_per_s"]} for k, v in sweep.items()}}
         log(f"[bench] serving {name} sweep: " + ", ".join(f"{k} p50 {v['p50_ms']} p99 {v['p99_ms']}"
@@ -494,6 +505,95 @@ def serving(gi, reads, genome, log, read_label: str = "100bp", locate_limit: int
         log(f"[bench] serving {name}: saturated {sat['achieved_reads_per_s'] / 1e6:.1f} M reads/s; at 70% "
             f"p50 {loaded['p50_ms']} ms p99 {loaded['p99_ms']} ms, {loaded['mean_batch_requests']} req/batch")
     gi.set_locate_limit(0)
+    return res
+
+
+def log_uniform_sizes(rng: np.random.Generator, lo: int = 1024, hi: int = 262144):
+    return lambda: int(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def serving(gi, reads, genome, log, read_label: str = "100bp", locate_limit: int = 0) -> dict:
+    """The serving form: 64k-read requests of the batch read model, and requests
+    of log-uniform 1k-256k reads of 50-300 bp.  A nonzero locate_limit leaves
+    lists covering more rows unlocated (against a 3.1 Gbp genome with perfect
+    tandem runs, a 50 bp read inside a homopolymer run covers millions of rows)."""
+    from hpgbwt import synth
+    rng = np.random.default_rng(7)
+    t = time.time()
+    mix = synth.reads_fast_var(genome, 600_000, 11, 50, 300, "subst_capped")
+    log(f"[bench] serving read pools ready ({time.time() - t:.1f}s)")
+    cases = [(f"requests_64k_{read_label}", reads, lambda: 65536),
+             ("requests_1k_256k_50_300bp", mix, log_uniform_sizes(rng))]
+    return serve_cases(gi, cases, log, locate_limit, rng, SERVE_MAX_BATCH)
+
+
+def served_parity(gi, index_dir: str, pool, rng: np.random.Generator, locate_limit: int, n_req: int = 16,
+                  max_reads: int = 300_000) -> dict:
+    """n_req requests of log-uniform 1k-64k reads (at most max_reads in all)
+    submitted together to one server, each result compared record for record
+    with the oracle's search of the same reads."""
+    from hpgbwt import lib
+    from oracle.pyoracle import PortOracle
+    draw = log_uniform_sizes(rng, 1024, 65536)
+    sizes = []
+    while len(sizes) < n_req and sum(sizes) < max_reads:
+        sizes.append(min(draw(), max_reads - sum(sizes)))
+    subs = []
+    for k in sizes:
+        a = int(rng.integers(0, len(pool) - k + 1))
+        subs.append(pool.subset(np.arange(a, a + k)))
+    gi.set_locate_limit(locate_limit)
+    srv = lib.Server(gi, max_batch_reads=SERVE_MAX_BATCH, max_results=MAX_RESULTS)
+    tickets = [srv.submit(r.seq, r.offsets) for r in subs]
+    got = [srv.wait(t)[0] for t in tickets]
+    st = srv.stats()
+    srv.close()
+    gi.set_locate_limit(0)
+    ora = PortOracle(index_dir)
+    threads = os.cpu_count() or 1
+    out = {"requests": len(subs), "reads": int(sum(sizes)), "batches": int(st["batches"]),
+           "max_batch_requests": int(st["max_batch_requests"]), "locate_limit": locate_limit,
+           "oracle": "oracle/fm_oracle.c (pinned bit-exact to the reference's own search code)",
+           "hits": 0, "located_rows": 0, "equal": True}
+    for i, (r, g) in enumerate(zip(subs, got)):
+        want = ora.search(r, mode=lib.MODE_SEARCH1, max_results=MAX_RESULTS, threads=threads,
+                          locate_limit=locate_limit)
+        out["hits"] += int(len(want.hits))
+        out["located_rows"] += int(len(want.locs))
+        c = compare_results(g, want)
+        if not c["equal"]:
+            out["equal"] = False
+            out.setdefault("differences", {})[f"request {i}"] = c
+    ora.close()
+    return out
+
+
+def serving_large(dist, log) -> dict:
+    """The serving form against the 3.1 Gbp index: the genome of the c4
+    workload, indexed on this GPU; requests of log-uniform 1k-256k reads of
+    uniform 50-300 bp at 0.5 % per-base substitution (uncapped), <=1 error
+    searched, Poisson arrivals at 10-90 % of the saturated rate; then a burst of
+    requests checked against the oracle."""
+    from hpgbwt import lib, synth
+    t0 = time.time()
+    wl = WORKLOADS["c4"]
+    index_dir, genome, t_gen = genome_and_index(wl, dist.rank, dist)
+    t_index = time.time() - t0
+    gi = lib.GpuIndex(index_dir, device=dist.local)
+    t = time.time()
+    pool = synth.reads_fast_var(genome, 600_000, 11, 50, 300, "none", subst_rate=0.005)
+    log(f"[bench] 3.1 Gbp serving: genome {t_gen:.1f}s, genome + index {t_index:.1f}s, read pool "
+        f"{time.time() - t:.1f}s")
+    rng = np.random.default_rng(7)
+    res = serve_cases(gi, [("requests_1k_256k_50_300bp", pool, log_uniform_sizes(rng))], log,
+                      SERVE_LOCATE_LIMIT, rng, SERVE_MAX_BATCH)
+    res["parity"] = served_parity(gi, index_dir, pool, rng, SERVE_LOCATE_LIMIT)
+    log(f"[bench] 3.1 Gbp serving parity against the oracle: {res['parity']}")
+    gi.close()
+    res["workload"] = ("3.1 Gbp genome of the c4 workload, index built on this GPU; requests of log-uniform "
+                       "1k-256k reads of uniform 50-300 bp at 0.5% per-base substitution (uncapped), <=1 error "
+                       "searched; Poisson arrivals at 10-90% of the saturated rate")
+    res["genome_and_index_s"] = round(t_index, 1)
     return res
 
 
@@ -815,6 +915,8 @@ def run_gb300(args, wl: dict, dist: Dist) -> dict | None:
                           "worst_search_ms": max(r["search_us"] for r in table) / 1e3} if table else None),
         }
     gi.close()
+    if out is not None and dist.world == 1 and wl["genome"] != "large" and not (args.no_serving or args.no_large):
+        out["serving_3g"] = serving_large(dist, log)
     return out
 
 
@@ -863,6 +965,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default batched tuning")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form latency measurement")
     ap.add_argument("--no-block", action="store_true", help="skip the k-error block search leg")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip serving against the 3.1 Gbp index (built on the GPU) after the workload's legs")
     ap.add_argument("--cal-reads", type=int, default=200_000,
                     help="reads of the batch taken through bwt_generate_cals_batch and bwt_map_inexact_batch "
                          "(0: skip)")

@@ -41,11 +41,20 @@ double now_ms() {
 // Per batch: segment s holds the reads [seg_read0[s], seg_read0[s+1]).  Hit
 // read ids and located-row hit ids become segment-relative; bounds[2s] and
 // bounds[2s+1] get the first hit and first row of each segment (s = n_seg is
-// the end).
+// the end).  With a summary (the replay's device summary: status, -, hits,
+// rows) the counts are read from it, n_hits and n_locs being their caps, and
+// a batch whose pools overflowed is left alone (it runs again and is rebased
+// after its rerun); so the kernel can follow the replay in stream order.
 __global__ void serve_rebase_kernel(hpg_hit_t* __restrict__ hits, uint64_t n_hits, hpg_loc_t* __restrict__ locs,
                                     uint64_t n_locs, const uint64_t* __restrict__ hit_off,
                                     const uint64_t* __restrict__ loc_off, const uint32_t* __restrict__ seg_read0,
-                                    uint32_t n_seg, uint64_t* __restrict__ bounds) {
+                                    uint32_t n_seg, uint64_t* __restrict__ bounds,
+                                    const uint64_t* __restrict__ summary) {
+  if (summary) {
+    if ((uint32_t)summary[0] != 0) return;
+    n_hits = min(summary[2], n_hits);
+    n_locs = min(summary[3], n_locs);
+  }
   const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t s = tid; s <= n_seg; s += stride) {
     const uint64_t h0 = hit_off[2ull * seg_read0[s]];
@@ -258,6 +267,13 @@ struct Server {
     b->t_launch = now_ms();
     if (timing) cudaEventRecord(tv0[k], cs);
     if (graph_launch(e, b->g, b->n, max_results, err) != 0) return -1;
+    // the rebase follows the replay on its stream: no wait for SMs that the next
+    // replay's persistent kernels hold, and the copies out need only this event
+    GraphPlan* g = b->g;
+    count_launches(1);
+    serve_rebase_kernel<<<e->num_sms * 2, 256, 0, cs>>>(g->hits, g->res_cap, g->locs, g->skip_locate ? 0 : g->locs_cap,
+                                                       g->hit_off, g->loc_off, d_seg[k], (uint32_t)b->reqs.size(),
+                                                       d_bounds[k], g->summary_d);
     if (timing) cudaEventRecord(tv1[k], cs);
     HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
     if (timing) t_issue += now_ms() - b->t_launch;
@@ -331,7 +347,8 @@ struct Server {
       *err = "internal error: inconsistent work counts in the warp-cooperative search";
       return -1;
     }
-    if (status) {  // a pool overflowed: drain the pipeline, grow the pool and run the batch again
+    const bool rerun = status != 0;
+    if (rerun) {  // a pool overflowed: drain the pipeline, grow the pool and run the batch again
       ++regrows;
       HPG_CUDA(cudaStreamSynchronize(h2d), "serving drain");
       HPG_CUDA(cudaStreamSynchronize(d2h), "serving drain");
@@ -351,11 +368,13 @@ struct Server {
     if (!rb) return -1;
     if (timing) t_take += now_ms() - k0;
     HPG_CUDA(cudaStreamWaitEvent(d2h, ev_run[k], 0), "serving order");
-    const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(nh, nl), nseg + 1);
-    const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
-    count_launches(1);
-    serve_rebase_kernel<<<grid, 256, 0, d2h>>>(g->hits, nh, g->locs, nl, g->hit_off, g->loc_off, d_seg[k],
-                                               (uint32_t)nseg, d_bounds[k]);
+    if (rerun) {  // the rebase that followed the replay left the overflowed batch alone
+      const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(nh, nl), nseg + 1);
+      const unsigned grid = (unsigned)std::min<uint64_t>((work + 255) / 256, (uint64_t)e->num_sms * 8);
+      count_launches(1);
+      serve_rebase_kernel<<<grid, 256, 0, d2h>>>(g->hits, nh, g->locs, nl, g->hit_off, g->loc_off, d_seg[k],
+                                                 (uint32_t)nseg, d_bounds[k], nullptr);
+    }
     if (nh)
       HPG_CUDA(cudaMemcpyAsync(rb->hits, g->hits, nh * sizeof(hpg_hit_t), cudaMemcpyDeviceToHost, d2h), "copy hits");
     if (nl)

@@ -259,9 +259,10 @@ def from_strings(seqs: list[bytes]) -> ReadSet:
 
 
 def reads_fast_var(g: np.ndarray, n: int, seed: int, lo: int, hi: int, edits: str = "none",
-                   chunk: int = 200_000) -> ReadSet:
+                   chunk: int = 200_000, subst_rate: float = 0.0) -> ReadSet:
     """Vectorised sampler for reads of uniform length in [lo, hi] (large read
-    sets): the same models as reads(), drawn row-wise over fixed-width tiles."""
+    sets): the same models as reads(), drawn row-wise over fixed-width tiles;
+    subst_rate adds independent per-base substitutions (uncapped) on top."""
     rng = np.random.default_rng(seed)
     lens = rng.integers(lo, hi + 1, size=n)
     plan = _edit_plan(edits, n, lens, rng)
@@ -290,6 +291,9 @@ def reads_fast_var(g: np.ndarray, n: int, seed: int, lo: int, hi: int, edits: st
         base[ii, at[a:b][ii]] = ins_base[a:b][ii]
         rows = np.nonzero(plan[a:b] == 1)[0]
         base[rows, sat[a:b][rows]] = (base[rows, sat[a:b][rows]] + sdelta[a:b][rows]) % 4
+        if subst_rate > 0:
+            m = rng.random(base.shape) < subst_rate
+            base[m] = (base[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
         rc = np.nonzero(strand[a:b] == 1)[0]
         if len(rc):
             ridx = np.clip(L[rc] - 1 - col, 0, hi - 1)
@@ -299,7 +303,64 @@ def reads_fast_var(g: np.ndarray, n: int, seed: int, lo: int, hi: int, edits: st
     return ReadSet(out, offs, pos, strand, plan)
 
 
-def genome_large(n: int, seed: int, chunk: int = 1 << 26) -> np.ndarray:
+def _skip(rng: np.random.Generator, n: int) -> None:
+    """Advance rng past n 64-bit outputs as drawing n doubles would: PCG64's
+    advance() drops the buffered half of a 64-bit output that 32-bit draws
+    keep, and drawing doubles leaves it in place, so it is put back."""
+    before = rng.bit_generator.state
+    rng.bit_generator.advance(n)
+    after = rng.bit_generator.state
+    after["has_uint32"], after["uinteger"] = before["has_uint32"], before["uinteger"]
+    rng.bit_generator.state = after
+
+
+def _uniform_threads(rng: np.random.Generator, shape, chunk: int = 1 << 22) -> np.ndarray:
+    """rng.random(shape), the same doubles (one 64-bit PCG64 output each), filled
+    by host threads from copies of the generator advanced to their slice."""
+    import concurrent.futures as cf
+    import os
+    out = np.empty(shape, dtype=np.float64)
+    flat = out.reshape(-1)
+    state = rng.bit_generator.state
+
+    def fill(a: int) -> None:
+        bg = np.random.PCG64()
+        bg.state = state
+        bg.advance(a)
+        np.random.Generator(bg).random(out=flat[a:a + chunk])
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(fill, range(0, flat.size, chunk)))
+    _skip(rng, flat.size)
+    return out
+
+
+def _background_draws(g: np.ndarray, rng: np.random.Generator, cum: np.ndarray, chunk: int) -> None:
+    """g[i] = number of thresholds in cum that are <= the i-th uniform double of
+    rng's stream (one 64-bit PCG64 output per double), filled by host threads
+    from copies of the generator advanced to their slice of the stream; rng
+    ends advanced past all len(g) draws, as if it had drawn them in order."""
+    import concurrent.futures as cf
+    import os
+    n = len(g)
+    state = rng.bit_generator.state
+
+    def fill(a: int) -> None:
+        bg = np.random.PCG64()
+        bg.state = state
+        bg.advance(a)
+        u = np.random.Generator(bg).random(min(chunk, n - a))
+        v = g[a:a + len(u)]
+        np.greater_equal(u, cum[0], out=v.view(bool))
+        for c in cum[1:]:
+            v += u >= c
+
+    with cf.ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(fill, range(0, n, chunk)))
+    _skip(rng, n)
+
+
+def genome_large(n: int, seed: int, chunk: int = 1 << 22) -> np.ndarray:
     """Human-like genome of n bases built in bounded memory (about 1.2 n bytes
     at peak): GC 41 % background, 10 % copies of 300 bp elements and 17 % of
     6 kbp elements at 80-98 % identity, 18 % tandem repeats of 1-6 bp units
@@ -312,10 +373,7 @@ def genome_large(n: int, seed: int, chunk: int = 1 << 26) -> np.ndarray:
     would need tens of GB of temporaries."""
     rng = np.random.default_rng(seed)
     g = np.empty(n, dtype=np.uint8)
-    cum = np.cumsum([0.295, 0.205, 0.205])
-    for a in range(0, n, chunk):
-        u = rng.random(min(chunk, n - a))
-        g[a:a + len(u)] = np.searchsorted(cum, u, side="right").astype(np.uint8)
+    _background_draws(g, rng, np.cumsum([0.295, 0.205, 0.205]), chunk)
     for frac, L, fams, batch in ((0.10, 300, 64, 100_000), (0.17, 6000, 32, 5_000)):
         elems = np.stack([background(L, rng, 0.41) for _ in range(fams)])
         copies = int(frac * n) // L
@@ -326,23 +384,41 @@ def genome_large(n: int, seed: int, chunk: int = 1 << 26) -> np.ndarray:
             starts = rng.integers(0, n - L, size=b)
             ident = rng.uniform(0.80, 0.98, size=b)
             mat = elems[fam]
-            m = rng.random((b, L)) > ident[:, None]
+            m = _uniform_threads(rng, (b, L)) > ident[:, None]
             mat[m] = (mat[m] + rng.integers(1, 4, size=int(m.sum()), dtype=np.uint8)) % 4
             g[starts[:, None] + col[None, :]] = mat
+    # tandem runs: parameters drawn in order (the two breakers of a run are its
+    # two flips, the one before the run first), positions and bases built by host
+    # threads, written in draw order so that later runs overwrite earlier ones
     target, done = int(0.18 * n), 0
     j = np.arange(-1, 151)  # run bases 0..rlen-1, breakers at -1 and rlen
+    runs = []
     while done < target:
         b = 200_000
         units = rng.integers(0, 4, size=(b, 6), dtype=np.uint8)
         ulen = rng.integers(1, 7, size=b)
         rlen = rng.integers(20, 150, size=b)
         starts = rng.integers(1, n - 151, size=b)
-        keep = (j[None, :] >= -1) & (j[None, :] <= rlen[:, None])
-        vals = np.take_along_axis(units, (j[None, :] % ulen[:, None]), axis=1)
-        ends = (j[None, :] == -1) | (j[None, :] == rlen[:, None])
-        vals[ends] = (vals[ends] + rng.integers(1, 4, size=int(ends.sum()), dtype=np.uint8)) % 4
-        g[(starts[:, None] + j[None, :])[keep]] = vals[keep]
+        flips = rng.integers(1, 4, size=2 * b, dtype=np.uint8)
+        runs.append((units, ulen, rlen, starts, flips))
         done += int(rlen.sum())
+
+    def tandem(run):
+        units, ulen, rlen, starts, flips = run
+        keep = j[None, :] <= rlen[:, None]
+        vals = np.take_along_axis(units, (j[None, :] % ulen[:, None]), axis=1)
+        r = np.arange(len(rlen))
+        vals[r, 0] = (vals[r, 0] + flips[0::2]) % 4
+        vals[r, rlen + 1] = (vals[r, rlen + 1] + flips[1::2]) % 4
+        return (starts[:, None] + j[None, :])[keep], vals[keep]
+
+    import concurrent.futures as cf
+    import os
+    w = min(8, os.cpu_count() or 1)
+    with cf.ThreadPoolExecutor(max_workers=w) as ex:
+        for a in range(0, len(runs), w):
+            for at, vals in ex.map(tandem, runs[a:a + w]):
+                g[at] = vals
     return g
 
 
