@@ -752,10 +752,26 @@ __global__ void scatter_hits_kernel(const PendingHit* __restrict__ res, const un
                                     uint32_t res_cap, uint32_t* __restrict__ cursor, const unsigned* gate) {
   if (gate && *gate) return;  // a pool overflowed: the graph's host reruns the batch
   const uint32_t n = min(*res_total, res_cap);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const PendingHit h = res[i];
-    if (h.rs == 0xFFFFFFFFu) continue;  // reserved but never written (chunk tail)
-    sorted[seg_off[h.rs] + atomicAdd(&cursor[h.rs], 1u)] = h;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // four entries a thread and round, each stage's loads and atomics issued together
+  for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    PendingHit h[4];
+    uint64_t at[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint32_t i = i0 + u * stride;
+      if (i < n) h[u] = res[i];
+      else h[u].rs = 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)  // 0xFFFFFFFF: past the pool, or reserved but never written (chunk tail)
+      if (h[u].rs != 0xFFFFFFFFu) at[u] = seg_off[h[u].rs];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (h[u].rs != 0xFFFFFFFFu) at[u] += atomicAdd(&cursor[h[u].rs], 1u);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (h[u].rs != 0xFFFFFFFFu) sorted[at[u]] = h[u];
   }
 }
 
@@ -764,7 +780,8 @@ constexpr int kRankTpb = 512, kRankTile = 2048;
 
 __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
                                      uint32_t n_rs, uint32_t max_results, uint32_t* __restrict__ kept,
-                                     uint8_t* __restrict__ trunc, const uint32_t* max_dev, const unsigned* gate) {
+                                     uint8_t* __restrict__ trunc, const uint32_t* max_dev, const unsigned* gate,
+                                     uint32_t* __restrict__ longs, unsigned* n_longs, uint32_t longs_cap) {
   const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
   if (rs >= n_rs) return;
   if (gate && *gate) return;
@@ -774,7 +791,14 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
   const uint32_t keep = (uint32_t)(cnt < max_results ? cnt : max_results);
   kept[rs] = keep;
   trunc[rs] = cnt > max_results ? 1 : 0;
-  if (keep == 0 || cnt > kLongList) return;
+  if (keep == 0) return;
+  if (cnt > kLongList) {  // the long sort's work (the list holds enough room for every such list)
+    if (longs) {
+      const unsigned q = atomicAdd(n_longs, 1u);
+      if (q < longs_cap) longs[q] = rs;
+    }
+    return;
+  }
   // insertion sort by key (short list; keys are unique within a list)
   for (uint64_t i = b + 1; i < e; ++i) {
     const PendingHit x = sorted[i];
@@ -796,17 +820,28 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
 __global__ void __launch_bounds__(kRankTpb)
     sort_long_lists_kernel(PendingHit* __restrict__ sorted, PendingHit* __restrict__ scratch,
                            const uint64_t* __restrict__ seg_off, uint32_t n_rs, const uint32_t* __restrict__ kept,
-                           const unsigned* gate) {
+                           const unsigned* gate, const uint32_t* __restrict__ work, const unsigned* n_work,
+                           uint32_t work_cap) {
   if (gate && *gate) return;
   __shared__ uint64_t tile[kRankTile];
   __shared__ uint32_t longs[kRankTpb];
   __shared__ uint32_t n_long;
-  for (uint64_t base = (uint64_t)blockIdx.x * kRankTpb; base < n_rs; base += (uint64_t)gridDim.x * kRankTpb) {
+  // with a work list: its entries, a block each in turn; else every list, found by a scan
+  const uint64_t n_items = work ? min(*n_work, work_cap) : n_rs;
+  const uint64_t per_round = work ? 1 : kRankTpb;
+  for (uint64_t base = (uint64_t)blockIdx.x * per_round; base < n_items; base += (uint64_t)gridDim.x * per_round) {
     if (threadIdx.x == 0) n_long = 0;
     __syncthreads();
-    const uint64_t rs = base + threadIdx.x;
-    if (rs < n_rs && seg_off[rs + 1] - seg_off[rs] > kLongList && kept[rs] > 0)
-      longs[atomicAdd(&n_long, 1u)] = (uint32_t)rs;
+    if (work) {
+      if (threadIdx.x == 0) {
+        longs[0] = work[base];
+        n_long = 1;
+      }
+    } else {
+      const uint64_t rs = base + threadIdx.x;
+      if (rs < n_rs && seg_off[rs + 1] - seg_off[rs] > kLongList && kept[rs] > 0)
+        longs[atomicAdd(&n_long, 1u)] = (uint32_t)rs;
+    }
     __syncthreads();
     const uint32_t nl = n_long;
     for (uint32_t q = 0; q < nl; ++q) {
@@ -867,10 +902,14 @@ __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const 
 
 // Rows on the backward index fill the item array from the front, rows on the
 // forward index from the back, so walks claimed in order touch one direction
-// at a time.
-__global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off,
-                                   uint32_t n_hits, uint64_t n_locs, const uint64_t* __restrict__ read_offs,
-                                   RowItem* __restrict__ items, unsigned int* __restrict__ side, LocateSizes z) {
+// at a time.  A block takes 256 consecutive hits a round: one scan of the
+// (backward, forward) row counts over the block, one atomic per direction.
+constexpr int kExpandTpb = 256;
+
+__global__ void __launch_bounds__(kExpandTpb)
+    expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uint64_t* __restrict__ loc_off, uint32_t n_hits,
+                       uint64_t n_locs, const uint64_t* __restrict__ read_offs, RowItem* __restrict__ items,
+                       unsigned int* __restrict__ side, LocateSizes z) {
   if (z.status) {  // graph form: sizes from device memory, rows checked against the item capacity
     if (*z.status) return;
     n_hits = (uint32_t)*z.n_hits;
@@ -880,30 +919,57 @@ __global__ void expand_rows_kernel(const hpg_hit_t* __restrict__ hits, const uin
       return;
     }
   }
-  for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < n_hits; h += gridDim.x * blockDim.x) {
-    const hpg_hit_t x = hits[h];
-    const uint64_t b = loc_off[h], e = loc_off[h + 1];
-    if (e == b) continue;
-    const uint64_t len = read_offs[x.read + 1] - read_offs[x.read];
-    const uint32_t err = x.nm ? x.err_kind : 0u;
-    const uint32_t phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir, type = !strand
-    RowItem it;
-    it.hit = h;
-    it.phys_len = (phys << 31) | (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
-    const unsigned cnt = (unsigned)(e - b);
-    // one atomic per direction and warp: rows of the lanes sharing a direction are laid out by a scan
-    cg::coalesced_group g = cg::coalesced_threads();
-    cg::coalesced_group sub = cg::labeled_partition(g, phys);
-    const unsigned incl = cg::inclusive_scan(sub, cnt);
-    unsigned base = 0;
-    if (sub.thread_rank() == sub.size() - 1) base = atomicAdd(&side[phys], incl);
-    base = sub.shfl(base, sub.size() - 1);
-    const unsigned at = base + incl - cnt;
-    for (unsigned i = 0; i < cnt; ++i) {
-      it.row = (uint32_t)((uint64_t)x.k + i);
+  __shared__ uint64_t s_warp[kExpandTpb / 32];
+  __shared__ uint64_t s_base;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint64_t h0 = (uint64_t)blockIdx.x * kExpandTpb; h0 < n_hits; h0 += (uint64_t)gridDim.x * kExpandTpb) {
+    const uint64_t h = h0 + threadIdx.x;
+    RowItem it{0, 0, 0, 0};
+    uint32_t cnt = 0, phys = 0, k = 0;
+    uint64_t b = 0;
+    if (h < n_hits) {
+      const hpg_hit_t x = hits[h];
+      b = loc_off[h];
+      cnt = (uint32_t)(loc_off[h + 1] - b);
+      if (cnt) {
+        const uint64_t len = read_offs[x.read + 1] - read_offs[x.read];
+        const uint32_t err = x.nm ? x.err_kind : 0u;
+        phys = (uint32_t)x.dir ^ (uint32_t)x.strand;  // direction = type ? dir : !dir, type = !strand
+        it.hit = (uint32_t)h;
+        it.phys_len = (phys << 31) | (uint32_t)(len - (err == 1 ? 1 : 0) + (err == 3 ? 1 : 0));
+        k = (uint32_t)x.k;
+      }
+    }
+    // (forward << 32 | backward) row counts, scanned over the block
+    const uint64_t v = phys ? (uint64_t)cnt << 32 : (uint64_t)cnt;
+    uint64_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t t = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= (uint32_t)o) incl += t;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint64_t tot = 0;
+      for (int w = 0; w < kExpandTpb / 32; ++w) {
+        const uint64_t t = s_warp[w];
+        s_warp[w] = tot;
+        tot += t;
+      }
+      const uint32_t b0 = (uint32_t)tot ? atomicAdd(&side[0], (uint32_t)tot) : 0u;
+      const uint32_t b1 = (uint32_t)(tot >> 32) ? atomicAdd(&side[1], (uint32_t)(tot >> 32)) : 0u;
+      s_base = (uint64_t)b1 << 32 | b0;
+    }
+    __syncthreads();
+    const uint64_t excl = s_base + s_warp[warp] + incl - v;
+    const uint32_t at = phys ? (uint32_t)(excl >> 32) : (uint32_t)excl;
+    for (uint32_t i = 0; i < cnt; ++i) {
+      it.row = k + i;
       it.out = (uint32_t)(b + i);
       items[phys ? n_locs - 1 - (at + i) : at + i] = it;
     }
+    __syncthreads();  // s_warp and s_base are rewritten next round
   }
 }
 
@@ -925,16 +991,16 @@ __global__ void __launch_bounds__(kBlock)
     n_locs = *z.n_locs;
   }
   uint32_t r = 0, left = 0;
-  uint32_t i = 0, j = 0;
+  uint32_t i = 0, j = 0, slot = 0;
   RowItem it{0, 0, 0, 0};
   // Software pipeline: the next row item of the lane's claim is loaded while the
-  // current walk runs, and a finished walk's sampled-SA value is loaded then
-  // written out at the lane's next refill, so a refill waits on no load.
+  // current walk runs, and a finished walk's sample is loaded then written out at
+  // the lane's next refill, so a refill waits on no load.
   RowItem nx{0, 0, 0, 0};
   RowItem pit{0, 0, 0, 0};  // the finished walk whose output is pending
   uint32_t ps = 0, pj = 0;  // its sample and steps
   bool pending = false;
-  bool active = false;
+  bool active = false, reached = false;
   uint32_t sectors = 0;
   auto finish = [&]() {  // the pending walk's key and chromosome
     const uint32_t sa = (ps + pj) % X.walk_mod;
@@ -963,45 +1029,55 @@ __global__ void __launch_bounds__(kBlock)
     pending = false;
   };
   for (;;) {
-    const bool done = !active || sampled_row(X, i);
+    // one step of the walk: the row's mark entry and block are fetched together;
+    // a text-sampled row ends it (at most ratio - 1 LF steps), else LF moves on
+    if (active && !reached) {
+      const DevDir D = dir_of(X, it.phys_len >> 31);
+      uint32_t cnt[4];
+      uint4 bits;
+      const uint4 mk = load_mark(D, i, X.load_mode);
+      load_block_m(D.occ + (i >> 6), X.load_mode, cnt, bits);
+      sectors += 2;
+      if (text_sampled(mk, i, slot)) {
+        reached = true;
+      } else {
+        i = lf_from(X, D, i, cnt, bits);
+        if (++j >= X.ratio) {  // only a corrupt index gets here
+          atomicOr(X.err, kErrWalk);
+          slot = 0;
+          reached = true;
+        }
+      }
+    }
+    const bool done = !active || reached;
     const unsigned grp = __activemask();
     const unsigned ready = __ballot_sync(grp, done);
-    if (done) {
-      if ((uint32_t)__popc(ready) < kLocateBatch && ready != grp) continue;  // wait for more lanes
-      if (pending) finish();  // the previous walk of this lane: its sample has arrived by now
-      if (active) {  // the walk reached a sampled row: load the sample, write the row next time
-        const DevDir D = dir_of(X, it.phys_len >> 31);
-        ps = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
-        ++sectors;
-        pj = j;
-        pit = it;
-        pending = true;
-        active = false;
-      }
-      if (left == 0) {
-        r = claim(row_ctr, kRowsPerClaim);
-        left = kRowsPerClaim;
-        if (r < n_locs) nx = items[r];
-      } else {
-        ++r;
-      }
-      --left;
-      if (r >= n_locs) break;
-      it = nx;
-      if (left > 0 && r + 1 < n_locs) nx = items[r + 1];  // the next row, loaded during this walk
-      i = it.row;
-      j = 0;
-      active = true;
-      continue;
+    if (!done) continue;
+    if ((uint32_t)__popc(ready) < kLocateBatch && ready != grp) continue;  // wait for more lanes
+    if (pending) finish();  // the previous walk of this lane: its sample has arrived by now
+    if (active) {  // the walk reached a text-sampled row: load the sample, write the row next time
+      ps = dir_of(X, it.phys_len >> 31).T[slot];
+      ++sectors;
+      pj = j;
+      pit = it;
+      pending = true;
+      active = false;
+      reached = false;
     }
-    // one LF step of the walk
-    const uint32_t phys = it.phys_len >> 31;
-    i = lf_step(X, dir_of(X, phys), i);
-    ++sectors;
-    if (++j > X.walk_mod) {
-      atomicOr(X.err, kErrWalk);
-      i = 0;
+    if (left == 0) {
+      r = claim(row_ctr, kRowsPerClaim);
+      left = kRowsPerClaim;
+      if (r < n_locs) nx = items[r];
+    } else {
+      ++r;
     }
+    --left;
+    if (r >= n_locs) break;
+    it = nx;
+    if (left > 0 && r + 1 < n_locs) nx = items[r + 1];  // the next row, loaded during this walk
+    i = it.row;
+    j = 0;
+    active = true;
   }
   if (pending) finish();
   if (census) atomicAdd(census, (unsigned long long)sectors);
@@ -1168,17 +1244,22 @@ void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, c
   scatter_hits_kernel<<<1024, 256, 0, s>>>(res, res_total, seg_off, sorted, res_cap, cursor, gate);
 }
 
+size_t long_lists_cap(size_t res_cap) { return res_cap / (kLongList + 1) + 2; }
+
 void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_t* seg_off, uint32_t n_rs,
                           uint32_t max_results, uint32_t* kept, uint8_t* trunc, int num_sms, cudaStream_t s,
-                          const uint32_t* max_dev, const unsigned* gate) {
+                          const uint32_t* max_dev, const unsigned* gate, uint32_t* longs, unsigned* n_longs,
+                          uint32_t longs_cap) {
   if (!n_rs) return;
+  const uint32_t cap = longs ? longs_cap : 0u;
   count_launches(1);
   sort_truncate_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, n_rs, max_results, kept, trunc, max_dev,
-                                                          gate);
+                                                          gate, longs, n_longs, cap);
   uint64_t blocks = ((uint64_t)n_rs + kRankTpb - 1) / kRankTpb;
   if (blocks > 2ull * (uint64_t)num_sms) blocks = 2ull * (uint64_t)num_sms;
   count_launches(1);
-  sort_long_lists_kernel<<<(unsigned)blocks, kRankTpb, 0, s>>>(sorted, scratch, seg_off, n_rs, kept, gate);
+  sort_long_lists_kernel<<<(unsigned)blocks, kRankTpb, 0, s>>>(sorted, scratch, seg_off, n_rs, kept, gate, longs,
+                                                               n_longs, cap);
 }
 
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
@@ -1198,9 +1279,10 @@ void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const ui
   unsigned int* side = row_ctr + 1;  // two counters after the row claim counter
   cudaMemsetAsync(side, 0, 8, s);
   count_launches(1);
-  const uint64_t hit_grid = z.status ? 4ull * num_sms : (n_hits + 255) / 256;  // graph form: grid-stride over hits
-  expand_rows_kernel<<<(unsigned)(hit_grid ? hit_grid : 1), 256, 0, s>>>(hits, loc_off, n_hits, n_locs, read_offs,
-                                                                         items, side, z);
+  // graph form: grid-stride over the hits, 8 blocks per SM
+  const uint64_t hit_grid = z.status ? 8ull * num_sms : (n_hits + kExpandTpb - 1) / kExpandTpb;
+  expand_rows_kernel<<<(unsigned)(hit_grid ? hit_grid : 1), kExpandTpb, 0, s>>>(hits, loc_off, n_hits, n_locs,
+                                                                                read_offs, items, side, z);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, locate_persistent_kernel, kBlock, 0);
   if (per_sm < 1) per_sm = 1;
@@ -1301,6 +1383,9 @@ void launch_search_stage(const DevIndex& X, const BatchedParams& p, const Batche
     BatchedTuning tl = t;
     tl.split = 0;
     tl.dir_split = 0;
+    // reads above kWaveLongMin bases are at most 1/4000 of the bases: two
+    // blocks per SM serve them, and an empty list costs a short launch
+    tl.blocks_per_sm = 2;
     pl.dir_split = 0;
     pl.chain_ctr = ctr + 11;
     pl.read_list = long_list;
@@ -1316,6 +1401,7 @@ void launch_search_stage(const DevIndex& X, const BatchedParams& p, const Batche
     pb.spill_head = ctr + 12;
     pb.spill_tail = ctr + 13;
     pb.spill_cap = block_cap;
+    tl.blocks_per_sm = t.blocks_per_sm;
     launch_batched_search(X, pb, tl, num_sms, true, s);
   } else if (p.dir_split == 2) {  // one index direction after the other, then the queued change points
     launch_batched_search(X, p, t, num_sms, false, s);

@@ -167,9 +167,15 @@ void launch_scatter_hits(const PendingHit* res, const unsigned int* res_total, c
 // Sorts every (read, strand) list by emission key and keeps the first max_results
 // (from max_dev when given); `scratch` holds at least as many entries as
 // `sorted` and its contents are overwritten (the scatter's input is dead by then).
+// With `longs` (longs_cap = long_lists_cap(entries of the pool) entries) and a
+// zeroed counter `n_longs`, the lists above kLongList entries are collected by
+// the short sort and the long sort visits only them; without, it scans every list.
 void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_t* seg_off, uint32_t n_rs,
                           uint32_t max_results, uint32_t* kept, uint8_t* trunc, int num_sms, cudaStream_t s,
-                          const uint32_t* max_dev = nullptr, const unsigned* gate = nullptr);
+                          const uint32_t* max_dev = nullptr, const unsigned* gate = nullptr, uint32_t* longs = nullptr,
+                          unsigned* n_longs = nullptr, uint32_t longs_cap = 0);
+// Room for the ids of the lists longer than kLongList entries among res_cap entries.
+size_t long_lists_cap(size_t res_cap);
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
                         const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
                         const unsigned* gate = nullptr);

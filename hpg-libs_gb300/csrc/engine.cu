@@ -209,6 +209,20 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   cudaDeviceGetAttribute(&en->num_sms, cudaDevAttrMultiProcessorCount, device);
   if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return fail("index upload", ce);
   {
+    const uint32_t n_samples[2] = {(uint32_t)S[0]->n, (uint32_t)S[1]->n};
+    std::string terr;
+    if (build_text_samples(en, n_samples, &terr) != 0) {
+      *err = terr;
+      engine_destroy(en);
+      return nullptr;
+    }
+    for (int d = 0; d < 2; ++d) {  // the row samples served only the derivation
+      cudaFree(en->d_S[d]);
+      en->d_S[d] = nullptr;
+      en->X.dir[d].S = nullptr;
+    }
+  }
+  {
     std::string kerr;
     if (engine_set_kmer(en, kDefaultKmer, &kerr) != 0) {
       *err = kerr;
@@ -232,6 +246,8 @@ void engine_destroy(Engine* e) {
   for (int d = 0; d < 2; ++d) {
     cudaFree(e->d_occ[d]);
     cudaFree(e->d_S[d]);
+    cudaFree(e->d_mark[d]);
+    cudaFree(e->d_T[d]);
   }
   cudaFree(e->d_kar_off);
   cudaFree(e->d_kar_start);

@@ -52,7 +52,7 @@ struct GraphPlan {
   uint8_t* ok = nullptr;
   unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
                             // [5..7] locate [8] phase-1 chains [9] forward-index reads [10] long reads
-                            // [11] long-read claims [12] block head [13] block tail
+                            // [11] long-read claims [12] block head [13] block tail [14] long lists
   uint32_t* arr = nullptr;  // arrivals per (read, strand)
   uint64_t* seg = nullptr;
   uint64_t* hit_off = nullptr;
@@ -70,6 +70,7 @@ struct GraphPlan {
   unsigned long long* census_d = nullptr;
   uint64_t* summary_d = nullptr;
   uint32_t* long_list = nullptr;  // reads too long for the warp-cooperative form's group buffers
+  uint32_t* longs = nullptr;  // lists above kLongList entries, found by the sort (ctr[14] counts them)
   uint32_t long_cap = 0;
   SpillEntry* blocks = nullptr;   // j = 1 / j = n-1 blocks of the warp-cooperative form (spill_cap entries)
   // pinned host words
@@ -89,7 +90,9 @@ struct Engine {
   cudaStream_t stream = nullptr;
   DevIndex X{};
   OccBlock* d_occ[2] = {nullptr, nullptr};
-  uint32_t* d_S[2] = {nullptr, nullptr};
+  uint32_t* d_S[2] = {nullptr, nullptr};  // freed once the text-sampled arrays are built
+  uint4* d_mark[2] = {nullptr, nullptr};
+  uint32_t* d_T[2] = {nullptr, nullptr};
   uint64_t* d_kar_off = nullptr;
   uint64_t* d_kar_start = nullptr;
   uint8_t* d_table = nullptr;
@@ -195,5 +198,8 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
 // neighbouring chunks' replays (graph.cu).
 int run_graph_pipelined(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint64_t total,
                         uint32_t max_results, hpg_result_set_t* out, std::string* err);
+// The text-sampled suffix array of both directions (mark + T), derived from the
+// row samples already on the device (text_samples.cu); called once at open.
+int build_text_samples(Engine* en, const uint32_t n_samples[2], std::string* err);
 
 }  // namespace hpgbwt

@@ -11,7 +11,15 @@
 //                bits[2..3] = high code bit; the '$' row is stored as
 //                code 0 and corrected in rank_block().  A rank inside the
 //                block is then two bitwise ops and one popcount.
-//   uint32 S[]           sampled SA, S[i/ratio] = SA[i] (the reference's S.vec)
+//   uint32 S[]           sampled SA, S[i/ratio] = SA[i] (the reference's S.vec);
+//                        read only to derive the two arrays below, then freed
+//   uint4 mark[nblk]     text-sampled rows (SA value a multiple of the ratio),
+//                        one entry per 64 rows: x = such rows before the block,
+//                        y/z = their bits for rows 0..31 / 32..63
+//   uint32 T[]           SA values of the text-sampled rows, in row order
+//
+// A locate walk (LF until a sampled row) therefore ends within ratio - 1 steps
+// instead of after a geometric number of them (text_samples.cu).
 //
 // One rank query therefore touches exactly one 32-byte sector, against two
 // separate arrays (a 4-byte desp and an 8-byte count word) per query in the
@@ -36,6 +44,8 @@ struct __align__(32) OccBlock {
 struct DevDir {
   const OccBlock* occ;
   const uint32_t* S;
+  const uint4* mark;
+  const uint32_t* T;
   uint32_t dollar;  // BWT row holding '$'
   uint32_t nblk;
 };
@@ -162,6 +172,8 @@ __device__ __forceinline__ DevDir dir_of(const DevIndex& X, uint32_t d) {
   DevDir D;
   D.occ = d ? X.dir[1].occ : X.dir[0].occ;
   D.S = d ? X.dir[1].S : X.dir[0].S;
+  D.mark = d ? X.dir[1].mark : X.dir[0].mark;
+  D.T = d ? X.dir[1].T : X.dir[0].T;
   D.dollar = d ? X.dir[1].dollar : X.dir[0].dollar;
   D.nblk = d ? X.dir[1].nblk : X.dir[0].nblk;
   return D;
@@ -208,36 +220,77 @@ __device__ __forceinline__ void bw_step(const DevIndex& X, View v, uint32_t b, u
   l = c + rl;
 }
 
-// LF of row i on a physical direction: row 0 for the '$' row, else
-// C[b] + get_O(b, i+1) with b the row's symbol (csafm.h:215-231).
-__device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, uint32_t i) {
+// LF of row i on a physical direction from its loaded block: row 0 for the
+// '$' row, else C[b] + get_O(b, i+1) with b the row's symbol (csafm.h:215-231).
+__device__ __forceinline__ uint32_t lf_from(const DevIndex& X, const DevDir& D, uint32_t i, const uint32_t (&cnt)[4],
+                                            const uint4& bits) {
   if (i == D.dollar) return 0;
   const uint32_t q = i >> 6, r = i & 63;
-  uint32_t cnt[4];
-  uint4 bits;
-  load_block_m(D.occ + q, X.load_mode, cnt, bits);
   const uint32_t lo = r < 32 ? bits.x : bits.y, hi = r < 32 ? bits.z : bits.w;
   const uint32_t b = ((lo >> (r & 31)) & 1u) | (((hi >> (r & 31)) & 1u) << 1);
   return sel4(X.C, b) + rank_block(D, q, b, r + 1, cnt, bits);
 }
 
+__device__ __forceinline__ uint32_t lf_step(const DevIndex& X, const DevDir& D, uint32_t i) {
+  uint32_t cnt[4];
+  uint4 bits;
+  load_block_m(D.occ + (i >> 6), X.load_mode, cnt, bits);
+  return lf_from(X, D, i, cnt, bits);
+}
+
+// The reference's sampled rows: row index a multiple of the ratio.
 __device__ __forceinline__ bool sampled_row(const DevIndex& X, uint32_t i) {
   return X.ratio_shift != 0xFFFFFFFFu ? (i & ((1u << X.ratio_shift) - 1u)) == 0 : (i % X.ratio) == 0;
 }
 
-// getScompValue (csafm.h:208-235): walk LF to a sampled row, add the steps.
-__device__ __forceinline__ uint32_t sa_value(const DevIndex& X, uint32_t d, uint32_t m) {
-  const DevDir D = dir_of(X, d);
-  uint32_t i = m, j = 0;
-  while (!sampled_row(X, i)) {
-    i = lf_step(X, D, i);
-    if (++j > X.walk_mod) {  // LF is one cycle over n+1 rows: only a corrupt index gets here
+__device__ __forceinline__ bool ratio_multiple(const DevIndex& X, uint32_t v) {
+  return X.ratio_shift != 0xFFFFFFFFu ? (v & ((1u << X.ratio_shift) - 1u)) == 0 : (v % X.ratio) == 0;
+}
+
+// Mark entry of row i, fetched like the blocks (mode 2/3: kept in L2).
+__device__ __forceinline__ uint4 load_mark(const DevDir& D, uint32_t i, uint32_t mode) {
+  const uint4* p = D.mark + (i >> 6);
+  uint4 m;
+  if (mode >= 2) {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+        : "=r"(m.x), "=r"(m.y), "=r"(m.z), "=r"(m.w)
+        : "l"(p), "l"(pol));
+  } else
+    m = __ldg(p);
+  return m;
+}
+
+// Whether row i is text-sampled, and its slot in T.
+__device__ __forceinline__ bool text_sampled(const uint4& m, uint32_t i, uint32_t& slot) {
+  const uint32_t r = i & 63;
+  const uint32_t w = r < 32 ? m.y : m.z;
+  slot = m.x + (r < 32 ? 0u : (uint32_t)__popc(m.y)) + (uint32_t)__popc(w & ((1u << (r & 31)) - 1u));
+  return (w >> (r & 31)) & 1u;
+}
+
+// getScompValue (csafm.h:208-235): walk LF to a sampled row, add the steps;
+// here to a text-sampled row, so at most ratio - 1 steps (a longer walk means
+// a corrupt index: the error bit is set and slot 0 taken).  The row's mark
+// entry and block are fetched together; `sectors` counts them and the sample.
+__device__ __forceinline__ uint32_t sa_value(const DevIndex& X, const DevDir& D, uint32_t m, uint32_t* sectors) {
+  uint32_t i = m, j = 0, slot = 0;
+  for (;;) {
+    uint32_t cnt[4];
+    uint4 bits;
+    const uint4 mk = load_mark(D, i, X.load_mode);
+    load_block_m(D.occ + (i >> 6), X.load_mode, cnt, bits);
+    if (text_sampled(mk, i, slot)) break;
+    i = lf_from(X, D, i, cnt, bits);
+    if (++j >= X.ratio) {
       atomicOr(X.err, kErrWalk);
+      slot = 0;
       break;
     }
   }
-  const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
-  return (s + j) % X.walk_mod;
+  *sectors = 2 * (j + 1) + 1;
+  return (D.T[slot] + j) % X.walk_mod;
 }
 
 // binsearch (search/io.h:43-64): first offset greater than key.

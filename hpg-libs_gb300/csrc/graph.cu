@@ -91,7 +91,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
       !grab(g, &g->rows, ((size_t)g->res_cap + 1) * 4) || !grab(g, &g->loc_off, ((size_t)g->res_cap + 2) * 8) ||
       !grab(g, &g->items, (g->locs_cap + 1) * locate_row_item_bytes()) ||
       !grab(g, &g->locs, (g->locs_cap + 1) * sizeof(hpg_loc_t)) || !grab(g, &g->census_d, 16) ||
-      !grab(g, &g->long_list, (size_t)g->long_cap * 4) ||
+      !grab(g, &g->long_list, (size_t)g->long_cap * 4) || !grab(g, &g->longs, long_lists_cap(g->res_cap) * 4) ||
       (g->tuning.split == 3 && !grab(g, &g->blocks, (size_t)g->spill_cap * sizeof(SpillEntry))) ||
       !grab(g, &g->summary_d, 64)) {
     *err = "out of device memory (graph plan)";
@@ -111,7 +111,6 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   record(g->ev[0], s);
   cudaMemsetAsync(ctr, 0, 64, s);
   cudaMemsetAsync(g->arr, 0, T * 4, s);
-  cudaMemsetAsync(g->rows, 0, (size_t)g->res_cap * 4, s);
   if (census) cudaMemsetAsync(census, 0, 8, s);
   launch_encode_dev(g->seqs, g->bases_cap, g->offs, g->hdr, g->n_cap, e->d_table, g->codes, g->ok, s);
   launch_check_offsets(g->offs, g->hdr, g->n_cap, g->bases_cap, g->ok, status, s);
@@ -150,12 +149,12 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   launch_scatter_hits(g->res, ctr + 3, g->seg, g->sorted, g->res_cap, reinterpret_cast<uint32_t*>(g->hit_off), s,
                       status);
   launch_sort_truncate(g->sorted, g->res, g->seg, (uint32_t)T, 0, g->kept, g->trunc, e->num_sms, s, g->hdr + 1,
-                       status);
+                       status, g->longs, ctr + 14, (uint32_t)long_lists_cap(g->res_cap));
   launch_scan(g->kept, T, g->hit_off, g->part, s);
   launch_expand_hits(g->sorted, g->seg, g->hit_off, g->kept, (uint32_t)T, g->hits, g->rows, s, status);
   launch_limit_rows(g->hit_off, g->rows, (uint32_t)T, 0, reinterpret_cast<const uint64_t*>(g->hdr + 2), g->trunc, s,
                     status);
-  launch_scan(g->rows, g->res_cap, g->loc_off, g->part, s);
+  launch_scan(g->rows, g->res_cap, g->loc_off, g->part, s, g->hit_off + T);  // over the hits found
   record(g->ev[4], s);
 
   LocateSizes z;

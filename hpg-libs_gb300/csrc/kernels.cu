@@ -39,13 +39,15 @@ __global__ void encode_kernel(const uint8_t* __restrict__ ascii, uint64_t total,
   __shared__ uint8_t tab[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tab[i] = table[i];
   __syncthreads();
-  const uint64_t base = 0;  // codes mirror d_seqs byte for byte over [0, total)
+  // codes mirror the bases byte for byte over [0, total), 16 a thread and round
+  const bool aligned = ((reinterpret_cast<uintptr_t>(ascii) | reinterpret_cast<uintptr_t>(codes)) & 15) == 0;
   for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c * 16 < total;
        c += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t b = base + c * 16;
+    const uint64_t b = c * 16;
     uint8_t in[16], out[16];
-    const uint64_t m = total - c * 16 < 16 ? total - c * 16 : 16;
-    if (m == 16 && (b & 15) == 0) {
+    const uint64_t m = total - b < 16 ? total - b : 16;
+    const bool full = aligned && m == 16;
+    if (full) {
       *reinterpret_cast<uint4*>(in) = *reinterpret_cast<const uint4*>(ascii + b);
     } else {
       for (uint64_t i = 0; i < m; ++i) in[i] = ascii[b + i];
@@ -56,7 +58,7 @@ __global__ void encode_kernel(const uint8_t* __restrict__ ascii, uint64_t total,
       out[i] = tab[in[i]];
       if (i < (int)m && out[i] == 0xFF) bad |= 1u << i;
     }
-    if (m == 16 && (b & 15) == 0) {
+    if (full) {
       *reinterpret_cast<uint4*>(codes + b) = *reinterpret_cast<const uint4*>(out);
     } else {
       for (uint64_t i = 0; i < m; ++i) codes[b + i] = out[i];
@@ -204,13 +206,31 @@ __device__ __forceinline__ uint64_t block_excl_scan(uint64_t v, uint64_t* total)
   return excl;
 }
 
+// The 8 values of a thread's chunk at `base` (zero past n): two 16-byte loads
+// when the chunk is whole and aligned.
+__device__ __forceinline__ void scan_load8(const uint32_t* __restrict__ in, size_t n, size_t base,
+                                           uint32_t (&v)[kScanItems]) {
+  if (base + kScanItems <= n && (reinterpret_cast<uintptr_t>(in + base) & 15) == 0) {
+    const uint4 a = __ldg(reinterpret_cast<const uint4*>(in + base));
+    const uint4 b = __ldg(reinterpret_cast<const uint4*>(in + base) + 1);
+    v[0] = a.x, v[1] = a.y, v[2] = a.z, v[3] = a.w, v[4] = b.x, v[5] = b.y, v[6] = b.z, v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) v[i] = base + i < n ? in[base + i] : 0;
+  }
+}
+
 __global__ void __launch_bounds__(kScanTpb) scan_reduce_kernel(const uint32_t* __restrict__ in, size_t n,
-                                                               uint64_t* __restrict__ part) {
+                                                               uint64_t* __restrict__ part,
+                                                               const uint64_t* __restrict__ n_dev) {
+  if (n_dev) n = min((uint64_t)n, *n_dev);
+  if ((size_t)blockIdx.x * kScanTile > n) return;  // past the count (uniform over the block)
   const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  scan_load8(in, n, base, v);
   uint64_t s = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i)
-    if (base + i < n) s += in[base + i];
+  for (int i = 0; i < kScanItems; ++i) s += v[i];
   uint64_t tot;
   block_excl_scan(s, &tot);
   if (threadIdx.x == 0) part[blockIdx.x] = tot;
@@ -228,25 +248,50 @@ __global__ void __launch_bounds__(1024) scan_parts_kernel(uint64_t* part, size_t
   }
 }
 
+// direct: part holds the tiles' sums and each tile adds up those before it
+// (few tiles); else part holds the tiles' exclusive prefixes already.
 __global__ void __launch_bounds__(kScanTpb) scan_apply_kernel(const uint32_t* __restrict__ in, size_t n,
                                                               const uint64_t* __restrict__ part,
-                                                              uint64_t* __restrict__ out) {
+                                                              uint64_t* __restrict__ out, int direct,
+                                                              const uint64_t* __restrict__ n_dev) {
+  const size_t n_cap = n;
+  if (n_dev) n = min((uint64_t)n, *n_dev);
+  if ((size_t)blockIdx.x * kScanTile > n) return;  // past the count (uniform over the block)
+  uint64_t pre;
+  if (direct) {
+    uint64_t own = 0;
+    for (unsigned t = threadIdx.x; t < blockIdx.x; t += blockDim.x) own += part[t];
+    block_excl_scan(own, &pre);
+  } else {
+    pre = part[blockIdx.x];
+  }
   const size_t base = (size_t)blockIdx.x * kScanTile + (size_t)threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
+  scan_load8(in, n, base, v);
   uint64_t s = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) {
-    v[i] = base + i < n ? in[base + i] : 0;
-    s += v[i];
-  }
+  for (int i = 0; i < kScanItems; ++i) s += v[i];
   uint64_t tot;
-  uint64_t run = part[blockIdx.x] + block_excl_scan(s, &tot);
+  uint64_t run = pre + block_excl_scan(s, &tot);
+  uint64_t o[kScanItems];
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
-    if (base + i < n) out[base + i] = run;
+    o[i] = run;
     run += v[i];
   }
-  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) out[n] = part[blockIdx.x] + tot;
+  if (base + kScanItems <= n && (reinterpret_cast<uintptr_t>(out + base) & 15) == 0) {
+    ulonglong2* q = reinterpret_cast<ulonglong2*>(out + base);
+#pragma unroll
+    for (int i = 0; i < kScanItems / 2; ++i) q[i] = make_ulonglong2(o[2 * i], o[2 * i + 1]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+      if (base + i < n) out[base + i] = o[i];
+  }
+  if (blockIdx.x == n / kScanTile && threadIdx.x == 0) {  // the tile holding position n: the total
+    out[n] = pre + tot;
+    if (n_cap != n) out[n_cap] = pre + tot;
+  }
 }
 
 // ---------------------------------------------------------------- gather --
@@ -342,19 +387,7 @@ __global__ void __launch_bounds__(kTpb)
   uint32_t steps = 0;
   uint64_t key;
   {
-    const DevDir D = dir_of(X, phys_fw);
-    uint32_t i = row, j = 0;
-    while (!sampled_row(X, i)) {
-      i = lf_step(X, D, i);
-      if (++j > X.walk_mod) {  // LF is one cycle over n+1 rows: only a corrupt index gets here
-        atomicOr(X.err, kErrWalk);
-        i = 0;
-        break;
-      }
-    }
-    steps = j + 1;
-    const uint32_t s = D.S[X.ratio_shift != 0xFFFFFFFFu ? (i >> X.ratio_shift) : (i / X.ratio)];
-    const uint32_t sa = (s + j) % X.walk_mod;
+    const uint32_t sa = sa_value(X, dir_of(X, phys_fw), row, &steps);
     key = phys_fw ? (uint64_t)((X.top + 1u) - sa) - len_calc - 1u : (uint64_t)sa;
   }
   const uint32_t id = kar_search(X, key);
@@ -446,18 +479,25 @@ void launch_plain_search1(const DevIndex& X, const uint8_t* codes, const uint64_
 
 size_t scan_parts(size_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
-void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cudaStream_t s) {
+void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cudaStream_t s,
+                 const uint64_t* n_dev) {
   if (n == 0) {
     cudaMemsetAsync(out, 0, sizeof(uint64_t), s);
     return;
   }
-  const unsigned nb = (unsigned)((n + kScanTile - 1) / kScanTile);
+  // tiles, plus one that only holds position n when n ends a tile
+  const unsigned nb = (unsigned)(n / kScanTile + 1);
+  // up to 2048 tiles, each tile of the apply pass sums the tile sums before it
+  // (at most 4 loads a thread); more, and one block scans the tile sums first
+  const int direct = nb <= 2048;
   count_launches(1);
-  scan_reduce_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part);
+  scan_reduce_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part, n_dev);
+  if (!direct) {
+    count_launches(1);
+    scan_parts_kernel<<<1, 1024, 0, s>>>(part, nb);
+  }
   count_launches(1);
-  scan_parts_kernel<<<1, 1024, 0, s>>>(part, nb);
-  count_launches(1);
-  scan_apply_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part, out);
+  scan_apply_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part, out, direct, n_dev);
 }
 
 void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t* ovf_count, uint32_t ovf_cap,

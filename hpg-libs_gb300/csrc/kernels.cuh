@@ -51,8 +51,11 @@ void launch_plain_search1(const DevIndex& X, const uint8_t* codes, const uint64_
                           uint32_t* rs_count, uint8_t* rs_trunc, unsigned long long* census, cudaStream_t s);
 
 // Exclusive scan: out[0..n] with out[n] = total.  `part` needs scan_parts(n) entries.
+// With n_dev the scan covers the first min(n, *n_dev) entries (a count found on
+// the device) and writes the total at that position and at out[n].
 size_t scan_parts(size_t n);
-void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cudaStream_t s);
+void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cudaStream_t s,
+                 const uint64_t* n_dev = nullptr);
 
 // Slots + overflow pool -> ordered hpg_hit_t records, hit i of (read, strand) t at off[t] + i.
 void launch_gather_hits(const uint4* slots, const OvfEntry* ovf, const uint32_t* ovf_count, uint32_t ovf_cap,
