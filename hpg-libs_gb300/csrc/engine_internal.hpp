@@ -47,7 +47,8 @@ struct GraphPlan {
   // device buffers
   uint8_t* seqs = nullptr;
   uint64_t* offs = nullptr;
-  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results, [2..3] locate limit (u64)
+  uint32_t* hdr = nullptr;  // [0] reads in this batch, [1] max_results, [2..3] locate limit (u64),
+                            // [4..5] source of the bases (u64, 0 = seqs), [6..7] its bytes
   uint8_t* codes = nullptr;
   uint8_t* ok = nullptr;
   unsigned* ctr = nullptr;  // as the direct form: [0] chains [1] spill head [2] spill tail [3] results [4] status
@@ -188,7 +189,10 @@ void graph_plans_destroy(Engine* e);
 // plan's input buffers: launch (header + replay), then collect (synchronize,
 // read the summary; returns 1 with `grow` filled when a pool overflowed, the
 // batch then has to run again through run_batched_graph).
-int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err);
+// `src` (device memory of src_bytes bases): the batch's bases are read there
+// in place instead of from the plan's own buffer.
+int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err,
+                 const void* src = nullptr, uint64_t src_bytes = 0);
 int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceResult* out, std::string* err);
 // The plan serving batches of n reads and `total` bases (captured on demand).
 // `pslot` (0/1) picks one of the two plans of a capacity class.

@@ -81,7 +81,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   const size_t T = 2ull * g->n_cap;
   const size_t parts = std::max(scan_parts(T), scan_parts(g->res_cap));
   if (!grab(g, &g->seqs, g->bases_cap + 64) || !grab(g, &g->offs, ((size_t)g->n_cap + 1) * 8) ||
-      !grab(g, &g->hdr, 16) || !grab(g, &g->codes, g->bases_cap + 64) || !grab(g, &g->ok, (size_t)g->n_cap + 16) ||
+      !grab(g, &g->hdr, 32) || !grab(g, &g->codes, g->bases_cap + 64) || !grab(g, &g->ok, (size_t)g->n_cap + 16) ||
       !grab(g, &g->ctr, 64) || !grab(g, &g->arr, T * 4 + 16) || !grab(g, &g->seg, (T + 1) * 8) ||
       !grab(g, &g->hit_off, (T + 1) * 8) || !grab(g, &g->kept, T * 4 + 16) || !grab(g, &g->trunc, T + 16) ||
       !grab(g, &g->part, parts * 8) || !grab(g, &g->res, (size_t)g->res_cap * sizeof(PendingHit)) ||
@@ -98,7 +98,7 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
     return -1;
   }
   HPG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->h_summary), 64, cudaHostAllocDefault), "pinned summary");
-  HPG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->h_hdr), 16, cudaHostAllocDefault), "pinned header");
+  HPG_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&g->h_hdr), 32, cudaHostAllocDefault), "pinned header");
   for (cudaEvent_t& ev : g->ev) HPG_CUDA(cudaEventCreate(&ev), "graph events");
   HPG_CUDA(cudaMemset(g->offs, 0, 8), "graph plan");  // an empty batch reads offs[0]
 
@@ -112,7 +112,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   cudaMemsetAsync(ctr, 0, 64, s);
   cudaMemsetAsync(g->arr, 0, T * 4, s);
   if (census) cudaMemsetAsync(census, 0, 8, s);
-  launch_encode_dev(g->seqs, g->bases_cap, g->offs, g->hdr, g->n_cap, e->d_table, g->codes, g->ok, s);
+  launch_encode_dev(g->seqs, g->bases_cap, g->offs, g->hdr, g->n_cap, e->d_table, g->codes, g->ok, s,
+                    reinterpret_cast<const uint64_t*>(g->hdr + 4));
   launch_check_offsets(g->offs, g->hdr, g->n_cap, g->bases_cap, g->ok, status, s);
   record(g->ev[1], s);
 
@@ -275,13 +276,16 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   return g;
 }
 
-int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err) {
+int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err, const void* src,
+                 uint64_t src_bytes) {
   cudaStream_t s = e->stream;
   g->h_hdr[0] = n;
   g->h_hdr[1] = max_results;
   const uint64_t limit = e->skip_locate ? 0 : e->locate_limit;  // hits-only calls locate nothing anyway
   std::memcpy(g->h_hdr + 2, &limit, 8);
-  HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 16, cudaMemcpyHostToDevice, s), "batch header");
+  const uint64_t src_hdr[2] = {reinterpret_cast<uint64_t>(src), src ? src_bytes : 0};
+  std::memcpy(g->h_hdr + 4, src_hdr, 16);
+  HPG_CUDA(cudaMemcpyAsync(g->hdr, g->h_hdr, 32, cudaMemcpyHostToDevice, s), "batch header");
   HPG_CUDA(cudaGraphLaunch(g->exec, s), "graph launch");
   count_launches((unsigned)g->kernels);
   return 0;
@@ -535,6 +539,15 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
         staged_in = e->plans[i];
         pslot = i % kPlanSlots;
       }
+  // bases already in this device's memory are encoded where they are; host
+  // (or other devices') bases are copied into the plan's buffer
+  bool in_place = false;
+  if (!staged_in && total) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, seqs) == cudaSuccess)
+      in_place = at.type == cudaMemoryTypeDevice && at.device == e->device;
+    cudaGetLastError();
+  }
   for (int attempt = 0; attempt < 8; ++attempt) {
     GraphPlan* g = graph_plan_for(e, n, total, attempt ? &grow : nullptr, staged_in != nullptr, err, pslot);
     if (!g) return -1;
@@ -543,10 +556,11 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
       offs = g->offs;
       staged_in = g;
     }
-    if (total && seqs != g->seqs) HPG_CUDA(cudaMemcpyAsync(g->seqs, seqs, total, cudaMemcpyDefault, s), "reads");
+    if (total && seqs != g->seqs && !in_place)
+      HPG_CUDA(cudaMemcpyAsync(g->seqs, seqs, total, cudaMemcpyDefault, s), "reads");
     if (offs != g->offs)
       HPG_CUDA(cudaMemcpyAsync(g->offs, offs, ((size_t)n + 1) * 8, cudaMemcpyDefault, s), "read offsets");
-    if (graph_launch(e, g, n, max_results, err) != 0) return -1;
+    if (graph_launch(e, g, n, max_results, err, in_place ? seqs : nullptr, total) != 0) return -1;
     const int rc = graph_collect(e, g, n, &grow, out, err);
     if (rc < 0) return -1;
     if (rc == 0) return 0;

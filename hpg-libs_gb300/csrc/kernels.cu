@@ -30,11 +30,15 @@ inline unsigned grid_for(size_t n, int tpb) { return (unsigned)((n + tpb - 1) / 
 // is offs[n] (graph replays); the grid is then sized for the capacity.
 __global__ void encode_kernel(const uint8_t* __restrict__ ascii, uint64_t total, const uint64_t* __restrict__ offs,
                               uint32_t n_reads, const uint8_t* __restrict__ table, uint8_t* __restrict__ codes,
-                              uint8_t* __restrict__ ok, const uint32_t* n_dev) {
+                              uint8_t* __restrict__ ok, const uint32_t* n_dev, const uint64_t* src_dev) {
   if (n_dev) {
     n_reads = *n_dev;
     const uint64_t t = offs[n_reads];
     total = t < total ? t : total;
+  }
+  if (src_dev && src_dev[0]) {  // the caller's device buffer, read in place (no more than it holds)
+    ascii = reinterpret_cast<const uint8_t*>(src_dev[0]);
+    total = src_dev[1] < total ? src_dev[1] : total;
   }
   __shared__ uint8_t tab[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) tab[i] = table[i];
@@ -418,7 +422,7 @@ void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, u
   const uint64_t chunks = (total + 15) / 16;
   const unsigned grid = (unsigned)(chunks < 152ull * 32 * 8 ? (chunks + 255) / 256 : 152ull * 32);
   count_launches(1);
-  encode_kernel<<<grid, 256, 0, s>>>(ascii, total, offs, n_reads, d_table, codes, ok, nullptr);
+  encode_kernel<<<grid, 256, 0, s>>>(ascii, total, offs, n_reads, d_table, codes, ok, nullptr, nullptr);
 }
 
 namespace {
@@ -449,12 +453,13 @@ void launch_check_offsets(const uint64_t* offs, const uint32_t* n_dev, uint32_t 
 }
 
 void launch_encode_dev(const uint8_t* ascii, uint64_t bases_cap, const uint64_t* offs, const uint32_t* n_dev,
-                       uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s) {
+                       uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s,
+                       const uint64_t* src_dev) {
   cudaMemsetAsync(ok, 1, n_cap, s);
   const uint64_t chunks = (bases_cap + 15) / 16;
   const unsigned grid = (unsigned)(chunks < 152ull * 32 * 8 ? (chunks + 255) / 256 : 152ull * 32);
   count_launches(1);
-  encode_kernel<<<grid ? grid : 1, 256, 0, s>>>(ascii, bases_cap, offs, 0, d_table, codes, ok, n_dev);
+  encode_kernel<<<grid ? grid : 1, 256, 0, s>>>(ascii, bases_cap, offs, 0, d_table, codes, ok, n_dev, src_dev);
 }
 
 void launch_exact(const DevIndex& X, const uint8_t* codes, const uint64_t* offs, const uint8_t* ok, uint32_t r0,

@@ -29,9 +29,12 @@ void launch_encode(const uint8_t* ascii, uint64_t total, const uint64_t* offs, u
                    const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
 
 // Graph form of launch_encode: n_reads read from device memory, byte count
-// offs[n] (at most bases_cap), flags cleared over n_cap reads.
+// offs[n] (at most bases_cap), flags cleared over n_cap reads.  src_dev (device
+// memory: source pointer, source bytes) names where the bases are when its
+// pointer is not 0 (a caller's device buffer, read in place), else `ascii`.
 void launch_encode_dev(const uint8_t* ascii, uint64_t bases_cap, const uint64_t* offs, const uint32_t* n_dev,
-                       uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s);
+                       uint32_t n_cap, const uint8_t* d_table, uint8_t* codes, uint8_t* ok, cudaStream_t s,
+                       const uint64_t* src_dev = nullptr);
 
 // Graph form: reads whose offsets are decreasing, longer than 32767 bases or
 // past the staged bases get ok = 0 and set bit 8 of *status.
