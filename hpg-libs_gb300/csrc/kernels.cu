@@ -492,9 +492,9 @@ void launch_scan(const uint32_t* in, size_t n, uint64_t* out, uint64_t* part, cu
   }
   // tiles, plus one that only holds position n when n ends a tile
   const unsigned nb = (unsigned)(n / kScanTile + 1);
-  // up to 2048 tiles, each tile of the apply pass sums the tile sums before it
-  // (at most 4 loads a thread); more, and one block scans the tile sums first
-  const int direct = nb <= 2048;
+  // up to 4096 tiles, each tile of the apply pass sums the tile sums before it
+  // (at most 8 loads a thread); more, and one block scans the tile sums first
+  const int direct = nb <= 4096;
   count_launches(1);
   scan_reduce_kernel<<<nb, kScanTpb, 0, s>>>(in, n, part, n_dev);
   if (!direct) {
