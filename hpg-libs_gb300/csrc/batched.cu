@@ -812,11 +812,12 @@ __global__ void sort_truncate_kernel(PendingHit* __restrict__ sorted, const uint
 }
 
 // Lists longer than kLongList (low-complexity reads emit thousands of pending
-// hits), one list at a time per block: the rank of an entry is the number of
-// entries of its list with a smaller (key, position) pair, counted against
-// tiles of the list's keys in shared memory; entries ranked below the kept
-// count are written to `scratch` (the unsorted pending array, dead after the
-// scatter) at their rank and copied back.  O(m^2 / 512) per list of m entries.
+// hits), one list at a time per block.  Up to kRankTile entries: a bitonic
+// sort of the (key, position) pairs in shared memory, O(m log^2 m / 512).
+// Longer: the rank of an entry is the number of entries of its list with a
+// smaller pair, counted against tiles of the list's keys in shared memory,
+// O(m^2 / 512).  Entries placed below the kept count are written to `scratch`
+// (the unsorted pending array, dead after the scatter) and copied back.
 __global__ void __launch_bounds__(kRankTpb)
     sort_long_lists_kernel(PendingHit* __restrict__ sorted, PendingHit* __restrict__ scratch,
                            const uint64_t* __restrict__ seg_off, uint32_t n_rs, const uint32_t* __restrict__ kept,
@@ -848,6 +849,33 @@ __global__ void __launch_bounds__(kRankTpb)
       const uint32_t r = longs[q];
       const uint64_t b = seg_off[r];
       const uint32_t m = (uint32_t)(seg_off[r + 1] - b), keep = kept[r];
+      if (m <= kRankTile) {
+        // bitonic sort of (key, position) pairs in shared memory, padded to a power of two
+        uint32_t P = 64;
+        while (P < m) P <<= 1;
+        __syncthreads();  // the previous list's tile is no longer read
+        for (uint32_t t = threadIdx.x; t < P; t += kRankTpb)
+          tile[t] = t < m ? ((uint64_t)sorted[b + t].key << 32 | t) : ~0ull;
+        __syncthreads();
+        for (uint32_t k = 2; k <= P; k <<= 1) {
+          for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t t = threadIdx.x; t < P / 2; t += kRankTpb) {
+              const uint32_t i = ((t & ~(j - 1)) << 1) | (t & (j - 1)), q2 = i + j;
+              const uint64_t x = tile[i], y = tile[q2];
+              if ((x > y) == ((i & k) == 0)) {
+                tile[i] = y;
+                tile[q2] = x;
+              }
+            }
+            __syncthreads();
+          }
+        }
+        for (uint32_t t = threadIdx.x; t < keep; t += kRankTpb) scratch[b + t] = sorted[b + (uint32_t)tile[t]];
+        __syncthreads();  // every entry written before the copy back
+        for (uint32_t i = threadIdx.x; i < keep; i += kRankTpb) sorted[b + i] = scratch[b + i];
+        __syncthreads();  // the list is final before the next one reuses the tile
+        continue;
+      }
       for (uint32_t i0 = 0; i0 < m; i0 += kRankTpb) {
         const uint32_t i = i0 + threadIdx.x;
         const uint64_t mine = i < m ? ((uint64_t)sorted[b + i].key << 32 | i) : ~0ull;
@@ -870,31 +898,52 @@ __global__ void __launch_bounds__(kRankTpb)
   }
 }
 
+__device__ __forceinline__ void write_hit_record(const PendingHit& x, uint32_t rs, hpg_hit_t* __restrict__ hits,
+                                                 uint32_t* __restrict__ rows, uint64_t at) {
+  hpg_hit_t h;
+  h.read = rs >> 1;
+  h.strand = (uint8_t)(rs & 1u);
+  h.dir = (uint8_t)(x.meta & 1u);
+  h.nm = (uint8_t)((x.meta >> 1) & 1u);
+  h.err_kind = (uint8_t)((x.meta >> 2) & 3u);
+  h.err_base = (uint8_t)((x.meta >> 4) & 0xFFu);
+  h.pad0 = 0;
+  h.err_pos = (int16_t)(uint16_t)(x.meta >> 16);
+  h.pad1 = 0;
+  h.k = (int64_t)x.k;
+  h.l = (int64_t)x.l;
+  hits[at] = h;
+  rows[at] = x.k <= x.l ? x.l - x.k + 1 : 0u;
+}
+
+// A thread per (read, strand) list; with skip_long the lists of more than
+// kLongList pending hits are left to expand_long_hits_kernel.
 __global__ void expand_hits_kernel(const PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
                                    const uint64_t* __restrict__ hit_off, const uint32_t* __restrict__ kept,
                                    uint32_t n_rs, hpg_hit_t* __restrict__ hits, uint32_t* __restrict__ rows,
-                                   const unsigned* gate) {
+                                   const unsigned* gate, int skip_long) {
   const uint32_t rs = blockIdx.x * blockDim.x + threadIdx.x;
   if (rs >= n_rs) return;
   if (gate && *gate) return;
   const uint32_t m = kept[rs];
   const uint64_t b = seg_off[rs], o = hit_off[rs];
-  for (uint32_t i = 0; i < m; ++i) {
-    const PendingHit x = sorted[b + i];
-    hpg_hit_t h;
-    h.read = rs >> 1;
-    h.strand = (uint8_t)(rs & 1u);
-    h.dir = (uint8_t)(x.meta & 1u);
-    h.nm = (uint8_t)((x.meta >> 1) & 1u);
-    h.err_kind = (uint8_t)((x.meta >> 2) & 3u);
-    h.err_base = (uint8_t)((x.meta >> 4) & 0xFFu);
-    h.pad0 = 0;
-    h.err_pos = (int16_t)(uint16_t)(x.meta >> 16);
-    h.pad1 = 0;
-    h.k = (int64_t)x.k;
-    h.l = (int64_t)x.l;
-    hits[o + i] = h;
-    rows[o + i] = x.k <= x.l ? x.l - x.k + 1 : 0u;
+  if (skip_long && seg_off[rs + 1] - b > kLongList) return;
+  for (uint32_t i = 0; i < m; ++i) write_hit_record(sorted[b + i], rs, hits, rows, o + i);
+}
+
+// The long lists the short sort collected, a block per list.
+__global__ void expand_long_hits_kernel(const PendingHit* __restrict__ sorted, const uint64_t* __restrict__ seg_off,
+                                        const uint64_t* __restrict__ hit_off, const uint32_t* __restrict__ kept,
+                                        hpg_hit_t* __restrict__ hits, uint32_t* __restrict__ rows,
+                                        const unsigned* gate, const uint32_t* __restrict__ work,
+                                        const unsigned* n_work, uint32_t work_cap) {
+  if (gate && *gate) return;
+  const uint32_t n = min(*n_work, work_cap);
+  for (uint32_t q = blockIdx.x; q < n; q += gridDim.x) {
+    const uint32_t rs = work[q];
+    const uint32_t m = kept[rs];
+    const uint64_t b = seg_off[rs], o = hit_off[rs];
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) write_hit_record(sorted[b + i], rs, hits, rows, o + i);
   }
 }
 
@@ -1264,10 +1313,17 @@ void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_
 
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
                         const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
-                        const unsigned* gate) {
+                        const unsigned* gate, const uint32_t* longs, const unsigned* n_longs, uint32_t longs_cap,
+                        int num_sms) {
   if (!n_rs) return;
   count_launches(1);
-  expand_hits_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, hit_off, kept, n_rs, hits, rows, gate);
+  expand_hits_kernel<<<(n_rs + 255) / 256, 256, 0, s>>>(sorted, seg_off, hit_off, kept, n_rs, hits, rows, gate,
+                                                        longs ? 1 : 0);
+  if (longs) {
+    count_launches(1);
+    expand_long_hits_kernel<<<2 * num_sms, 256, 0, s>>>(sorted, seg_off, hit_off, kept, hits, rows, gate, longs,
+                                                        n_longs, longs_cap);
+  }
 }
 
 void launch_locate_persistent(const DevIndex& X, const hpg_hit_t* hits, const uint64_t* loc_off, uint32_t n_hits,

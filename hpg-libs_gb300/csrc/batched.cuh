@@ -176,9 +176,12 @@ void launch_sort_truncate(PendingHit* sorted, PendingHit* scratch, const uint64_
                           unsigned* n_longs = nullptr, uint32_t longs_cap = 0);
 // Room for the ids of the lists longer than kLongList entries among res_cap entries.
 size_t long_lists_cap(size_t res_cap);
+// With the long-list work list of launch_sort_truncate, those lists' records are
+// written a block per list.
 void launch_expand_hits(const PendingHit* sorted, const uint64_t* seg_off, const uint64_t* hit_off,
                         const uint32_t* kept, uint32_t n_rs, hpg_hit_t* hits, uint32_t* rows, cudaStream_t s,
-                        const unsigned* gate = nullptr);
+                        const unsigned* gate = nullptr, const uint32_t* longs = nullptr,
+                        const unsigned* n_longs = nullptr, uint32_t longs_cap = 0, int num_sms = 152);
 
 // Persistent locate: lanes pull rows from a counter and refill when their walk
 // ends.  In the graph form n_hits / n_locs are capacities and `z` the sizes.

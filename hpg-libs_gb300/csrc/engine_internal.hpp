@@ -128,6 +128,10 @@ struct Engine {
   cudaEvent_t pev[3][2];                    // per plan slot: inputs copied, replay done, results copied
   bool pev_made = false;
   double hits_per_read = 2.0, rows_per_read = 2.0;  // result sizing of pipelined calls (running estimate)
+  // Graph-plan pools per read of the capacity class, raised whenever a batch
+  // overflows one: a class whose first batch comes later starts at the rates
+  // earlier batches needed instead of overflowing (and rerunning) first.
+  double res_per_read = 4.0, spill_per_read = 0.0, locs_per_read = 8.0;
   size_t pipe_chunk = 0;  // reads per pipelined chunk: 0 automatic, SIZE_MAX never pipelined
   bool use_graph = true;
   bool skip_locate = false;  // batched form: hits only, no located rows

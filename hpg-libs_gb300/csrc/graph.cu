@@ -152,7 +152,8 @@ int capture(Engine* e, GraphPlan* g, std::string* err) {
   launch_sort_truncate(g->sorted, g->res, g->seg, (uint32_t)T, 0, g->kept, g->trunc, e->num_sms, s, g->hdr + 1,
                        status, g->longs, ctr + 14, (uint32_t)long_lists_cap(g->res_cap));
   launch_scan(g->kept, T, g->hit_off, g->part, s);
-  launch_expand_hits(g->sorted, g->seg, g->hit_off, g->kept, (uint32_t)T, g->hits, g->rows, s, status);
+  launch_expand_hits(g->sorted, g->seg, g->hit_off, g->kept, (uint32_t)T, g->hits, g->rows, s, status, g->longs,
+                     ctr + 14, (uint32_t)long_lists_cap(g->res_cap), e->num_sms);
   launch_limit_rows(g->hit_off, g->rows, (uint32_t)T, 0, reinterpret_cast<const uint64_t*>(g->hdr + 2), g->trunc, s,
                     status);
   launch_scan(g->rows, g->res_cap, g->loc_off, g->part, s, g->hit_off + T);  // over the hits found
@@ -224,10 +225,20 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   const int slot = log2_of(n_cap) * kPlanSlots + (pslot & 1);
   GraphPlan* g = e->plans[slot];
   const uint64_t bases_cap = pow2_at_least(total, n_cap * 128);
-  uint32_t res_cap = (uint32_t)std::min<uint64_t>(4 * n_cap + 4096, 0xFFFFFFF0u);
-  uint32_t spill_cap = (uint32_t)std::min<uint64_t>(
-      e->tuning.split ? 4 * n_cap + 4096 + (uint64_t)e->num_sms * 16 * 128 * 8 : n_cap / 4 + 4096, 0xFFFFFFF0u);
-  uint64_t locs_cap = std::min<uint64_t>(8 * n_cap + 4096, kMaxLocateRows);
+  // a plan captured now starts at the per-read rates earlier overflows showed; a
+  // plan that exists keeps its pools until a batch of its own overflows them (a
+  // recapture drains every stream, which a serving pipeline should not pay for
+  // a batch that fits)
+  const double nc = (double)n_cap;
+  const bool fresh = !g || !same_settings(g, e);
+  const double res_rate = fresh ? std::max(4.0, e->res_per_read) : 4.0;
+  const double locs_rate = fresh ? std::max(8.0, e->locs_per_read) : 8.0;
+  const double spill_rate = fresh ? e->spill_per_read : 0.0;
+  uint32_t res_cap = (uint32_t)std::min<double>(res_rate * nc + 4096, 0xFFFFFFF0u);
+  uint32_t spill_cap = (uint32_t)std::min<double>(
+      std::max(spill_rate * nc, e->tuning.split ? 4 * nc + 4096 + (double)e->num_sms * 16 * 128 * 8 : nc / 4 + 4096),
+      0xFFFFFFF0u);
+  uint64_t locs_cap = (uint64_t)std::min<double>(locs_rate * nc + 4096, kMaxLocateRows);
   if (g) {  // keep what earlier batches of this class needed
     res_cap = std::max(res_cap, g->res_cap);
     spill_cap = std::max(spill_cap, g->spill_cap);
@@ -304,6 +315,11 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
     return -1;
   }
   if (status) {
+    // the rates this batch needed, with room, for every capacity class from now on
+    const double nr = std::max<double>(n, 1.0);
+    if (status & kStatusResFull) e->res_per_read = std::max(e->res_per_read, 1.5 * (double)(h[0] >> 32) / nr);
+    if (status & kStatusSpillFull) e->spill_per_read = std::max(e->spill_per_read, 1.5 * (double)h[1] / nr);
+    if (status & kStatusLocFull) e->locs_per_read = std::max(e->locs_per_read, 1.25 * (double)h[3] / nr);
     grow->res_cap = g->res_cap;
     grow->spill_cap = g->spill_cap;
     grow->locs_cap = g->locs_cap;
