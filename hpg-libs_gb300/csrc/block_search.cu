@@ -412,7 +412,59 @@ struct PartState {
   uint8_t* refused;               // a list of the block refused a result
   uint8_t* aflag;                 // put_anchor / block-0 match bits
   hpg_block_anchor_t* anchor;     // the block's anchor
+  // results past the slots (tail pass): chunks of kOvfChunk, chained per block
+  uint8_t* lost;                  // the pool ran out for this block: it runs again
+  uint32_t* ovf_head;             // the block's first chunk
+  uint32_t* ovf_next;             // the chunk after each chunk
+  hpg_hit_t* ovf_hits;
+  uint32_t* ovf_ctr;              // chunks handed out
+  uint32_t ovf_cap;               // chunks in the pool
 };
+
+constexpr uint32_t kOvfChunk = 32;
+
+// emit() in the tail pass: results past the block's slots go to chunks of the
+// overflow pool (one atomic per chunk), so that the pack pass can place them
+// and the block need not run again; when the pool runs out the block is marked
+// lost and the retry pass runs it into its final range as before.
+__device__ __forceinline__ bool emit_tail(ItemOut& o, const PartState& ps, uint32_t it, uint32_t& chunk, bool& lost,
+                                          uint32_t dir, uint32_t nm, uint32_t kind, uint32_t base, int pos,
+                                          uint32_t k, uint32_t l) {
+  if (o.n >= o.cap) {
+    o.refused = true;
+    return false;
+  }
+  hpg_hit_t h;
+  h.read = o.read;
+  h.strand = (uint8_t)o.strand;
+  h.dir = (uint8_t)dir;
+  h.nm = (uint8_t)nm;
+  h.err_kind = (uint8_t)(nm ? kind : 0);
+  h.err_base = (uint8_t)(nm ? base : 0);
+  h.pad0 = 0;
+  h.err_pos = (int16_t)(nm ? pos : 0);
+  h.pad1 = 0;
+  h.k = k;
+  h.l = l;
+  if (o.n < kBlockSlots) {
+    o.slot[o.n] = h;
+  } else if (!lost) {
+    const uint32_t j = o.n - kBlockSlots, off = j % kOvfChunk;
+    if (off == 0) {
+      const uint32_t nc = atomicAdd(ps.ovf_ctr, 1u);
+      if (nc >= ps.ovf_cap) {
+        lost = true;
+      } else {
+        if (j == 0) ps.ovf_head[it] = nc;
+        else ps.ovf_next[chunk] = nc;
+        chunk = nc;
+      }
+    }
+    if (!lost) ps.ovf_hits[(uint64_t)chunk * kOvfChunk + off] = h;
+  }
+  ++o.n;
+  return true;
+}
 
 // Head pass over physical direction `phys`: thread g runs the head of the
 // block of its list that is on that direction (the '+' lists in the first half
@@ -468,33 +520,307 @@ __global__ void __launch_bounds__(kBlockTpb) block_head_kernel(
   }
 }
 
-// Tail pass over the queued blocks of one direction (the launch covers the
-// largest queue; threads past its length return): every lane starts a block
-// whose fragment matched.
+// BWExactFinalResult{Forward,Backward}'s block rule (search.h:67-155) at the
+// start position of an extension, for block 0 (part 0, forward) or the last
+// block (part 1, backward); C division truncates toward zero (pos may be -1).
+__device__ __forceinline__ bool ext_rule_ok(uint32_t part, int pos, int end, int bs) {
+  const int cb = pos / bs;
+  if (part == 0) {
+    if (!(cb > 0 || pos == end + 1)) {
+      if (cb < 0) return false;
+      if (pos % bs == 0) return false;
+    }
+  } else {
+    if (!(cb < 0 || pos == -1)) {
+      if (cb > 0) return false;
+      if ((pos + 1) % bs == 0) return false;
+    }
+  }
+  return true;
+}
+
+// Lane modes of the persistent tail.  The first four make one backward-
+// extension step per loop iteration; the others are transitions between them.
+enum : uint32_t {
+  kFirst = 0,   // first walk (restarts and branch points), position i
+  kSecond,      // second walk, position i, up to the last branch point
+  kExt,         // an extension of a branch (ekind) to the read's end, position ei
+  kCStep,       // the branch point's step with base c
+  kIdle,        // claim the next queued block
+  kFirstEnd,    // the first walk is over
+  kExtStart,    // check the block rule and range of an extension starting at ei
+  kExtDone,     // an extension ended (esurv: it reached the read's end)
+  kCNext,       // the next base of the branch point
+  kBranchDone,  // the branch point's extensions are all done
+  kFinish       // write the block's counts
+};
+enum : uint32_t { kExtDel = 0, kExtIns, kExtMis };
+
+// Tail pass over the queued blocks of one direction, persistent: lane g takes
+// the queued blocks g, g + G, g + 2G, ... (G lanes in the grid; no claim
+// counter, whose atomics serialised on one address when lanes finished blocks
+// one by one), runs each as a machine that takes one step per loop iteration
+// whatever part of the block it is in (first walk, second walk, a branch
+// point's base step or an extension), and starts the next when it is done, so
+// a warp's lanes keep stepping together instead of waiting for the block with
+// the most branches.  Same walks, branches, order and results as block_tail
+// (which the retry pass runs).
 template <bool C>
 __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint4* __restrict__ queue,
     const uint32_t* __restrict__ n_queue, uint32_t max_results, PartState ps, unsigned long long* census) {
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= *n_queue) return;
-  const uint4 q = queue[g];
-  const uint32_t it = q.x, list = it >> 1, part = it & 1u;
-  const uint32_t read = list >> 1, strand = list & 1u;
-  const uint64_t b0 = offs[read];
-  const int len = (int)(offs[read + 1] - b0);
+  const uint32_t nq = *n_queue;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  uint32_t next = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint8_t* W = nullptr;
+  View v{0, 0};
+  int end = 0, frag = 30, dstep = 1;
+  uint32_t it = 0, part = 0;
   ItemOut o;
-  o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+  o.slot = nullptr;
   o.room = kBlockSlots;
   o.cap = max_results;
   o.n = 0;
-  o.read = read;
-  o.strand = strand;
+  o.read = 0;
+  o.strand = 0;
   o.refused = false;
   o.sectors = 0;
-  block_tail<C>(X, codes + b0, len, strand, (int)part, o, q.y, q.z);
-  ps.count[it] = o.n;
-  ps.refused[it] = o.refused ? 1 : 0;
-  if (C) atomicAdd(census, (unsigned long long)o.sectors);
+  uint32_t lane_sectors = 0;
+  uint32_t mode = kIdle;
+  int i = 0, to = 0;
+  uint32_t a = 0, b = 0, k0 = 0, l0 = 0;
+  uint32_t fk = 0, fl = 0, z = 0, changes = 0, left = 0;
+  bool alive = false, failed_step = false, ok_before = false, ok_at = false;
+  uint32_t na = 0, nb = 0;
+  bool sw_failed = false;
+  int bp = 0;
+  uint32_t pk = 0, pl = 0, c = 0, wp = 0, rk = 0, rl = 0;
+  uint32_t ekind = 0, ea = 0, eb = 0;
+  int ei = 0;
+  bool esurv = false;
+  uint32_t chunk = 0;  // the block's current overflow chunk
+  bool lost = false;
+  for (;;) {
+    // transitions until the lane needs a step
+    bool quit = false;
+    while (mode >= kIdle) {
+      if (mode == kIdle) {
+        if (next >= nq) {
+          quit = true;
+          break;
+        }
+        const uint4 q = queue[next];
+        next += stride;
+        it = q.x;
+        const uint32_t list = it >> 1;
+        part = it & 1u;
+        const uint32_t read = list >> 1, strand = list & 1u;
+        const uint64_t b0 = offs[read];
+        const int len = (int)(offs[read + 1] - b0);
+        W = codes + b0;
+        frag = 30;
+        fragments_of(len, frag);
+        end = len - 1;
+        v = part == 0 ? forward_view(strand) : backward_view(strand);
+        dstep = part == 0 ? 1 : -1;
+        o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+        o.n = 0;
+        o.read = read;
+        o.strand = strand;
+        o.refused = false;
+        o.sectors = 0;
+        lost = false;
+        k0 = q.y;
+        l0 = q.z;
+        a = k0;
+        b = l0;
+        fk = k0;
+        fl = l0;
+        z = 0;
+        changes = 0;
+        alive = true;
+        failed_step = false;
+        // part 0: the rest of the read after block 0; part 1: block 0 from above
+        i = part == 0 ? frag : frag - 1;
+        to = part == 0 ? end : 0;
+        mode = kFirst;
+      } else if (mode == kFirstEnd) {
+        const uint32_t zt = z & 255u;
+        const bool bound_before = zt <= 1u, bound_at = ((zt - 1u) & 255u) <= 1u;
+        const uint32_t points = (bound_before ? changes : 0u) + (failed_step && bound_at ? 1u : 0u);
+        mode = kFinish;
+        if (points > o.cap) {
+          o.refused = true;  // rl_next overflows: the block's branches are dropped
+        } else if (part == 0 && alive && !emit_tail(o, ps, it, chunk, lost, 1, 0, 0, 0, 0, fk, fl)) {
+          // the complete result of block 0 was refused
+        } else if (points) {
+          ok_before = bound_before;
+          ok_at = bound_at;
+          left = points;
+          a = k0;
+          b = l0;
+          i = part == 0 ? frag : frag - 1;
+          mode = kSecond;
+        }
+      } else if (mode == kExtStart) {
+        if (!ext_rule_ok(part, ei, end, frag)) {
+          esurv = false;
+          mode = kExtDone;
+        } else if (part == 0 ? ei > end : ei < 0) {  // nothing left to walk
+          esurv = true;
+          mode = kExtDone;
+        } else {
+          mode = kExt;
+        }
+      } else if (mode == kExtDone) {
+        const uint32_t dir = part == 0 ? 1u : 0u;
+        if (ekind == kExtDel) {
+          if (esurv && !emit_tail(o, ps, it, chunk, lost, dir, 1, HPG_BWT_DELETION, 0xFF, bp, ea, eb)) {
+            mode = kFinish;
+          } else {
+            c = 0;
+            mode = kCNext;
+          }
+        } else if (ekind == kExtIns) {
+          if (esurv && !emit_tail(o, ps, it, chunk, lost, dir, 1, HPG_BWT_INSERTION, c, bp, ea, eb)) {
+            mode = kFinish;
+          } else {
+            if (esurv) {  // the mismatch starts from the interval the insertion reached
+              rk = ea;
+              rl = eb;
+            }
+            ekind = kExtMis;
+            ei = bp + dstep;
+            ea = rk;
+            eb = rl;
+            mode = kExtStart;
+          }
+        } else {
+          if (esurv && !emit_tail(o, ps, it, chunk, lost, dir, 1, HPG_BWT_MISMATCH, c, bp, ea, eb)) {
+            mode = kFinish;
+          } else {
+            ++c;
+            mode = kCNext;
+          }
+        }
+      } else if (mode == kCNext) {
+        while (c < 4 && c == wp) {  // the read's own base: the reference's step whose result it drops
+          if (C) o.sectors += (pk >> 6) == (pl >> 6) ? 1u : 2u;
+          ++c;
+        }
+        mode = c < 4 ? kCStep : kBranchDone;
+      } else if (mode == kBranchDone) {
+        mode = kFinish;
+        if (--left != 0 && !sw_failed) {
+          a = na;
+          b = nb;
+          i += dstep;
+          if (part == 0 ? i <= end : i >= 0) mode = kSecond;
+        }
+      } else {  // kFinish
+        ps.count[it] = o.n;
+        ps.refused[it] = o.refused ? 1 : 0;
+        ps.lost[it] = lost ? 1 : 0;
+        if (C) lane_sectors += o.sectors;
+        mode = kIdle;
+      }
+    }
+    if (quit) break;
+    // one step
+    uint32_t sym, x, y;
+    if (mode == kExt) {
+      sym = W[ei];
+      x = ea;
+      y = eb;
+    } else if (mode == kCStep) {
+      sym = c;
+      x = pk;
+      y = pl;
+    } else {
+      sym = W[i];
+      x = a;
+      y = b;
+    }
+    step<C>(X, v, sym, x, y, o.sectors);
+    if (mode == kFirst) {
+      const int64_t before = (int64_t)b - (int64_t)a;
+      if (alive) {
+        if (x > y) {
+          alive = false;
+          failed_step = true;  // the step that empties the interval changes its size
+        } else {
+          if ((int64_t)y - (int64_t)x != before) ++changes;
+          fk = x;
+          fl = y;
+        }
+      }
+      bool over = false;
+      if (x > y) {
+        a = 0;
+        b = X.top;
+        ++z;
+        // three restarts with too few steps left for the byte count to wrap: D
+        // allows no error anywhere in the range, so there is no branch point
+        if (z >= 3 && z + (uint32_t)(dstep > 0 ? to - i : i - to) < 256) over = true;
+      } else {
+        a = x;
+        b = y;
+      }
+      i += dstep;
+      if (over || i == to + dstep) mode = kFirstEnd;
+    } else if (mode == kSecond) {
+      const bool failed = x > y;
+      const bool changed = failed || (int64_t)y - (int64_t)x != (int64_t)b - (int64_t)a;
+      if (changed && (failed ? ok_at : ok_before)) {  // a branch point: its extensions, then on
+        na = x;
+        nb = y;
+        sw_failed = failed;
+        bp = i;
+        pk = a;
+        pl = b;
+        wp = W[i];
+        ekind = kExtDel;
+        ei = i + dstep;
+        ea = a;
+        eb = b;
+        mode = kExtStart;
+      } else if (failed) {
+        mode = kFinish;
+      } else {
+        a = x;
+        b = y;
+        i += dstep;
+        if (part == 0 ? i > end : i < 0) mode = kFinish;
+      }
+    } else if (mode == kExt) {
+      if (x > y) {
+        esurv = false;
+        mode = kExtDone;
+      } else {
+        ea = x;
+        eb = y;
+        ei += dstep;
+        if (part == 0 ? ei > end : ei < 0) {
+          esurv = true;
+          mode = kExtDone;
+        }
+      }
+    } else {  // kCStep
+      if (x > y) {
+        ++c;
+        mode = kCNext;
+      } else {
+        rk = x;
+        rl = y;
+        ekind = kExtIns;
+        ei = bp;
+        ea = x;
+        eb = y;
+        mode = kExtStart;
+      }
+    }
+  }
+  if (C) atomicAdd(census, (unsigned long long)lane_sectors);
 }
 
 // Retry: block items[g] = 2 * list + part, whose results did not fit its
@@ -543,8 +869,8 @@ __global__ void block_merge_kernel(PartState ps, uint32_t n_lists, uint32_t max_
   const uint32_t room1 = max_results - n0;
   const uint32_t m1 = n1 < room1 ? n1 : room1;
   count[t] = n0 + m1;
-  if (n0 > kBlockSlots) retry[atomicAdd(n_retry, 1u)] = 2 * t;
-  if (m1 > kBlockSlots) retry[atomicAdd(n_retry, 1u)] = 2 * t + 1;
+  if (n0 > kBlockSlots && ps.lost[2 * t]) retry[atomicAdd(n_retry, 1u)] = 2 * t;
+  if (m1 > kBlockSlots && ps.lost[2 * t + 1]) retry[atomicAdd(n_retry, 1u)] = 2 * t + 1;
   refused[t] = (ps.refused[2 * t] | ps.refused[2 * t + 1] | (n1 > room1 ? 1 : 0)) ? 1 : 0;
   const uint32_t f0 = ps.aflag[2 * t], f1 = ps.aflag[2 * t + 1];
   uint32_t na = 0;
@@ -561,10 +887,20 @@ __global__ void block_pack_kernel(PartState ps, const uint64_t* __restrict__ off
   const uint32_t n0 = ps.count[2 * t], n1 = ps.count[2 * t + 1];
   const uint32_t room1 = max_results - n0;
   const uint32_t m1 = n1 < room1 ? n1 : room1;
-  const uint32_t c0 = n0 < kBlockSlots ? n0 : kBlockSlots, c1 = m1 < kBlockSlots ? m1 : kBlockSlots;
   hpg_hit_t* dst = out + off[t];
-  for (uint32_t j = 0; j < c0; ++j) dst[j] = ps.slots[(2ull * t) * kBlockSlots + j];
-  for (uint32_t j = 0; j < c1; ++j) dst[n0 + j] = ps.slots[(2ull * t + 1) * kBlockSlots + j];
+  for (uint32_t part = 0; part < 2; ++part) {  // a lost block's range is written by the retry pass
+    const uint32_t b = 2 * t + part, m = part ? m1 : n0;
+    hpg_hit_t* d = dst + (part ? n0 : 0u);
+    const uint32_t c = m < kBlockSlots ? m : kBlockSlots;
+    for (uint32_t j = 0; j < c; ++j) d[j] = ps.slots[(uint64_t)b * kBlockSlots + j];
+    if (m <= kBlockSlots || ps.lost[b]) continue;
+    uint32_t ch = ps.ovf_head[b];
+    for (uint32_t j = kBlockSlots; j < m; ++j) {
+      const uint32_t o = (j - kBlockSlots) % kOvfChunk;
+      if (o == 0 && j > kBlockSlots) ch = ps.ovf_next[ch];
+      d[j] = ps.ovf_hits[(uint64_t)ch * kOvfChunk + o];
+    }
+  }
 }
 
 // Rows of each hit for the locate pass: l - k + 1, or 0 for every hit of a
@@ -622,7 +958,7 @@ unsigned grid_of(size_t n) { return (unsigned)((n + kBlockTpb - 1) / kBlockTpb);
 int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* total_out, std::string* err) {
   const size_t T = 2 * n, P = 4 * n;
   if (!ensure(e, e->b_res, P * kBlockSlots * sizeof(hpg_hit_t) + 16) || !ensure(e, e->b_arr, P * 4 + 16) ||
-      !ensure(e, e->b_sorted, 2 * P + 16) || !ensure(e, e->b_seg, P * sizeof(hpg_block_anchor_t) + 16) ||
+      !ensure(e, e->b_sorted, 3 * P + 16) || !ensure(e, e->b_seg, P * sizeof(hpg_block_anchor_t) + 16) ||
       !ensure(e, e->rs_count, T * 4 + 16) || !ensure(e, e->rs_trunc, T + 16) || !ensure(e, e->hit_off, (T + 1) * 8) ||
       !ensure(e, e->scan_part, scan_parts(T) * 8) || !ensure(e, e->vecs, 2 * T * sizeof(hpg_block_anchor_t) + 16) ||
       !ensure(e, e->ovf, T + 16) || !ensure(e, e->census, 16) || !ensure(e, e->rows, P * 4 + 16) ||
@@ -637,9 +973,23 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   ps.refused = ptr<uint8_t>(e->b_sorted);
   ps.aflag = ps.refused + P;
   ps.anchor = ptr<hpg_block_anchor_t>(e->b_seg);
+  ps.lost = ps.refused + 2 * P;
+  // overflow pool: four results a read in chunks, heads per block, a chunk chain
+  const uint32_t ovf_cap = (uint32_t)std::min<size_t>(n / 8 + 1024, 0x7FFFFFFFu);
+  const size_t ovf_bytes = (size_t)ovf_cap * (kOvfChunk * sizeof(hpg_hit_t) + 4) + P * 4 + 64;
+  if (!ensure(e, e->b_bovf, ovf_bytes)) {
+    *err = oom_message("block search overflow pool", ovf_bytes);
+    return -1;
+  }
+  ps.ovf_hits = ptr<hpg_hit_t>(e->b_bovf);
+  ps.ovf_next = reinterpret_cast<uint32_t*>(ps.ovf_hits + (size_t)ovf_cap * kOvfChunk);
+  ps.ovf_head = ps.ovf_next + ovf_cap;
+  ps.ovf_ctr = ptr<uint32_t>(e->b_ctr) + 14;
+  ps.ovf_cap = ovf_cap;
   uint32_t* n_retry = ptr<uint32_t>(e->b_ctr) + 12;
   cudaMemsetAsync(ps.count, 0, P * 4, s);
-  cudaMemsetAsync(ps.refused, 0, 2 * P, s);
+  cudaMemsetAsync(ps.refused, 0, 3 * P, s);
+  cudaMemsetAsync(ps.ovf_ctr, 0, 4, s);
   cudaMemsetAsync(n_retry, 0, 4, s);
   uint32_t* d_count = ptr<uint32_t>(e->rs_count);
   uint64_t* d_off = ptr<uint64_t>(e->hit_off);
@@ -650,6 +1000,13 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   const uint8_t* ok = ptr<uint8_t>(e->ok);
   uint4* queue = ptr<uint4>(e->b_spill);
   uint32_t* n_queue = ptr<uint32_t>(e->b_ctr) + 13;
+  // the tail is persistent: as many blocks as fit, at most one lane per list
+  int per_sm = 0;
+  if (census)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, block_tail_kernel<true>, kBlockTpb, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, block_tail_kernel<false>, kBlockTpb, 0);
+  const unsigned tail_grid = std::max(1u, std::min(grid_of(T), (unsigned)(std::max(per_sm, 1) * e->num_sms)));
   cudaEventRecord(e->cev[0], s);
   for (uint32_t phys = 0; phys < 2; ++phys) {  // one head and one tail launch per index direction
     cudaMemsetAsync(n_queue, 0, 4, s);
@@ -657,13 +1014,13 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
     if (census) {
       block_head_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys, max_results,
                                                                ps, queue, n_queue, census);
-      block_tail_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
-                                                               census);
+      block_tail_kernel<true><<<tail_grid, kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
+                                                              census);
     } else {
       block_head_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys,
                                                                 max_results, ps, queue, n_queue, nullptr);
-      block_tail_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
-                                                                nullptr);
+      block_tail_kernel<false><<<tail_grid, kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
+                                                               nullptr);
     }
   }
   cudaEventRecord(e->cev[1], s);

@@ -258,7 +258,8 @@ void engine_destroy(Engine* e) {
   DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
                     &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
                     &e->census, &e->b_ctr, &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg,
-                    &e->b_rowhit};
+                    &e->b_rowhit, &e->b_long, &e->b_blocks, &e->b_bovf, &e->m_hitoff, &e->m_part, &e->m_offs,
+                    &e->m_rows, &e->m_pflag, &e->m_rowoff, &e->m_nrec, &e->m_flags, &e->m_rec};
   for (DevBuf* b : bufs) cudaFree(b->p);
   for (int i = 0; i <= kStageCount; ++i)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);

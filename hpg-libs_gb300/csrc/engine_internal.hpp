@@ -106,6 +106,7 @@ struct Engine {
       loc_off, locs, census;
   // batched form
   DevBuf b_ctr, b_res, b_sorted, b_spill, b_arr, b_seg, b_rowhit, b_long, b_blocks;
+  DevBuf b_bovf;  // block search: results past a block's slots, in chunks
   // alignment-list records (map_device.cu)
   DevBuf m_hitoff, m_part, m_offs, m_rows, m_pflag, m_rowoff, m_nrec, m_flags, m_rec;
   double map_device_s = 0;  // wall time of the last alignment-list call's device pass
