@@ -435,8 +435,8 @@ __device__ __forceinline__ bool emit_tail(ItemOut& o, const PartState& ps, uint3
     return false;
   }
   hpg_hit_t h;
-  h.read = o.read;
-  h.strand = (uint8_t)o.strand;
+  h.read = it >> 2;  // it = 2 * (2 * read + strand) + part
+  h.strand = (uint8_t)((it >> 1) & 1u);
   h.dir = (uint8_t)dir;
   h.nm = (uint8_t)nm;
   h.err_kind = (uint8_t)(nm ? kind : 0);
@@ -572,10 +572,12 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
   const uint32_t nq = *n_queue;
   const uint32_t stride = gridDim.x * blockDim.x;
   uint32_t next = blockIdx.x * blockDim.x + threadIdx.x;
+  // (register pressure: the block's part, strand and read come from `it`; the
+  // interval before a branch point's step lives in a, b while the branch runs)
   const uint8_t* W = nullptr;
   View v{0, 0};
-  int end = 0, frag = 30, dstep = 1;
-  uint32_t it = 0, part = 0;
+  int end = 0, frag = 30;
+  uint32_t it = 0;
   ItemOut o;
   o.slot = nullptr;
   o.room = kBlockSlots;
@@ -587,14 +589,14 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
   o.sectors = 0;
   uint32_t lane_sectors = 0;
   uint32_t mode = kIdle;
-  int i = 0, to = 0;
+  int i = 0;
   uint32_t a = 0, b = 0, k0 = 0, l0 = 0;
-  uint32_t fk = 0, fl = 0, z = 0, changes = 0, left = 0;
+  uint32_t z = 0, changes = 0, left = 0;
   bool alive = false, failed_step = false, ok_before = false, ok_at = false;
   uint32_t na = 0, nb = 0;
   bool sw_failed = false;
   int bp = 0;
-  uint32_t pk = 0, pl = 0, c = 0, wp = 0, rk = 0, rl = 0;
+  uint32_t c = 0, wp = 0, rk = 0, rl = 0;
   uint32_t ekind = 0, ea = 0, eb = 0;
   int ei = 0;
   bool esurv = false;
@@ -612,8 +614,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         const uint4 q = queue[next];
         next += stride;
         it = q.x;
-        const uint32_t list = it >> 1;
-        part = it & 1u;
+        const uint32_t list = it >> 1, part = it & 1u;
         const uint32_t read = list >> 1, strand = list & 1u;
         const uint64_t b0 = offs[read];
         const int len = (int)(offs[read + 1] - b0);
@@ -622,11 +623,8 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         fragments_of(len, frag);
         end = len - 1;
         v = part == 0 ? forward_view(strand) : backward_view(strand);
-        dstep = part == 0 ? 1 : -1;
         o.slot = ps.slots + (uint64_t)it * kBlockSlots;
         o.n = 0;
-        o.read = read;
-        o.strand = strand;
         o.refused = false;
         o.sectors = 0;
         lost = false;
@@ -634,15 +632,12 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         l0 = q.z;
         a = k0;
         b = l0;
-        fk = k0;
-        fl = l0;
         z = 0;
         changes = 0;
         alive = true;
         failed_step = false;
         // part 0: the rest of the read after block 0; part 1: block 0 from above
         i = part == 0 ? frag : frag - 1;
-        to = part == 0 ? end : 0;
         mode = kFirst;
       } else if (mode == kFirstEnd) {
         const uint32_t zt = z & 255u;
@@ -651,29 +646,30 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         mode = kFinish;
         if (points > o.cap) {
           o.refused = true;  // rl_next overflows: the block's branches are dropped
-        } else if (part == 0 && alive && !emit_tail(o, ps, it, chunk, lost, 1, 0, 0, 0, 0, fk, fl)) {
-          // the complete result of block 0 was refused
+        } else if ((it & 1u) == 0 && alive && !emit_tail(o, ps, it, chunk, lost, 1, 0, 0, 0, 0, a, b)) {
+          // the complete result of block 0 was refused (a walk that stayed alive
+          // never restarted: a, b is its last interval)
         } else if (points) {
           ok_before = bound_before;
           ok_at = bound_at;
           left = points;
           a = k0;
           b = l0;
-          i = part == 0 ? frag : frag - 1;
+          i = (it & 1u) == 0 ? frag : frag - 1;
           mode = kSecond;
         }
       } else if (mode == kExtStart) {
-        if (!ext_rule_ok(part, ei, end, frag)) {
+        if (!ext_rule_ok(it & 1u, ei, end, frag)) {
           esurv = false;
           mode = kExtDone;
-        } else if (part == 0 ? ei > end : ei < 0) {  // nothing left to walk
+        } else if ((it & 1u) == 0 ? ei > end : ei < 0) {  // nothing left to walk
           esurv = true;
           mode = kExtDone;
         } else {
           mode = kExt;
         }
       } else if (mode == kExtDone) {
-        const uint32_t dir = part == 0 ? 1u : 0u;
+        const uint32_t dir = (it & 1u) == 0 ? 1u : 0u;
         if (ekind == kExtDel) {
           if (esurv && !emit_tail(o, ps, it, chunk, lost, dir, 1, HPG_BWT_DELETION, 0xFF, bp, ea, eb)) {
             mode = kFinish;
@@ -690,7 +686,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
               rl = eb;
             }
             ekind = kExtMis;
-            ei = bp + dstep;
+            ei = bp + ((it & 1u) == 0 ? 1 : -1);
             ea = rk;
             eb = rl;
             mode = kExtStart;
@@ -705,7 +701,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         }
       } else if (mode == kCNext) {
         while (c < 4 && c == wp) {  // the read's own base: the reference's step whose result it drops
-          if (C) o.sectors += (pk >> 6) == (pl >> 6) ? 1u : 2u;
+          if (C) o.sectors += (a >> 6) == (b >> 6) ? 1u : 2u;
           ++c;
         }
         mode = c < 4 ? kCStep : kBranchDone;
@@ -714,8 +710,8 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         if (--left != 0 && !sw_failed) {
           a = na;
           b = nb;
-          i += dstep;
-          if (part == 0 ? i <= end : i >= 0) mode = kSecond;
+          i += (it & 1u) == 0 ? 1 : -1;
+          if ((it & 1u) == 0 ? i <= end : i >= 0) mode = kSecond;
         }
       } else {  // kFinish
         ps.count[it] = o.n;
@@ -732,26 +728,25 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
       sym = W[ei];
       x = ea;
       y = eb;
-    } else if (mode == kCStep) {
+    } else if (mode == kCStep) {  // a, b: the interval before the branch point's step
       sym = c;
-      x = pk;
-      y = pl;
+      x = a;
+      y = b;
     } else {
       sym = W[i];
       x = a;
       y = b;
     }
     step<C>(X, v, sym, x, y, o.sectors);
+    const int dstep = (it & 1u) == 0 ? 1 : -1;
     if (mode == kFirst) {
       const int64_t before = (int64_t)b - (int64_t)a;
       if (alive) {
         if (x > y) {
           alive = false;
           failed_step = true;  // the step that empties the interval changes its size
-        } else {
-          if ((int64_t)y - (int64_t)x != before) ++changes;
-          fk = x;
-          fl = y;
+        } else if ((int64_t)y - (int64_t)x != before) {
+          ++changes;
         }
       }
       bool over = false;
@@ -761,13 +756,13 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         ++z;
         // three restarts with too few steps left for the byte count to wrap: D
         // allows no error anywhere in the range, so there is no branch point
-        if (z >= 3 && z + (uint32_t)(dstep > 0 ? to - i : i - to) < 256) over = true;
+        if (z >= 3 && z + (uint32_t)(dstep > 0 ? end - i : i) < 256) over = true;
       } else {
         a = x;
         b = y;
       }
       i += dstep;
-      if (over || i == to + dstep) mode = kFirstEnd;
+      if (over || (dstep > 0 ? i > end : i < 0)) mode = kFirstEnd;
     } else if (mode == kSecond) {
       const bool failed = x > y;
       const bool changed = failed || (int64_t)y - (int64_t)x != (int64_t)b - (int64_t)a;
@@ -775,9 +770,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         na = x;
         nb = y;
         sw_failed = failed;
-        bp = i;
-        pk = a;
-        pl = b;
+        bp = i;  // a, b stay the interval before the step for the branch
         wp = W[i];
         ekind = kExtDel;
         ei = i + dstep;
@@ -790,7 +783,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         a = x;
         b = y;
         i += dstep;
-        if (part == 0 ? i > end : i < 0) mode = kFinish;
+        if (dstep > 0 ? i > end : i < 0) mode = kFinish;
       }
     } else if (mode == kExt) {
       if (x > y) {
@@ -800,7 +793,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         ea = x;
         eb = y;
         ei += dstep;
-        if (part == 0 ? ei > end : ei < 0) {
+        if (dstep > 0 ? ei > end : ei < 0) {
           esurv = true;
           mode = kExtDone;
         }
