@@ -280,6 +280,29 @@ __device__ __forceinline__ View forward_view(uint32_t strand) { return strand ? 
 // the block goes on (its fragment matched and the lists have room).  aflag
 // bit 0: the anchor was set; bit 1: the block-0 fragment matched (with lists
 // of capacity 0 BWSearchCPU then returns before the last block).
+// The first L steps of an exact search from the full interval over view v, W[from],
+// W[from + dir], ..., by one lookup in the start table (L = X.kmer_len, the
+// table's entries already hold the interval after those steps); true with
+// k, l set when that interval is not empty, else the caller steps from the
+// start (it needs the position where the search failed).  Not in the census
+// instance, whose count stays that of the reference's steps.
+template <bool C>
+__device__ __forceinline__ bool start_lookup(const DevIndex& X, View v, const uint8_t* W, int from, int dir, int steps,
+                                             uint32_t& k, uint32_t& l) {
+  const uint32_t L = X.kmer_len;
+  if (C || L == 0 || steps < (int)L) return false;
+  uint32_t code = 0;
+  for (uint32_t j = 0; j < L; ++j) {
+    const uint32_t b = W[from + dir * (int)j];
+    code = (code << 2) | (v.comp ? sel4(X.comp, b) : b);
+  }
+  const uint2 t = __ldg((v.d ? X.kmer[1] : X.kmer[0]) + code);
+  if (t.x > t.y) return false;
+  k = t.x;
+  l = t.y;
+  return true;
+}
+
 template <bool C>
 __device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
                            hpg_block_anchor_t* anchor, uint32_t& aflag, uint32_t& k, uint32_t& l) {
@@ -287,13 +310,20 @@ __device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_
   int frag = 30;
   const int fragments = fragments_of(len, frag);
   const int end = len - 1;
+  const int L = (int)X.kmer_len;
   uint32_t gk = 0, gl = 0;
   int i;
   k = 0;
   l = X.top;
   if (fragments <= 1) {  // search.c:1191-1224: one exact search of the whole read
     if (strand) {  // type 0: forward search from the first base
-      for (i = 0; i <= end; ++i) {
+      i = 0;
+      if (start_lookup<C>(X, fw, W, 0, 1, end + 1, k, l)) {
+        gk = k;
+        gl = l;
+        i = L;
+      }
+      for (; i <= end; ++i) {
         step<C>(X, fw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
@@ -302,7 +332,13 @@ __device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_
       put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
       if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
     } else {
-      for (i = end; i >= 0; --i) {
+      i = end;
+      if (start_lookup<C>(X, bw, W, end, -1, end + 1, k, l)) {
+        gk = k;
+        gl = l;
+        i = end - L;
+      }
+      for (; i >= 0; --i) {
         step<C>(X, bw, W[i], k, l, o.sectors);
         if (k > l) break;
         gk = k;
@@ -314,7 +350,13 @@ __device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_
     return false;
   }
   if (part == 0) {  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
-    for (i = 0; i <= frag - 1; ++i) {
+    i = 0;
+    if (start_lookup<C>(X, fw, W, 0, 1, frag, k, l)) {
+      gk = k;
+      gl = l;
+      i = L;
+    }
+    for (; i <= frag - 1; ++i) {
       step<C>(X, fw, W[i], k, l, o.sectors);
       if (k > l) break;
       gk = k;
@@ -324,7 +366,13 @@ __device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_
     if (k > l) return false;
     aflag |= 2u;
   } else {  // last block: backward over W[frag .. len-1] (search.c:1360-1402)
-    for (i = end; i >= frag; --i) {
+    i = end;
+    if (start_lookup<C>(X, bw, W, end, -1, end - frag + 1, k, l)) {
+      gk = k;
+      gl = l;
+      i = end - L;
+    }
+    for (; i >= frag; --i) {
       step<C>(X, bw, W[i], k, l, o.sectors);
       if (k > l) break;
       gk = k;
@@ -575,7 +623,6 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
   // (register pressure: the block's part, strand and read come from `it`; the
   // interval before a branch point's step lives in a, b while the branch runs)
   const uint8_t* W = nullptr;
-  View v{0, 0};
   int end = 0, frag = 30;
   uint32_t it = 0;
   ItemOut o;
@@ -590,7 +637,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
   uint32_t lane_sectors = 0;
   uint32_t mode = kIdle;
   int i = 0;
-  uint32_t a = 0, b = 0, k0 = 0, l0 = 0;
+  uint32_t a = 0, b = 0;
   uint32_t z = 0, changes = 0, left = 0;
   bool alive = false, failed_step = false, ok_before = false, ok_at = false;
   uint32_t na = 0, nb = 0;
@@ -615,23 +662,20 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
         next += stride;
         it = q.x;
         const uint32_t list = it >> 1, part = it & 1u;
-        const uint32_t read = list >> 1, strand = list & 1u;
+        const uint32_t read = list >> 1;
         const uint64_t b0 = offs[read];
         const int len = (int)(offs[read + 1] - b0);
         W = codes + b0;
         frag = 30;
         fragments_of(len, frag);
         end = len - 1;
-        v = part == 0 ? forward_view(strand) : backward_view(strand);
         o.slot = ps.slots + (uint64_t)it * kBlockSlots;
         o.n = 0;
         o.refused = false;
         o.sectors = 0;
         lost = false;
-        k0 = q.y;
-        l0 = q.z;
-        a = k0;
-        b = l0;
+        a = q.y;  // the fragment's interval (read again from the queue for the second walk)
+        b = q.z;
         z = 0;
         changes = 0;
         alive = true;
@@ -653,8 +697,9 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
           ok_before = bound_before;
           ok_at = bound_at;
           left = points;
-          a = k0;
-          b = l0;
+          const uint4 q = queue[next - stride];  // the block claimed last
+          a = q.y;
+          b = q.z;
           i = (it & 1u) == 0 ? frag : frag - 1;
           mode = kSecond;
         }
@@ -737,6 +782,7 @@ __global__ void __launch_bounds__(kBlockTpb) block_tail_kernel(
       x = a;
       y = b;
     }
+    const View v = (it & 1u) == 0 ? forward_view((it >> 1) & 1u) : backward_view((it >> 1) & 1u);
     step<C>(X, v, sym, x, y, o.sectors);
     const int dstep = (it & 1u) == 0 ? 1 : -1;
     if (mode == kFirst) {
