@@ -1013,10 +1013,31 @@ __global__ void __launch_bounds__(kExpandTpb)
     __syncthreads();
     const uint64_t excl = s_base + s_warp[warp] + incl - v;
     const uint32_t at = phys ? (uint32_t)(excl >> 32) : (uint32_t)excl;
-    for (uint32_t i = 0; i < cnt; ++i) {
-      it.row = k + i;
-      it.out = (uint32_t)(b + i);
-      items[phys ? n_locs - 1 - (at + i) : at + i] = it;
+    // a hit's rows: up to 4 by its own thread; more (repeats, up to the locate
+    // limit) by the whole warp, 32 rows a round, so one long hit does not hold
+    // the block for thousands of serial stores
+    if (cnt <= 4) {
+      for (uint32_t i = 0; i < cnt; ++i) {
+        it.row = k + i;
+        it.out = (uint32_t)(b + i);
+        items[phys ? n_locs - 1 - (at + i) : at + i] = it;
+      }
+    }
+    unsigned big = __ballot_sync(0xFFFFFFFFu, cnt > 4);
+    while (big) {
+      const int j = __ffs(big) - 1;
+      big &= big - 1;
+      const uint32_t cj = __shfl_sync(0xFFFFFFFFu, cnt, j), aj = __shfl_sync(0xFFFFFFFFu, at, j);
+      const uint32_t kj = __shfl_sync(0xFFFFFFFFu, k, j), pj = __shfl_sync(0xFFFFFFFFu, phys, j);
+      const uint32_t bj = (uint32_t)__shfl_sync(0xFFFFFFFFu, b, j);
+      RowItem w;
+      w.hit = __shfl_sync(0xFFFFFFFFu, it.hit, j);
+      w.phys_len = __shfl_sync(0xFFFFFFFFu, it.phys_len, j);
+      for (uint32_t i = lane; i < cj; i += 32) {
+        w.row = kj + i;
+        w.out = bj + i;
+        items[pj ? n_locs - 1 - (aj + i) : aj + i] = w;
+      }
     }
     __syncthreads();  // s_warp and s_base are rewritten next round
   }
