@@ -564,8 +564,11 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
       in_place = at.type == cudaMemoryTypeDevice && at.device == e->device;
     cudaGetLastError();
   }
+  // a batch staged in a plan stays in that plan's capacity class (a server may
+  // run small batches in a larger class's plan)
+  const uint32_t n_plan = staged_in ? std::max<uint32_t>(n, staged_in->n_cap) : n;
   for (int attempt = 0; attempt < 8; ++attempt) {
-    GraphPlan* g = graph_plan_for(e, n, total, attempt ? &grow : nullptr, staged_in != nullptr, err, pslot);
+    GraphPlan* g = graph_plan_for(e, n_plan, total, attempt ? &grow : nullptr, staged_in != nullptr, err, pslot);
     if (!g) return -1;
     if (staged_in) {  // follow the batch into a replacement plan
       seqs = g->seqs;

@@ -148,6 +148,7 @@ struct Server {
   uint64_t budget = 0;
   uint32_t max_results = 0;
   size_t max_segs = 4096;
+  uint32_t floor_n = 4096;  // smallest capacity class a batch runs in (plans captured at start)
 
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_sets;
@@ -234,7 +235,7 @@ struct Server {
     cudaStream_t cs = e->stream, h2d = e->xs[0];
     const int k = b->slot;
     const double p0 = now_ms();
-    b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err, k);
+    b->g = graph_plan_for(e, std::max<uint32_t>(b->n, floor_n), b->bases, nullptr, false, err, k);
     if (!b->g) return -1;
     HPG_CUDA(cudaEventSynchronize(ev_in[k]), "serving staging");  // the slot's previous tables were sent
     const double p1 = now_ms();
@@ -355,7 +356,7 @@ struct Server {
       HPG_CUDA(cudaStreamSynchronize(cs), "serving drain");
       DeviceResult r;
       if (run_batched_graph(e, g->seqs, g->offs, b->n, b->bases, max_results, &r, err) != 0) return -1;
-      g = b->g = graph_plan_for(e, b->n, b->bases, nullptr, false, err, k);
+      g = b->g = graph_plan_for(e, std::max<uint32_t>(b->n, floor_n), b->bases, nullptr, false, err, k);
       if (!g) return -1;
       h = g->h_summary;
       HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
@@ -553,6 +554,28 @@ Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_base
     *err = "out of memory (serving buffers)";
     server_destroy(S);
     return nullptr;
+  }
+  // the graph plans of every capacity class a batch can run in, both slots,
+  // captured now: a capture (allocations that wait for the device, then the
+  // capture itself) in the middle of serving stalled the pipeline for tens of
+  // ms.  Batches below 1/64 of the capacity run in that smallest class.
+  {
+    uint64_t cls = 4096;
+    while (cls < max_batch_reads / 64) cls <<= 1;
+    S->floor_n = (uint32_t)cls;
+    const uint64_t bases_per_read = std::max<uint64_t>(1, S->max_bases / max_batch_reads);
+    for (;; cls <<= 1) {
+      for (int k = 0; k < 2; ++k) {
+        std::string perr;
+        if (!graph_plan_for(e, (uint32_t)cls, std::min<uint64_t>(cls * bases_per_read, S->max_bases), nullptr, false,
+                            &perr, k)) {
+          *err = "serving plans: " + perr;
+          server_destroy(S);
+          return nullptr;
+        }
+      }
+      if (cls >= max_batch_reads) break;
+    }
   }
   S->worker = std::thread([S] { S->run(); });
   return S;
