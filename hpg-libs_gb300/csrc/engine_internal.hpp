@@ -203,6 +203,11 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
 // `pslot` (0/1) picks one of the two plans of a capacity class.
 GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
                           std::string* err, int pslot = 0);
+// Recapture, at the per-read pool rates learned so far, every plan whose pools
+// are below them, except keep0 and keep1 (plans that hold a batch); for a
+// caller that has just drained its streams after an overflow, so that each
+// capacity class does not overflow (and drain) in turn.
+int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, std::string* err);
 // Host reads in, host records out, in chunks whose copies overlap the
 // neighbouring chunks' replays (graph.cu).
 int run_graph_pipelined(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint64_t total,

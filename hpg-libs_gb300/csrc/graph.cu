@@ -287,6 +287,22 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   return g;
 }
 
+int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, std::string* err) {
+  if (!e->plans) return 0;
+  for (int i = 0; i < kMaxPlans * kPlanSlots; ++i) {
+    GraphPlan* g = e->plans[i];
+    if (!g || g == keep0 || g == keep1 || !same_settings(g, e)) continue;
+    const double nc = (double)g->n_cap;
+    GraphPlan grow;
+    grow.res_cap = (uint32_t)std::min<double>(std::max(4.0, e->res_per_read) * nc + 4096, 0xFFFFFFF0u);
+    grow.spill_cap = (uint32_t)std::min<double>(e->spill_per_read * nc, 0xFFFFFFF0u);
+    grow.locs_cap = (uint64_t)std::min<double>(std::max(8.0, e->locs_per_read) * nc + 4096, kMaxLocateRows);
+    if (g->res_cap >= grow.res_cap && g->spill_cap >= grow.spill_cap && g->locs_cap >= grow.locs_cap) continue;
+    if (!graph_plan_for(e, g->n_cap, g->bases_cap, &grow, false, err, i % kPlanSlots)) return -1;
+  }
+  return 0;
+}
+
 int graph_launch(Engine* e, GraphPlan* g, uint32_t n, uint32_t max_results, std::string* err, const void* src,
                  uint64_t src_bytes) {
   cudaStream_t s = e->stream;

@@ -326,7 +326,7 @@ struct Server {
   // output stream (the other slot's batch keeps the GPU busy meanwhile).  The
   // slot's inputs are free from here on: the next batch of the slot is sent
   // before these results are waited for.
-  int collect_start(Batch* b, std::string* err) {
+  int collect_start(Batch* b, const GraphPlan* other, std::string* err) {
     cudaStream_t cs = e->stream, h2d = e->xs[0], d2h = e->xs[1];
     const int k = b->slot;
     const double w0 = now_ms();
@@ -358,6 +358,9 @@ struct Server {
       if (run_batched_graph(e, g->seqs, g->offs, b->n, b->bases, max_results, &r, err) != 0) return -1;
       g = b->g = graph_plan_for(e, std::max<uint32_t>(b->n, floor_n), b->bases, nullptr, false, err, k);
       if (!g) return -1;
+      // the streams are drained: bring the other classes' plans to the rates this
+      // overflow showed now, rather than one overflow (and drain) per class
+      if (graph_plans_refresh(e, g, other, err) != 0) return -1;
       h = g->h_summary;
       HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
     }
@@ -484,7 +487,7 @@ struct Server {
       Batch* b = inflight.front();
       inflight.pop_front();
       std::string err;
-      int rc = collect_start(b, &err);
+      int rc = collect_start(b, inflight.empty() ? nullptr : inflight.front()->g, &err);
       if (rc == 0) {
         fill(false);  // the freed slot's next inputs travel while its results come out
         rc = collect_finish(b, &err);
