@@ -62,7 +62,7 @@ struct DevIndex {
   const uint64_t* kar_offset;  // kar_size + 1 entries
   const uint64_t* kar_start;
   uint32_t kar_size;
-  uint32_t* err;          // device error word (bit 0: LF walk exceeded n+1 steps)
+  uint32_t* err;          // device error word (bit 0: an LF walk passed its bound: a corrupt index)
   uint32_t load_mode;     // how blocks are fetched, see load_block()
   // Start table of the batched search: for every string of kmer_len symbols
   // (first symbol in the top bits, in search order) the interval the search
