@@ -233,6 +233,23 @@ Engine* engine_create(const HostIndex& h, int device, std::string* err) {
   return en;
 }
 
+void engine_release_workspace(Engine* e, uint64_t keep_n_cap) {
+  graph_plans_drop_above(e, keep_n_cap);
+  cudaStreamSynchronize(e->stream);
+  DevBuf* bufs[] = {&e->seqs, &e->offs, &e->codes, &e->ok, &e->rs_count, &e->rs_trunc, &e->vecs, &e->slots,
+                    &e->ovf, &e->ovf_count, &e->hit_off, &e->scan_part, &e->hits, &e->rows, &e->loc_off, &e->locs,
+                    &e->b_res, &e->b_sorted, &e->b_spill, &e->b_arr, &e->b_seg, &e->b_rowhit, &e->b_long,
+                    &e->b_blocks, &e->b_bovf, &e->m_hitoff, &e->m_part, &e->m_offs, &e->m_rows, &e->m_pflag,
+                    &e->m_rowoff, &e->m_nrec, &e->m_flags, &e->m_rec};
+  for (DevBuf* b : bufs) {
+    cudaFree(b->p);
+    b->p = nullptr;
+    b->cap = 0;
+  }
+  e->b_res_cap = e->b_spill_cap = 0;
+  e->last = DeviceResult();
+}
+
 void engine_destroy(Engine* e) {
   if (!e) return;
   cudaSetDevice(e->device);

@@ -190,6 +190,12 @@ int run_batched_graph(Engine* e, const void* seqs, const uint64_t* offs, uint32_
                       uint32_t max_results, DeviceResult* out, std::string* err);
 void graph_plan_destroy(GraphPlan* g);
 void graph_plans_destroy(Engine* e);
+// Free the plans of more than max_n_cap reads (after the streams finish).
+void graph_plans_drop_above(Engine* e, uint64_t max_n_cap);
+// Free the grow-only workspaces of the direct, plain, block-search and
+// alignment-list calls (they are allocated again on demand) and the plans of
+// more than keep_n_cap reads: a server on the index keeps only what it uses.
+void engine_release_workspace(Engine* e, uint64_t keep_n_cap);
 // Asynchronous halves of run_batched_graph for a batch already staged in the
 // plan's input buffers: launch (header + replay), then collect (synchronize,
 // read the summary; returns 1 with `grow` filled when a pool overflowed, the
@@ -203,11 +209,14 @@ int graph_collect(Engine* e, GraphPlan* g, uint32_t n, GraphPlan* grow, DeviceRe
 // `pslot` (0/1) picks one of the two plans of a capacity class.
 GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan* grow, bool carry,
                           std::string* err, int pslot = 0);
-// Recapture, at the per-read pool rates learned so far, every plan whose pools
-// are below them, except keep0 and keep1 (plans that hold a batch); for a
-// caller that has just drained its streams after an overflow, so that each
-// capacity class does not overflow (and drain) in turn.
-int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, std::string* err);
+// Recapture, at the per-read pool rates learned so far, every plan of at most
+// max_n_cap reads whose pools are below them, except keep0 and keep1 (plans
+// that hold a batch); for a caller that has just drained its streams after an
+// overflow, so that each capacity class does not overflow (and drain) in turn.
+// (Plans above max_n_cap, e.g. a large batched call's, are left alone: a
+// recapture holds the old plan and the new one at once.)
+int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, uint64_t max_n_cap,
+                        std::string* err);
 // Host reads in, host records out, in chunks whose copies overlap the
 // neighbouring chunks' replays (graph.cu).
 int run_graph_pipelined(Engine* e, const char* seqs, const uint64_t* offs, size_t n, uint64_t total,

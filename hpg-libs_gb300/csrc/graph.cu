@@ -206,6 +206,18 @@ void graph_plans_destroy(Engine* e) {
   e->plans = nullptr;
 }
 
+void graph_plans_drop_above(Engine* e, uint64_t max_n_cap) {
+  if (!e->plans) return;
+  cudaStreamSynchronize(e->stream);
+  for (cudaStream_t x : e->xs)
+    if (x) cudaStreamSynchronize(x);
+  for (int i = 0; i < kMaxPlans * kPlanSlots; ++i)
+    if (e->plans[i] && e->plans[i]->n_cap > max_n_cap) {
+      graph_plan_destroy(e->plans[i]);
+      e->plans[i] = nullptr;
+    }
+}
+
 // The plan for a batch of n reads and `total` bases: one per power-of-two read
 // capacity, captured again when the tuning, block-load form or census setting
 // changed, or when a pool has to grow.
@@ -287,11 +299,12 @@ GraphPlan* graph_plan_for(Engine* e, uint32_t n, uint64_t total, const GraphPlan
   return g;
 }
 
-int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, std::string* err) {
+int graph_plans_refresh(Engine* e, const GraphPlan* keep0, const GraphPlan* keep1, uint64_t max_n_cap,
+                        std::string* err) {
   if (!e->plans) return 0;
   for (int i = 0; i < kMaxPlans * kPlanSlots; ++i) {
     GraphPlan* g = e->plans[i];
-    if (!g || g == keep0 || g == keep1 || !same_settings(g, e)) continue;
+    if (!g || g == keep0 || g == keep1 || g->n_cap > max_n_cap || !same_settings(g, e)) continue;
     const double nc = (double)g->n_cap;
     GraphPlan grow;
     grow.res_cap = (uint32_t)std::min<double>(std::max(4.0, e->res_per_read) * nc + 4096, 0xFFFFFFF0u);

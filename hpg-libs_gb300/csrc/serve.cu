@@ -360,7 +360,9 @@ struct Server {
       if (!g) return -1;
       // the streams are drained: bring the other classes' plans to the rates this
       // overflow showed now, rather than one overflow (and drain) per class
-      if (graph_plans_refresh(e, g, other, err) != 0) return -1;
+      uint64_t top = 4096;
+      while (top < max_reads) top <<= 1;
+      if (graph_plans_refresh(e, g, other, top, err) != 0) return -1;
       h = g->h_summary;
       HPG_CUDA(cudaEventRecord(ev_run[k], cs), "serving order");
     }
@@ -563,6 +565,11 @@ Server* server_create(Engine* e, size_t max_batch_reads, uint64_t max_batch_base
   // capture itself) in the middle of serving stalled the pipeline for tens of
   // ms.  Batches below 1/64 of the capacity run in that smallest class.
   {
+    // the index's batch-call workspaces and larger plans go first (a device
+    // result of an earlier call on the index is valid until the next call)
+    uint64_t top = 4096;
+    while (top < max_batch_reads) top <<= 1;
+    engine_release_workspace(e, top);
     uint64_t cls = 4096;
     while (cls < max_batch_reads / 64) cls <<= 1;
     S->floor_n = (uint32_t)cls;

@@ -335,7 +335,10 @@ const char *bwt_gpu_noalloc_last_error(void);
  * worker thread admits waiting requests in arrival order while they fit the
  * batch capacity and the HBM budget (0 = a quarter of the device memory free
  * at creation), runs them as one graph replay, and forms the next batch from
- * new arrivals while a batch is on the GPU.
+ * new arrivals while a batch is on the GPU.  Creating a server frees the
+ * index's batch-call workspaces and its graph plans above the batch capacity
+ * (a device result of an earlier call is invalid after it, as after any call)
+ * and captures the plans of every capacity class the server runs in.
  *
  * submit: the reads stay in the caller's memory (pinned memory copies fastest)
  * until wait returns for the ticket.  wait: 0 done, 1 timed out (timeout_ms
