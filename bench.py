@@ -636,8 +636,11 @@ def alignment_lists(gi, reads, log, n: int) -> dict:
     first n reads of the batch with filter_read_mappings 200: BWSearch1, the row
     filter, the located rows, the 10 bp merge and the list order on the device
     (device_seconds), the alignment_t records and their strings allocated on the
-    host threads; the best of three calls."""
+    host threads; the best of three calls.  A fastq batch's indices are C ints, so
+    n stops where the bases (with one terminator a read) reach 2^31 bytes."""
     n = min(n, len(reads))
+    fit = np.asarray(reads.offsets[1:], dtype=np.int64) + np.arange(1, len(reads) + 1) < 2 ** 31 - 1
+    n = min(n, int(np.count_nonzero(fit)))
     seq = reads.seq[:int(reads.offsets[n])]
     offs = reads.offsets[:n + 1]
     best, dev, count = None, None, 0

@@ -427,6 +427,8 @@ class GpuIndex:
                         ("header_indices", ctypes.c_void_p), ("header", ctypes.c_void_p),
                         ("data_indices", ctypes.c_void_p), ("seq", ctypes.c_void_p), ("quality", ctypes.c_void_p)]
         offs = np.asarray(offsets, dtype=np.int64)
+        if int(offs[-1]) + n >= 2 ** 31:  # fastq_batch_t's data_indices are C ints
+            raise ValueError("a fastq batch holds less than 2^31 bytes of bases (its indices are int)")
         data = np.insert(np.asarray(seq, dtype=np.uint8), offs[1:], 0)
         qual = np.where(data == 0, 0, ord("I")).astype(np.uint8)
         didx = (offs + np.arange(n + 1)).astype(np.int32)
