@@ -173,6 +173,12 @@ struct Server {
   cudaEvent_t tv0[2] = {nullptr, nullptr}, tv1[2] = {nullptr, nullptr};
   double t_replay = 0, t_wait_run = 0, t_wait_out = 0, t_issue = 0, t_plan = 0, t_prep = 0, t_copies = 0,
          t_take = 0, t_publish = 0, t_form = 0;
+  // the longest single instance of each, the replay's and the host's parts
+  double m_replay = 0, m_wait_run = 0, m_wait_out = 0, m_plan = 0, m_take = 0, m_cycle = 0, last_cycle = 0;
+  static void note(double& sum, double& mx, double v) {
+    sum += v;
+    mx = v > mx ? v : mx;
+  }
 
   // admission estimates, updated from finished batches
   double hits_per_read = 4.0, rows_per_read = 16.0;
@@ -242,7 +248,7 @@ struct Server {
     prepare(b);
     const double p2 = now_ms();
     if (timing) {
-      t_plan += p1 - p0;
+      note(t_plan, m_plan, p1 - p0);
       t_prep += p2 - p1;
     }
     // inputs once the slot's previous replay has read its own, the segment table once
@@ -332,10 +338,10 @@ struct Server {
     const double w0 = now_ms();
     HPG_CUDA(cudaEventSynchronize(ev_run[k]), "batched pipeline");
     if (timing) {
-      t_wait_run += now_ms() - w0;
+      note(t_wait_run, m_wait_run, now_ms() - w0);
       float ms = 0;
       cudaEventElapsedTime(&ms, tv0[k], tv1[k]);
-      t_replay += ms;
+      note(t_replay, m_replay, ms);
     }
     GraphPlan* g = b->g;
     const uint64_t* h = g->h_summary;
@@ -372,7 +378,7 @@ struct Server {
     const double k0 = now_ms();
     ResultBuf* rb = take_set(nh, nl, 2ull * b->n, nseg, err);
     if (!rb) return -1;
-    if (timing) t_take += now_ms() - k0;
+    if (timing) note(t_take, m_take, now_ms() - k0);
     HPG_CUDA(cudaStreamWaitEvent(d2h, ev_run[k], 0), "serving order");
     if (rerun) {  // the rebase that followed the replay left the overflowed batch alone
       const uint64_t work = std::max<uint64_t>(std::max<uint64_t>(nh, nl), nseg + 1);
@@ -405,7 +411,7 @@ struct Server {
     const size_t nseg = b->reqs.size();
     const double w1 = now_ms();
     HPG_CUDA(cudaEventSynchronize(rb->done), "result copies");
-    if (timing) t_wait_out += now_ms() - w1;
+    if (timing) note(t_wait_out, m_wait_out, now_ms() - w1);
     HPG_CUDA(cudaGetLastError(), "rebase kernel");
     if (h_err[k]) {
       cudaMemsetAsync(e->d_err, 0, 4, e->xs[1]);
@@ -444,7 +450,12 @@ struct Server {
       if (e->plans && e->plans[i]) plan_bytes += e->plans[i]->bytes;
     b->reqs.clear();
     cv_done.notify_all();
-    if (timing) t_publish += now_ms() - t;
+    if (timing) {
+      t_publish += now_ms() - t;
+      const double c = now_ms();  // one batch published to the next
+      if (last_cycle > 0) m_cycle = std::max(m_cycle, c - last_cycle);
+      last_cycle = c;
+    }
     return 0;
   }
 
@@ -613,6 +624,11 @@ void server_destroy(Server* S) {
                  S->t_wait_run / S->batches, S->t_wait_out / S->batches, S->t_form / S->batches,
                  S->t_plan / S->batches, S->t_prep / S->batches, S->t_copies / S->batches, S->t_issue / S->batches,
                  S->t_take / S->batches, S->t_publish / S->batches);
+  if (S->timing && S->batches)
+    std::fprintf(stderr,
+                 "[hpgbwt] server: longest: replay %.3f ms, host blocked on a replay %.3f and on result copies %.3f, "
+                 "plan %.3f, result set %.3f; publish to publish %.3f ms\n",
+                 S->m_replay, S->m_wait_run, S->m_wait_out, S->m_plan, S->m_take, S->m_cycle);
   for (ResultBuf& rb : S->sets) {
     cudaFreeHost(rb.hits);
     cudaFreeHost(rb.locs);
