@@ -259,7 +259,7 @@ class ClockSampler:
             except (ValueError, IndexError):
                 continue
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "sm_min_mhz": min(sm) if sm else None}
 
 
 def measured_peaks() -> tuple[float, str]:
@@ -429,6 +429,10 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
 
     th = threading.Thread(target=waiter, daemon=True)
     th.start()
+    import torch
+    clk = ClockSampler(torch.cuda.current_device()) if load is not None else None
+    if clk:
+        clk.__enter__()
     t0 = time.perf_counter()
     offered = None
     n_req = 0
@@ -455,6 +459,8 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
             n_req += 1
     pend.put(None)
     th.join()
+    if clk:
+        clk.__exit__(None, None, None)
     st = srv.stats()
     if own:
         srv.close()
@@ -468,7 +474,7 @@ def serve_run(gi, seq_ptr: int, off_ptr: int, pool_n: int, draw_size, load: floa
            "max_batch_requests": int(st["max_batch_requests"]), "pool_regrowths": int(st["regrowths"] - st0["regrowths"]),
            "plan_hbm_bytes": int(st["plan_bytes"]), "hbm_budget_bytes": int(st["hbm_budget"])}
     if offered is not None:
-        out = {"offered_load": load, "offered_reads_per_s": round(offered, 1), **out}
+        out = {"offered_load": load, "offered_reads_per_s": round(offered, 1), **out, "clocks": clk.summary()}
     return out
 
 
@@ -499,7 +505,9 @@ def serve_cases(gi, cases, log, locate_limit: int, rng: np.random.Generator, max
         res[name] = {"saturated_reads_per_s": sat["achieved_reads_per_s"], "saturated_burst_requests": burst,
                      "saturated_mean_batch_reads": sat["mean_batch_reads"], "at_70pct_load": loaded,
                      "load_sweep": {k: {"p50_ms": v["p50_ms"], "p99_ms": v["p99_ms"],
-                                        "achieved_reads_per_s": v["achieved_reads_per_s"]} for k, v in sweep.items()}}
+                                        "achieved_reads_per_s": v["achieved_reads_per_s"],
+                                        "sm_mhz": v["clocks"].get("sm_mhz"), "sm_min_mhz": v["clocks"].get("sm_min_mhz"),
+                                        "clock_reasons": v["clocks"].get("reasons")} for k, v in sweep.items()}}
         log(f"[bench] serving {name} sweep: " + ", ".join(f"{k} p50 {v['p50_ms']} p99 {v['p99_ms']}"
                                                          for k, v in sweep.items()))
         log(f"[bench] serving {name}: saturated {sat['achieved_reads_per_s'] / 1e6:.1f} M reads/s; at 70% "
