@@ -158,3 +158,27 @@ def test_pipelined_host_batches(tmp_path_factory):
             _same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
         g.set_graph(False)
         _same(g.search(reads, mode=lib.MODE_SEARCH1, form=lib.FORM_BATCHED), want)
+
+
+def test_device_bases_at_any_address(case_factory):
+    """The graph form encodes a caller's device bases where they are: a buffer
+    that starts one byte past an aligned address (16-byte vector loads cannot
+    be used) gives the same records as the plain form and the oracle."""
+    torch = pytest.importorskip("torch")
+    c = case_factory("repeats", 300_000, 3, 3)
+    reads = synth.reads(c.genome, 5000, 62, length=(36, 250), edits="mix_30_50_20")
+    want = PortOracle(c.index).search(reads, mode=lib.MODE_SEARCH1, max_results=1 << 16, threads=8)
+    buf = torch.zeros(len(reads.seq) + 64, dtype=torch.uint8, device="cuda")
+    buf[1:1 + len(reads.seq)] = torch.from_numpy(reads.seq).cuda()
+    d_off = torch.from_numpy(reads.offsets.view(np.int64)).cuda()
+    with lib.GpuIndex(c.index) as g:
+        for form in (lib.FORM_BATCHED, lib.FORM_PLAIN, lib.FORM_BATCHED):
+            rs = g.search_device(buf.data_ptr() + 1, d_off.data_ptr(), len(reads), int(reads.offsets[-1]),
+                                 int(np.diff(reads.offsets).max()), form=form)
+            hits = np.zeros(rs.n_hits, lib.HIT_DTYPE)
+            locs = np.zeros(rs.n_locs, lib.LOC_DTYPE)
+            cnt = np.zeros(2 * len(reads), np.uint32)
+            tr = np.zeros(2 * len(reads), np.uint8)
+            g.copy_result(rs, hits.ctypes.data, locs.ctypes.data, cnt.ctypes.data, tr.ctypes.data)
+            assert np.array_equal(cnt, want.rs_count) and np.array_equal(tr, want.rs_truncated)
+            assert np.array_equal(hits, want.hits) and np.array_equal(locs, want.locs)

@@ -64,3 +64,30 @@ def test_reads_fast_var_models():
                 k = next(k for k in range(L) if k >= L - 1 or c[k] != f[k])
                 assert np.array_equal(np.delete(c, k), f) or any(
                     np.array_equal(np.delete(c, j), f) for j in range(1, L - 1))
+
+
+def test_threaded_draws_equal_sequential_ones():
+    """genome_large's background and element copies draw doubles from copies of
+    the generator advanced to their slice: the same numbers, and the generator
+    left where drawing them in order would leave it (the 32-bit half a bounded
+    integer draw buffered included)."""
+    rng_a, rng_b = np.random.default_rng(11), np.random.default_rng(11)
+    rng_a.integers(0, 4, size=5)  # leaves a buffered half in both
+    rng_b.integers(0, 4, size=5)
+    want = rng_a.random((37, 1001))
+    got = synth._uniform_threads(rng_b, (37, 1001), chunk=4096)
+    assert np.array_equal(want, got)
+    assert np.array_equal(rng_a.integers(0, 4, size=9, dtype=np.uint8), rng_b.integers(0, 4, size=9, dtype=np.uint8))
+    assert rng_a.random() == rng_b.random()
+    cum = np.cumsum([0.295, 0.205, 0.205])
+    rng_a, rng_b = np.random.default_rng(12), np.random.default_rng(12)
+    want = np.searchsorted(cum, rng_a.random(100_003), side="right").astype(np.uint8)
+    got = np.empty(100_003, dtype=np.uint8)
+    synth._background_draws(got, rng_b, cum, 8192)
+    assert np.array_equal(want, got) and rng_a.random() == rng_b.random()
+
+
+def test_large_genome_is_seeded():
+    a = synth.genome_large(3_000_000, 4)
+    assert np.array_equal(a, synth.genome_large(3_000_000, 4)) and a.max() <= 3
+    assert not np.array_equal(a, synth.genome_large(3_000_000, 5))
