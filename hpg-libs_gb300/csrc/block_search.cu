@@ -303,89 +303,106 @@ __device__ __forceinline__ bool start_lookup(const DevIndex& X, View v, const ui
   return true;
 }
 
-template <bool C>
-__device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
-                           hpg_block_anchor_t* anchor, uint32_t& aflag, uint32_t& k, uint32_t& l) {
-  const View bw = backward_view(strand), fw = forward_view(strand);
+// The fragment walk of a block's head: view, first and last position, step
+// direction, and the anchor's direction (1: forward from the read's start).
+struct HeadWalk {
+  View v;
+  int from, to, dir;
+  uint32_t adir;
+  bool single;
+};
+
+__device__ __forceinline__ HeadWalk head_walk(int len, uint32_t strand, int part) {
+  HeadWalk h;
   int frag = 30;
   const int fragments = fragments_of(len, frag);
   const int end = len - 1;
-  const int L = (int)X.kmer_len;
-  uint32_t gk = 0, gl = 0;
-  int i;
-  k = 0;
-  l = X.top;
-  if (fragments <= 1) {  // search.c:1191-1224: one exact search of the whole read
-    if (strand) {  // type 0: forward search from the first base
-      i = 0;
-      if (start_lookup<C>(X, fw, W, 0, 1, end + 1, k, l)) {
-        gk = k;
-        gl = l;
-        i = L;
-      }
-      for (; i <= end; ++i) {
-        step<C>(X, fw, W[i], k, l, o.sectors);
-        if (k > l) break;
-        gk = k;
-        gl = l;
-      }
-      put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
-      if (k <= l) emit(o, 1, 0, 0, 0, 0, k, l);
-    } else {
-      i = end;
-      if (start_lookup<C>(X, bw, W, end, -1, end + 1, k, l)) {
-        gk = k;
-        gl = l;
-        i = end - L;
-      }
-      for (; i >= 0; --i) {
-        step<C>(X, bw, W[i], k, l, o.sectors);
-        if (k > l) break;
-        gk = k;
-        gl = l;
-      }
-      put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
-      if (k <= l) emit(o, 0, 0, 0, 0, 0, k, l);
-    }
+  h.single = fragments <= 1;
+  if (h.single ? strand != 0 : part == 0) {
+    // search.c:1191-1224 type 0 (one exact search forward from the first base), or
+    // block 0 forward over W[0 .. frag-1] (search.c:1276-1311)
+    h.v = forward_view(strand);
+    h.from = 0;
+    h.to = h.single ? end : frag - 1;
+    h.dir = 1;
+    h.adir = 1;
+  } else {
+    // type 1 (backward from the last base), or the last block backward over
+    // W[frag .. len-1] (search.c:1360-1402)
+    h.v = backward_view(strand);
+    h.from = end;
+    h.to = h.single ? 0 : frag;
+    h.dir = -1;
+    h.adir = 0;
+  }
+  return h;
+}
+
+// Steps of a head walk from position i with the non-empty interval k..l, while
+// it stays non-empty, at most `budget` of them (negative: no limit); gk, gl keep
+// the last non-empty interval.  True when the walk is over (it failed, i at the
+// failing position, or it passed `to`); false when the budget ran out first.
+template <bool C>
+__device__ __forceinline__ bool head_steps(const DevIndex& X, const HeadWalk& h, const uint8_t* W, int& i,
+                                           uint32_t& k, uint32_t& l, uint32_t& gk, uint32_t& gl, int budget,
+                                           uint32_t& sec) {
+  while (h.dir > 0 ? i <= h.to : i >= h.to) {
+    if (budget-- == 0) return false;
+    step<C>(X, h.v, W[i], k, l, sec);
+    if (k > l) return true;
+    gk = k;
+    gl = l;
+    i += h.dir;
+  }
+  return true;
+}
+
+// The end of a head: the anchor, then the single search's result, or the
+// block's match (block 0's flag) and whether the block goes on to the tail.
+__device__ __forceinline__ bool head_finish(const HeadWalk& h, int len, ItemOut& o, hpg_block_anchor_t* anchor,
+                                            uint32_t& aflag, int i, uint32_t k, uint32_t l, uint32_t gk,
+                                            uint32_t gl) {
+  if (h.adir) put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
+  else put_anchor(anchor, aflag, 0, i + 1, len - 1, i, gk, gl);
+  if (h.single) {
+    if (k <= l) emit(o, h.adir, 0, 0, 0, 0, k, l);
     return false;
   }
-  if (part == 0) {  // block 0: forward over W[0 .. frag-1] (search.c:1276-1311)
-    i = 0;
-    if (start_lookup<C>(X, fw, W, 0, 1, frag, k, l)) {
-      gk = k;
-      gl = l;
-      i = L;
-    }
-    for (; i <= frag - 1; ++i) {
-      step<C>(X, fw, W[i], k, l, o.sectors);
-      if (k > l) break;
-      gk = k;
-      gl = l;
-    }
-    put_anchor(anchor, aflag, 1, 0, i - 1, i, gk, gl);
-    if (k > l) return false;
-    aflag |= 2u;
-  } else {  // last block: backward over W[frag .. len-1] (search.c:1360-1402)
-    i = end;
-    if (start_lookup<C>(X, bw, W, end, -1, end - frag + 1, k, l)) {
-      gk = k;
-      gl = l;
-      i = end - L;
-    }
-    for (; i >= frag; --i) {
-      step<C>(X, bw, W[i], k, l, o.sectors);
-      if (k > l) break;
-      gk = k;
-      gl = l;
-    }
-    put_anchor(anchor, aflag, 0, i + 1, end, i, gk, gl);
-    if (k > l) return false;
-  }
+  if (k > l) return false;
+  if (h.adir) aflag |= 2u;  // block 0 matched
   if (o.cap == 0) {  // add_result(&r, rl_prev) returns from BWSearchCPU
     o.refused = true;
     return false;
   }
   return true;
+}
+
+// The head's first steps: the start-table lookup for the first L steps when
+// the walk is that long (one lookup for them), from the full interval.
+template <bool C>
+__device__ __forceinline__ void head_start(const DevIndex& X, const HeadWalk& h, const uint8_t* W, int& i,
+                                           uint32_t& k, uint32_t& l, uint32_t& gk, uint32_t& gl) {
+  i = h.from;
+  k = 0;
+  l = X.top;
+  gk = gl = 0;
+  const int steps = h.dir > 0 ? h.to - h.from + 1 : h.from - h.to + 1;
+  if (start_lookup<C>(X, h.v, W, h.from, h.dir, steps, k, l)) {
+    gk = k;
+    gl = l;
+    i = h.from + h.dir * (int)X.kmer_len;
+  }
+}
+
+template <bool C>
+__device__ bool block_head(const DevIndex& X, const uint8_t* W, int len, uint32_t strand, int part, ItemOut& o,
+                           hpg_block_anchor_t* anchor, uint32_t& aflag, uint32_t& k, uint32_t& l) {
+  const HeadWalk h = head_walk(len, strand, part);
+  int i;
+  uint32_t gk, gl;
+  head_start<C>(X, h, W, i, k, l, gk, gl);
+  head_steps<C>(X, h, W, i, k, l, gk, gl, -1, o.sectors);
+  return head_finish(h, len, o, anchor, aflag, i, k, l, gk, gl);
 }
 
 // Tail of a block whose fragment matched with interval k..l: the rest of the
@@ -514,17 +531,37 @@ __device__ __forceinline__ bool emit_tail(ItemOut& o, const PartState& ps, uint3
   return true;
 }
 
+// Warp-aggregated append of {it, k, l, w} to a queue.
+__device__ __forceinline__ void queue_append(bool go, uint4* __restrict__ queue, uint32_t* __restrict__ n_queue,
+                                             uint32_t it, uint32_t k, uint32_t l, uint32_t w) {
+  const unsigned mask = __ballot_sync(__activemask(), go);
+  if (go) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(n_queue, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = make_uint4(it, k, l, w);
+  }
+}
+
+constexpr int kHeadSteps = 4;  // the head's steps past the start table before its walk is compacted
+
 // Head pass over physical direction `phys`: thread g runs the head of the
 // block of its list that is on that direction (the '+' lists in the first half
 // of the threads, the '-' ones in the second, so that a warp's lanes run the
-// same block code), and appends the blocks that go on to `queue` as {block,
-// k, l}.  One launch per direction, so that it reads one direction's
-// occurrence blocks.
+// same block code): the start-table lookup and up to kHeadSteps steps, which
+// end most walks of the wrong strand.  Walks still going are appended to
+// `cont` as {block, k, l, position} for block_head_rest_kernel, so that their
+// long remainder runs in warps of walks that all go on; the blocks whose head
+// ended here and go on are appended to `queue` as {block, k, l}.  One launch
+// per direction, so that it reads one direction's occurrence blocks.
 template <bool C>
 __global__ void __launch_bounds__(kBlockTpb) block_head_kernel(
     DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint8_t* __restrict__ ok,
     uint32_t n_lists, uint32_t phys, uint32_t max_results, PartState ps, uint4* __restrict__ queue,
-    uint32_t* __restrict__ n_queue, unsigned long long* census) {
+    uint32_t* __restrict__ n_queue, uint4* __restrict__ cont, uint32_t* __restrict__ n_cont,
+    unsigned long long* census) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_lists) return;
   const uint32_t half = n_lists >> 1;
@@ -532,8 +569,9 @@ __global__ void __launch_bounds__(kBlockTpb) block_head_kernel(
   const uint32_t read = list >> 1, strand = list & 1u;
   const uint64_t b0 = offs[read];
   const int len = (int)(offs[read + 1] - b0);
-  bool go = false;
+  bool go = false, more = false;
   uint32_t it = 0, k = 0, l = 0;
+  int i = 0;
   if (ok[read] && len >= 3 && len <= 32767) {
     int frag = 30;
     const int part = part_on(strand, fragments_of(len, frag), phys);
@@ -548,24 +586,61 @@ __global__ void __launch_bounds__(kBlockTpb) block_head_kernel(
       o.strand = strand;
       o.refused = false;
       o.sectors = 0;
-      uint32_t aflag = 0;
-      go = block_head<C>(X, codes + b0, len, strand, part, o, ps.anchor + it, aflag, k, l);
-      ps.count[it] = o.n;
-      ps.refused[it] = o.refused ? 1 : 0;
-      ps.aflag[it] = (uint8_t)aflag;
+      const HeadWalk h = head_walk(len, strand, part);
+      const uint8_t* W = codes + b0;
+      uint32_t gk, gl;
+      head_start<C>(X, h, W, i, k, l, gk, gl);
+      if (!head_steps<C>(X, h, W, i, k, l, gk, gl, kHeadSteps, o.sectors)) {
+        more = true;  // still matching: the rest of the walk in the compacted pass
+      } else {
+        uint32_t aflag = 0;
+        go = head_finish(h, len, o, ps.anchor + it, aflag, i, k, l, gk, gl);
+        ps.count[it] = o.n;
+        ps.refused[it] = o.refused ? 1 : 0;
+        ps.aflag[it] = (uint8_t)aflag;
+      }
       if (C) atomicAdd(census, (unsigned long long)o.sectors);
     }
   }
-  // warp-aggregated append
-  const unsigned mask = __ballot_sync(__activemask(), go);
-  if (go) {
-    const uint32_t lane = threadIdx.x & 31u;
-    const int leader = __ffs(mask) - 1;
-    uint32_t base = 0;
-    if ((int)lane == leader) base = atomicAdd(n_queue, (uint32_t)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    queue[base + (uint32_t)__popc(mask & ((1u << lane) - 1u))] = make_uint4(it, k, l, 0u);
-  }
+  queue_append(go, queue, n_queue, it, k, l, 0u);
+  queue_append(more, cont, n_cont, it, k, l, (uint32_t)i);
+}
+
+// The rest of the head walks block_head_kernel compacted: thread g resumes
+// cont[g] at its position with its interval (non-empty, so also the last
+// non-empty one), ends the walk, and appends the blocks that go on to `queue`.
+template <bool C>
+__global__ void __launch_bounds__(kBlockTpb) block_head_rest_kernel(
+    DevIndex X, const uint8_t* __restrict__ codes, const uint64_t* __restrict__ offs, const uint4* __restrict__ cont,
+    const uint32_t* __restrict__ n_cont, uint32_t max_results, PartState ps, uint4* __restrict__ queue,
+    uint32_t* __restrict__ n_queue, unsigned long long* census) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= *n_cont) return;
+  const uint4 q = cont[g];
+  const uint32_t it = q.x, list = it >> 1, part = it & 1u;
+  const uint32_t read = list >> 1, strand = list & 1u;
+  const uint64_t b0 = offs[read];
+  const int len = (int)(offs[read + 1] - b0);
+  ItemOut o;
+  o.slot = ps.slots + (uint64_t)it * kBlockSlots;
+  o.room = kBlockSlots;
+  o.cap = max_results;
+  o.n = 0;
+  o.read = read;
+  o.strand = strand;
+  o.refused = false;
+  o.sectors = 0;
+  const HeadWalk h = head_walk(len, strand, (int)part);
+  int i = (int)q.w;
+  uint32_t k = q.y, l = q.z, gk = q.y, gl = q.z;
+  head_steps<C>(X, h, codes + b0, i, k, l, gk, gl, -1, o.sectors);
+  uint32_t aflag = 0;
+  const bool go = head_finish(h, len, o, ps.anchor + it, aflag, i, k, l, gk, gl);
+  ps.count[it] = o.n;
+  ps.refused[it] = o.refused ? 1 : 0;
+  ps.aflag[it] = (uint8_t)aflag;
+  if (C) atomicAdd(census, (unsigned long long)o.sectors);
+  queue_append(go, queue, n_queue, it, k, l, 0u);
 }
 
 // BWExactFinalResult{Forward,Backward}'s block rule (search.h:67-155) at the
@@ -1015,7 +1090,7 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   ps.lost = ps.refused + 2 * P;
   // overflow pool: four results a read in chunks, heads per block, a chunk chain
   const uint32_t ovf_cap = (uint32_t)std::min<size_t>(n / 8 + 1024, 0x7FFFFFFFu);
-  const size_t ovf_bytes = (size_t)ovf_cap * (kOvfChunk * sizeof(hpg_hit_t) + 4) + P * 4 + 64;
+  const size_t ovf_bytes = (size_t)ovf_cap * (kOvfChunk * sizeof(hpg_hit_t) + 4) + P * 4 + T * sizeof(uint4) + 64;
   if (!ensure(e, e->b_bovf, ovf_bytes)) {
     *err = oom_message("block search overflow pool", ovf_bytes);
     return -1;
@@ -1023,6 +1098,9 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
   ps.ovf_hits = ptr<hpg_hit_t>(e->b_bovf);
   ps.ovf_next = reinterpret_cast<uint32_t*>(ps.ovf_hits + (size_t)ovf_cap * kOvfChunk);
   ps.ovf_head = ps.ovf_next + ovf_cap;
+  // the head walks going on past their first steps (one direction at a time)
+  uint4* cont = reinterpret_cast<uint4*>(
+      (reinterpret_cast<uintptr_t>(ps.ovf_head + P) + 15) & ~static_cast<uintptr_t>(15));
   ps.ovf_ctr = ptr<uint32_t>(e->b_ctr) + 14;
   ps.ovf_cap = ovf_cap;
   uint32_t* n_retry = ptr<uint32_t>(e->b_ctr) + 12;
@@ -1047,17 +1125,24 @@ int block_search_device(Engine* e, size_t n, uint32_t max_results, uint64_t* tot
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, block_tail_kernel<false>, kBlockTpb, 0);
   const unsigned tail_grid = std::max(1u, std::min(grid_of(T), (unsigned)(std::max(per_sm, 1) * e->num_sms)));
   cudaEventRecord(e->cev[0], s);
-  for (uint32_t phys = 0; phys < 2; ++phys) {  // one head and one tail launch per index direction
+  uint32_t* n_cont = n_queue + 2;
+  for (uint32_t phys = 0; phys < 2; ++phys) {  // per index direction: head, the heads' rest, tail
     cudaMemsetAsync(n_queue, 0, 4, s);
-    count_launches(2);
+    cudaMemsetAsync(n_cont, 0, 4, s);
+    count_launches(3);
     if (census) {
       block_head_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys, max_results,
-                                                               ps, queue, n_queue, census);
+                                                               ps, queue, n_queue, cont, n_cont, census);
+      block_head_rest_kernel<true><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, cont, n_cont, max_results, ps,
+                                                                    queue, n_queue, census);
       block_tail_kernel<true><<<tail_grid, kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
                                                               census);
     } else {
       block_head_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, ok, (uint32_t)T, phys,
-                                                                max_results, ps, queue, n_queue, nullptr);
+                                                                max_results, ps, queue, n_queue, cont, n_cont,
+                                                                nullptr);
+      block_head_rest_kernel<false><<<grid_of(T), kBlockTpb, 0, s>>>(e->X, codes, offs, cont, n_cont, max_results,
+                                                                     ps, queue, n_queue, nullptr);
       block_tail_kernel<false><<<tail_grid, kBlockTpb, 0, s>>>(e->X, codes, offs, queue, n_queue, max_results, ps,
                                                                nullptr);
     }
